@@ -1,0 +1,68 @@
+"""Pin the CPU oracle against the reference's own golden files.
+
+Cases and tolerances follow the reference test-suite (tests/test_list and
+tests/generate_cmake_tests.py:8-9,95-100 of OpenMMPol): induced dipoles with
+rtol 1e-6 / atol 1e-5 (1e-3 for the FMM-produced 1ubq goldens) and the
+polarization energy EP with rtol 1e-6 / atol 1e-6.  The goldens were produced
+with the default CG solver at tolerance 1e-8.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES
+from oracle.oracle import OracleSystem, SOLVER_CG, SOLVER_DIIS, SOLVER_INVERSION, MATV_INCORE
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("with_field", [0, 1])
+def test_oracle_matches_reference_golden(case, with_field, golden, golden_mmp):
+    s = OracleSystem(golden_mmp[case])
+    ef = golden[case + "_ef1"] if with_field else np.zeros((s.pol_atoms, 3))
+    s.set_external_field(ef)
+    ep = s.get_polelec_energy()
+    ref = golden[f"{case}_ipd{with_field}"]
+    atol = float(golden[case + "_atol"])
+    ipd = s.ipd.reshape(-1, 3)
+    assert ipd.shape == ref.shape
+    np.testing.assert_allclose(ipd, ref, rtol=1e-6, atol=atol)
+    key = f"{case}_ep{with_field}"
+    if key in golden.files:
+        e_atol = 1e-6 if atol <= 1e-5 else 1e-3
+        np.testing.assert_allclose(ep, float(golden[key]), rtol=1e-6, atol=e_atol)
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "nma_wang", "1crn_wang"])
+def test_oracle_solvers_agree(case, golden, golden_mmp):
+    """DIIS and inversion have no golden of their own in the reference: pin
+    DIIS against the exact (LU) inversion at a tight tolerance, and CG against
+    both at the accuracy its quick exit allows.  The reference CG leaves the
+    loop as converged once |p.Tp| < 100*eps (mod_solvers.F90:177-181), an
+    absolute threshold that stops it near rms residual sqrt(2.2e-14/n)."""
+    ef = golden[case + "_ef1"]
+    res = {}
+    for solver in (SOLVER_CG, SOLVER_DIIS, SOLVER_INVERSION):
+        s = OracleSystem(golden_mmp[case])
+        s.set_tol(1e-11)
+        s.set_default_solver(solver)
+        s.set_external_field(ef)
+        res[solver] = s.ipd
+    scale = np.abs(res[SOLVER_INVERSION]).max()
+    assert np.abs(res[SOLVER_DIIS] - res[SOLVER_INVERSION]).max() <= 1e-9 * scale
+    assert np.abs(res[SOLVER_CG] - res[SOLVER_INVERSION]).max() <= 5e-6 * scale
+
+
+def test_oracle_incore_matches_direct(golden, golden_mmp):
+    s = OracleSystem(golden_mmp["1crn_amoeba"])
+    x = np.random.default_rng(0).standard_normal((s.pol_atoms, 3))
+    y_direct = s.tmatvec(x)
+    y_incore = s.tmatvec(x, matv=MATV_INCORE)
+    np.testing.assert_allclose(y_incore, y_direct, rtol=1e-12, atol=1e-12 * np.abs(y_direct).max())
+
+
+def test_oracle_nomm_solves_only_set_one(golden, golden_mmp):
+    """ommp_set_external_field_nomm solves the D set only (mod_interface.F90:223-230)."""
+    s = OracleSystem(golden_mmp["nma_amoeba"])
+    s.set_external_field(golden["nma_amoeba_ef1"], nomm=True)
+    ipd = s.ipd
+    assert np.abs(ipd[0]).max() > 0
+    assert np.all(ipd[1] == 0)

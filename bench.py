@@ -1,0 +1,378 @@
+"""Benchmark: induced-dipole solves/s on GB300 (one JSON line on stdout).
+
+Workload (default ``--config w30k``): the 90,000-site AMOEBA water box
+(30,000 molecules, jittered lattice at 0.0334 molecules/A^3, seed 1), each
+step solving both AMOEBA systems (D and P) to an RMS preconditioned residual
+of 1e-10 for a fresh external field of 30 random point charges (per-step seed,
+cold start), with the permanent-multipole field computed once per geometry as
+in the reference (src/mod_electrostatics.F90:1487-1596, M2D_done cache).
+
+* ``value``: solves/s of the mixed-precision solver (FP32 inner CG, FP64
+  residual / refinement / convergence test), fields resident in HBM, timed with
+  CUDA events on the library's stream; L2 is flushed between steps.
+* ``e2e``: the same through the reference-facing call ``ommp_set_external_field``
+  with host buffers (field H2D and dipoles D2H inside the timed region).
+* ``fp64``: one plain FP64 CG solve on the same workload (the reference's
+  algorithm on the GPU) and the relative error of the mixed result against it.
+* ``roofline``: the dominant pair kernel, its algorithmic flops (45 per ordered
+  pair per right-hand side) over its CUDA-event time, against the FMA pipe
+  peak measured in the same run.
+* ``cpu_baseline``: the C/OpenMP oracle (restatement of the reference's
+  OpenMP path) timed on a bounded sample of target rows of one matrix-vector
+  product, scaled to a full solve with the FP64 solve's product count.
+
+``--impl reference`` times that CPU implementation alone and prints its line.
+Multi-GPU (``--gpus N`` under torchrun): independent replicas, one per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "induced-dipole solves/s (mixed FP32/FP64 at <=1e-7 rel. error vs FP64)"
+FLOP_PER_PAIR = 45.0  # per ordered T.mu pair and right-hand side
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="w30k", choices=["w30k", "w1k"])
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "ommp_gb300_bench"))
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(cfg, cache):
+    from openmmpol_gb300 import synth
+    nw = {"w30k": 30000, "w1k": 1000}[cfg]
+    os.makedirs(cache, exist_ok=True)
+    path = os.path.join(cache, f"water_{nw}_seed1.mmp")
+    w = synth.water_cluster(nw, seed=1)
+    if not os.path.exists(path):
+        synth.write_mmp(path + ".tmp", w)
+        os.replace(path + ".tmp", path)
+    return path, w
+
+
+def fields_for(cpol, cmm, center, seeds):
+    from openmmpol_gb300 import synth
+    out = []
+    for sd in seeds:
+        ef, _, _ = synth.point_charge_field(cpol, center, seed=sd, all_sites_bohr=cmm)
+        out.append(np.ascontiguousarray(ef))
+    return out
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_sample(path, rows_n, threads=None):
+    """Oracle T.mu over a bounded sample of target rows: seconds per full product."""
+    from oracle import oracle as orc
+    if threads:
+        orc.set_num_threads(threads)
+    o = orc.OracleSystem(path)
+    n = o.pol_atoms
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((n, 3)) * 0.01
+    rows = np.sort(rng.choice(n, size=min(rows_n, n), replace=False)).astype(np.int32)
+    o.tmatvec_rows(x, rows[: max(1, len(rows) // 20)])  # warm-up
+    t0 = time.perf_counter()
+    o.tmatvec_rows(x, rows)
+    dt = time.perf_counter() - t0
+    return dt * n / len(rows), len(rows), n
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    orc.build()
+    path, _ = workload(args.config, args.cache)
+    cores = os.cpu_count() or 1
+    # matrix-vector products per plain CG solve on this workload (D + P,
+    # counting the initial residual product the reference always evaluates)
+    mv_per_solve = {"w30k": 2 * (16 + 1) + 2, "w1k": 2 * (15 + 1) + 2}[args.config]
+    rows = args.cpu_rows or (1500 if args.config == "w30k" else 3000)
+    times = []
+    for k in range(args.warmup + args.steps):
+        sec_per_mv, nrows, n = cpu_sample(path, rows, cores)
+        if k >= args.warmup:
+            times.append(sec_per_mv * mv_per_solve)
+    v = 1.0 / statistics.mean(times)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"water box {args.config}: {n} AMOEBA sites, 30-charge field, "
+                                   "CG tol 1e-10, direct matvec", "sites": n},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": f"{nrows} of {n} target rows of one T.mu product per step, "
+                                       f"scaled by {n}/{nrows} rows and {mv_per_solve} products per solve"},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import ctypes as C
+
+    import openmmpol_gb300 as og
+    from openmmpol_gb300 import _lib
+    from openmmpol_gb300 import build as b
+    b.build()
+    L = _lib.load()
+    og.set_verbose(0)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    path, w = workload(args.config, args.cache)
+    sys_ = og.OMMPSystem(path)
+    sys_.set_solver_tol(1e-10)
+    n = sys_.pol_atoms
+    cpol, cmm = sys_.cpol, sys_.cmm
+    center = w.box_center()
+    K, W = args.steps, args.warmup
+    e2e_k = args.e2e_steps if args.e2e_steps is not None else max(2, K // 2)
+    fields = fields_for(cpol, cmm, center, [100 + s for s in range(W + K + e2e_k + 1)])
+    nv = 3 * n
+    # device-resident fields (inputs in HBM before the timed region)
+    dev = []
+    for f in fields[: W + K]:
+        p = C.c_void_p()
+        assert L.ommp_gpu_device_alloc(nv * 8, C.byref(p)) == 0
+        assert L.ommp_gpu_copy_to_device(p, f.ctypes.data, nv * 8) == 0
+        dev.append(p)
+    h = sys_._h
+    # first solve on this geometry computes E_M2D (timed separately)
+    t0 = time.perf_counter()
+    st = L.ommp_gpu_get_e_m2d(h, np.zeros((sys_.n_ipd, n, 3)).ctypes.data_as(_lib._dp))
+    m2d_s = time.perf_counter() - t0
+    assert st == 0, L.ommp_gpu_last_error()
+    sys_.set_precision("mixed")
+    flush = 256 << 20
+
+    def one_step(k, timed):
+        sys_.clear_guess()
+        L.ommp_gpu_flush_l2(h, flush)
+        L.ommp_gpu_timer_record(h, 0)
+        st = L.ommp_gpu_set_external_field_device(h, dev[k], 0, 0, 1)
+        if st:
+            raise RuntimeError(L.ommp_gpu_last_error().decode())
+        L.ommp_gpu_timer_record(h, 1)
+        ms = C.c_double(0)
+        L.ommp_gpu_timer_elapsed(h, 0, 1, C.byref(ms))
+        return ms.value
+
+    for k in range(W):
+        one_step(k, False)
+    if dist:
+        dist.barrier()
+    sys_.synchronize()
+    L.ommp_gpu_reset_kernel_stats(h)
+    sys_.enable_kernel_timing(True)
+    launches0 = L.ommp_gpu_kernel_launch_count()
+    clk = Clocks(local if ws > 1 else 0)
+    step_ms = []
+    counters = []
+    wall0 = time.perf_counter()
+    for k in range(W, W + K):
+        step_ms.append(one_step(k, True))
+        counters.append((sys_.counter(0), sys_.counter(1), sys_.counter(2), sys_.counter(3)))
+    sys_.synchronize()
+    wall = time.perf_counter() - wall0
+    clocks = clk.stop()
+    launches = L.ommp_gpu_kernel_launch_count() - launches0
+    sys_.enable_kernel_timing(False)
+    k64 = sys_.kernel_stats(0)
+    k32 = sys_.kernel_stats(1)
+    total_ms = sum(step_ms)
+    if dist:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * K / (total_ms * 1e-3)
+    mixed_ipd = sys_.ipd.copy()
+    mixed_ep = sys_.get_polelec_energy()
+
+    # e2e through the reference-facing call with host buffers
+    e2e_ms = []
+    ipd_ptr = None
+    for k in range(e2e_k):
+        f = fields[W + K + k]
+        sys_.clear_guess()
+        L.ommp_gpu_flush_l2(h, flush)
+        sys_.synchronize()
+        t0 = time.perf_counter()
+        L.ommp_set_external_field(h, f.ctypes.data_as(_lib._dp), 0, 0)
+        ipd_ptr = L.ommp_get_ipd(h)
+        out = np.ctypeslib.as_array(ipd_ptr, shape=(sys_.n_ipd * nv,)).copy()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_value = ws * e2e_k / (sum(e2e_ms) * 1e-3)
+
+    # plain FP64 solve of the last timed field, and the mixed error against it
+    fp64 = None
+    if not args.no_fp64:
+        sys_.set_precision("fp64")
+        sys_.clear_guess()
+        t0 = time.perf_counter()
+        st = L.ommp_gpu_set_external_field_device(h, dev[W + K - 1], 0, 0, 1)
+        fp64_s = time.perf_counter() - t0
+        assert st == 0, L.ommp_gpu_last_error()
+        ref = sys_.ipd
+        ref_ep = sys_.get_polelec_energy()
+        fp64 = {"solves_per_s": 1.0 / fp64_s, "s_per_solve": fp64_s,
+                "t_mu_products": sys_.counter(0), "cg_iterations": [sys_.iterations(0), sys_.iterations(1)],
+                "residual_history_D": [float(x) for x in sys_.residual_history(0)],
+                "residual_history_P": [float(x) for x in sys_.residual_history(1)],
+                "mixed_rel_err_ipd": float(np.linalg.norm(mixed_ipd - ref) / np.linalg.norm(ref)),
+                "mixed_rel_err_energy": float(abs(mixed_ep - ref_ep) / abs(ref_ep)),
+                "energy": ref_ep, "speedup_mixed_over_fp64": value / ws * fp64_s}
+    # roofline of the dominant pair kernel
+    peak64 = C.c_double(0)
+    peak32 = C.c_double(0)
+    L.ommp_gpu_measure_pipe_peak(1, C.byref(peak64))
+    L.ommp_gpu_measure_pipe_peak(0, C.byref(peak32))
+    pairs = float(n) * (n - 1)
+    kstats = {}
+    for name, (cnt, ms), pk in (("tmu_fp64", k64, peak64.value), ("tmu_fp32", k32, peak32.value)):
+        if cnt:
+            # every launch in the mixed solver carries both AMOEBA sets
+            avg = ms / cnt
+            flop = FLOP_PER_PAIR * pairs * 2
+            ach = flop / (avg * 1e-3) / 1e12
+            kstats[name] = {"launches": cnt, "total_ms": ms, "avg_ms": avg, "achieved_tflops": ach,
+                            "peak_tflops": pk, "frac": ach / pk if pk else None}
+    dom = max(kstats, key=lambda k: kstats[k]["total_ms"]) if kstats else None
+    roof = None
+    if dom:
+        d = kstats[dom]
+        roof = {"bound": "fp64" if dom == "tmu_fp64" else "fp32", "kernel": dom,
+                "achieved": d["achieved_tflops"], "peak": d["peak_tflops"], "unit": "TFLOP/s",
+                "frac": d["frac"], "traffic": None,
+                "peak_source": "FMA-chain kernel measured in this run (pipe peak; "
+                               "MEASURED_PEAKS.json has no FP32/FP64 CUDA-core figure)",
+                "algorithmic": f"{FLOP_PER_PAIR:.0f} flop per ordered pair x N(N-1) pairs x 2 sets per launch",
+                "share_of_timed": d["total_ms"] / total_ms}
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32+f64", "data": "synthetic",
+            "config": {"workload": f"AMOEBA water box, {n} polarizable sites "
+                                   f"({n // 3} molecules, seed 1), fresh 30-charge field per step, "
+                                   "D+P solved to RMS residual 1e-10, cold start, E_M2D cached per geometry",
+                       "sites": n, "l2": "flushed (256 MiB write) between steps",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nv * 8,
+                    "d2h_bytes_per_step": sys_.n_ipd * nv * 8, "ms": e2e_ms},
+            "gpu_launches": int(launches), "wall_s_timed": wall, "m2d_first_solve_s": m2d_s,
+            "steps_ms": step_ms, "solver_counters_per_step": counters, "kernels": kstats,
+            "roofline": roof, "clocks": clocks, "fp64": fp64}
+    if rank == 0:
+        # CPU baseline on the host cores (oracle port, bounded sample)
+        try:
+            cores = os.cpu_count() or 1
+            rows = args.cpu_rows or (1500 if n > 30000 else 3000)
+            sec_mv, nrows, _ = cpu_sample(path, rows, cores)
+            mv = fp64["t_mu_products"] if fp64 else 36
+            cpu_v = 1.0 / (sec_mv * mv)
+            line["cpu_baseline"] = {"value": cpu_v, "unit": "solves/s", "cores": cores, "kind": "port",
+                                    "sample": f"{nrows} of {n} target rows of one T.mu product, scaled to "
+                                              f"{mv} products (the plain FP64 CG solve on this workload)",
+                                    "s_per_tmu_product": sec_mv}
+        except Exception as ex:  # report, do not hide
+            line["cpu_baseline"] = {"value": None, "error": repr(ex)}
+        print(json.dumps(line), flush=True)
+    for p in dev:
+        L.ommp_gpu_device_free(p)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

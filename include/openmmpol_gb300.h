@@ -1,0 +1,199 @@
+/*
+ * openmmpol_gb300.h -- C ABI of the GB300 induced-point-dipole library
+ * (libommp_gb300.so).
+ *
+ * The first block repeats, with the same names, types and meaning, the subset
+ * of OpenMMPol's C interface that drives the polarization path; each entry
+ * cites the declaration it replaces in the reference's include/openmmpol.h
+ * and the Fortran binding behind it in src/mod_c_interface.F90.  A host that
+ * only uses these symbols links against this library instead of the
+ * reference's and gets the same results (the direct O(N^2) sums, solved on
+ * the GPU).  As in the reference, these calls print a message and terminate
+ * the process (exit status 1) on any error.
+ *
+ * The second block (ommp_gpu_*) adds what the reference does not have:
+ * status-returning variants, solver tolerance and iteration controls, the
+ * FP32-inner / FP64-refinement precision mode, convergence history, kernel
+ * timing, and direct access to the E_M2D field and the T matrix-vector
+ * product for verification.
+ *
+ * Layout conventions (identical to the reference's Fortran arrays seen from C):
+ *   coordinates   double [mm_atoms][3], atomic units (bohr)
+ *   fields        double [pol_atoms][3], atomic units
+ *   dipoles       double [n_ipd][pol_atoms][3]; set 0 = direct (D), set 1 =
+ *                 polarization (P) for AMOEBA (include/f_cart_components.h)
+ * Pointers returned by getters point into library memory and stay valid until
+ * ommp_terminate(); input arrays are only read during the call.
+ */
+#ifndef OPENMMPOL_GB300_H
+#define OPENMMPOL_GB300_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifndef _OPENMMPOL_CONST
+/* values of config/openmmpol_const.h.in */
+#define OMMP_VERBOSE_DEBUG 3
+#define OMMP_VERBOSE_HIGH 2
+#define OMMP_VERBOSE_LOW 1
+#define OMMP_VERBOSE_NONE 0
+#define OMMP_VERBOSE_DEFAULT OMMP_VERBOSE_LOW
+#define OMMP_SOLVER_NONE 0
+#define OMMP_SOLVER_CG 1
+#define OMMP_SOLVER_DIIS 2
+#define OMMP_SOLVER_INVERSION 3
+#define OMMP_SOLVER_DEFAULT OMMP_SOLVER_CG
+#define OMMP_MATV_NONE 0
+#define OMMP_MATV_INCORE 1
+#define OMMP_MATV_DIRECT 2
+#define OMMP_MATV_DEFAULT OMMP_MATV_DIRECT
+#define OMMP_AMOEBA_D 1
+#define OMMP_AMOEBA_P 2
+#define OMMP_STR_CHAR_MAX 4096
+#endif
+
+/* precision modes of ommp_gpu_set_precision */
+#define OMMP_GPU_PREC_FP64 0  /* plain FP64 solver (default) */
+#define OMMP_GPU_PREC_MIXED 1 /* FP32 inner CG + FP64 iterative refinement */
+
+/* status codes of the ommp_gpu_* calls */
+#define OMMP_GPU_OK 0
+#define OMMP_GPU_ERR_INPUT 1
+#define OMMP_GPU_ERR_NOT_CONVERGED 2
+#define OMMP_GPU_ERR_BAD_ARG 3
+#define OMMP_GPU_ERR_NUMERIC 4
+#define OMMP_GPU_ERR_CUDA 5
+#define OMMP_GPU_ERR_MEMORY 6
+
+typedef void *OMMP_SYSTEM_PRT;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference-compatible subset ------------------------------------- */
+
+/* include/openmmpol.h:17 ; src/mod_c_interface.F90:216-231 */
+OMMP_SYSTEM_PRT ommp_init_mmp(const char *filename);
+/* include/openmmpol.h:19 ; src/mod_c_interface.F90:59-69 */
+void ommp_set_default_solver(OMMP_SYSTEM_PRT s, int32_t solver);
+/* include/openmmpol.h:20 ; src/mod_c_interface.F90:71-81 */
+void ommp_set_default_matv(OMMP_SYSTEM_PRT s, int32_t matv);
+/* include/openmmpol.h:24 ; src/mod_c_interface.F90:274-282 */
+void ommp_terminate(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:28 */
+void ommp_set_verbose(int32_t level);
+/* include/openmmpol.h:29 */
+void ommp_set_outputfile(const char *path);
+/* include/openmmpol.h:30 */
+void ommp_close_outputfile(void);
+/* include/openmmpol.h:31 */
+void ommp_message(const char *msg, int32_t level, const char *tag);
+/* include/openmmpol.h:32 */
+void ommp_fatal(const char *msg);
+/* include/openmmpol.h:33-34 (timers print at OMMP_VERBOSE_HIGH) */
+void ommp_time_pull(const char *label);
+void ommp_time_push(void);
+/* include/openmmpol.h:38 ; src/mod_c_interface.F90:378-388 */
+double ommp_get_polelec_energy(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:40 ; src/mod_c_interface.F90:289-305.
+ * ext_field: [pol_atoms][3].  Like the reference, `matv` is ignored on this
+ * path and the default matrix-vector method is used (mod_interface.F90:222). */
+void ommp_set_external_field(OMMP_SYSTEM_PRT s, const double *ext_field, int32_t solver, int32_t matv);
+/* include/openmmpol.h:41 ; src/mod_c_interface.F90:307-325.  Solves the D
+ * set only, from ext_field alone (no permanent-multipole field). */
+void ommp_set_external_field_nomm(OMMP_SYSTEM_PRT s, const double *ext_field, int32_t solver,
+                                  int32_t matv);
+/* include/openmmpol.h:66 */
+bool ommp_ff_is_amoeba(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:68-71 */
+int32_t ommp_get_n_ipd(OMMP_SYSTEM_PRT s);
+int32_t ommp_get_ld_cart(OMMP_SYSTEM_PRT s);
+int32_t ommp_get_mm_atoms(OMMP_SYSTEM_PRT s);
+int32_t ommp_get_pol_atoms(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:73 : [mm_atoms][3] */
+double *ommp_get_cmm(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:76 : [pol_atoms][3] */
+double *ommp_get_cpol(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:77 : [mm_atoms][ld_cart], lab frame */
+double *ommp_get_q(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:78 ; src/mod_c_interface.F90:999-1008 : [n_ipd][pol_atoms][3] */
+double *ommp_get_ipd(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:79 ; src/mod_c_interface.F90:1010-1028 : 0-based */
+int32_t *ommp_get_polar_mm(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:86 : new coordinates [mm_atoms][3] */
+void ommp_update_coordinates(OMMP_SYSTEM_PRT s, const double *cmm);
+/* include/openmmpol.h:153-155 ; src/mod_c_interface.F90:1843-1879.  The fast
+ * multipole method is not part of this library: enabling it logs a warning
+ * and the direct sums are kept; ommp_use_fmm always returns false. */
+void ommp_enable_fmm(OMMP_SYSTEM_PRT s);
+void ommp_disable_fmm(OMMP_SYSTEM_PRT s);
+bool ommp_use_fmm(OMMP_SYSTEM_PRT s);
+
+/* ---- extensions (no counterpart in the reference) ---------------------- */
+
+/* status-returning versions of the calls above (no process exit) */
+int32_t ommp_gpu_init_mmp(const char *filename, OMMP_SYSTEM_PRT *out);
+int32_t ommp_gpu_set_external_field(OMMP_SYSTEM_PRT s, const double *ext_field, int32_t solver,
+                                    int32_t matv, int32_t add_mm_field);
+/* same with a device pointer ext_field [pol_atoms][3] (no host copy) */
+int32_t ommp_gpu_set_external_field_device(OMMP_SYSTEM_PRT s, const double *ext_field_dev,
+                                           int32_t solver, int32_t matv, int32_t add_mm_field);
+int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *energy);
+int32_t ommp_gpu_update_coordinates(OMMP_SYSTEM_PRT s, const double *cmm);
+int32_t ommp_gpu_set_default_solver(OMMP_SYSTEM_PRT s, int32_t solver);
+int32_t ommp_gpu_set_default_matv(OMMP_SYSTEM_PRT s, int32_t matv);
+/* text of the last error of any call (thread-local to the library) */
+const char *ommp_gpu_last_error(void);
+
+/* solver controls; the reference hard-codes tol 1e-8 / 200 iterations
+ * (src/mod_solvers.F90:30-35) */
+void ommp_gpu_set_solver_tol(OMMP_SYSTEM_PRT s, double tol);
+void ommp_gpu_set_solver_maxiter(OMMP_SYSTEM_PRT s, int32_t maxiter);
+void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode);
+/* forget the last dipoles as a starting guess */
+void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s);
+
+/* results of the last solve: iterations of set k (CG/DIIS) or refinement
+ * steps (mixed), residual history (returns the length, copies up to maxn) */
+int32_t ommp_gpu_get_iterations(OMMP_SYSTEM_PRT s, int32_t set);
+int32_t ommp_gpu_get_residual_history(OMMP_SYSTEM_PRT s, int32_t set, double *out, int32_t maxn);
+/* counters of the last solve: 0 FP64 T.mu products, 1 FP32 products,
+ * 2 refinement steps, 3 inner FP32 iterations */
+int64_t ommp_gpu_get_counter(OMMP_SYSTEM_PRT s, int32_t which);
+/* device time of the last polarization solve (ms, CUDA events) */
+double ommp_gpu_last_solve_ms(OMMP_SYSTEM_PRT s);
+
+/* verification hooks: E_M2D [n_ipd][pol_atoms][3]; y = T x for nrhs (1|2)
+ * columns [nrhs][pol_atoms][3]; dodiag = 0 leaves out the 1/alpha diagonal */
+int32_t ommp_gpu_get_e_m2d(OMMP_SYSTEM_PRT s, double *out);
+int32_t ommp_gpu_tmatvec(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs, int32_t dodiag,
+                         int32_t matv);
+int32_t ommp_gpu_tmatvec_fp32(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs);
+
+/* CUDA-event timing of the pair kernels: which 0 = FP64 T.mu, 1 = FP32 T.mu */
+void ommp_gpu_enable_kernel_timing(OMMP_SYSTEM_PRT s, int32_t on);
+void ommp_gpu_kernel_stats(OMMP_SYSTEM_PRT s, int32_t which, int64_t *launches, double *total_ms);
+void ommp_gpu_reset_kernel_stats(OMMP_SYSTEM_PRT s);
+int32_t ommp_gpu_synchronize(OMMP_SYSTEM_PRT s);
+/* stream-ordered timers on the system's stream: record slot 0..7, then the
+ * elapsed device time between two recorded slots (waits for the second) */
+int32_t ommp_gpu_timer_record(OMMP_SYSTEM_PRT s, int32_t slot);
+int32_t ommp_gpu_timer_elapsed(OMMP_SYSTEM_PRT s, int32_t a, int32_t b, double *ms);
+/* overwrite `bytes` of a scratch buffer on the system's stream (L2 flush) */
+int32_t ommp_gpu_flush_l2(OMMP_SYSTEM_PRT s, int64_t bytes);
+/* kernels launched by this library since it was loaded */
+int64_t ommp_gpu_kernel_launch_count(void);
+/* device buffers for hosts without their own CUDA runtime (device-pointer API) */
+int32_t ommp_gpu_device_alloc(int64_t bytes, void **ptr);
+int32_t ommp_gpu_device_free(void *ptr);
+int32_t ommp_gpu_copy_to_device(void *dst, const void *src, int64_t bytes);
+/* measured FMA throughput of the FP64 (fp64 = 1) or FP32 pipe, TFLOP/s */
+int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops);
+/* SM count of the current device, 0 without a GPU */
+int32_t ommp_gpu_device_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

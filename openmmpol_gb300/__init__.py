@@ -1,0 +1,211 @@
+"""GB300-native induced-point-dipole polarization (OpenMMPol's polarization path).
+
+``OMMPSystem`` mirrors the polarization subset of pyopenmmpol's ``OMMPSystem``
+(pythonapi/pyopenmmpol/pyommp_interface.cpp:482-505 set_external_field,
+:258-266 ipd, get_polelec_energy) on top of the C ABI of libommp_gb300.so;
+every computation runs on the GPU through that library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+__all__ = ["OMMPSystem", "OMMPError", "available_solvers", "available_matrix_vector",
+           "set_verbose", "PREC_FP64", "PREC_MIXED"]
+
+# pythonapi/pyopenmmpol/pyommp_interface.cpp:9-23
+available_solvers = {"none": 0, "default": 1, "conjugate gradient": 1, "cg": 1,
+                     "inversion": 3, "diis": 2}
+available_matrix_vector = {"none": 0, "default": 2, "incore": 1, "direct": 2}
+verbosity = {"none": 0, "low": 1, "high": 2, "debug": 3}
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class OMMPError(RuntimeError):
+    """A library call returned a non-zero status."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[status {status}] {msg}")
+        self.status = status
+
+
+def _check(st: int):
+    if st != 0:
+        raise OMMPError(st, _lib.load().ommp_gpu_last_error().decode())
+
+
+def set_verbose(level) -> None:
+    lvl = verbosity[level] if isinstance(level, str) else int(level)
+    _lib.load().ommp_set_verbose(lvl)
+
+
+def _as_c(a, shape, dtype=np.float64):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    if a.shape != shape:
+        raise ValueError(f"array should be shaped {list(shape)}, got {list(a.shape)}")
+    return a
+
+
+class OMMPSystem:
+    """A polarizable system read from a ``.mmp`` file (revision 2 or 3)."""
+
+    def __init__(self, mmp_path: str):
+        L = _lib.load()
+        h = C.c_void_p()
+        _check(L.ommp_gpu_init_mmp(str(mmp_path).encode(), C.byref(h)))
+        self._h = h
+        self._L = L
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.ommp_terminate(h)
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    # --- sizes ---------------------------------------------------------------
+    @property
+    def pol_atoms(self) -> int:
+        return self._L.ommp_get_pol_atoms(self._h)
+
+    @property
+    def mm_atoms(self) -> int:
+        return self._L.ommp_get_mm_atoms(self._h)
+
+    @property
+    def n_ipd(self) -> int:
+        return self._L.ommp_get_n_ipd(self._h)
+
+    @property
+    def ld_cart(self) -> int:
+        return self._L.ommp_get_ld_cart(self._h)
+
+    @property
+    def is_amoeba(self) -> bool:
+        return bool(self._L.ommp_ff_is_amoeba(self._h))
+
+    # --- arrays (copies of library memory) -----------------------------------
+    def _view(self, ptr, shape, dtype=np.float64):
+        n = int(np.prod(shape))
+        if n == 0:
+            return np.zeros(shape, dtype=dtype)
+        return np.ctypeslib.as_array(ptr, shape=(n,)).reshape(shape).copy()
+
+    @property
+    def ipd(self) -> np.ndarray:
+        """Induced dipoles [n_ipd, pol_atoms, 3] (set 0 = D, 1 = P for AMOEBA)."""
+        return self._view(self._L.ommp_get_ipd(self._h), (self.n_ipd, self.pol_atoms, 3))
+
+    @property
+    def cpol(self) -> np.ndarray:
+        return self._view(self._L.ommp_get_cpol(self._h), (self.pol_atoms, 3))
+
+    @property
+    def cmm(self) -> np.ndarray:
+        return self._view(self._L.ommp_get_cmm(self._h), (self.mm_atoms, 3))
+
+    @property
+    def q(self) -> np.ndarray:
+        return self._view(self._L.ommp_get_q(self._h), (self.mm_atoms, self.ld_cart))
+
+    @property
+    def polar_mm(self) -> np.ndarray:
+        return self._view(self._L.ommp_get_polar_mm(self._h), (self.pol_atoms,), np.int32)
+
+    # --- polarization path ------------------------------------------------------
+    def set_external_field(self, ext_field, nomm: bool = False, solver: str = "none",
+                           matv: str = "none") -> None:
+        if solver not in available_solvers:
+            raise ValueError("Selected solver is not available!")
+        if matv not in available_matrix_vector:
+            raise ValueError("Selected matrix-vector method is not available!")
+        ef = _as_c(ext_field, (self.pol_atoms, 3))
+        _check(self._L.ommp_gpu_set_external_field(
+            self._h, ef.ctypes.data_as(_lib._dp), available_solvers[solver],
+            available_matrix_vector[matv], 0 if nomm else 1))
+
+    def get_polelec_energy(self) -> float:
+        e = C.c_double(0.0)
+        _check(self._L.ommp_gpu_get_polelec_energy(self._h, C.byref(e)))
+        return e.value
+
+    def update_coordinates(self, c) -> None:
+        c = _as_c(c, (self.mm_atoms, 3))
+        _check(self._L.ommp_gpu_update_coordinates(self._h, c.ctypes.data_as(_lib._dp)))
+
+    def set_default_solver(self, solver: str) -> None:
+        _check(self._L.ommp_gpu_set_default_solver(self._h, available_solvers[solver]))
+
+    def set_default_matv(self, matv: str) -> None:
+        _check(self._L.ommp_gpu_set_default_matv(self._h, available_matrix_vector[matv]))
+
+    def use_fmm(self) -> bool:
+        return bool(self._L.ommp_use_fmm(self._h))
+
+    # --- extensions ---------------------------------------------------------------
+    def set_solver_tol(self, tol: float) -> None:
+        self._L.ommp_gpu_set_solver_tol(self._h, float(tol))
+
+    def set_solver_maxiter(self, n: int) -> None:
+        self._L.ommp_gpu_set_solver_maxiter(self._h, int(n))
+
+    def set_precision(self, mode) -> None:
+        m = {"fp64": PREC_FP64, "mixed": PREC_MIXED}.get(mode, mode)
+        self._L.ommp_gpu_set_precision(self._h, int(m))
+
+    def clear_guess(self) -> None:
+        self._L.ommp_gpu_clear_guess(self._h)
+
+    def iterations(self, s: int = 0) -> int:
+        return self._L.ommp_gpu_get_iterations(self._h, s)
+
+    def residual_history(self, s: int = 0) -> np.ndarray:
+        out = np.zeros(4096)
+        n = self._L.ommp_gpu_get_residual_history(self._h, s, out.ctypes.data_as(_lib._dp), 4096)
+        return out[: min(n, 4096)].copy()
+
+    def counter(self, which: int) -> int:
+        return int(self._L.ommp_gpu_get_counter(self._h, which))
+
+    def last_solve_ms(self) -> float:
+        return float(self._L.ommp_gpu_last_solve_ms(self._h))
+
+    def e_m2d(self) -> np.ndarray:
+        out = np.zeros((self.n_ipd, self.pol_atoms, 3))
+        _check(self._L.ommp_gpu_get_e_m2d(self._h, out.ctypes.data_as(_lib._dp)))
+        return out
+
+    def tmatvec(self, x, dodiag: bool = True, matv: str = "direct") -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        nrhs = 1 if x.ndim == 2 else x.shape[0]
+        x = x.reshape(nrhs, self.pol_atoms, 3)
+        y = np.zeros_like(x)
+        _check(self._L.ommp_gpu_tmatvec(self._h, x.ctypes.data_as(_lib._dp), y.ctypes.data_as(_lib._dp),
+                                        nrhs, int(dodiag), available_matrix_vector[matv]))
+        return y[0] if nrhs == 1 else y
+
+    def tmatvec_fp32(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        nrhs = 1 if x.ndim == 2 else x.shape[0]
+        x = x.reshape(nrhs, self.pol_atoms, 3)
+        y = np.zeros_like(x)
+        _check(self._L.ommp_gpu_tmatvec_fp32(self._h, x.ctypes.data_as(_lib._dp),
+                                             y.ctypes.data_as(_lib._dp), nrhs))
+        return y[0] if nrhs == 1 else y
+
+    def enable_kernel_timing(self, on: bool = True) -> None:
+        self._L.ommp_gpu_enable_kernel_timing(self._h, int(on))
+
+    def kernel_stats(self, which: int):
+        n = C.c_int64(0)
+        ms = C.c_double(0.0)
+        self._L.ommp_gpu_kernel_stats(self._h, which, C.byref(n), C.byref(ms))
+        return n.value, ms.value
+
+    def synchronize(self) -> None:
+        _check(self._L.ommp_gpu_synchronize(self._h))

@@ -1,0 +1,106 @@
+"""ctypes binding of libommp_gb300.so (include/openmmpol_gb300.h).
+
+The shared library is built in-tree by ``openmmpol_gb300.build``.  Loading
+fails with an explicit error when it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libommp_gb300.so")
+
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+
+# name -> (restype, argtypes); every symbol declared in include/openmmpol_gb300.h
+SIGNATURES = {
+    "ommp_init_mmp": (_vp, [C.c_char_p]),
+    "ommp_set_default_solver": (None, [_vp, C.c_int32]),
+    "ommp_set_default_matv": (None, [_vp, C.c_int32]),
+    "ommp_terminate": (None, [_vp]),
+    "ommp_set_verbose": (None, [C.c_int32]),
+    "ommp_set_outputfile": (None, [C.c_char_p]),
+    "ommp_close_outputfile": (None, []),
+    "ommp_message": (None, [C.c_char_p, C.c_int32, C.c_char_p]),
+    "ommp_fatal": (None, [C.c_char_p]),
+    "ommp_time_pull": (None, [C.c_char_p]),
+    "ommp_time_push": (None, []),
+    "ommp_get_polelec_energy": (C.c_double, [_vp]),
+    "ommp_set_external_field": (None, [_vp, _dp, C.c_int32, C.c_int32]),
+    "ommp_set_external_field_nomm": (None, [_vp, _dp, C.c_int32, C.c_int32]),
+    "ommp_ff_is_amoeba": (C.c_bool, [_vp]),
+    "ommp_get_n_ipd": (C.c_int32, [_vp]),
+    "ommp_get_ld_cart": (C.c_int32, [_vp]),
+    "ommp_get_mm_atoms": (C.c_int32, [_vp]),
+    "ommp_get_pol_atoms": (C.c_int32, [_vp]),
+    "ommp_get_cmm": (_dp, [_vp]),
+    "ommp_get_cpol": (_dp, [_vp]),
+    "ommp_get_q": (_dp, [_vp]),
+    "ommp_get_ipd": (_dp, [_vp]),
+    "ommp_get_polar_mm": (_ip, [_vp]),
+    "ommp_update_coordinates": (None, [_vp, _dp]),
+    "ommp_enable_fmm": (None, [_vp]),
+    "ommp_disable_fmm": (None, [_vp]),
+    "ommp_use_fmm": (C.c_bool, [_vp]),
+    "ommp_gpu_init_mmp": (C.c_int32, [C.c_char_p, C.POINTER(_vp)]),
+    "ommp_gpu_set_external_field": (C.c_int32, [_vp, _dp, C.c_int32, C.c_int32, C.c_int32]),
+    "ommp_gpu_set_external_field_device": (C.c_int32, [_vp, _vp, C.c_int32, C.c_int32, C.c_int32]),
+    "ommp_gpu_get_polelec_energy": (C.c_int32, [_vp, _dp]),
+    "ommp_gpu_update_coordinates": (C.c_int32, [_vp, _dp]),
+    "ommp_gpu_set_default_solver": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_set_default_matv": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_last_error": (C.c_char_p, []),
+    "ommp_gpu_set_solver_tol": (None, [_vp, C.c_double]),
+    "ommp_gpu_set_solver_maxiter": (None, [_vp, C.c_int32]),
+    "ommp_gpu_set_precision": (None, [_vp, C.c_int32]),
+    "ommp_gpu_clear_guess": (None, [_vp]),
+    "ommp_gpu_get_iterations": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_get_residual_history": (C.c_int32, [_vp, C.c_int32, _dp, C.c_int32]),
+    "ommp_gpu_get_counter": (C.c_int64, [_vp, C.c_int32]),
+    "ommp_gpu_last_solve_ms": (C.c_double, [_vp]),
+    "ommp_gpu_get_e_m2d": (C.c_int32, [_vp, _dp]),
+    "ommp_gpu_tmatvec": (C.c_int32, [_vp, _dp, _dp, C.c_int32, C.c_int32, C.c_int32]),
+    "ommp_gpu_tmatvec_fp32": (C.c_int32, [_vp, _dp, _dp, C.c_int32]),
+    "ommp_gpu_enable_kernel_timing": (None, [_vp, C.c_int32]),
+    "ommp_gpu_kernel_stats": (None, [_vp, C.c_int32, _i64p, _dp]),
+    "ommp_gpu_synchronize": (C.c_int32, [_vp]),
+    "ommp_gpu_reset_kernel_stats": (None, [_vp]),
+    "ommp_gpu_timer_record": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_timer_elapsed": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp]),
+    "ommp_gpu_flush_l2": (C.c_int32, [_vp, C.c_int64]),
+    "ommp_gpu_kernel_launch_count": (C.c_int64, []),
+    "ommp_gpu_device_alloc": (C.c_int32, [C.c_int64, C.POINTER(_vp)]),
+    "ommp_gpu_device_free": (C.c_int32, [_vp]),
+    "ommp_gpu_copy_to_device": (C.c_int32, [_vp, _vp, C.c_int64]),
+    "ommp_gpu_measure_pipe_peak": (C.c_int32, [C.c_int32, _dp]),
+    "ommp_gpu_device_sm_count": (C.c_int32, []),
+}
+
+_lib = None
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def load(path: str | None = None):
+    """Load (once) and type the library; raises LibraryMissing if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise LibraryMissing(
+            f"{p} not found: build it with `python -m openmmpol_gb300.build` "
+            "(CUDA toolkit with sm_103a support required); there is no CPU fallback")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

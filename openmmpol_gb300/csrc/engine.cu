@@ -1,0 +1,916 @@
+// System lifetime, device residency and the polarization solvers.
+//
+// Solver semantics follow the reference (file:line in OpenMMPol):
+//   polarization driver     src/mod_polarization.F90:49-313
+//   conjugate gradient      src/mod_solvers.F90:86-216
+//   Jacobi + Pulay DIIS     src/mod_solvers.F90:218-469
+//   inversion               src/mod_solvers.F90:41-84
+//   set_external_field      src/mod_interface.F90:184-233
+//   get_polelec_energy      src/mod_interface.F90:343-370, energy_MM_pol
+//                           src/mod_electrostatics.F90:943-976
+//   update_coordinates      src/mod_mmpol.F90:325-371
+// Every vector lives on the device; the host reads one small status record
+// per iteration to decide when to stop.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+
+#include "engine.h"
+#include "log.h"
+
+namespace ommp {
+
+namespace {
+std::string g_last_error;
+constexpr size_t kMaxDenseBytes = size_t(24) << 30;  // incore T / inversion budget
+
+template <typename T>
+int dalloc(T *&p, size_t count) {
+  p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)&p, count * sizeof(T)) == cudaSuccess ? 0 : 1;
+}
+}  // namespace
+
+void set_last_error(const std::string &s) { g_last_error = s; }
+const char *last_error() { return g_last_error.c_str(); }
+
+int System::check(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return kOk;
+  set_last_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+  return kErrCuda;
+}
+
+System::~System() {
+  if (st_) cudaStreamSynchronize(st_);
+  void *bufs[] = {d_.pol_pos, d_.pol_a, d_.pol_alpha, d_.polar_mm, d_.pol_pos32, d_.pol_a32, d_.mm_pos,
+                  d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
+                  d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
+                  alpha32_, scratch_, scratch32_, partial_, dots_, hist_, cols_, flag_, tmat_, piv_,
+                  info_, diis_x_, diis_e_};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  if (flush_buf_) cudaFree(flush_buf_);
+  kt_resolve();
+  for (auto &e : kfree_) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  for (auto ev : tev_)
+    if (ev) cudaEventDestroy(ev);
+  if (cols_h_) cudaFreeHost(cols_h_);
+  if (scal_h_) cudaFreeHost(scal_h_);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (st_) cudaStreamDestroy(st_);
+}
+
+System *System::from_mmp(const std::string &path, std::string &err, int &status) {
+  System *s = new System();
+  if (!read_mmp(path, s->m_, err) || !prepare_model(s->m_, err)) {
+    status = kErrInput;
+    delete s;
+    return nullptr;
+  }
+  build_m2d_pairs(s->m_, s->m2d_pairs_);
+  build_d2d_pairs(s->m_, s->d2d_pairs_);
+  if (s->m_.fmm_requested)
+    log_msg(kVerbHigh, nullptr,
+            "More than 1000 MM atoms: the reference would enable FMM here; this library "
+            "always evaluates the direct sums.");
+  status = s->upload_static();
+  if (status != kOk) {
+    err = last_error();
+    delete s;
+    return nullptr;
+  }
+  return s;
+}
+
+int System::upload_static() {
+  const HostModel &m = m_;
+  int n = m.npol, mm = m.mm;
+  int st = check(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking), "stream");
+  if (st) return st;
+  cudaEventCreate(&ev0_);
+  cudaEventCreate(&ev1_);
+  d_.n = n;
+  d_.m = mm;
+  d_.amoeba = m.amoeba;
+  d_.ld = m.ld_cart;
+  int sms = gpu::sm_count();
+  nsplit_m2d_ = gpu::m2d_pick_split(d_, sms);
+  nsplit_tmu_ = gpu::tmu_pick_split(d_, 2, sms, false);
+  nsplit_tmu32_ = gpu::tmu_pick_split(d_, 2, sms, true);
+  size_t nv = 3 * (size_t)n;
+  int nipd = m.n_ipd;
+  int bad = 0;
+  bad |= dalloc(d_.pol_pos, n) | dalloc(d_.pol_a, n) | dalloc(d_.pol_alpha, n) | dalloc(d_.polar_mm, n);
+  bad |= dalloc(d_.pol_pos32, n) | dalloc(d_.pol_a32, n) | dalloc(alpha32_, n);
+  bad |= dalloc(d_.mm_pos, mm) | dalloc(d_.mm_a, mm) | dalloc(d_.mm_q, (size_t)mm * m.ld_cart);
+  bad |= dalloc(d_.m2d_ri, n + 1) | dalloc(d_.m2d_src, m2d_pairs_.src.size()) |
+         dalloc(d_.m2d_sP, m2d_pairs_.src.size()) | dalloc(d_.m2d_sD, m2d_pairs_.src.size());
+  bad |= dalloc(d_.d2d_ri, n + 1) | dalloc(d_.d2d_src, d2d_pairs_.src.size()) |
+         dalloc(d_.d2d_s, d2d_pairs_.src.size());
+  bad |= dalloc(e_m2d_, nv * nipd) | dalloc(ipd_, nv * nipd) | dalloc(rhs_, nv * 2) | dalloc(ext_, nv);
+  bad |= dalloc(x_, nv * 2) | dalloc(r_, nv * 2) | dalloc(p_, nv * 2) | dalloc(h_, nv * 2) | dalloc(z_, nv * 2);
+  bad |= dalloc(x32_, nv * 2) | dalloc(r32_, nv * 2) | dalloc(p32_, nv * 2) | dalloc(h32_, nv * 2) |
+         dalloc(z32_, nv * 2);
+  scratch_n_ = std::max(gpu::m2d_scratch_doubles(d_, nsplit_m2d_), gpu::tmu_scratch_doubles(d_, 2, nsplit_tmu_));
+  bad |= dalloc(scratch_, scratch_n_) | dalloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, nsplit_tmu32_));
+  bad |= dalloc(partial_, (size_t)gpu::kRedBlocks * 32) | dalloc(dots_, 64) | dalloc(hist_, 2 * (size_t)maxhist_);
+  bad |= dalloc(cols_, 2) | dalloc(flag_, 1) | dalloc(info_, 1);
+  if (bad || cudaMallocHost((void **)&cols_h_, 2 * sizeof(gpu::CgCol)) != cudaSuccess ||
+      cudaMallocHost((void **)&scal_h_, 64 * sizeof(double)) != cudaSuccess) {
+    set_last_error("out of device memory while allocating the system");
+    return kErrMemory;
+  }
+  d_.m2d_nnz = (int)m2d_pairs_.src.size();
+  d_.d2d_nnz = (int)d2d_pairs_.src.size();
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
+  };
+  up(d_.m2d_ri, m2d_pairs_.ri.data(), (n + 1) * sizeof(int));
+  up(d_.m2d_src, m2d_pairs_.src.data(), m2d_pairs_.src.size() * sizeof(int));
+  up(d_.m2d_sP, m2d_pairs_.sP.data(), m2d_pairs_.sP.size() * sizeof(double));
+  up(d_.m2d_sD, m2d_pairs_.sD.data(), m2d_pairs_.sD.size() * sizeof(double));
+  up(d_.d2d_ri, d2d_pairs_.ri.data(), (n + 1) * sizeof(int));
+  up(d_.d2d_src, d2d_pairs_.src.data(), d2d_pairs_.src.size() * sizeof(int));
+  up(d_.d2d_s, d2d_pairs_.sP.data(), d2d_pairs_.sP.size() * sizeof(double));
+  std::vector<double> alpha(m.pol), a(m.damping);
+  std::vector<float> alpha32(n), a32(n);
+  for (int k = 0; k < n; ++k) {
+    alpha32[k] = (float)alpha[k];
+    a32[k] = (float)a[k];
+  }
+  up(d_.pol_alpha, alpha.data(), n * sizeof(double));
+  up(d_.pol_a, a.data(), n * sizeof(double));
+  up(alpha32_, alpha32.data(), n * sizeof(float));
+  up(d_.pol_a32, a32.data(), n * sizeof(float));
+  up(d_.polar_mm, m.polar_mm.data(), n * sizeof(int));
+  cudaMemsetAsync(ipd_, 0, nv * nipd * sizeof(double), st_);
+  cudaMemsetAsync(e_m2d_, 0, nv * nipd * sizeof(double), st_);
+  ipd_h_.assign(nv * nipd, 0.0);
+  polar_mm_h_ = m.polar_mm;
+  st = upload_geometry();
+  if (st) return st;
+  return check(cudaStreamSynchronize(st_), "upload");
+}
+
+int System::upload_geometry() {
+  const HostModel &m = m_;
+  int n = m.npol, mm = m.mm;
+  const double inf = std::numeric_limits<double>::infinity();
+  std::vector<gpu::Pos64> pp(n), mp(mm);
+  std::vector<float4> pp32(n);
+  std::vector<double> ma(mm, 0.0);
+  double c[3] = {0, 0, 0};
+  for (int i = 0; i < mm; ++i)
+    for (int k = 0; k < 3; ++k) c[k] += m.cmm[3 * (size_t)i + k] / mm;
+  cpol_h_.resize(3 * (size_t)n);
+  for (int j = 0; j < n; ++j) {
+    int a = m.polar_mm[j];
+    const double *x = &m.cmm[3 * (size_t)a];
+    double w = 1.0 / m.thole[a];
+    pp[j] = gpu::Pos64{x[0], x[1], x[2], w};
+    pp32[j] = make_float4((float)(x[0] - c[0]), (float)(x[1] - c[1]), (float)(x[2] - c[2]), (float)w);
+    for (int k = 0; k < 3; ++k) cpol_h_[3 * (size_t)j + k] = x[k];
+  }
+  for (int i = 0; i < mm; ++i) {
+    const double *x = &m.cmm[3 * (size_t)i];
+    double t = m.thole[i];
+    mp[i] = gpu::Pos64{x[0], x[1], x[2], t > 0.0 ? 1.0 / t : inf};
+    if (m.mm_polar[i] >= 0) ma[i] = m.damping[m.mm_polar[i]];
+  }
+  cudaMemcpyAsync(d_.pol_pos, pp.data(), n * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
+  cudaMemcpyAsync(d_.pol_pos32, pp32.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st_);
+  cudaMemcpyAsync(d_.mm_pos, mp.data(), mm * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
+  cudaMemcpyAsync(d_.mm_a, ma.data(), mm * sizeof(double), cudaMemcpyHostToDevice, st_);
+  cudaMemcpyAsync(d_.mm_q, m.q.data(), m.q.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
+  // the host vectors above die at return: wait for the copies
+  return check(cudaStreamSynchronize(st_), "geometry upload");
+}
+
+int System::sync() {
+  int st = check(cudaStreamSynchronize(st_), "synchronize");
+  return st;
+}
+
+System::KEv System::kt_begin(int kind) {
+  KEv e;
+  if (!kfree_.empty()) {
+    e = kfree_.back();
+    kfree_.pop_back();
+  } else {
+    cudaEventCreate(&e.a);
+    cudaEventCreate(&e.b);
+  }
+  e.kind = kind;
+  cudaEventRecord(e.a, st_);
+  return e;
+}
+
+void System::kt_end(KEv &e) {
+  cudaEventRecord(e.b, st_);
+  kpending_.push_back(e);
+  if (kpending_.size() > 4096) kt_resolve();
+}
+
+void System::kt_resolve() {
+  for (auto &e : kpending_) {
+    cudaEventSynchronize(e.b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e.a, e.b);
+    klaunch_[e.kind] += 1;
+    kms_[e.kind] += ms;
+    kfree_.push_back(e);
+  }
+  kpending_.clear();
+}
+
+void System::kernel_stats(int which, long long &launches, double &ms) {
+  kt_resolve();
+  launches = klaunch_[which & 1];
+  ms = kms_[which & 1];
+}
+
+void System::reset_kernel_stats() {
+  kt_resolve();
+  klaunch_[0] = klaunch_[1] = 0;
+  kms_[0] = kms_[1] = 0.0;
+}
+
+int System::timer_record(int slot) {
+  if (slot < 0 || slot > 7) {
+    set_last_error("timer slot must be 0..7");
+    return kErrBadArg;
+  }
+  if (!tev_[slot]) cudaEventCreate(&tev_[slot]);
+  return check(cudaEventRecord(tev_[slot], st_), "timer record");
+}
+
+int System::timer_elapsed(int a, int b, double &ms) {
+  if (a < 0 || a > 7 || b < 0 || b > 7 || !tev_[a] || !tev_[b]) {
+    set_last_error("timer slots not recorded");
+    return kErrBadArg;
+  }
+  int st = check(cudaEventSynchronize(tev_[b]), "timer sync");
+  if (st) return st;
+  float f = 0.f;
+  st = check(cudaEventElapsedTime(&f, tev_[a], tev_[b]), "timer elapsed");
+  ms = f;
+  return st;
+}
+
+int System::flush_l2(size_t bytes) {
+  if (bytes > flush_bytes_) {
+    if (flush_buf_) cudaFree(flush_buf_);
+    flush_buf_ = nullptr;
+    flush_bytes_ = 0;
+    if (cudaMalloc(&flush_buf_, bytes) != cudaSuccess) {
+      set_last_error("out of device memory for the L2 flush buffer");
+      return kErrMemory;
+    }
+    flush_bytes_ = bytes;
+  }
+  return check(cudaMemsetAsync(flush_buf_, (int)(++flush_tag_ & 0xff), bytes, st_), "L2 flush");
+}
+
+int System::ensure_m2d() {
+  if (m2d_done_) return kOk;
+  cudaMemsetAsync(flag_, 0, sizeof(int), st_);
+  gpu::launch_m2d(d_, e_m2d_, scratch_, nsplit_m2d_, flag_, st_);
+  int flag = 0;
+  cudaMemcpyAsync(&flag, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  int st = check(cudaStreamSynchronize(st_), "M2D field");
+  if (st) return st;
+  if (flag) {
+    set_last_error(
+        "Requesting Coulomb kernel for two atoms placed in the same point, this could be an internal bug or "
+        "a problem in your input file, please check.");
+    return kErrNumeric;
+  }
+  m2d_done_ = true;
+  return kOk;
+}
+
+int System::e_m2d(double *out) {
+  int st = ensure_m2d();
+  if (st) return st;
+  size_t bytes = 3 * (size_t)d_.n * m_.n_ipd * sizeof(double);
+  cudaMemcpyAsync(out, e_m2d_, bytes, cudaMemcpyDeviceToHost, st_);
+  return check(cudaStreamSynchronize(st_), "E_M2D copy");
+}
+
+int System::ensure_tmat() {
+  if (tmat_ok_) return kOk;
+  size_t nn = 3 * (size_t)d_.n;
+  if (nn * nn * sizeof(double) > kMaxDenseBytes) {
+    set_last_error("the dense T matrix does not fit the in-core budget");
+    return kErrMemory;
+  }
+  if (!tmat_) {
+    if (dalloc(tmat_, nn * nn) || dalloc(piv_, nn)) {
+      set_last_error("out of device memory for the dense T matrix");
+      return kErrMemory;
+    }
+  }
+  gpu::launch_build_tmat(d_, tmat_, st_);
+  tmat_ok_ = true;
+  lu_ok_ = false;
+  return check(cudaGetLastError(), "T matrix");
+}
+
+int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag) {
+  if (matv == kMatvIncore && tmat_ok_) {
+    gpu::launch_gemv(3 * d_.n, tmat_, x, y, dodiag, d_.pol_alpha, ncol, st_);
+  } else {
+    if (ktime_on_) {
+      KEv e = kt_begin(0);
+      gpu::launch_tmu_f64(d_, ncol, x, y, dodiag, scratch_, nsplit_tmu_, st_);
+      kt_end(e);
+    } else {
+      gpu::launch_tmu_f64(d_, ncol, x, y, dodiag, scratch_, nsplit_tmu_, st_);
+    }
+    stats_.f64_matvecs += 1;
+  }
+  return kOk;
+}
+
+// Conjugate gradient over ncol independent columns sharing each matvec.
+int System::cg64(int matv, int ncol, const double *rhs, double *x, int set0) {
+  const int n = d_.n;
+  const size_t nv = 3 * (size_t)n;
+  log_msg(kVerbLow, nullptr, "Solving linear system with CG solver");
+  log_msg(kVerbLow, nullptr, "Max iter: %4d", maxiter_);
+  log_msg(kVerbLow, nullptr, "Tolerance: %8.1E", tol_);
+  // guess: a zero-norm input is replaced by precnd(x) = alpha * x (:151-157)
+  gpu::launch_dots(ncol, nv, x, x, partial_, st_);
+  gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+  cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  int st = check(cudaStreamSynchronize(st_), "CG start");
+  if (st) return st;
+  bool all_zero = true;
+  for (int k = 0; k < ncol; ++k) {
+    if (scal_h_[k] < kEpsRp) {
+      log_msg(kVerbHigh, nullptr, "Input guess has zero norm, generating a guess from preconditioner.");
+      gpu::launch_scale_by_alpha(1, n, d_.pol_alpha, x + k * nv, x + k * nv, st_);
+    } else {
+      log_msg(kVerbHigh, nullptr, "Using input guess as a starting point for iterative solver.");
+    }
+    if (scal_h_[k] != 0.0) all_zero = false;
+  }
+  // r = rhs - T x; an exactly zero x gives T x = 0 without the pair sum
+  if (all_zero) {
+    cudaMemcpyAsync(r_, rhs, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+  } else {
+    matvec64(matv, ncol, x, z_, true);
+    gpu::launch_residual(ncol * nv, rhs, z_, r_, st_);
+  }
+  gpu::launch_scale_by_alpha(ncol, n, d_.pol_alpha, r_, z_, st_);
+  cudaMemcpyAsync(p_, z_, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+  gpu::launch_dots(ncol, nv, r_, z_, partial_, st_);
+  gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+  cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  st = check(cudaStreamSynchronize(st_), "CG init");
+  if (st) return st;
+  for (int k = 0; k < ncol; ++k) {
+    gpu::CgCol c{};
+    c.gold = scal_h_[k];
+    c.active = 1;
+    cols_h_[k] = c;
+  }
+  cudaMemcpyAsync(cols_, cols_h_, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
+  for (int it = 1; it <= maxiter_; ++it) {
+    matvec64(matv, ncol, p_, h_, true);
+    gpu::launch_dots(ncol, nv, h_, p_, partial_, st_);
+    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+    gpu::launch_cg_alpha(ncol, dots_, cols_, kEpsRp, st_);
+    gpu::launch_cg_update(ncol, n, x, r_, p_, h_, z_, d_.pol_alpha, cols_, partial_, st_);
+    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+    gpu::launch_cg_gnew(ncol, n, dots_, cols_, tol_, hist_, maxhist_, st_);
+    gpu::launch_cg_pupdate(ncol, n, p_, z_, cols_, st_);
+    cudaMemcpyAsync(cols_h_, cols_, ncol * sizeof(gpu::CgCol), cudaMemcpyDeviceToHost, st_);
+    st = check(cudaStreamSynchronize(st_), "CG iteration");
+    if (st) return st;
+    bool any = false;
+    for (int k = 0; k < ncol; ++k) {
+      if (cols_h_[k].active) any = true;
+      if (log_level() >= kVerbHigh && cols_h_[k].iters == it)
+        log_msg(kVerbHigh, nullptr, "iter=%4d residual rms norm: %14.4E", it, cols_h_[k].rms);
+    }
+    if (!any) break;
+  }
+  std::vector<double> h(maxhist_);
+  int rc = kOk;
+  for (int k = 0; k < ncol; ++k) {
+    const gpu::CgCol &c = cols_h_[k];
+    int set = set0 + k;
+    stats_.iters[set] = c.iters;
+    int nh = std::min(c.iters, maxhist_);
+    cudaMemcpy(h.data(), hist_ + (size_t)k * maxhist_, nh * sizeof(double), cudaMemcpyDeviceToHost);
+    stats_.hist[set].assign(h.begin(), h.begin() + nh);
+    if (c.quick) log_msg(kVerbHigh, nullptr, "Direction vector with zero norm, exiting iterative solver.");
+    if (c.converged)
+      log_msg(kVerbHigh, nullptr, "Required convergence threshold reached, exiting iterative solver.");
+    if (!std::isfinite(c.rms)) {
+      set_last_error("non-finite residual in the iterative solver (coincident sites?)");
+      rc = kErrNumeric;
+    } else if (!c.converged && !c.quick && c.rms > tol_ && std::fabs(c.gama) > kEpsRp) {
+      set_last_error("Iterative solver did not converged");
+      rc = kErrNotConverged;
+    }
+  }
+  return rc;
+}
+
+// Pulay DIIS extrapolation state lives on the host (tiny B matrix).
+namespace {
+int small_lu_solve(int n, std::vector<double> &a, std::vector<double> &b) {
+  // column-major a (n x n), partial pivoting; returns 0 on success
+  for (int k = 0; k < n; ++k) {
+    int pr = k;
+    double mx = std::fabs(a[(size_t)k * n + k]);
+    for (int r = k + 1; r < n; ++r)
+      if (std::fabs(a[(size_t)k * n + r]) > mx) mx = std::fabs(a[(size_t)k * n + r]), pr = r;
+    if (a[(size_t)k * n + pr] == 0.0) return k + 1;
+    if (pr != k) {
+      for (int c = 0; c < n; ++c) std::swap(a[(size_t)c * n + k], a[(size_t)c * n + pr]);
+      std::swap(b[k], b[pr]);
+    }
+    double d = a[(size_t)k * n + k];
+    for (int r = k + 1; r < n; ++r) a[(size_t)k * n + r] /= d;
+    for (int c = k + 1; c < n; ++c) {
+      double f = a[(size_t)c * n + k];
+      if (f != 0.0)
+        for (int r = k + 1; r < n; ++r) a[(size_t)c * n + r] -= a[(size_t)k * n + r] * f;
+    }
+  }
+  for (int k = 0; k < n; ++k)
+    for (int r = k + 1; r < n; ++r) b[r] -= a[(size_t)k * n + r] * b[k];
+  for (int k = n - 1; k >= 0; --k) {
+    b[k] /= a[(size_t)k * n + k];
+    for (int r = 0; r < k; ++r) b[r] -= a[(size_t)k * n + r] * b[k];
+  }
+  return 0;
+}
+}  // namespace
+
+int System::diis64(int matv, const double *rhs, double *x, int set) {
+  const int n = d_.n;
+  const size_t nv = 3 * (size_t)n;
+  const int nd = diis_max_;
+  log_msg(kVerbLow, nullptr, "Solving linear system with jacobi solver");
+  log_msg(kVerbLow, nullptr, "Max iter: %4d", maxiter_);
+  log_msg(kVerbLow, nullptr, "Tolerance: %8.1E", tol_);
+  log_msg(kVerbLow, nullptr, "DIIS is enabled with n = %4d", nd);
+  if (!diis_x_ && (dalloc(diis_x_, nv * nd) || dalloc(diis_e_, nv * nd))) {
+    set_last_error("out of device memory for the DIIS history");
+    return kErrMemory;
+  }
+  double *xnew = z_, *y = h_;
+  std::vector<double> B((size_t)(nd + 1) * (nd + 1), 0.0);
+  auto Bat = [&](int r, int c) -> double & { return B[(size_t)c * (nd + 1) + r]; };
+  gpu::launch_dots(1, nv, x, x, partial_, st_);
+  gpu::launch_reduce_partials(1, partial_, dots_, st_);
+  cudaMemcpyAsync(scal_h_, dots_, sizeof(double), cudaMemcpyDeviceToHost, st_);
+  int st = check(cudaStreamSynchronize(st_), "DIIS start");
+  if (st) return st;
+  if (scal_h_[0] < kEpsRp) gpu::launch_scale_by_alpha(1, n, d_.pol_alpha, rhs, x, st_);
+  int nmat = 1;
+  double mx = 0.0;
+  stats_.hist[set].clear();
+  stats_.iters[set] = 0;
+  for (int it = 1; it <= maxiter_; ++it) {
+    matvec64(matv, 1, x, y, false);
+    gpu::launch_residual(nv, rhs, y, y, st_);
+    gpu::launch_scale_by_alpha(1, n, d_.pol_alpha, y, xnew, st_);
+    if (nd > 0) {
+      cudaMemcpyAsync(diis_x_ + (size_t)(nmat - 1) * nv, xnew, nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+      // error vector e = xnew - x
+      cudaMemcpyAsync(diis_e_ + (size_t)(nmat - 1) * nv, xnew, nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+      gpu::launch_axpby(nv, -1.0, x, 1.0, diis_e_ + (size_t)(nmat - 1) * nv, st_);
+      if (nmat >= nd) {  // drop the ten oldest points
+        for (int j = 2; j <= nmat - 10; ++j)
+          for (int k = 2; k <= nmat - 10; ++k) Bat(j - 1, k - 1) = Bat(j + 10 - 1, k + 10 - 1);
+        size_t cnt = (size_t)(nmat - 10) * nv;
+        cudaMemcpyAsync(diis_x_, diis_x_ + 10 * nv, cnt * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+        cudaMemcpyAsync(diis_e_, diis_e_ + 10 * nv, cnt * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+        nmat -= 10;
+      }
+      // makeb: new row/column of B from dots against the newest error vector
+      gpu::launch_dots_bcast(nmat, nv, diis_e_, diis_e_ + (size_t)(nmat - 1) * nv, partial_, st_);
+      gpu::launch_reduce_partials(nmat, partial_, dots_, st_);
+      cudaMemcpyAsync(scal_h_, dots_, nmat * sizeof(double), cudaMemcpyDeviceToHost, st_);
+      st = check(cudaStreamSynchronize(st_), "DIIS dots");
+      if (st) return st;
+      if (nmat == 1) {
+        Bat(0, 0) = 0.0;
+        Bat(0, 1) = 1.0;
+        Bat(1, 0) = 1.0;
+        Bat(1, 1) = scal_h_[0];
+      } else {
+        Bat(nmat, 0) = 1.0;
+        Bat(0, nmat) = 1.0;
+        for (int i = 1; i <= nmat - 1; ++i) Bat(nmat, i) = Bat(i, nmat) = scal_h_[i - 1];
+        Bat(nmat, nmat) = scal_h_[nmat - 1];
+      }
+      int nm1 = nmat + 1;
+      std::vector<double> bl((size_t)nm1 * nm1), cex(nm1, 0.0);
+      for (int c = 0; c < nm1; ++c)
+        for (int r = 0; r < nm1; ++r) bl[(size_t)c * nm1 + r] = Bat(r, c);
+      cex[0] = 1.0;
+      if (small_lu_solve(nm1, bl, cex) != 0) {
+        nmat = 1;
+      } else {
+        cudaMemcpyAsync(dots_, cex.data() + 1, nmat * sizeof(double), cudaMemcpyHostToDevice, st_);
+        gpu::launch_lincomb(nmat, nv, diis_x_, nv, dots_, xnew, st_);
+        nmat += 1;
+      }
+    }
+    gpu::launch_diff_norms(nv, xnew, x, partial_, st_);
+    gpu::launch_reduce_norms(partial_, dots_ + 32, st_);
+    cudaMemcpyAsync(x, xnew, nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+    cudaMemcpyAsync(scal_h_, dots_ + 32, 2 * sizeof(double), cudaMemcpyDeviceToHost, st_);
+    st = check(cudaStreamSynchronize(st_), "DIIS iteration");
+    if (st) return st;
+    double rms = std::sqrt(scal_h_[0] / (double)nv);
+    mx = scal_h_[1];
+    stats_.hist[set].push_back(mx);
+    stats_.iters[set] = it;
+    log_msg(kVerbHigh, nullptr, "iter=%4d residual norm (rms, max): %14.4E%14.4E", it, rms, mx);
+    if (!std::isfinite(mx)) {
+      set_last_error("non-finite increment in the Jacobi/DIIS solver");
+      return kErrNumeric;
+    }
+    if (mx < tol_) {
+      log_msg(kVerbHigh, nullptr, "Required convergence threshold reached, exiting iterative solver.");
+      break;
+    }
+  }
+  if (mx > tol_) {
+    set_last_error("Iterative solver did not converged");
+    return kErrNotConverged;
+  }
+  return kOk;
+}
+
+int System::inversion64(const double *rhs, double *x) {
+  int st = ensure_tmat();
+  if (st) return st;
+  size_t nn = 3 * (size_t)d_.n;
+  if (!lu_ok_) {
+    double *lu = nullptr;
+    if (dalloc(lu, nn * nn)) {
+      set_last_error("out of device memory for the LU factors");
+      return kErrMemory;
+    }
+    cudaMemcpyAsync(lu, tmat_, nn * nn * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+    gpu::launch_lu_factor((int)nn, lu, piv_, info_, nullptr, st_);
+    int info = 0;
+    cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+    st = check(cudaStreamSynchronize(st_), "LU");
+    if (st) {
+      cudaFree(lu);
+      return st;
+    }
+    if (info) {
+      cudaFree(lu);
+      set_last_error("inversion solver: singular interaction matrix");
+      return kErrNumeric;
+    }
+    // the factors replace T; an in-core matvec rebuilds T on demand
+    std::swap(lu, tmat_);
+    cudaFree(lu);
+    tmat_ok_ = false;
+    lu_ok_ = true;
+  }
+  cudaMemcpyAsync(x, rhs, nn * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+  gpu::launch_lu_solve((int)nn, tmat_, piv_, x, st_);
+  return check(cudaStreamSynchronize(st_), "LU solve");
+}
+
+// FP32 preconditioned CG on r32_ (columns normalised to unit rms); result in x32_.
+int System::pcg32(int ncol, double *rms0_out, int max_it, double eta) {
+  (void)rms0_out;
+  const int n = d_.n;
+  const size_t nv = 3 * (size_t)n;
+  // x = 0; p = h = 0 so that an update step with alpha = 0 only forms
+  // z = alpha_pol r and the partial r.z
+  cudaMemsetAsync(x32_, 0, ncol * nv * sizeof(float), st_);
+  cudaMemsetAsync(p32_, 0, ncol * nv * sizeof(float), st_);
+  cudaMemsetAsync(h32_, 0, ncol * nv * sizeof(float), st_);
+  gpu::CgCol c0{};
+  for (int k = 0; k < ncol; ++k) {
+    c0.active = 1;
+    c0.alpha = 0.0;
+    cols_h_[k] = c0;
+  }
+  cudaMemcpyAsync(cols_, cols_h_, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
+  // with alpha = 0 the update kernel leaves x, r unchanged and writes
+  // z = alpha_pol r and the partial r.z
+  gpu::launch_cg_update_f32(ncol, n, x32_, r32_, p32_, h32_, z32_, alpha32_, cols_, partial_, st_);
+  gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+  cudaMemcpyAsync(p32_, z32_, ncol * nv * sizeof(float), cudaMemcpyDeviceToDevice, st_);
+  cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  int st = check(cudaStreamSynchronize(st_), "inner CG init");
+  if (st) return st;
+  for (int k = 0; k < ncol; ++k) {
+    gpu::CgCol c{};
+    c.gold = scal_h_[k];
+    c.active = scal_h_[k] > 0.0 ? 1 : 0;
+    cols_h_[k] = c;
+  }
+  cudaMemcpyAsync(cols_, cols_h_, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
+  int it = 0;
+  for (it = 1; it <= max_it; ++it) {
+    if (ktime_on_) {
+      KEv e = kt_begin(1);
+      gpu::launch_tmu_f32(d_, ncol, p32_, h32_, scratch32_, nsplit_tmu32_, st_);
+      kt_end(e);
+    } else {
+      gpu::launch_tmu_f32(d_, ncol, p32_, h32_, scratch32_, nsplit_tmu32_, st_);
+    }
+    stats_.f32_matvecs += 1;
+    gpu::launch_dots_f32(ncol, nv, h32_, p32_, partial_, st_);
+    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+    gpu::launch_cg_alpha(ncol, dots_, cols_, 1e-300, st_);
+    gpu::launch_cg_update_f32(ncol, n, x32_, r32_, p32_, h32_, z32_, alpha32_, cols_, partial_, st_);
+    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+    gpu::launch_cg_gnew(ncol, n, dots_, cols_, eta, nullptr, 0, st_);
+    gpu::launch_cg_pupdate_f32(ncol, n, p32_, z32_, cols_, st_);
+    cudaMemcpyAsync(cols_h_, cols_, ncol * sizeof(gpu::CgCol), cudaMemcpyDeviceToHost, st_);
+    st = check(cudaStreamSynchronize(st_), "inner CG iteration");
+    if (st) return st;
+    bool any = false;
+    for (int k = 0; k < ncol; ++k) any |= cols_h_[k].active != 0;
+    if (!any) break;
+  }
+  stats_.inner_iters += std::min(it, max_it);
+  return kOk;
+}
+
+// Iterative refinement: FP64 residual, FP32 inner PCG, FP64 accumulation.
+int System::mixed_ir(int ncol, const double *rhs, double *x, int set0, bool have_guess) {
+  const int n = d_.n;
+  const size_t nv = 3 * (size_t)n;
+  const int max_outer = 30;
+  log_msg(kVerbLow, nullptr, "Solving linear system with mixed-precision CG (FP32 inner, FP64 refinement)");
+  if (have_guess) {
+    matvec64(kMatvDirect, ncol, x, h_, true);
+    gpu::launch_residual(ncol * nv, rhs, h_, r_, st_);
+  } else {
+    cudaMemsetAsync(x, 0, ncol * nv * sizeof(double), st_);
+    cudaMemcpyAsync(r_, rhs, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+  }
+  for (int k = 0; k < ncol; ++k) stats_.hist[set0 + k].clear();
+  std::vector<double> rms(ncol);
+  int outer = 0;
+  bool done = false;
+  while (true) {
+    gpu::launch_scale_by_alpha(ncol, n, d_.pol_alpha, r_, z_, st_);
+    gpu::launch_dots(ncol, nv, r_, z_, partial_, st_);
+    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
+    cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
+    int st = check(cudaStreamSynchronize(st_), "refinement residual");
+    if (st) return st;
+    done = true;
+    for (int k = 0; k < ncol; ++k) {
+      rms[k] = std::sqrt(std::max(scal_h_[k], 0.0) / (double)nv);
+      stats_.hist[set0 + k].push_back(rms[k]);
+      if (!std::isfinite(rms[k])) {
+        set_last_error("non-finite residual in the refinement loop (coincident sites?)");
+        return kErrNumeric;
+      }
+      if (!(rms[k] < tol_)) done = false;
+      log_msg(kVerbHigh, nullptr, "refinement step %3d set %d residual rms norm: %14.4E", outer, set0 + k, rms[k]);
+    }
+    if (done || outer >= max_outer) break;
+    // normalise each unconverged column to unit preconditioned rms; converged
+    // columns get a zero right-hand side (the inner CG leaves them at zero)
+    double worst_eta = 1e-5;
+    for (int k = 0; k < ncol; ++k) {
+      scal_h_[8 + k] = rms[k] < tol_ ? 0.0 : 1.0 / rms[k];
+      scal_h_[16 + k] = rms[k] < tol_ ? 0.0 : rms[k];
+      if (rms[k] >= tol_) worst_eta = std::max(worst_eta, std::min(1e-2, 0.3 * tol_ / rms[k]));
+    }
+    double eta = worst_eta;
+    cudaMemcpyAsync(dots_ + 8, scal_h_ + 8, 16 * sizeof(double), cudaMemcpyHostToDevice, st_);
+    for (int k = 0; k < ncol; ++k) gpu::launch_to_f32(nv, r_ + k * nv, dots_ + 8 + k, r32_ + k * nv, st_);
+    st = pcg32(ncol, nullptr, 200, eta);
+    if (st) return st;
+    gpu::launch_ir_accumulate(ncol, n, x, x32_, dots_ + 16, st_);
+    matvec64(kMatvDirect, ncol, x, h_, true);
+    gpu::launch_residual(ncol * nv, rhs, h_, r_, st_);
+    ++outer;
+  }
+  stats_.outer += outer;
+  for (int k = 0; k < ncol; ++k) stats_.iters[set0 + k] = outer;
+  if (!done) {
+    set_last_error("Iterative solver did not converged");
+    return kErrNotConverged;
+  }
+  return kOk;
+}
+
+int System::polarization(const double *e, int solver, int matv, const bool *mask_in) {
+  const int n = d_.n;
+  const size_t nv = 3 * (size_t)n;
+  if (n == 0) return kOk;
+  if (solver == kSolverNone) solver = def_solver_;
+  if (matv == kMatvNone) matv = def_matv_;
+  bool mask[2] = {true, true};
+  if (mask_in && m_.n_ipd > 1) mask[0] = mask_in[0], mask[1] = mask_in[1];
+  const int nipd = m_.n_ipd;
+  stats_ = SolveStats();
+  if (matv == kMatvIncore || solver == kSolverInversion) {
+    int st = ensure_tmat();
+    if (st == kErrMemory && solver != kSolverInversion) {
+      log_msg(kVerbHigh, nullptr, "In-core T does not fit the memory budget: using the direct matrix-vector product");
+      matv = kMatvDirect;
+    } else if (st) {
+      return st;
+    }
+    if (matv == kMatvIncore && !tmat_ok_) {
+      st = ensure_tmat();
+      if (st) return st;
+    }
+  }
+  cudaEventRecord(ev0_, st_);
+  cudaMemsetAsync(x_, 0, nv * nipd * sizeof(double), st_);
+  if (solver != kSolverInversion) {
+    if (ipd_use_guess_)
+      for (int k = 0; k < nipd; ++k)
+        if (mask[k]) cudaMemcpyAsync(x_ + k * nv, ipd_ + k * nv, nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+    if (matv == kMatvIncore)
+      log_msg(kVerbHigh, nullptr, "Matrix-Vector will be performed in-memory");
+    else if (matv == kMatvDirect)
+      log_msg(kVerbHigh, nullptr, "Matrix-Vector will be performed on-the-fly");
+    else {
+      set_last_error("Unknown matrix-vector method requested");
+      return kErrBadArg;
+    }
+  }
+  int st = kOk;
+  if (solver == kSolverCG || solver == kSolverDIIS) {
+    bool mixed = solver == kSolverCG && precision_ == kPrecMixed && matv == kMatvDirect;
+    if (mixed) {
+      // both AMOEBA sets share every pair evaluation
+      if (nipd == 2 && mask[0] && mask[1])
+        st = mixed_ir(2, e, x_, 0, ipd_use_guess_);
+      else
+        for (int k = 0; k < nipd && !st; ++k)
+          if (mask[k]) st = mixed_ir(1, e + k * nv, x_ + k * nv, k, ipd_use_guess_);
+    } else {
+      auto run = [&](int k) {
+        return solver == kSolverCG ? cg64(matv, 1, e + k * nv, x_ + k * nv, k) : diis64(matv, e + k * nv, x_ + k * nv, k);
+      };
+      if (nipd == 2) {
+        if (mask[0]) st = run(0);
+        // without a guess, D seeds P (:237-243)
+        if (!st && mask[0] && mask[1] && !ipd_use_guess_)
+          cudaMemcpyAsync(x_ + nv, x_, nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+        if (!st && mask[1]) st = run(1);
+      } else {
+        st = run(0);
+      }
+    }
+  } else if (solver == kSolverInversion) {
+    for (int k = 0; k < nipd && !st; ++k)
+      if (mask[k]) st = inversion64(e + k * nv, x_ + k * nv);
+  } else {
+    set_last_error("Unknown solver for calculation of the induced point dipoles");
+    return kErrBadArg;
+  }
+  if (st) return st;
+  cudaMemcpyAsync(ipd_, x_, nv * nipd * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+  cudaEventRecord(ev1_, st_);
+  ipd_done_ = true;
+  ipd_use_guess_ = true;
+  st = fetch_ipd();
+  cudaEventElapsedTime(&last_ms_, ev0_, ev1_);
+  return st;
+}
+
+int System::fetch_ipd() {
+  size_t bytes = ipd_h_.size() * sizeof(double);
+  cudaMemcpyAsync(ipd_h_.data(), ipd_, bytes, cudaMemcpyDeviceToHost, st_);
+  return check(cudaStreamSynchronize(st_), "dipole copy");
+}
+
+int System::set_external_field(const double *ext_host, int solver, int matv, bool add_mm) {
+  const size_t nv = 3 * (size_t)d_.n;
+  cudaMemcpyAsync(ext_, ext_host, nv * sizeof(double), cudaMemcpyHostToDevice, st_);
+  return set_external_field_device(ext_, solver, matv, add_mm);
+}
+
+int System::set_external_field_device(const double *ext, int solver, int matv, bool add_mm) {
+  const size_t nv = 3 * (size_t)d_.n;
+  ipd_done_ = false;
+  if (d_.n == 0) return kOk;
+  int st = kOk;
+  if (add_mm) {
+    st = ensure_m2d();
+    if (st) return st;
+    // rhs_[k] = E_M2D[k] + ext
+    for (int k = 0; k < m_.n_ipd; ++k) gpu::launch_add(nv, e_m2d_ + k * nv, ext, rhs_ + k * nv, st_);
+    // the reference does not forward matv on this path (mod_interface.F90:222)
+    return polarization(rhs_, solver, kMatvNone, nullptr);
+  }
+  if (ext != rhs_) cudaMemcpyAsync(rhs_, ext, nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+  if (m_.n_ipd == 2) cudaMemsetAsync(rhs_ + nv, 0, nv * sizeof(double), st_);
+  bool mask[2] = {true, false};
+  return polarization(rhs_, solver, matv, mask);
+}
+
+int System::polelec_energy(double &e) {
+  e = 0.0;
+  const int n = d_.n;
+  if (n == 0) return kOk;
+  const size_t nv = 3 * (size_t)n;
+  int st;
+  if (!ipd_done_) {
+    st = ensure_m2d();
+    if (st) return st;
+    st = polarization(e_m2d_, kSolverNone, kMatvNone, nullptr);
+    if (st) return st;
+  }
+  st = ensure_m2d();
+  if (st) return st;
+  // -1/2 sum ipd(D) . E_M2D(P) for AMOEBA, -1/2 sum ipd . E_M2D otherwise
+  const double *ef = m_.amoeba ? e_m2d_ + nv : e_m2d_;
+  gpu::launch_dots(1, nv, ipd_, ef, partial_, st_);
+  gpu::launch_reduce_partials(1, partial_, dots_, st_);
+  cudaMemcpyAsync(scal_h_, dots_, sizeof(double), cudaMemcpyDeviceToHost, st_);
+  st = check(cudaStreamSynchronize(st_), "energy");
+  if (st) return st;
+  e = -0.5 * scal_h_[0];
+  return kOk;
+}
+
+int System::update_coordinates(const double *c) {
+  std::copy(c, c + 3 * (size_t)m_.mm, m_.cmm.begin());
+  std::string err;
+  if (m_.amoeba && !rotate_multipoles(m_, err)) {
+    set_last_error(err);
+    return kErrInput;
+  }
+  m2d_done_ = ipd_done_ = ipd_use_guess_ = false;
+  tmat_ok_ = lu_ok_ = false;
+  return upload_geometry();
+}
+
+int System::set_default_solver(int s) {
+  if (s != kSolverCG && s != kSolverInversion && s != kSolverDIIS) {
+    set_last_error("Unrecognized setting for default solver method");
+    return kErrBadArg;
+  }
+  def_solver_ = s;
+  return kOk;
+}
+
+int System::set_default_matv(int mv) {
+  if (mv != kMatvIncore && mv != kMatvDirect) {
+    set_last_error("Unrecognized setting for default matrix-vector method");
+    return kErrBadArg;
+  }
+  def_matv_ = mv;
+  return kOk;
+}
+
+int System::tmatvec(const double *xh, double *yh, int nrhs, bool dodiag, int matv) {
+  const size_t nv = 3 * (size_t)d_.n;
+  if (nrhs < 1 || nrhs > 2) {
+    set_last_error("tmatvec: nrhs must be 1 or 2");
+    return kErrBadArg;
+  }
+  if (matv == kMatvNone) matv = def_matv_;
+  if (matv == kMatvIncore) {
+    int st = ensure_tmat();
+    if (st) return st;
+  }
+  cudaMemcpyAsync(p_, xh, nrhs * nv * sizeof(double), cudaMemcpyHostToDevice, st_);
+  matvec64(matv, nrhs, p_, h_, dodiag);
+  cudaMemcpyAsync(yh, h_, nrhs * nv * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  return check(cudaStreamSynchronize(st_), "tmatvec");
+}
+
+int System::tmatvec_f32(const double *xh, double *yh, int nrhs) {
+  const size_t nv = 3 * (size_t)d_.n;
+  if (nrhs < 1 || nrhs > 2) {
+    set_last_error("tmatvec_f32: nrhs must be 1 or 2");
+    return kErrBadArg;
+  }
+  cudaMemcpyAsync(p_, xh, nrhs * nv * sizeof(double), cudaMemcpyHostToDevice, st_);
+  gpu::launch_to_f32(nrhs * nv, p_, nullptr, p32_, st_);
+  gpu::launch_tmu_f32(d_, nrhs, p32_, h32_, scratch32_, nsplit_tmu32_, st_);
+  std::vector<float> tmp(nrhs * nv);
+  cudaMemcpyAsync(tmp.data(), h32_, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, st_);
+  int st = check(cudaStreamSynchronize(st_), "tmatvec_f32");
+  for (size_t i = 0; i < tmp.size(); ++i) yh[i] = tmp[i];
+  return st;
+}
+
+}  // namespace ommp

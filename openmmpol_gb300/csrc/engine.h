@@ -1,0 +1,157 @@
+// Device-resident system and the polarization solvers (FP64 CG, Jacobi/DIIS,
+// inversion, and the FP32-inner / FP64-refinement solver).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "ommp_internal.h"
+
+namespace ommp {
+
+enum Status : int {
+  kOk = 0,
+  kErrInput = 1,
+  kErrNotConverged = 2,
+  kErrBadArg = 3,
+  kErrNumeric = 4,
+  kErrCuda = 5,
+  kErrMemory = 6,
+};
+
+struct SolveStats {
+  int iters[2] = {0, 0};
+  std::vector<double> hist[2];
+  int outer = 0;          // refinement steps of the mixed solver
+  int inner_iters = 0;    // FP32 iterations summed over outer steps
+  int f64_matvecs = 0;
+  int f32_matvecs = 0;
+};
+
+class System {
+ public:
+  ~System();
+  static System *from_mmp(const std::string &path, std::string &err, int &status);
+
+  // --- reference API semantics -------------------------------------------------
+  int set_external_field(const double *ext_host, int solver, int matv, bool add_mm);
+  int set_external_field_device(const double *ext_dev, int solver, int matv, bool add_mm);
+  int polelec_energy(double &e);
+  int update_coordinates(const double *c_host);
+  int set_default_solver(int s);
+  int set_default_matv(int m);
+
+  // --- extensions --------------------------------------------------------------
+  int tmatvec(const double *x_host, double *y_host, int nrhs, bool dodiag, int matv);
+  int tmatvec_f32(const double *x_host, double *y_host, int nrhs);
+  int e_m2d(double *out_host);
+  void clear_guess() { ipd_use_guess_ = false; }
+  void set_tol(double t) { tol_ = t; }
+  void set_maxiter(int n) { maxiter_ = n; }
+  void set_precision(int p) { precision_ = p; }
+  int precision() const { return precision_; }
+  double tol() const { return tol_; }
+  const SolveStats &stats() const { return stats_; }
+  float last_solve_ms() const { return last_ms_; }
+  int sync();
+
+  // kernel timing of the dominant pair kernels (CUDA events on the stream,
+  // resolved lazily so that timing adds no synchronisation)
+  void enable_kernel_timing(bool on) { ktime_on_ = on; }
+  void kernel_stats(int which, long long &launches, double &ms);
+  void reset_kernel_stats();
+  // stream-ordered event timers (slots 0..7) and an L2 flush on the stream
+  int timer_record(int slot);
+  int timer_elapsed(int a, int b, double &ms);
+  int flush_l2(size_t bytes);
+
+  const HostModel &model() const { return m_; }
+  double *ipd_host() { return ipd_h_.data(); }
+  double *cpol_host() { return cpol_h_.data(); }
+  int *polar_mm_host() { return polar_mm_h_.data(); }
+  double *cmm_host() { return m_.cmm.data(); }
+  double *q_host() { return m_.q.data(); }
+  cudaStream_t stream() const { return st_; }
+  const gpu::DevSites &dev() const { return d_; }
+
+ private:
+  System() = default;
+  int upload_static();
+  int upload_geometry();
+  int ensure_m2d();
+  int ensure_tmat();
+  int polarization(const double *e_dev, int solver, int matv, const bool *mask);
+  int matvec64(int matv, int ncol, const double *x, double *y, bool dodiag);
+  int cg64(int matv, int ncol, const double *rhs, double *x, int set0);
+  int diis64(int matv, const double *rhs, double *x, int set);
+  int inversion64(const double *rhs, double *x);
+  int mixed_ir(int ncol, const double *rhs, double *x, int set0, bool have_guess);
+  int pcg32(int ncol, double *rms0_out, int max_it, double eta);
+  int check(cudaError_t e, const char *what);
+  int fetch_ipd();
+
+  HostModel m_;
+  ScaledPairs m2d_pairs_, d2d_pairs_;
+  gpu::DevSites d_;
+  cudaStream_t st_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  // solver state
+  int def_solver_ = kSolverCG, def_matv_ = kMatvDirect;
+  int precision_ = kPrecFP64;
+  double tol_ = 1e-8;
+  int maxiter_ = 200;
+  int diis_max_ = 20;
+  bool m2d_done_ = false, ipd_done_ = false, ipd_use_guess_ = false;
+  // device buffers
+  double *e_m2d_ = nullptr;   // [n_ipd][n][3]
+  double *ipd_ = nullptr;     // [n_ipd][n][3]
+  double *rhs_ = nullptr;     // [2][n][3] right-hand sides of the solve
+  double *ext_ = nullptr;     // [n][3] staging of a host external field
+  double *x_ = nullptr, *r_ = nullptr, *p_ = nullptr, *h_ = nullptr, *z_ = nullptr;  // [2][n][3]
+  float *x32_ = nullptr, *r32_ = nullptr, *p32_ = nullptr, *h32_ = nullptr, *z32_ = nullptr;
+  float *alpha32_ = nullptr;
+  double *scratch_ = nullptr;  // pair-kernel split partials
+  size_t scratch_n_ = 0;
+  float *scratch32_ = nullptr;
+  double *partial_ = nullptr;  // reduction partials [kRedBlocks][8]
+  double *dots_ = nullptr;     // [8]
+  double *hist_ = nullptr;     // [2][maxhist]
+  gpu::CgCol *cols_ = nullptr;
+  gpu::CgCol *cols_h_ = nullptr;  // pinned
+  double *scal_h_ = nullptr;      // pinned scalars
+  int *flag_ = nullptr;
+  double *tmat_ = nullptr;
+  int *piv_ = nullptr;
+  int *info_ = nullptr;
+  bool tmat_ok_ = false, lu_ok_ = false;
+  double *diis_x_ = nullptr, *diis_e_ = nullptr;
+  int nsplit_m2d_ = 1, nsplit_tmu_ = 1, nsplit_tmu32_ = 1;
+  int maxhist_ = 1024;
+  // host mirrors
+  std::vector<double> ipd_h_, cpol_h_;
+  std::vector<int> polar_mm_h_;
+  SolveStats stats_;
+  float last_ms_ = 0.f;
+  bool ktime_on_ = false;
+  long long klaunch_[2] = {0, 0};
+  double kms_[2] = {0, 0};
+  struct KEv {
+    cudaEvent_t a, b;
+    int kind;
+  };
+  std::vector<KEv> kpending_, kfree_;
+  KEv kt_begin(int kind);
+  void kt_end(KEv &e);
+  void kt_resolve();
+  cudaEvent_t tev_[8] = {};
+  void *flush_buf_ = nullptr;
+  size_t flush_bytes_ = 0;
+  unsigned flush_tag_ = 0;
+};
+
+// process-wide error text of the last failing call
+void set_last_error(const std::string &s);
+const char *last_error();
+
+}  // namespace ommp

@@ -1,0 +1,144 @@
+// Launch interface of the GB300 kernels (implemented in kernels.cu).
+//
+// Layout conventions (device memory, all 0-based):
+//   site arrays are structure-of-arrays or packed Pos64 (x, y, z, w);
+//   field / dipole vectors are [nrhs][n][3] contiguous (C order), the same
+//   as the reference's Fortran (3, n, n_ipd) arrays seen from C.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace ommp {
+namespace gpu {
+
+// One site: position and a per-site scalar, 32-byte aligned so that a tile
+// load is two 16-byte transactions per thread.
+struct __align__(32) Pos64 {
+  double x, y, z, w;
+};
+
+// Immutable per-geometry device data of one system.
+struct DevSites {
+  int n = 0;      // polarizable sites
+  int m = 0;      // MM (static) sites
+  bool amoeba = false;
+  // polarizable sites
+  Pos64 *pol_pos = nullptr;   // x, y, z, 1/thole
+  double *pol_a = nullptr;      // Thole damping a
+  double *pol_alpha = nullptr;  // polarizability
+  int *polar_mm = nullptr;      // mm index of each polarizable site
+  float4 *pol_pos32 = nullptr;  // centred FP32 copy: x, y, z, 1/thole
+  float *pol_a32 = nullptr;
+  // static sites
+  Pos64 *mm_pos = nullptr;    // x, y, z, thole (0 when not polarizable)
+  double *mm_a = nullptr;       // damping a of the source (AMOEBA)
+  double *mm_q = nullptr;       // [m][ld] lab-frame multipoles
+  int ld = 1;
+  // scaled pairs, target-major
+  int *m2d_ri = nullptr, *m2d_src = nullptr;
+  double *m2d_sP = nullptr, *m2d_sD = nullptr;
+  int m2d_nnz = 0;
+  int *d2d_ri = nullptr, *d2d_src = nullptr;
+  double *d2d_s = nullptr;
+  int d2d_nnz = 0;
+  double damp_thr = 50.0;       // AMOEBA: damping applied when a u^3 < 50
+};
+
+// ---- pair kernels ---------------------------------------------------------
+// Permanent-multipole field at the polarizable sites (E_M2D), n_ipd sets:
+// out [n_ipd][n][3]; scratch holds split partials (m2d_scratch_doubles()).
+size_t m2d_scratch_doubles(const DevSites &s, int nsplit);
+int m2d_pick_split(const DevSites &s, int sm_count);
+void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag,
+                cudaStream_t st);
+
+// y = T x (dodiag) or y = -E_dd(x) (no diagonal); x,y [nrhs][n][3], FP64.
+size_t tmu_scratch_doubles(const DevSites &s, int nrhs, int nsplit);
+int tmu_pick_split(const DevSites &s, int nrhs, int sm_count, bool fp32);
+void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag,
+                    double *scratch, int nsplit, cudaStream_t st);
+// FP32 inner operator with compensated cross-tile sums; x,y float.
+void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch,
+                    int nsplit, cudaStream_t st);
+
+// ---- dense T (incore matvec / inversion) ---------------------------------
+void launch_build_tmat(const DevSites &s, double *tmat, cudaStream_t st);  // [3n][3n] col-major
+void launch_gemv(int nn, const double *A, const double *x, double *y, bool dodiag,
+                 const double *alpha, int nrhs, cudaStream_t st);
+// LU with partial pivoting in place (column major); info (device int) 0 = ok.
+void launch_lu_factor(int nn, double *A, int *piv, int *info, double *work, cudaStream_t st);
+void launch_lu_solve(int nn, const double *A, const int *piv, double *b, cudaStream_t st);
+
+// ---- BLAS-1 and reductions (deterministic) --------------------------------
+constexpr int kRedBlocks = 456;  // 3 x 152 SMs
+constexpr int kRedThreads = 256;
+// partial[b][k] for k < ncol: sum over i of a[k*n+i]*b[k*n+i]
+void launch_dots(int ncol, size_t n, const double *a, const double *b, double *partial,
+                 cudaStream_t st);
+// partial[b][k] = sum_i a[k*n+i] * v[i]  (one vector against ncol columns)
+void launch_dots_bcast(int ncol, size_t n, const double *a, const double *v, double *partial,
+                       cudaStream_t st);
+void launch_dots_f32(int ncol, size_t n, const float *a, const float *b, double *partial,
+                     cudaStream_t st);
+// result[k] = sum_b partial[b][k]  (fixed order)
+void launch_reduce_partials(int ncol, const double *partial, double *result, cudaStream_t st);
+
+// misc elementwise
+void launch_axpby(size_t n, double a, const double *x, double b, double *y, cudaStream_t st);
+void launch_add(size_t n, const double *a, const double *b, double *out, cudaStream_t st);
+void launch_scale_by_alpha(int nrhs, int n, const double *alpha, const double *x, double *y,
+                           cudaStream_t st);
+void launch_to_f32(size_t n, const double *x, const double *scale, float *y, cudaStream_t st);
+
+// Multi-column PCG state kept on the device (one entry per column).
+struct CgCol {
+  double gold, gama, alpha, gnew, rms, beta;
+  int active;     // column still iterating
+  int quick;      // left through |p.Tp| < eps
+  int converged;  // rms < tol
+  int iters;
+};
+// gama_k = (h.p)_k from reduced dots; alpha = gold/gama; quick-exit flags.
+void launch_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps, cudaStream_t st);
+// x += alpha p; r -= alpha h; z = alpha_pol r; partial r.z per column
+void launch_cg_update(int ncol, int n, double *x, double *r, const double *p, const double *h,
+                      double *z, const double *alpha_pol, const CgCol *cols, double *partial,
+                      cudaStream_t st);
+void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double tol, double *hist,
+                    int hist_stride, cudaStream_t st);
+void launch_cg_pupdate(int ncol, int n, double *p, const double *z, const CgCol *cols,
+                       cudaStream_t st);
+// FP32 vectors, FP64 scalars (inner solver of the mixed-precision path)
+void launch_cg_update_f32(int ncol, int n, float *x, float *r, const float *p, const float *h,
+                          float *z, const float *alpha_pol, const CgCol *cols, double *partial,
+                          cudaStream_t st);
+void launch_cg_pupdate_f32(int ncol, int n, float *p, const float *z, const CgCol *cols,
+                           cudaStream_t st);
+// mu[k] += scale[k] * dmu32[k]  (IR correction, FP64 accumulate)
+void launch_ir_accumulate(int ncol, int n, double *mu, const float *d32, const double *scale,
+                          cudaStream_t st);
+// r = rhs - Tmu (all columns), into r; and r32 = r / scale
+void launch_residual(size_t total, const double *rhs, const double *tmu, double *r,
+                     cudaStream_t st);
+// DIIS: x_new = sum_i c_i X[:, i]
+void launch_lincomb(int nvec, size_t n, const double *X, size_t ldx, const double *c, double *out,
+                    cudaStream_t st);
+// rms and max of (a - b): out[0] = sum sq, out[1] = max abs (per-block partials then reduce)
+void launch_diff_norms(size_t n, const double *a, const double *b, double *partial,
+                       cudaStream_t st);
+void launch_reduce_norms(const double *partial, double *out, cudaStream_t st);
+// NaN / Inf check: flag set to 1 when any entry is not finite
+void launch_check_finite(size_t n, const double *x, int *flag, cudaStream_t st);
+
+// Number of SMs of the current device (cached).
+int sm_count();
+// Kernels launched by this library since load (all streams).
+long long launch_count();
+// FMA-chain kernel for the FP32 / FP64 pipe peak; returns its flop count.
+double launch_fma_peak(bool fp64, int iters, void *out, cudaStream_t st);
+
+}  // namespace gpu
+}  // namespace ommp

@@ -91,6 +91,7 @@ struct orc_sys {
     int maxiter, diis_max;
     double *tmat;  /* [3n][3n] column-major like the reference */
     int last_iters[2];
+    long matvecs; /* T.mu products since the last polarization() call */
     int hist_n[2];
     double hist[2][MAX_HIST];
 };
@@ -148,7 +149,7 @@ static int rd_skip(rdr_t *r, long n) {
 
 /* list-directed read of `want` numbers: continues over records until
  * satisfied, the rest of the last record is discarded.  Fortran 'D'
- * exponents are accepted. */
+ * exponents and r*c repeat counts are accepted. */
 static int rd_values(rdr_t *r, double *out, int want) {
     int got = 0;
     while (got < want) {
@@ -165,10 +166,19 @@ static int rd_values(rdr_t *r, double *out, int want) {
                 tok[k++] = c;
             }
             tok[k] = 0;
+            long rep = 1;
+            char *num = tok;
+            char *star = strchr(tok, '*');
+            if (star) {
+                *star = 0;
+                rep = strtol(tok, NULL, 10);
+                num = star + 1;
+                if (rep <= 0) return 0;
+            }
             char *end;
-            double v = strtod(tok, &end);
-            if (end == tok) return 0;
-            out[got++] = v;
+            double v = strtod(num, &end);
+            if (end == num) return 0;
+            for (long t = 0; t < rep && got < want; t++) out[got++] = v;
         }
     }
     return 1;
@@ -1131,6 +1141,7 @@ static int create_tmat(orc_sys *s) {
 /* TMatVec_otf / TMatVec_incore + TMatVec_diag (mod_polarization.F90:437-504) */
 static int matvec(orc_sys *s, int matv, const double *x, double *y, int dodiag) {
     int np = s->npol, n = 3 * np;
+    s->matvecs++;
     if (matv == MATV_INCORE) {
         int st = create_tmat(s);
         if (st) return st;
@@ -1394,6 +1405,7 @@ static int inversion_solve(orc_sys *s, const double *rhs, double *x) {
 /* polarization (mod_polarization.F90:49-313); e: [n_ipd][npol][3] */
 static int polarization(orc_sys *s, const double *e, int solver, int mv, const int *mask_in) {
     int np = s->npol, n = 3 * np;
+    s->matvecs = 0;
     if (np == 0) return 0;
     if (solver == SOLVER_NONE) solver = s->def_solver;
     if (mv == MATV_NONE) mv = s->def_matv;
@@ -1504,6 +1516,7 @@ double orc_get_polelec_energy(orc_sys *s, int32_t *status) {
 }
 
 int32_t orc_last_iterations(const orc_sys *s, int32_t set) { return s->last_iters[set & 1]; }
+int64_t orc_matvec_count(const orc_sys *s) { return s->matvecs; }
 int32_t orc_residual_history(const orc_sys *s, int32_t set, double *out, int32_t maxn) {
     int k = s->hist_n[set & 1];
     if (k > maxn) k = maxn;

@@ -91,6 +91,8 @@ int orc_set_external_field(orc_sys *s, const double *ext, int32_t solver, int32_
 double orc_get_polelec_energy(orc_sys *s, int32_t *status);
 /* per-set iteration count and residual history of the last solve */
 int32_t orc_last_iterations(const orc_sys *s, int32_t set);
+/* T.mu products evaluated by the last polarization solve */
+int64_t orc_matvec_count(const orc_sys *s);
 int32_t orc_residual_history(const orc_sys *s, int32_t set, double *out, int32_t maxn);
 /* ommp_update_coordinates: c [mm][3] bohr */
 int orc_update_coordinates(orc_sys *s, const double *c);

@@ -62,6 +62,7 @@ def lib():
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
             "orc_last_iterations": (C.c_int32, [vp, C.c_int32]),
+            "orc_matvec_count": (C.c_int64, [vp]),
             "orc_residual_history": (C.c_int32, [vp, C.c_int32, dp, C.c_int32]),
             "orc_update_coordinates": (C.c_int, [vp, dp]),
             "orc_clear_guess": (None, [vp]),
@@ -206,6 +207,9 @@ class OracleSystem:
 
     def last_iterations(self, s=0):
         return lib().orc_last_iterations(self._h, s)
+
+    def matvec_count(self):
+        return int(lib().orc_matvec_count(self._h))
 
     def residual_history(self, s=0):
         o = np.zeros(1024)

@@ -1,0 +1,229 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's golden
+files and against the CPU oracle on the same inputs.
+
+Tolerances:
+* reference goldens: the reference's own (ipd rtol 1e-6 / atol 1e-5, or 1e-3
+  for the FMM-produced 1ubq files; EP rtol 1e-6 / atol 1e-6);
+* E_M2D and T.mu against the oracle: relative 1e-12 (same FP64 formulas,
+  different summation order);
+* FP64 solves against the oracle at the same tolerance: relative 1e-9 in
+  dipoles and energy (the plain-method contract);
+* mixed precision (FP32 inner CG + FP64 refinement) against the FP64 oracle:
+  relative 1e-7 in dipoles and energy.
+Relative error of an array = ||a - b||_2 / ||b||_2.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES
+from openmmpol_gb300 import OMMPSystem, synth
+from oracle.oracle import (MATV_DIRECT, MATV_INCORE, SOLVER_CG, SOLVER_DIIS, SOLVER_INVERSION,
+                           OracleSystem)
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def quiet():
+    from openmmpol_gb300 import set_verbose
+    set_verbose(0)
+
+
+@pytest.fixture(scope="module")
+def w1k(tmp_path_factory):
+    w = synth.water_cluster(1000, seed=1)
+    p = synth.write_mmp(str(tmp_path_factory.mktemp("w1k") / "w1k.mmp"), w)
+    o = OracleSystem(p)
+    cmm = o.cmm
+    ef, _, _ = synth.point_charge_field(cmm[o.polar_mm], w.box_center(), seed=1, all_sites_bohr=cmm)
+    return p, ef
+
+
+@pytest.fixture(scope="module")
+def chains(tmp_path_factory):
+    c = synth.chain_system(n_chains=10, chain_len=40, n_waters=600, seed=2)
+    p = synth.write_mmp(str(tmp_path_factory.mktemp("chains") / "c.mmp"), c)
+    o = OracleSystem(p)
+    cmm = o.cmm
+    ef, _, _ = synth.point_charge_field(cmm[o.polar_mm], c.box_center(), seed=3, all_sites_bohr=cmm)
+    return p, ef
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("with_field", [0, 1])
+def test_gpu_matches_reference_golden(case, with_field, golden, golden_mmp):
+    s = OMMPSystem(golden_mmp[case])
+    ef = golden[case + "_ef1"] if with_field else np.zeros((s.pol_atoms, 3))
+    s.set_external_field(ef)
+    ep = s.get_polelec_energy()
+    atol = float(golden[case + "_atol"])
+    np.testing.assert_allclose(s.ipd.reshape(-1, 3), golden[f"{case}_ipd{with_field}"], rtol=1e-6, atol=atol)
+    key = f"{case}_ep{with_field}"
+    if key in golden.files:
+        np.testing.assert_allclose(ep, float(golden[key]), rtol=1e-6, atol=1e-6 if atol <= 1e-5 else 1e-3)
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "nma_amoeba_cut", "nma_wang", "1crn_amoeba", "1crn_wang",
+                                  "1ao6cut_wang", "1ubq_amoeba"])
+def test_gpu_m2d_field_and_tmatvec_match_oracle(case, golden_mmp):
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    assert g.pol_atoms == o.pol_atoms and g.mm_atoms == o.mm_atoms
+    np.testing.assert_array_equal(g.polar_mm, o.polar_mm)
+    np.testing.assert_allclose(g.q, o.q, rtol=0, atol=1e-14)
+    assert rel(g.e_m2d(), o.e_m2d()) < 1e-12
+    x = np.random.default_rng(7).standard_normal((o.pol_atoms, 3))
+    assert rel(g.tmatvec(x), o.tmatvec(x)) < 1e-12
+    assert rel(g.tmatvec(x, dodiag=False), o.tmatvec(x, dodiag=False)) < 1e-12
+    x2 = np.random.default_rng(8).standard_normal((2, o.pol_atoms, 3))
+    y2 = g.tmatvec(x2)
+    assert rel(y2[1], o.tmatvec(x2[1])) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "nma_wang_cut", "1crn_amoeba", "1crn_wang"])
+@pytest.mark.parametrize("solver", ["cg", "diis", "inversion"])
+def test_gpu_solvers_match_oracle(case, solver, golden, golden_mmp):
+    code = {"cg": SOLVER_CG, "diis": SOLVER_DIIS, "inversion": SOLVER_INVERSION}[solver]
+    ef = golden[case + "_ef1"]
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    for s in (g, o):
+        s.set_solver_tol(1e-10) if s is g else s.set_tol(1e-10)
+    g.set_default_solver(solver)
+    o.set_default_solver(code)
+    g.set_external_field(ef)
+    o.set_external_field(ef)
+    assert rel(g.ipd, o.ipd) < 1e-9
+    assert abs(g.get_polelec_energy() - o.get_polelec_energy()) <= 1e-9 * abs(o.get_polelec_energy())
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "1crn_wang"])
+def test_gpu_incore_matvec_matches_oracle(case, golden, golden_mmp):
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    x = np.random.default_rng(3).standard_normal((o.pol_atoms, 3))
+    assert rel(g.tmatvec(x, matv="incore"), o.tmatvec(x, matv=MATV_INCORE)) < 1e-12
+    # nomm path forwards matv (mod_interface.F90:223-230)
+    ef = golden[case + "_ef1"]
+    g.set_external_field(ef, nomm=True, matv="incore")
+    o.set_external_field(ef, nomm=True, matv=MATV_INCORE)
+    assert rel(g.ipd, o.ipd) < 1e-9
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "1crn_wang"])
+def test_gpu_nomm_solves_set_one_only(case, golden, golden_mmp):
+    ef = golden[case + "_ef1"]
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    g.set_external_field(ef, nomm=True)
+    o.set_external_field(ef, nomm=True)
+    assert rel(g.ipd, o.ipd) < 1e-9
+    if g.n_ipd == 2:
+        assert np.all(g.ipd[1] == 0)
+
+
+def test_gpu_warm_start_and_update_coordinates(golden, golden_mmp):
+    case = "1crn_amoeba"
+    ef = golden[case + "_ef1"]
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    g.set_external_field(ef)
+    o.set_external_field(ef)
+    # second solve starts from the previous dipoles (ipd_use_guess)
+    ef2 = ef * 1.01
+    g.set_external_field(ef2)
+    o.set_external_field(ef2)
+    assert rel(g.ipd, o.ipd) < 1e-9
+    assert abs(g.iterations(0) - o.last_iterations(0)) <= 1
+    # new geometry: M2D and the guess are recomputed / dropped
+    c = o.cmm + np.random.default_rng(1).normal(0, 0.02, o.cmm.shape)
+    g.update_coordinates(c)
+    o.update_coordinates(c)
+    np.testing.assert_allclose(g.q, o.q, rtol=0, atol=1e-13)
+    g.set_external_field(ef)
+    o.set_external_field(ef)
+    assert rel(g.ipd, o.ipd) < 1e-9
+    assert abs(g.get_polelec_energy() - o.get_polelec_energy()) <= 1e-9 * abs(o.get_polelec_energy())
+
+
+def test_w1k_fp64_parity_and_energy(w1k):
+    p, ef = w1k
+    g = OMMPSystem(p)
+    o = OracleSystem(p)
+    g.set_solver_tol(1e-10)
+    o.set_tol(1e-10)
+    g.set_external_field(ef)
+    o.set_external_field(ef)
+    assert rel(g.ipd, o.ipd) < 1e-9
+    eg, eo = g.get_polelec_energy(), o.get_polelec_energy()
+    assert abs(eg - eo) <= 1e-9 * abs(eo)
+    assert abs(g.iterations(0) - o.last_iterations(0)) <= 1
+    hg, ho = g.residual_history(0), o.residual_history(0)
+    m = min(len(hg), len(ho))
+    np.testing.assert_allclose(hg[:m], ho[:m], rtol=1e-6)
+    # the GPU skips only the product with the all-zero first guess
+    assert abs(g.counter(0) + 1 - o.matvec_count()) <= 2
+
+
+def test_w1k_mixed_precision_within_1e7(w1k):
+    p, ef = w1k
+    g = OMMPSystem(p)
+    o = OracleSystem(p)
+    g.set_solver_tol(1e-10)
+    o.set_tol(1e-10)
+    g.set_precision("mixed")
+    g.set_external_field(ef)
+    o.set_external_field(ef)
+    assert rel(g.ipd, o.ipd) < 1e-7
+    eg, eo = g.get_polelec_energy(), o.get_polelec_energy()
+    assert abs(eg - eo) <= 1e-7 * abs(eo)
+    assert g.counter(2) >= 1 and g.counter(1) > 0  # refinement steps, FP32 products
+    hist = g.residual_history(0)
+    assert hist[-1] < 1e-10
+
+
+def test_fp32_operator_accuracy(w1k):
+    p, _ = w1k
+    g = OMMPSystem(p)
+    x = np.random.default_rng(2).standard_normal((g.pol_atoms, 3)) * 0.05
+    y64 = g.tmatvec(x)
+    y32 = g.tmatvec_fp32(x)
+    assert rel(y32, y64) < 1e-5
+
+
+def test_chain_system_wang_exclusions(chains):
+    p, ef = chains
+    g = OMMPSystem(p)
+    o = OracleSystem(p)
+    assert rel(g.e_m2d(), o.e_m2d()) < 1e-12
+    x = np.random.default_rng(4).standard_normal((o.pol_atoms, 3))
+    assert rel(g.tmatvec(x), o.tmatvec(x)) < 1e-12
+    g.set_solver_tol(1e-10)
+    o.set_tol(1e-10)
+    g.set_external_field(ef)
+    o.set_external_field(ef)
+    assert rel(g.ipd, o.ipd) < 1e-9
+    ref = o.ipd
+    g.clear_guess()
+    g.set_precision("mixed")
+    g.set_external_field(ef)
+    assert rel(g.ipd, ref) < 1e-7
+
+
+def test_solver_not_converged_reports_status(golden, golden_mmp):
+    from openmmpol_gb300 import OMMPError
+    g = OMMPSystem(golden_mmp["1crn_amoeba"])
+    g.set_solver_maxiter(2)
+    with pytest.raises(OMMPError) as e:
+        g.set_external_field(golden["1crn_amoeba_ef1"])
+    assert e.value.status == 2
+    # the system stays usable
+    g.set_solver_maxiter(200)
+    g.set_external_field(golden["1crn_amoeba_ef1"])
+    np.testing.assert_allclose(g.ipd.reshape(-1, 3), golden["1crn_amoeba_ipd1"], rtol=1e-6, atol=1e-5)

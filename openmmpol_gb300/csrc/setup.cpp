@@ -347,7 +347,10 @@ bool rotate_multipoles(HostModel &m, std::string &err) {
 }
 
 bool prepare_model(HostModel &m, std::string &err) {
-  distance_layers(m.conn[0], 4, m.conn);
+  {
+    const Csr adj = m.conn[0];  // the layers overwrite conn[0]: read from a copy
+    distance_layers(adj, 4, m.conn);
+  }
   // remove_null_pol: |alpha| <= 100 eps is dropped
   {
     std::vector<double> pol;

@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="w30k", choices=["w30k", "w1k"])
+    ap.add_argument("--config", default="w30k", choices=["w30k", "w10k", "w1k"])
+    ap.add_argument("--skip-cpu", action="store_true", help="leave out the CPU baseline (profiling runs)")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
     ap.add_argument("--no-fp64", action="store_true")
@@ -67,7 +68,7 @@ def dist_env():
 
 def workload(cfg, cache):
     from openmmpol_gb300 import synth
-    nw = {"w30k": 30000, "w1k": 1000}[cfg]
+    nw = {"w30k": 30000, "w10k": 10000, "w1k": 1000}[cfg]
     os.makedirs(cache, exist_ok=True)
     path = os.path.join(cache, f"water_{nw}_seed1.mmp")
     w = synth.water_cluster(nw, seed=1)
@@ -344,7 +345,10 @@ def run_gb300(args):
             "gpu_launches": int(launches), "wall_s_timed": wall, "m2d_first_solve_s": m2d_s,
             "steps_ms": step_ms, "solver_counters_per_step": counters, "kernels": kstats,
             "roofline": roof, "clocks": clocks, "fp64": fp64}
-    if rank == 0:
+    if rank == 0 and args.skip_cpu:
+        line["cpu_baseline"] = {"value": None, "skipped": "--skip-cpu"}
+        print(json.dumps(line), flush=True)
+    elif rank == 0:
         # CPU baseline on the host cores (oracle port, bounded sample)
         try:
             cores = os.cpu_count() or 1

@@ -29,6 +29,18 @@ def rel(a, b):
     return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
 
 
+def converged_reference(path, ef):
+    """Oracle solution converged far below the comparison threshold: Jacobi/DIIS
+    to a 1e-12 max increment.  The reference CG leaves its loop as converged
+    once |p.Tp| < 100*eps (mod_solvers.F90:177-181), which for small systems is
+    long before a 1e-10 residual, so it is not an accuracy reference."""
+    o = OracleSystem(path)
+    o.set_tol(1e-12)
+    o.set_default_solver(SOLVER_DIIS)
+    o.set_external_field(ef)
+    return o
+
+
 @pytest.fixture(scope="module", autouse=True)
 def quiet():
     from openmmpol_gb300 import set_verbose
@@ -93,8 +105,10 @@ def test_gpu_solvers_match_oracle(case, solver, golden, golden_mmp):
     ef = golden[case + "_ef1"]
     g = OMMPSystem(golden_mmp[case])
     o = OracleSystem(golden_mmp[case])
-    for s in (g, o):
-        s.set_solver_tol(1e-10) if s is g else s.set_tol(1e-10)
+    # tight tolerance: DIIS stops on its increment, so runs that differ by
+    # rounding stop a tolerance apart
+    g.set_solver_tol(1e-12)
+    o.set_tol(1e-12)
     g.set_default_solver(solver)
     o.set_default_solver(code)
     g.set_external_field(ef)
@@ -174,12 +188,10 @@ def test_w1k_fp64_parity_and_energy(w1k):
 def test_w1k_mixed_precision_within_1e7(w1k):
     p, ef = w1k
     g = OMMPSystem(p)
-    o = OracleSystem(p)
+    o = converged_reference(p, ef)
     g.set_solver_tol(1e-10)
-    o.set_tol(1e-10)
     g.set_precision("mixed")
     g.set_external_field(ef)
-    o.set_external_field(ef)
     assert rel(g.ipd, o.ipd) < 1e-7
     eg, eo = g.get_polelec_energy(), o.get_polelec_energy()
     assert abs(eg - eo) <= 1e-7 * abs(eo)
@@ -209,7 +221,7 @@ def test_chain_system_wang_exclusions(chains):
     g.set_external_field(ef)
     o.set_external_field(ef)
     assert rel(g.ipd, o.ipd) < 1e-9
-    ref = o.ipd
+    ref = converged_reference(p, ef).ipd
     g.clear_guess()
     g.set_precision("mixed")
     g.set_external_field(ef)

@@ -188,6 +188,7 @@ int64_t ommp_gpu_kernel_launch_count(void);
 int32_t ommp_gpu_device_alloc(int64_t bytes, void **ptr);
 int32_t ommp_gpu_device_free(void *ptr);
 int32_t ommp_gpu_copy_to_device(void *dst, const void *src, int64_t bytes);
+int32_t ommp_gpu_copy_to_host(void *dst, const void *src, int64_t bytes);
 /* measured FMA throughput of the FP64 (fp64 = 1) or FP32 pipe, TFLOP/s */
 int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops);
 /* SM count of the current device, 0 without a GPU */

@@ -195,6 +195,14 @@ int32_t ommp_gpu_copy_to_device(void *dst, const void *src, int64_t bytes) {
   }
   return ommp::kOk;
 }
+int32_t ommp_gpu_copy_to_host(void *dst, const void *src, int64_t bytes) {
+  cudaError_t e = cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    ommp::set_last_error(std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    return ommp::kErrCuda;
+  }
+  return ommp::kOk;
+}
 int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops) {
   *tflops = 0.0;
   void *out = nullptr;

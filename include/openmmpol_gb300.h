@@ -194,6 +194,19 @@ int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops);
 /* SM count of the current device, 0 without a GPU */
 int32_t ommp_gpu_device_sm_count(void);
 
+/* No counterpart in the reference.  y = T x (dodiag = 1) or y = -E_dd(x)
+ * (dodiag = 0) for nrhs (1|2) columns [nrhs][pol_atoms][3], with x and y in
+ * caller-owned DEVICE memory, and no memory allocation inside the call: for
+ * hosts that manage all GPU memory themselves (a QM code's SCF loop with its
+ * own memory pool, an MD step that must not stall on cudaMalloc).  Scratch is
+ * a 16 MiB static device array, so pol_atoms * nrhs <= 699050; larger sizes
+ * are rejected with OMMP_GPU_ERR_BAD_ARG.  The first call on each device
+ * looks the array up (cudaGetSymbolAddress): make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race.  The
+ * call returns after its kernels have finished. */
+int32_t ommp_gpu_tmatvec_noalloc(OMMP_SYSTEM_PRT s, const double *x_dev, double *y_dev, int32_t nrhs,
+                                 int32_t dodiag);
+
 #ifdef __cplusplus
 }
 #endif

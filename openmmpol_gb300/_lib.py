@@ -79,6 +79,7 @@ SIGNATURES = {
     "ommp_gpu_copy_to_host": (C.c_int32, [_vp, _vp, C.c_int64]),
     "ommp_gpu_measure_pipe_peak": (C.c_int32, [C.c_int32, _dp]),
     "ommp_gpu_device_sm_count": (C.c_int32, []),
+    "ommp_gpu_tmatvec_noalloc": (C.c_int32, [_vp, _vp, _vp, C.c_int32, C.c_int32]),
 }
 
 _lib = None

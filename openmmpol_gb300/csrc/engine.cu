@@ -45,7 +45,8 @@ int System::check(cudaError_t e, const char *what) {
 
 System::~System() {
   if (st_) cudaStreamSynchronize(st_);
-  void *bufs[] = {d_.pol_pos, d_.pol_a, d_.pol_alpha, d_.polar_mm, d_.pol_pos32, d_.pol_a32, d_.mm_pos,
+  void *bufs[] = {d_.pol_pos, d_.pol_a, d_.pol_alpha, d_.polar_mm, d_.pol_pos32, d_.pol_a32, d_.pol_wa32,
+                  d_.mm_wa32, d_.mm_pos,
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
                   alpha32_, scratch_, scratch32_, partial_, dots_, hist_, cols_, flag_, tmat_, piv_,
@@ -109,6 +110,7 @@ int System::upload_static() {
   int bad = 0;
   bad |= dalloc(d_.pol_pos, n) | dalloc(d_.pol_a, n) | dalloc(d_.pol_alpha, n) | dalloc(d_.polar_mm, n);
   bad |= dalloc(d_.pol_pos32, n) | dalloc(d_.pol_a32, n) | dalloc(alpha32_, n);
+  bad |= dalloc(d_.pol_wa32, n) | dalloc(d_.mm_wa32, mm);
   bad |= dalloc(d_.mm_pos, mm) | dalloc(d_.mm_a, mm) | dalloc(d_.mm_q, (size_t)mm * m.ld_cart);
   bad |= dalloc(d_.m2d_ri, n + 1) | dalloc(d_.m2d_src, m2d_pairs_.src.size()) |
          dalloc(d_.m2d_sP, m2d_pairs_.src.size()) | dalloc(d_.m2d_sD, m2d_pairs_.src.size());
@@ -150,6 +152,21 @@ int System::upload_static() {
   up(alpha32_, alpha32.data(), n * sizeof(float));
   up(d_.pol_a32, a32.data(), n * sizeof(float));
   up(d_.polar_mm, m.polar_mm.data(), n * sizeof(int));
+  // FP32 damping pre-test data: (1/thole)^2 and a^2 (inf / 0 for static sites)
+  std::vector<float2> pwa(n), mwa(mm);
+  for (int j = 0; j < n; ++j) {
+    double w = 1.0 / m.thole[m.polar_mm[j]];
+    pwa[j] = make_float2((float)(w * w), (float)(m.damping[j] * m.damping[j]));
+  }
+  for (int i = 0; i < mm; ++i) {
+    int p = m.mm_polar[i];
+    double w = m.thole[i] > 0.0 ? 1.0 / m.thole[i] : std::numeric_limits<double>::infinity();
+    double a = p >= 0 ? m.damping[p] : 0.0;
+    mwa[i] = make_float2((float)(w * w), (float)(a * a));
+  }
+  up(d_.pol_wa32, pwa.data(), n * sizeof(float2));
+  up(d_.mm_wa32, mwa.data(), mm * sizeof(float2));
+  cudaStreamSynchronize(st_);  // pwa / mwa are host temporaries
   cudaMemsetAsync(ipd_, 0, nv * nipd * sizeof(double), st_);
   cudaMemsetAsync(e_m2d_, 0, nv * nipd * sizeof(double), st_);
   ipd_h_.assign(nv * nipd, 0.0);
@@ -757,12 +774,34 @@ int System::polarization(const double *e, int solver, int matv, const bool *mask
   if (solver == kSolverCG || solver == kSolverDIIS) {
     bool mixed = solver == kSolverCG && precision_ == kPrecMixed && matv == kMatvDirect;
     if (mixed) {
-      // both AMOEBA sets share every pair evaluation
-      if (nipd == 2 && mask[0] && mask[1])
-        st = mixed_ir(2, e, x_, 0, ipd_use_guess_);
-      else
+      if (nipd == 2 && mask[0] && mask[1]) {
+        // Identical D and P systems (right-hand sides and starting guesses
+        // equal bit for bit, as for AMOEBA water where both fields exclude
+        // the whole molecule) have identical solutions: the reference's P
+        // solve seeded with the D dipoles returns them unchanged
+        // (mod_polarization.F90:237-243).  Solve once and copy.
+        cudaMemsetAsync(flag_, 0, sizeof(int), st_);
+        gpu::launch_any_diff(nv, e, e + nv, flag_, st_);
+        if (ipd_use_guess_) gpu::launch_any_diff(nv, x_, x_ + nv, flag_, st_);
+        int differ = 1;
+        cudaMemcpyAsync(&differ, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        st = check(cudaStreamSynchronize(st_), "D/P comparison");
+        if (st) return st;
+        if (differ) {
+          // both sets share every pair evaluation
+          st = mixed_ir(2, e, x_, 0, ipd_use_guess_);
+        } else {
+          st = mixed_ir(1, e, x_, 0, ipd_use_guess_);
+          if (!st) {
+            cudaMemcpyAsync(x_ + nv, x_, nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
+            stats_.hist[1] = stats_.hist[0];
+            stats_.iters[1] = stats_.iters[0];
+          }
+        }
+      } else {
         for (int k = 0; k < nipd && !st; ++k)
           if (mask[k]) st = mixed_ir(1, e + k * nv, x_ + k * nv, k, ipd_use_guess_);
+      }
     } else {
       auto run = [&](int k) {
         return solver == kSolverCG ? cg64(matv, 1, e + k * nv, x_ + k * nv, k) : diis64(matv, e + k * nv, x_ + k * nv, k);

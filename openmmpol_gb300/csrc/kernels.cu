@@ -22,6 +22,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 #include "kernels.h"
 
@@ -32,33 +33,54 @@ namespace {
 constexpr int TPB = 128;   // targets per CTA
 constexpr int TILE = 128;  // sources per shared-memory tile
 
-__device__ __forceinline__ double rsqrt_f64(double x) { return rsqrt(x); }
+// 1/sqrt(r2) in FP64 from the FP32 hardware estimate and one Newton-Raphson
+// step y <- y + y (1 - r2 y^2) / 2 (quadratic convergence: the ~2^-23
+// relative error of the seed becomes ~2e-14).  GB300 runs FP64 at 1/64 of
+// the FP32 rate, so the seed and the conversions cost less than a full-
+// precision FP64 reciprocal square root.
+__device__ __forceinline__ double rinv_f64(double r2, float r2f) {
+  double y = (double)rsqrtf(r2f);
+  double e = fma(-r2, y * y, 1.0);
+  return fma(0.5 * y, e, y);
+}
 
-// Scaled-pair correction helpers evaluate one pair exactly like the
-// all-pairs kernels do.
-struct M2DPair {
-  double e[3];
-};
+// Damping pre-test in FP32 for the FP64 kernels.  AMOEBA damps when
+// a u^3 < thr with u = r / (thole_t thole_s); squared: a^2 q^3 < thr^2 with
+// q = r^2 (1/thole_t)^2 (1/thole_s)^2.  The FP32 test carries a relative
+// margin of 1e-5 (FP32 rounding of q is ~1e-7), so every pair that the exact
+// FP64 test damps enters the branch, where the FP64 test decides.
+__device__ __forceinline__ bool maybe_damped_amoeba(float r2f, float2 wat, float2 was, float thr2m) {
+  float q = r2f * wat.x * was.x;
+  return fminf(wat.y, was.y) * (q * q * q) < thr2m;
+}
+// Wang-AL damps when r < thole_t thole_s, i.e. q < 1.
+__device__ __forceinline__ bool maybe_damped_wang(float r2f, float2 wat, float2 was) {
+  return r2f * wat.x * was.x < 1.00001f;
+}
 
 // Field at target (position pt, 1/thole wt, damping at) of source s.
 template <bool AMOEBA>
 __device__ __forceinline__ void m2d_pair_f64(double dx, double dy, double dz, double wt, double ws,
-                                             double at, double as, const double *q, double thr,
+                                             double at, double as, float2 wat, float2 was,
+                                             const double *q, double thr, float thr2m,
                                              double &ex, double &ey, double &ez) {
   double r2 = dx * dx + dy * dy + dz * dz;
-  double rinv = rsqrt_f64(r2);
+  float r2f = (float)r2;
+  double rinv = rinv_f64(r2, r2f);
   double ir2 = rinv * rinv;
   double k3 = rinv * ir2;
-  double u = r2 * rinv * (wt * ws);  // r / (thole_t thole_s); inf if one is not polarizable
   if (AMOEBA) {
     double k5 = k3 * ir2;
     double k7 = k5 * ir2;
-    double au3 = fmin(at, as) * u * u * u;
-    if (au3 < thr) {
-      double e = exp(-au3);
-      k3 *= 1.0 - e;
-      k5 *= 1.0 - (1.0 + au3) * e;
-      k7 *= 1.0 - (1.0 + au3 + 0.6 * au3 * au3) * e;
+    if (maybe_damped_amoeba(r2f, wat, was, thr2m)) {
+      double u = r2 * rinv * (wt * ws);  // r / (thole_t thole_s)
+      double au3 = fmin(at, as) * u * u * u;
+      if (au3 < thr) {
+        double e = exp(-au3);
+        k3 *= 1.0 - e;
+        k5 *= 1.0 - (1.0 + au3) * e;
+        k7 *= 1.0 - (1.0 + au3 + 0.6 * au3 * au3) * e;
+      }
     }
     double mdr = q[1] * dx + q[2] * dy + q[3] * dz;
     double qx = q[4] * dx + q[5] * dy + q[7] * dz;
@@ -71,9 +93,12 @@ __device__ __forceinline__ void m2d_pair_f64(double dx, double dy, double dz, do
     ey += c * dy - q[2] * k3 - k5x6 * qy;
     ez += c * dz - q[3] * k3 - k5x6 * qz;
   } else {
-    if (u < 1.0) {
-      double u3 = u * u * u;
-      k3 *= 4.0 * u3 - 3.0 * u3 * u;
+    if (maybe_damped_wang(r2f, wat, was)) {
+      double u = r2 * rinv * (wt * ws);
+      if (u < 1.0) {
+        double u3 = u * u * u;
+        k3 *= 4.0 * u3 - 3.0 * u3 * u;
+      }
     }
     double c = q[0] * k3;
     ex += c * dx;
@@ -89,11 +114,14 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
                                                       const Pos64 *__restrict__ mm_pos,
                                                       const double *__restrict__ mm_a,
                                                       const double *__restrict__ mm_q, int ld,
+                                                      const float2 *__restrict__ pol_wa,
+                                                      const float2 *__restrict__ mm_wa,
                                                       double *__restrict__ partial, int per_split,
-                                                      double thr, int *err_flag) {
+                                                      double thr, float thr2m, int *err_flag) {
   constexpr int LD = AMOEBA ? 10 : 1;
   __shared__ Pos64 s_pos[TILE];
   __shared__ double s_a[TILE];
+  __shared__ float2 s_wa[TILE];
   __shared__ double s_q[TILE * LD];
   const int j = blockIdx.x * TPB + threadIdx.x;
   const bool valid = j < n;
@@ -101,6 +129,7 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
   // the target's own mm index and its thole (pol_pos stores 1/thole)
   const int tm = valid ? polar_mm[j] : -1;
   const double at = valid && AMOEBA ? pol_a[j] : 0.0;
+  const float2 wat = valid ? pol_wa[j] : make_float2(0.f, 0.f);
   double ex = 0, ey = 0, ez = 0;
   int bad = 0;
   const int s0 = blockIdx.y * per_split;
@@ -112,6 +141,7 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
       if (i < s1) {
         s_pos[k] = mm_pos[i];
         s_a[k] = AMOEBA ? mm_a[i] : 0.0;
+        s_wa[k] = mm_wa[i];
       }
     }
     for (int k = threadIdx.x; k < TILE * LD; k += TPB) {
@@ -131,7 +161,8 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
         bad = 1;
         continue;
       }
-      m2d_pair_f64<AMOEBA>(dx, dy, dz, pt.w, ps.w, at, s_a[k], &s_q[k * LD], thr, ex, ey, ez);
+      m2d_pair_f64<AMOEBA>(dx, dy, dz, pt.w, ps.w, at, s_a[k], wat, s_wa[k], &s_q[k * LD], thr, thr2m, ex,
+                           ey, ez);
     }
   }
   if (bad) atomicOr(err_flag, 1);
@@ -149,9 +180,11 @@ template <bool AMOEBA>
 __global__ void k_m2d_finish(int n, int nsplit, const double *__restrict__ partial,
                              const Pos64 *__restrict__ pol_pos, const double *__restrict__ pol_a,
                              const Pos64 *__restrict__ mm_pos, const double *__restrict__ mm_a,
-                             const double *__restrict__ mm_q, const int *__restrict__ ri,
+                             const double *__restrict__ mm_q, const float2 *__restrict__ pol_wa,
+                             const float2 *__restrict__ mm_wa, const int *__restrict__ ri,
                              const int *__restrict__ src, const double *__restrict__ sP,
-                             const double *__restrict__ sD, double thr, double *__restrict__ out) {
+                             const double *__restrict__ sD, double thr, float thr2m,
+                             double *__restrict__ out) {
   constexpr int LD = AMOEBA ? 10 : 1;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
@@ -161,6 +194,7 @@ __global__ void k_m2d_finish(int n, int nsplit, const double *__restrict__ parti
   double eP[3] = {e[0], e[1], e[2]}, eD[3] = {e[0], e[1], e[2]};
   Pos64 pt = pol_pos[j];
   double at = AMOEBA ? pol_a[j] : 0.0;
+  float2 wat = pol_wa[j];
   for (int k = ri[j]; k < ri[j + 1]; ++k) {
     int i = src[k];
     Pos64 ps = mm_pos[i];
@@ -168,7 +202,7 @@ __global__ void k_m2d_finish(int n, int nsplit, const double *__restrict__ parti
     for (int c = 0; c < LD; ++c) q[c] = mm_q[(size_t)i * LD + c];
     double fx = 0, fy = 0, fz = 0;
     m2d_pair_f64<AMOEBA>(pt.x - ps.x, pt.y - ps.y, pt.z - ps.z, pt.w, ps.w, at,
-                         AMOEBA ? mm_a[i] : 0.0, q, thr, fx, fy, fz);
+                         AMOEBA ? mm_a[i] : 0.0, wat, mm_wa[i], q, thr, thr2m, fx, fy, fz);
     double cp = sP[k] - 1.0, cd = sD[k] - 1.0;
     eP[0] += cp * fx;
     eP[1] += cp * fy;
@@ -232,14 +266,57 @@ __device__ __forceinline__ void dd_kernel(T r2, T wt, T ws, T at, T as, T thr, T
   k5x3 = T(3) * k5;
 }
 
+// The pair factors in the precision of the kernel.  FP64: reciprocal square
+// root from the FP32 seed plus one Newton step and the FP32 damping
+// pre-test, so that only the arithmetic that needs FP64 runs on GB300's
+// FP64 pipe.  FP32: the plain formulas.
+template <typename T, bool AMOEBA>
+__device__ __forceinline__ void dd_pair(T r2, T wt, T ws, T at, T as, float2 wat, float2 was, T thr,
+                                        float thr2m, T &k3, T &k5x3) {
+  if constexpr (std::is_same<T, double>::value) {
+    float r2f = (float)r2;
+    double rinv = rinv_f64(r2, r2f);
+    double ir2 = rinv * rinv;
+    k3 = rinv * ir2;
+    double k5 = k3 * ir2;
+    if (AMOEBA) {
+      if (maybe_damped_amoeba(r2f, wat, was, thr2m)) {
+        double u = r2 * rinv * (wt * ws);
+        double au3 = fmin(at, as) * u * u * u;
+        if (au3 < thr) {
+          double e = exp(-au3);
+          k3 *= 1.0 - e;
+          k5 *= 1.0 - (1.0 + au3) * e;
+        }
+      }
+    } else {
+      if (maybe_damped_wang(r2f, wat, was)) {
+        double u = r2 * rinv * (wt * ws);
+        if (u < 1.0) {
+          double u3 = u * u * u;
+          double u4 = u3 * u;
+          k3 *= 4.0 * u3 - 3.0 * u4;
+          k5 *= u4;
+        }
+      }
+    }
+    k5x3 = 3.0 * k5;
+  } else {
+    dd_kernel<T, AMOEBA>(r2, wt, ws, at, as, thr, k3, k5x3);
+  }
+}
+
 // partial[split][rhs][j][3] = E_dd(x)_j over the split's source range.
 template <typename T, int NRHS, bool AMOEBA, bool KAHAN>
 __global__ void __launch_bounds__(TPB) k_tmu(int n, const typename Vec4<T>::type *__restrict__ pos,
-                                             const T *__restrict__ damp, const T *__restrict__ x,
-                                             T *__restrict__ partial, int per_split, T thr) {
+                                             const T *__restrict__ damp, const float2 *__restrict__ wa,
+                                             const T *__restrict__ x, T *__restrict__ partial,
+                                             int per_split, T thr, float thr2m) {
   using V4 = typename Vec4<T>::type;
+  constexpr bool F64 = std::is_same<T, double>::value;
   __shared__ V4 s_pos[TILE];
   __shared__ T s_a[TILE];
+  __shared__ float2 s_wa[TILE];
   __shared__ T s_mu[NRHS * 3][TILE];
   const int j = blockIdx.x * TPB + threadIdx.x;
   const bool valid = j < n;
@@ -250,6 +327,7 @@ __global__ void __launch_bounds__(TPB) k_tmu(int n, const typename Vec4<T>::type
     pt.x = pt.y = pt.z = pt.w = T(0);
   }
   const T at = (valid && AMOEBA) ? damp[j] : T(0);
+  const float2 wat = (F64 && valid) ? wa[j] : make_float2(0.f, 0.f);
   T acc[NRHS * 3], sum[NRHS * 3], comp[NRHS * 3];
 #pragma unroll
   for (int c = 0; c < NRHS * 3; ++c) sum[c] = comp[c] = T(0);
@@ -263,6 +341,7 @@ __global__ void __launch_bounds__(TPB) k_tmu(int n, const typename Vec4<T>::type
       if (i < s1) {
         s_pos[k] = pos[i];
         s_a[k] = AMOEBA ? damp[i] : T(0);
+        if (F64) s_wa[k] = wa[i];
 #pragma unroll
         for (int r = 0; r < NRHS; ++r)
 #pragma unroll
@@ -281,7 +360,7 @@ __global__ void __launch_bounds__(TPB) k_tmu(int n, const typename Vec4<T>::type
         T dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
         T r2 = dx * dx + dy * dy + dz * dz;
         T k3, k5x3;
-        dd_kernel<T, AMOEBA>(r2, pt.w, ps.w, at, s_a[k], thr, k3, k5x3);
+        dd_pair<T, AMOEBA>(r2, pt.w, ps.w, at, s_a[k], wat, F64 ? s_wa[k] : wat, thr, thr2m, k3, k5x3);
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
           T mx = s_mu[r * 3 + 0][k], my = s_mu[r * 3 + 1][k], mz = s_mu[r * 3 + 2][k];
@@ -318,10 +397,11 @@ __global__ void __launch_bounds__(TPB) k_tmu(int n, const typename Vec4<T>::type
 template <typename T, bool AMOEBA>
 __global__ void k_tmu_finish(int n, int nrhs, int nsplit, const T *__restrict__ partial,
                              const typename Vec4<T>::type *__restrict__ pos,
-                             const T *__restrict__ damp, const T *__restrict__ x,
-                             const double *__restrict__ alpha, bool dodiag,
+                             const T *__restrict__ damp, const float2 *__restrict__ wa,
+                             const T *__restrict__ x, const double *__restrict__ alpha, bool dodiag,
                              const int *__restrict__ ri, const int *__restrict__ src,
-                             const double *__restrict__ scale, T thr, T *__restrict__ y) {
+                             const double *__restrict__ scale, T thr, float thr2m, T *__restrict__ y) {
+  constexpr bool F64 = std::is_same<T, double>::value;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int r = blockIdx.y;
   if (j >= n) return;
@@ -331,13 +411,15 @@ __global__ void k_tmu_finish(int n, int nrhs, int nsplit, const T *__restrict__ 
   if (ri) {
     auto pt = pos[j];
     T at = AMOEBA ? damp[j] : T(0);
+    float2 wat = F64 ? wa[j] : make_float2(0.f, 0.f);
     for (int k = ri[j]; k < ri[j + 1]; ++k) {
       int i = src[k];
       auto ps = pos[i];
       T dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
       T r2 = dx * dx + dy * dy + dz * dz;
       T k3, k5x3;
-      dd_kernel<T, AMOEBA>(r2, pt.w, ps.w, at, AMOEBA ? damp[i] : T(0), thr, k3, k5x3);
+      dd_pair<T, AMOEBA>(r2, pt.w, ps.w, at, AMOEBA ? damp[i] : T(0), wat, F64 ? wa[i] : wat, thr, thr2m, k3,
+                         k5x3);
       const T *mu = &x[((size_t)r * n + i) * 3];
       T f = k5x3 * (mu[0] * dx + mu[1] * dy + mu[2] * dz);
       double cs = scale[k] - 1.0;
@@ -696,6 +778,16 @@ __global__ void k_reduce_norms(int nb, const double *partial, double *out) {
   }
 }
 
+__global__ void k_any_diff(size_t n, const double *a, const double *b, int *flag) {
+  const unsigned long long *ua = reinterpret_cast<const unsigned long long *>(a);
+  const unsigned long long *ub = reinterpret_cast<const unsigned long long *>(b);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (ua[i] != ub[i]) {
+      *flag = 1;
+      return;
+    }
+}
+
 __global__ void k_check_finite(size_t n, const double *x, int *flag) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     if (!isfinite(x[i])) {
@@ -721,6 +813,11 @@ __global__ void __launch_bounds__(256) k_fma_peak(T *out, int iters, T a, T b) {
   }
   T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
   if (s == T(-1.2345)) out[blockIdx.x] = s;  // keeps the chains alive
+}
+
+// thr^2 with the relative safety margin of the FP32 damping pre-test
+inline float damp_thr2_margin(const DevSites &s) {
+  return (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));
 }
 
 inline int blocks_for(size_t n, int tpb, int cap = 4 * 152 * 4) {
@@ -778,17 +875,21 @@ void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int
   dim3 grid((s.n + TPB - 1) / TPB, nsplit);
   if (s.amoeba)
     k_m2d_allpairs<true><<<grid, TPB, 0, st>>>(s.n, s.m, s.pol_pos, s.pol_a, s.polar_mm, s.mm_pos, s.mm_a,
-                                               s.mm_q, s.ld, scratch, per, s.damp_thr, err_flag);
+                                               s.mm_q, s.ld, s.pol_wa32, s.mm_wa32, scratch, per, s.damp_thr,
+                                               damp_thr2_margin(s), err_flag);
   else
     k_m2d_allpairs<false><<<grid, TPB, 0, st>>>(s.n, s.m, s.pol_pos, s.pol_a, s.polar_mm, s.mm_pos, s.mm_a,
-                                                s.mm_q, s.ld, scratch, per, s.damp_thr, err_flag);
+                                                s.mm_q, s.ld, s.pol_wa32, s.mm_wa32, scratch, per, s.damp_thr,
+                                                damp_thr2_margin(s), err_flag);
   int fb = (s.n + 127) / 128;
   if (s.amoeba)
     k_m2d_finish<true><<<fb, 128, 0, st>>>(s.n, nsplit, scratch, s.pol_pos, s.pol_a, s.mm_pos, s.mm_a, s.mm_q,
-                                           s.m2d_ri, s.m2d_src, s.m2d_sP, s.m2d_sD, s.damp_thr, out);
+                                           s.pol_wa32, s.mm_wa32, s.m2d_ri, s.m2d_src, s.m2d_sP, s.m2d_sD,
+                                           s.damp_thr, damp_thr2_margin(s), out);
   else
     k_m2d_finish<false><<<fb, 128, 0, st>>>(s.n, nsplit, scratch, s.pol_pos, s.pol_a, s.mm_pos, s.mm_a,
-                                            s.mm_q, s.m2d_ri, s.m2d_src, s.m2d_sP, s.m2d_sD, s.damp_thr, out);
+                                            s.mm_q, s.pol_wa32, s.mm_wa32, s.m2d_ri, s.m2d_src, s.m2d_sP,
+                                            s.m2d_sD, s.damp_thr, damp_thr2_margin(s), out);
 }
 
 // ---- T.mu -----------------------------------------------------------------
@@ -816,10 +917,12 @@ static void tmu_allpairs(const DevSites &s, const typename Vec4<T>::type *pos, c
   int per = ((tiles + nsplit - 1) / nsplit) * TILE;
   dim3 grid((s.n + TPB - 1) / TPB, nsplit);
   T thr = (T)s.damp_thr;
+  const float2 *wa = std::is_same<T, double>::value ? s.pol_wa32 : nullptr;
+  float thr2m = damp_thr2_margin(s);
   if (s.amoeba)
-    k_tmu<T, NRHS, true, KAHAN><<<grid, TPB, 0, st>>>(s.n, pos, damp, x, partial, per, thr);
+    k_tmu<T, NRHS, true, KAHAN><<<grid, TPB, 0, st>>>(s.n, pos, damp, wa, x, partial, per, thr, thr2m);
   else
-    k_tmu<T, NRHS, false, KAHAN><<<grid, TPB, 0, st>>>(s.n, pos, damp, x, partial, per, thr);
+    k_tmu<T, NRHS, false, KAHAN><<<grid, TPB, 0, st>>>(s.n, pos, damp, wa, x, partial, per, thr, thr2m);
 }
 
 template <typename T, bool KAHAN>
@@ -860,14 +963,16 @@ static void tmu_finish(const DevSites &s, int nrhs, int nsplit, const T *partial
     g_launches.fetch_add(1, std::memory_order_relaxed);
     dim3 grid((s.n + 127) / 128, g);
     size_t xo = (size_t)done * s.n * 3;
+    const float2 *wa = std::is_same<T, double>::value ? s.pol_wa32 : nullptr;
+    float thr2m = damp_thr2_margin(s);
     if (s.amoeba)
-      k_tmu_finish<T, true><<<grid, 128, 0, st>>>(s.n, g, nsplit, pg, pos, damp, x + xo, s.pol_alpha, dodiag,
-                                                  s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src, s.d2d_s,
-                                                  (T)s.damp_thr, y + xo);
+      k_tmu_finish<T, true><<<grid, 128, 0, st>>>(s.n, g, nsplit, pg, pos, damp, wa, x + xo, s.pol_alpha,
+                                                  dodiag, s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src, s.d2d_s,
+                                                  (T)s.damp_thr, thr2m, y + xo);
     else
-      k_tmu_finish<T, false><<<grid, 128, 0, st>>>(s.n, g, nsplit, pg, pos, damp, x + xo, s.pol_alpha, dodiag,
-                                                   s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src, s.d2d_s,
-                                                   (T)s.damp_thr, y + xo);
+      k_tmu_finish<T, false><<<grid, 128, 0, st>>>(s.n, g, nsplit, pg, pos, damp, wa, x + xo, s.pol_alpha,
+                                                   dodiag, s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src, s.d2d_s,
+                                                   (T)s.damp_thr, thr2m, y + xo);
     done += g;
   }
 }
@@ -1006,6 +1111,10 @@ void launch_diff_norms(size_t n, const double *a, const double *b, double *parti
 void launch_reduce_norms(const double *partial, double *out, cudaStream_t st) {
   g_launches.fetch_add(1, std::memory_order_relaxed);
   k_reduce_norms<<<1, 32, 0, st>>>(kRedBlocks, partial, out);
+}
+void launch_any_diff(size_t n, const double *a, const double *b, int *flag, cudaStream_t st) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_any_diff<<<blocks_for(n, 256), 256, 0, st>>>(n, a, b, flag);
 }
 void launch_check_finite(size_t n, const double *x, int *flag, cudaStream_t st) {
   g_launches.fetch_add(1, std::memory_order_relaxed);

@@ -32,6 +32,8 @@ struct DevSites {
   int *polar_mm = nullptr;      // mm index of each polarizable site
   float4 *pol_pos32 = nullptr;  // centred FP32 copy: x, y, z, 1/thole
   float *pol_a32 = nullptr;
+  float2 *pol_wa32 = nullptr;   // (1/thole)^2, a^2 in FP32: damping pre-test of the FP64 kernels
+  float2 *mm_wa32 = nullptr;    // same for the static sites (inf when not polarizable)
   // static sites
   Pos64 *mm_pos = nullptr;    // x, y, z, thole (0 when not polarizable)
   double *mm_a = nullptr;       // damping a of the source (AMOEBA)
@@ -132,6 +134,8 @@ void launch_diff_norms(size_t n, const double *a, const double *b, double *parti
 void launch_reduce_norms(const double *partial, double *out, cudaStream_t st);
 // NaN / Inf check: flag set to 1 when any entry is not finite
 void launch_check_finite(size_t n, const double *x, int *flag, cudaStream_t st);
+// flag set to 1 when a and b differ in any bit of any entry
+void launch_any_diff(size_t n, const double *a, const double *b, int *flag, cudaStream_t st);
 
 // Number of SMs of the current device (cached).
 int sm_count();

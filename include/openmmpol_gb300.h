@@ -151,6 +151,9 @@ const char *ommp_gpu_last_error(void);
 void ommp_gpu_set_solver_tol(OMMP_SYSTEM_PRT s, double tol);
 void ommp_gpu_set_solver_maxiter(OMMP_SYSTEM_PRT s, int32_t maxiter);
 void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode);
+/* FP64 direct T.mu kernel: 0 auto (symmetric from 2048 sites), 1 all ordered
+ * pairs, 2 symmetric (each unordered pair once, deterministic) */
+int32_t ommp_gpu_set_fp64_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
 /* forget the last dipoles as a starting guess */
 void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s);
 
@@ -171,9 +174,11 @@ int32_t ommp_gpu_tmatvec(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t 
                          int32_t matv);
 int32_t ommp_gpu_tmatvec_fp32(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs);
 
-/* CUDA-event timing of the pair kernels: which 0 = FP64 T.mu, 1 = FP32 T.mu */
+/* CUDA-event timing of the pair kernels: which 0 = FP64 T.mu, 1 = FP32 T.mu;
+ * columns = right-hand sides summed over the timed launches (may be NULL) */
 void ommp_gpu_enable_kernel_timing(OMMP_SYSTEM_PRT s, int32_t on);
-void ommp_gpu_kernel_stats(OMMP_SYSTEM_PRT s, int32_t which, int64_t *launches, double *total_ms);
+void ommp_gpu_kernel_stats(OMMP_SYSTEM_PRT s, int32_t which, int64_t *launches, double *total_ms,
+                           int64_t *columns);
 void ommp_gpu_reset_kernel_stats(OMMP_SYSTEM_PRT s);
 int32_t ommp_gpu_synchronize(OMMP_SYSTEM_PRT s);
 /* stream-ordered timers on the system's stream: record slot 0..7, then the

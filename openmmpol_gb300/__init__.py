@@ -158,6 +158,11 @@ class OMMPSystem:
         m = {"fp64": PREC_FP64, "mixed": PREC_MIXED}.get(mode, mode)
         self._L.ommp_gpu_set_precision(self._h, int(m))
 
+    def set_fp64_kernel(self, mode) -> None:
+        """'auto' | 'ordered' (all ordered pairs) | 'symmetric' (unordered pairs)."""
+        m = {"auto": 0, "ordered": 1, "symmetric": 2}.get(mode, mode)
+        _check(self._L.ommp_gpu_set_fp64_kernel(self._h, int(m)))
+
     def clear_guess(self) -> None:
         self._L.ommp_gpu_clear_guess(self._h)
 
@@ -202,10 +207,13 @@ class OMMPSystem:
         self._L.ommp_gpu_enable_kernel_timing(self._h, int(on))
 
     def kernel_stats(self, which: int):
+        """(launches, total ms, right-hand-side columns) of the timed pair
+        kernel: which 0 = FP64 T.mu, 1 = FP32 T.mu."""
         n = C.c_int64(0)
         ms = C.c_double(0.0)
-        self._L.ommp_gpu_kernel_stats(self._h, which, C.byref(n), C.byref(ms))
-        return n.value, ms.value
+        cols = C.c_int64(0)
+        self._L.ommp_gpu_kernel_stats(self._h, which, C.byref(n), C.byref(ms), C.byref(cols))
+        return n.value, ms.value, cols.value
 
     def synchronize(self) -> None:
         _check(self._L.ommp_gpu_synchronize(self._h))

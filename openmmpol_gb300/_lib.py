@@ -57,6 +57,7 @@ SIGNATURES = {
     "ommp_gpu_set_solver_tol": (None, [_vp, C.c_double]),
     "ommp_gpu_set_solver_maxiter": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_precision": (None, [_vp, C.c_int32]),
+    "ommp_gpu_set_fp64_kernel": (C.c_int32, [_vp, C.c_int32]),
     "ommp_gpu_clear_guess": (None, [_vp]),
     "ommp_gpu_get_iterations": (C.c_int32, [_vp, C.c_int32]),
     "ommp_gpu_get_residual_history": (C.c_int32, [_vp, C.c_int32, _dp, C.c_int32]),
@@ -66,7 +67,7 @@ SIGNATURES = {
     "ommp_gpu_tmatvec": (C.c_int32, [_vp, _dp, _dp, C.c_int32, C.c_int32, C.c_int32]),
     "ommp_gpu_tmatvec_fp32": (C.c_int32, [_vp, _dp, _dp, C.c_int32]),
     "ommp_gpu_enable_kernel_timing": (None, [_vp, C.c_int32]),
-    "ommp_gpu_kernel_stats": (None, [_vp, C.c_int32, _i64p, _dp]),
+    "ommp_gpu_kernel_stats": (None, [_vp, C.c_int32, _i64p, _dp, _i64p]),
     "ommp_gpu_synchronize": (C.c_int32, [_vp]),
     "ommp_gpu_reset_kernel_stats": (None, [_vp]),
     "ommp_gpu_timer_record": (C.c_int32, [_vp, C.c_int32]),

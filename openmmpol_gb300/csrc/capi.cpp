@@ -130,6 +130,7 @@ const char *ommp_gpu_last_error(void) { return ommp::last_error(); }
 void ommp_gpu_set_solver_tol(OMMP_SYSTEM_PRT s, double tol) { S(s)->set_tol(tol); }
 void ommp_gpu_set_solver_maxiter(OMMP_SYSTEM_PRT s, int32_t n) { S(s)->set_maxiter(n); }
 void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode) { S(s)->set_precision(mode); }
+int32_t ommp_gpu_set_fp64_kernel(OMMP_SYSTEM_PRT s, int32_t mode) { return S(s)->set_fp64_kernel(mode); }
 void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s) { S(s)->clear_guess(); }
 
 int32_t ommp_gpu_get_iterations(OMMP_SYSTEM_PRT s, int32_t set) { return S(s)->stats().iters[set & 1]; }
@@ -159,12 +160,14 @@ int32_t ommp_gpu_tmatvec_fp32(OMMP_SYSTEM_PRT s, const double *x, double *y, int
   return S(s)->tmatvec_f32(x, y, nrhs);
 }
 void ommp_gpu_enable_kernel_timing(OMMP_SYSTEM_PRT s, int32_t on) { S(s)->enable_kernel_timing(on != 0); }
-void ommp_gpu_kernel_stats(OMMP_SYSTEM_PRT s, int32_t which, int64_t *launches, double *total_ms) {
-  long long l = 0;
+void ommp_gpu_kernel_stats(OMMP_SYSTEM_PRT s, int32_t which, int64_t *launches, double *total_ms,
+                           int64_t *columns) {
+  long long l = 0, c = 0;
   double ms = 0;
-  S(s)->kernel_stats(which, l, ms);
+  S(s)->kernel_stats(which, l, ms, c);
   *launches = l;
   *total_ms = ms;
+  if (columns) *columns = c;
 }
 int32_t ommp_gpu_synchronize(OMMP_SYSTEM_PRT s) { return S(s)->sync(); }
 void ommp_gpu_reset_kernel_stats(OMMP_SYSTEM_PRT s) { S(s)->reset_kernel_stats(); }

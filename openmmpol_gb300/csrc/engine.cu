@@ -54,6 +54,7 @@ System::~System() {
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (flush_buf_) cudaFree(flush_buf_);
+  if (sym_scratch_) cudaFree(sym_scratch_);
   kt_resolve();
   for (auto &e : kfree_) {
     cudaEventDestroy(e.a);
@@ -215,7 +216,7 @@ int System::sync() {
   return st;
 }
 
-System::KEv System::kt_begin(int kind) {
+System::KEv System::kt_begin(int kind, int cols) {
   KEv e;
   if (!kfree_.empty()) {
     e = kfree_.back();
@@ -225,6 +226,7 @@ System::KEv System::kt_begin(int kind) {
     cudaEventCreate(&e.b);
   }
   e.kind = kind;
+  e.cols = cols;
   cudaEventRecord(e.a, st_);
   return e;
 }
@@ -241,21 +243,24 @@ void System::kt_resolve() {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e.a, e.b);
     klaunch_[e.kind] += 1;
+    kcols_[e.kind] += e.cols;
     kms_[e.kind] += ms;
     kfree_.push_back(e);
   }
   kpending_.clear();
 }
 
-void System::kernel_stats(int which, long long &launches, double &ms) {
+void System::kernel_stats(int which, long long &launches, double &ms, long long &columns) {
   kt_resolve();
   launches = klaunch_[which & 1];
   ms = kms_[which & 1];
+  columns = kcols_[which & 1];
 }
 
 void System::reset_kernel_stats() {
   kt_resolve();
   klaunch_[0] = klaunch_[1] = 0;
+  kcols_[0] = kcols_[1] = 0;
   kms_[0] = kms_[1] = 0.0;
 }
 
@@ -344,13 +349,21 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
   if (matv == kMatvIncore && tmat_ok_) {
     gpu::launch_gemv(3 * d_.n, tmat_, x, y, dodiag, d_.pol_alpha, ncol, st_);
   } else {
-    if (ktime_on_) {
-      KEv e = kt_begin(0);
-      gpu::launch_tmu_f64(d_, ncol, x, y, dodiag, scratch_, nsplit_tmu_, st_);
-      kt_end(e);
-    } else {
-      gpu::launch_tmu_f64(d_, ncol, x, y, dodiag, scratch_, nsplit_tmu_, st_);
+    bool sym = fp64_kernel_ == 2 || (fp64_kernel_ == 0 && d_.n >= 2048);
+    if (sym && !sym_scratch_) {
+      if (dalloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 2))) {
+        sym_scratch_ = nullptr;
+        sym = false;  // not enough memory for the partials: all-ordered-pairs kernel
+        log_msg(kVerbHigh, nullptr, "symmetric T.mu scratch does not fit: using the target-outer kernel");
+      }
     }
+    KEv e;
+    if (ktime_on_) e = kt_begin(0, ncol);
+    if (sym)
+      gpu::launch_tmu_f64_sym(d_, ncol, x, y, dodiag, sym_scratch_, st_);
+    else
+      gpu::launch_tmu_f64(d_, ncol, x, y, dodiag, scratch_, nsplit_tmu_, st_);
+    if (ktime_on_) kt_end(e);
     stats_.f64_matvecs += 1;
   }
   return kOk;
@@ -644,7 +657,7 @@ int System::pcg32(int ncol, double *rms0_out, int max_it, double eta) {
   int it = 0;
   for (it = 1; it <= max_it; ++it) {
     if (ktime_on_) {
-      KEv e = kt_begin(1);
+      KEv e = kt_begin(1, ncol);
       gpu::launch_tmu_f32(d_, ncol, p32_, h32_, scratch32_, nsplit_tmu32_, st_);
       kt_end(e);
     } else {
@@ -899,6 +912,15 @@ int System::update_coordinates(const double *c) {
   m2d_done_ = ipd_done_ = ipd_use_guess_ = false;
   tmat_ok_ = lu_ok_ = false;
   return upload_geometry();
+}
+
+int System::set_fp64_kernel(int mode) {
+  if (mode < 0 || mode > 2) {
+    set_last_error("FP64 kernel mode must be 0 (auto), 1 (all ordered pairs) or 2 (symmetric)");
+    return kErrBadArg;
+  }
+  fp64_kernel_ = mode;
+  return kOk;
 }
 
 int System::set_default_solver(int s) {

@@ -50,6 +50,9 @@ class System {
   void set_tol(double t) { tol_ = t; }
   void set_maxiter(int n) { maxiter_ = n; }
   void set_precision(int p) { precision_ = p; }
+  // FP64 direct product: 0 auto (symmetric from 2048 sites), 1 all ordered
+  // pairs (target-outer), 2 symmetric (unordered pairs)
+  int set_fp64_kernel(int mode);
   int precision() const { return precision_; }
   double tol() const { return tol_; }
   const SolveStats &stats() const { return stats_; }
@@ -59,7 +62,7 @@ class System {
   // kernel timing of the dominant pair kernels (CUDA events on the stream,
   // resolved lazily so that timing adds no synchronisation)
   void enable_kernel_timing(bool on) { ktime_on_ = on; }
-  void kernel_stats(int which, long long &launches, double &ms);
+  void kernel_stats(int which, long long &launches, double &ms, long long &columns);
   void reset_kernel_stats();
   // stream-ordered event timers (slots 0..7) and an L2 flush on the stream
   int timer_record(int slot);
@@ -113,6 +116,8 @@ class System {
   float *alpha32_ = nullptr;
   double *scratch_ = nullptr;  // pair-kernel split partials
   size_t scratch_n_ = 0;
+  double *sym_scratch_ = nullptr;  // symmetric-kernel partials (allocated on first use)
+  int fp64_kernel_ = 0;
   float *scratch32_ = nullptr;
   double *partial_ = nullptr;  // reduction partials [kRedBlocks][8]
   double *dots_ = nullptr;     // [8]
@@ -135,13 +140,15 @@ class System {
   float last_ms_ = 0.f;
   bool ktime_on_ = false;
   long long klaunch_[2] = {0, 0};
+  long long kcols_[2] = {0, 0};
   double kms_[2] = {0, 0};
   struct KEv {
     cudaEvent_t a, b;
     int kind;
+    int cols;  // right-hand sides carried by the timed launch
   };
   std::vector<KEv> kpending_, kfree_;
-  KEv kt_begin(int kind);
+  KEv kt_begin(int kind, int cols);
   void kt_end(KEv &e);
   void kt_resolve();
   cudaEvent_t tev_[8] = {};

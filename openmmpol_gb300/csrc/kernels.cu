@@ -435,6 +435,148 @@ __global__ void k_tmu_finish(int n, int nrhs, int nsplit, const T *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
+// Symmetric FP64 dipole field: every unordered pair is evaluated once and
+// both directions are accumulated (T_ij = T_ji), halving the FP64 work of
+// the geometry.  Sites are grouped in super-tiles of 128 (4 warps x 32
+// lanes).  CTA (I, part) owns super-tile I and the slots k of its half shell
+// J = (I + k) mod ntile, k = 0..K (K = ntile / 2); slot 0 is the diagonal
+// block (target side only, all ordered pairs); for even ntile the slot
+// k = ntile/2 is handled by the lower of the two tiles only.  Inside a slot a
+// warp pairs its 32 targets with each 32-site sub-tile of J in 32 rotation
+// steps: at step t lane l meets source (l + t) mod 32, read from shared
+// memory, and the source-side accumulators travel one lane per step by
+// shuffle, so no lane ever shares an accumulator.  Source sides are summed
+// over the 4 warps in shared memory and written to jpart[I][k]; target sides
+// go to ipart[I][part].  k_tmu_sym_reduce adds them in a fixed order, so the
+// product is deterministic.
+// ---------------------------------------------------------------------------
+constexpr int SYM_TILE = 128;
+
+template <int NRHS, bool AMOEBA>
+__global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, int nparts, int per_part,
+                                                       const Pos64 *__restrict__ pos,
+                                                       const double *__restrict__ damp,
+                                                       const float2 *__restrict__ wa,
+                                                       const double *__restrict__ x,
+                                                       double *__restrict__ jpart, double *__restrict__ ipart,
+                                                       double thr, float thr2m) {
+  constexpr int C = 3 * NRHS;
+  __shared__ double s_x[SYM_TILE], s_y[SYM_TILE], s_z[SYM_TILE], s_w[SYM_TILE], s_a[SYM_TILE];
+  __shared__ float2 s_wa[SYM_TILE];
+  __shared__ double s_mu[C][SYM_TILE];
+  __shared__ double s_accj[4][C][SYM_TILE];
+  const int I = blockIdx.x, part = blockIdx.y;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ti = I * SYM_TILE + tid;
+  const bool vi = ti < n;
+  const Pos64 pi = vi ? pos[ti] : Pos64{0, 0, 0, 0};
+  const double ai = (AMOEBA && vi) ? damp[ti] : 0.0;
+  const float2 wai = vi ? wa[ti] : make_float2(0.f, 0.f);
+  double mui[C], acci[C];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    mui[c] = vi ? x[((size_t)(c / 3) * n + ti) * 3 + (c % 3)] : 0.0;
+    acci[c] = 0.0;
+  }
+  const int k0 = part * per_part;
+  const int k1 = min(K + 1, k0 + per_part);
+  for (int k = k0; k < k1; ++k) {
+    int J = I + k;
+    if (J >= ntile) J -= ntile;
+    double *jp = jpart + ((size_t)I * (K + 1) + k) * SYM_TILE * C;
+    if (k > 0 && 2 * k == ntile && I >= ntile / 2) {  // the other tile of the pair owns it
+#pragma unroll
+      for (int c = 0; c < C; ++c) jp[(size_t)c * SYM_TILE + tid] = 0.0;
+      continue;
+    }
+    const bool diag = (k == 0);
+    __syncthreads();
+    {
+      int sj = J * SYM_TILE + tid;
+      bool v = sj < n;
+      Pos64 p = v ? pos[sj] : Pos64{0, 0, 0, 0};
+      s_x[tid] = p.x;
+      s_y[tid] = p.y;
+      s_z[tid] = p.z;
+      s_w[tid] = p.w;
+      s_a[tid] = (AMOEBA && v) ? damp[sj] : 0.0;
+      s_wa[tid] = v ? wa[sj] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < C; ++c) s_mu[c][tid] = v ? x[((size_t)(c / 3) * n + sj) * 3 + (c % 3)] : 0.0;
+    }
+    __syncthreads();
+    for (int js = 0; js < 4; ++js) {
+      double accj[C];
+#pragma unroll
+      for (int c = 0; c < C; ++c) accj[c] = 0.0;
+      for (int t = 0; t < 32; ++t) {
+        const int jl = js * 32 + ((lane + t) & 31);
+        const int gj = J * SYM_TILE + jl;
+        if (vi && gj < n && gj != ti) {
+          double dx = pi.x - s_x[jl], dy = pi.y - s_y[jl], dz = pi.z - s_z[jl];
+          double r2 = dx * dx + dy * dy + dz * dz;
+          double k3, k5x3;
+          dd_pair<double, AMOEBA>(r2, pi.w, s_w[jl], ai, s_a[jl], wai, s_wa[jl], thr, thr2m, k3, k5x3);
+#pragma unroll
+          for (int r = 0; r < NRHS; ++r) {
+            double mx = s_mu[3 * r][jl], my = s_mu[3 * r + 1][jl], mz = s_mu[3 * r + 2][jl];
+            double f = k5x3 * (mx * dx + my * dy + mz * dz);
+            acci[3 * r] += f * dx - k3 * mx;
+            acci[3 * r + 1] += f * dy - k3 * my;
+            acci[3 * r + 2] += f * dz - k3 * mz;
+            if (!diag) {
+              double g = k5x3 * (mui[3 * r] * dx + mui[3 * r + 1] * dy + mui[3 * r + 2] * dz);
+              accj[3 * r] += g * dx - k3 * mui[3 * r];
+              accj[3 * r + 1] += g * dy - k3 * mui[3 * r + 1];
+              accj[3 * r + 2] += g * dz - k3 * mui[3 * r + 2];
+            }
+          }
+        }
+        if (!diag) {
+          // the accumulator of source s moves to the lane that meets s next
+#pragma unroll
+          for (int c = 0; c < C; ++c) accj[c] = __shfl_sync(0xffffffffu, accj[c], (lane + 1) & 31);
+        }
+      }
+      if (!diag) {
+        // after 32 steps lane l holds the accumulator of source js*32 + l
+#pragma unroll
+        for (int c = 0; c < C; ++c) s_accj[warp][c][js * 32 + lane] = accj[c];
+      }
+    }
+    if (!diag) {
+      __syncthreads();
+#pragma unroll
+      for (int c = 0; c < C; ++c)
+        jp[(size_t)c * SYM_TILE + tid] = ((s_accj[0][c][tid] + s_accj[1][c][tid]) + s_accj[2][c][tid]) +
+                                         s_accj[3][c][tid];
+    }
+  }
+  double *ip = ipart + ((size_t)I * nparts + part) * SYM_TILE * C;
+#pragma unroll
+  for (int c = 0; c < C; ++c) ip[(size_t)c * SYM_TILE + tid] = acci[c];
+}
+
+// out[r][t][c] = sum_part ipart[J][part] + sum_{k=1..K} jpart[(J - k) mod ntile][k]
+__global__ void k_tmu_sym_reduce(int n, int nrhs, int ntile, int K, int nparts, const double *__restrict__ jpart,
+                                 const double *__restrict__ ipart, double *__restrict__ out) {
+  const int C = 3 * nrhs;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  int J = t / SYM_TILE, l = t % SYM_TILE;
+  for (int c = 0; c < C; ++c) {
+    double e = 0.0;
+    for (int p = 0; p < nparts; ++p) e += ipart[(((size_t)J * nparts + p) * C + c) * SYM_TILE + l];
+    for (int k = 1; k <= K; ++k) {
+      int I = J - k;
+      if (I < 0) I += ntile;
+      e += jpart[(((size_t)I * (K + 1) + k) * C + c) * SYM_TILE + l];
+    }
+    out[((size_t)(c / 3) * n + t) * 3 + (c % 3)] = e;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // dense T matrix (create_tmat / dipole_T, src/mod_polarization.F90:327-435)
 // ---------------------------------------------------------------------------
 template <bool AMOEBA>
@@ -982,6 +1124,77 @@ void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, boo
   if (s.n == 0) return;
   tmu_dispatch<double, false>(s, nrhs, s.pol_pos, s.pol_a, x, scratch, nsplit, st);
   tmu_finish<double>(s, nrhs, nsplit, scratch, s.pol_pos, s.pol_a, x, dodiag, y, st);
+}
+
+namespace {
+struct SymPlan {
+  int ntile, K, nparts, per_part;
+};
+SymPlan sym_plan(int n) {
+  SymPlan p;
+  p.ntile = (n + SYM_TILE - 1) / SYM_TILE;
+  p.K = p.ntile / 2;
+  int want = (4 * sm_count() + p.ntile - 1) / p.ntile;  // >= 4 CTAs per SM in total
+  if (want < 1) want = 1;
+  if (want > p.K + 1) want = p.K + 1;
+  p.per_part = (p.K + 1 + want - 1) / want;
+  p.nparts = (p.K + 1 + p.per_part - 1) / p.per_part;
+  return p;
+}
+}  // namespace
+
+size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs) {
+  if (s.n == 0) return 0;
+  SymPlan p = sym_plan(s.n);
+  size_t C = 3 * (size_t)nrhs;
+  return (size_t)p.ntile * (p.K + 1) * SYM_TILE * C + (size_t)p.ntile * p.nparts * SYM_TILE * C +
+         (size_t)nrhs * s.n * 3;
+}
+
+void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
+                        cudaStream_t st) {
+  if (s.n == 0) return;
+  SymPlan p = sym_plan(s.n);
+  float thr2m = damp_thr2_margin(s);
+  // columns in groups of 2 (and a last single one) share the pair geometry
+  int done = 0;
+  while (done < nrhs) {
+    int g = (nrhs - done) >= 2 ? 2 : 1;
+    size_t C = 3 * (size_t)g;
+    double *jpart = scratch;
+    double *ipart = jpart + (size_t)p.ntile * (p.K + 1) * SYM_TILE * C;
+    double *e = ipart + (size_t)p.ntile * p.nparts * SYM_TILE * C;
+    const double *xg = x + (size_t)done * s.n * 3;
+    dim3 grid(p.ntile, p.nparts);
+    g_launches.fetch_add(3, std::memory_order_relaxed);
+    if (g == 2) {
+      if (s.amoeba)
+        k_tmu_sym<2, true><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos, s.pol_a,
+                                                      s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+      else
+        k_tmu_sym<2, false><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos,
+                                                       s.pol_a, s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+    } else {
+      if (s.amoeba)
+        k_tmu_sym<1, true><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos, s.pol_a,
+                                                      s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+      else
+        k_tmu_sym<1, false><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos,
+                                                       s.pol_a, s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+    }
+    k_tmu_sym_reduce<<<(s.n + 127) / 128, 128, 0, st>>>(s.n, g, p.ntile, p.K, p.nparts, jpart, ipart, e);
+    const float2 *wa = s.pol_wa32;
+    dim3 fgrid((s.n + 127) / 128, g);
+    if (s.amoeba)
+      k_tmu_finish<double, true><<<fgrid, 128, 0, st>>>(s.n, g, 1, e, s.pol_pos, s.pol_a, wa, xg, s.pol_alpha,
+                                                        dodiag, s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src,
+                                                        s.d2d_s, s.damp_thr, thr2m, y + (size_t)done * s.n * 3);
+    else
+      k_tmu_finish<double, false><<<fgrid, 128, 0, st>>>(s.n, g, 1, e, s.pol_pos, s.pol_a, wa, xg, s.pol_alpha,
+                                                         dodiag, s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src,
+                                                         s.d2d_s, s.damp_thr, thr2m, y + (size_t)done * s.n * 3);
+    done += g;
+  }
 }
 
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch, int nsplit,

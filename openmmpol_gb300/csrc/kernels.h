@@ -62,6 +62,11 @@ size_t tmu_scratch_doubles(const DevSites &s, int nrhs, int nsplit);
 int tmu_pick_split(const DevSites &s, int nrhs, int sm_count, bool fp32);
 void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag,
                     double *scratch, int nsplit, cudaStream_t st);
+// Same product with each unordered pair evaluated once (deterministic
+// half-shell schedule); scratch of tmu_sym_scratch_doubles(s, nrhs_max).
+size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs);
+void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
+                        cudaStream_t st);
 // FP32 inner operator with compensated cross-tile sums; x,y float.
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch,
                     int nsplit, cudaStream_t st);

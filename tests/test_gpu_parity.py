@@ -98,6 +98,38 @@ def test_gpu_m2d_field_and_tmatvec_match_oracle(case, golden_mmp):
     assert rel(y2[1], o.tmatvec(x2[1])) < 1e-12
 
 
+@pytest.mark.parametrize("case", ["nma_amoeba", "1crn_amoeba", "1crn_wang", "1ao6cut_wang", "1ubq_amoeba",
+                                  "1ubq_wang"])
+@pytest.mark.parametrize("kernel", ["ordered", "symmetric"])
+def test_fp64_kernel_variants_match_oracle(case, kernel, golden, golden_mmp):
+    """Both FP64 T.mu kernels (all ordered pairs; each unordered pair once in
+    the half-shell schedule) on 1, 6 (even) and 11 (odd) tiles of 128 sites,
+    partial last tiles, and Wang exclusions."""
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    g.set_fp64_kernel(kernel)
+    x = np.random.default_rng(5).standard_normal((2, o.pol_atoms, 3))
+    y = g.tmatvec(x)
+    for r in range(2):
+        assert rel(y[r], o.tmatvec(x[r])) < 1e-12
+    assert rel(g.tmatvec(x[0], dodiag=False), o.tmatvec(x[0], dodiag=False)) < 1e-12
+    g.set_solver_tol(1e-10)
+    o.set_tol(1e-10)
+    ef = golden[case + "_ef1"]
+    g.set_external_field(ef)
+    o.set_external_field(ef)
+    assert rel(g.ipd, o.ipd) < 1e-9
+
+
+def test_symmetric_kernel_is_deterministic(w1k):
+    p, _ = w1k
+    g = OMMPSystem(p)
+    g.set_fp64_kernel("symmetric")
+    x = np.random.default_rng(9).standard_normal((g.pol_atoms, 3))
+    a, b = g.tmatvec(x), g.tmatvec(x)
+    assert np.array_equal(a, b)
+
+
 @pytest.mark.parametrize("case", ["nma_amoeba", "nma_wang_cut", "1crn_amoeba", "1crn_wang"])
 @pytest.mark.parametrize("solver", ["cg", "diis", "inversion"])
 def test_gpu_solvers_match_oracle(case, solver, golden, golden_mmp):

@@ -156,6 +156,23 @@ void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode);
 int32_t ommp_gpu_set_fp64_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
 /* forget the last dipoles as a starting guess */
 void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s);
+/* capture the inner FP32 iteration as a CUDA graph (default on) */
+void ommp_gpu_set_use_graphs(OMMP_SYSTEM_PRT s, int32_t on);
+
+/* Batched right-hand sides: nfields external fields (e.g. from several QM
+ * densities) solved together, each as ommp_set_external_field would solve it
+ * from a zero guess, in the system's precision mode; the columns of all
+ * fields share every pair evaluation (mixed mode: one block of columns
+ * through the FP32-inner / FP64-refinement solver).  fields [nfields]
+ * [pol_atoms][3]; ipd_out [nfields][n_ipd][pol_atoms][3]; energies [nfields]
+ * (host, may be NULL) = ommp_get_polelec_energy of each solution.  The
+ * system's own dipoles and warm-start guess are not touched. */
+int32_t ommp_gpu_set_external_fields_batch(OMMP_SYSTEM_PRT s, int32_t nfields, const double *fields,
+                                           double *ipd_out, double *energies);
+/* same with fields and ipd_out in device memory */
+int32_t ommp_gpu_set_external_fields_batch_device(OMMP_SYSTEM_PRT s, int32_t nfields,
+                                                  const double *fields_dev, double *ipd_out_dev,
+                                                  double *energies);
 
 /* results of the last solve: iterations of set k (CG/DIIS) or refinement
  * steps (mixed), residual history (returns the length, copies up to maxn) */

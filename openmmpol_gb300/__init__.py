@@ -129,6 +129,23 @@ class OMMPSystem:
             self._h, ef.ctypes.data_as(_lib._dp), available_solvers[solver],
             available_matrix_vector[matv], 0 if nomm else 1))
 
+    def set_external_fields_batch(self, fields):
+        """Solve several external fields together (cold start each); returns
+        (ipd [nfields, n_ipd, pol_atoms, 3], energies [nfields])."""
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        if f.ndim != 3 or f.shape[1:] != (self.pol_atoms, 3):
+            raise ValueError("fields should be shaped [nfields, pol_atoms, 3]")
+        nf = f.shape[0]
+        out = np.zeros((nf, self.n_ipd, self.pol_atoms, 3))
+        e = np.zeros(nf)
+        _check(self._L.ommp_gpu_set_external_fields_batch(self._h, nf, f.ctypes.data_as(_lib._dp),
+                                                          out.ctypes.data_as(_lib._dp),
+                                                          e.ctypes.data_as(_lib._dp)))
+        return out, e
+
+    def set_use_graphs(self, on: bool = True) -> None:
+        self._L.ommp_gpu_set_use_graphs(self._h, int(on))
+
     def get_polelec_energy(self) -> float:
         e = C.c_double(0.0)
         _check(self._L.ommp_gpu_get_polelec_energy(self._h, C.byref(e)))

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libommp_gb300.so")
 
-CU_SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "engine.cu", "solvers.cu", "noalloc.cu"]
 CXX_SOURCES = ["setup.cpp", "capi.cpp", "log.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -45,6 +45,8 @@ int System::check(cudaError_t e, const char *what) {
 
 System::~System() {
   if (st_) cudaStreamSynchronize(st_);
+  free_ws(ws_);
+  free_ws(wsb_);
   void *bufs[] = {d_.pol_pos, d_.pol_a, d_.pol_alpha, d_.polar_mm, d_.pol_pos32, d_.pol_a32, d_.pol_wa32,
                   d_.mm_wa32, d_.mm_pos,
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
@@ -122,7 +124,8 @@ int System::upload_static() {
   bad |= dalloc(x32_, nv * 2) | dalloc(r32_, nv * 2) | dalloc(p32_, nv * 2) | dalloc(h32_, nv * 2) |
          dalloc(z32_, nv * 2);
   scratch_n_ = std::max(gpu::m2d_scratch_doubles(d_, nsplit_m2d_), gpu::tmu_scratch_doubles(d_, 2, nsplit_tmu_));
-  bad |= dalloc(scratch_, scratch_n_) | dalloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, nsplit_tmu32_));
+  // FP32 scratch for twice the default source split (the autotuner tries both)
+  bad |= dalloc(scratch_, scratch_n_) | dalloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, 2 * nsplit_tmu32_));
   bad |= dalloc(partial_, (size_t)gpu::kRedBlocks * 32) | dalloc(dots_, 64) | dalloc(hist_, 2 * (size_t)maxhist_);
   bad |= dalloc(cols_, 2) | dalloc(flag_, 1) | dalloc(info_, 1);
   if (bad || cudaMallocHost((void **)&cols_h_, 2 * sizeof(gpu::CgCol)) != cudaSuccess ||
@@ -130,6 +133,14 @@ int System::upload_static() {
     set_last_error("out of device memory while allocating the system");
     return kErrMemory;
   }
+  ws_.cap = 2;
+  ws_.x = x_, ws_.r = r_, ws_.p = p_, ws_.h = h_, ws_.z = z_, ws_.rhs = rhs_;
+  ws_.x32 = x32_, ws_.r32 = r32_, ws_.p32 = p32_, ws_.h32 = h32_, ws_.z32 = z32_;
+  ws_.scratch32 = scratch32_;
+  ws_.scratch32_nsplit = 2 * nsplit_tmu32_;
+  ws_.partial = partial_, ws_.dots = dots_, ws_.hist = hist_;
+  ws_.cols = cols_, ws_.cols_h = cols_h_, ws_.scal_h = scal_h_;
+  ws_.owned = false;
   d_.m2d_nnz = (int)m2d_pairs_.src.size();
   d_.d2d_nnz = (int)d2d_pairs_.src.size();
   auto up = [&](void *dst, const void *src, size_t bytes) {
@@ -359,101 +370,19 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
     }
     KEv e;
     if (ktime_on_) e = kt_begin(0, ncol);
-    if (sym)
+    if (sym) {
       gpu::launch_tmu_f64_sym(d_, ncol, x, y, dodiag, sym_scratch_, st_);
-    else
-      gpu::launch_tmu_f64(d_, ncol, x, y, dodiag, scratch_, nsplit_tmu_, st_);
+    } else {
+      // the split partials hold two columns: larger blocks go two at a time
+      const size_t nv = 3 * (size_t)d_.n;
+      for (int c0 = 0; c0 < ncol; c0 += 2)
+        gpu::launch_tmu_f64(d_, std::min(2, ncol - c0), x + c0 * nv, y + c0 * nv, dodiag, scratch_, nsplit_tmu_,
+                            st_);
+    }
     if (ktime_on_) kt_end(e);
     stats_.f64_matvecs += 1;
   }
   return kOk;
-}
-
-// Conjugate gradient over ncol independent columns sharing each matvec.
-int System::cg64(int matv, int ncol, const double *rhs, double *x, int set0) {
-  const int n = d_.n;
-  const size_t nv = 3 * (size_t)n;
-  log_msg(kVerbLow, nullptr, "Solving linear system with CG solver");
-  log_msg(kVerbLow, nullptr, "Max iter: %4d", maxiter_);
-  log_msg(kVerbLow, nullptr, "Tolerance: %8.1E", tol_);
-  // guess: a zero-norm input is replaced by precnd(x) = alpha * x (:151-157)
-  gpu::launch_dots(ncol, nv, x, x, partial_, st_);
-  gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-  cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
-  int st = check(cudaStreamSynchronize(st_), "CG start");
-  if (st) return st;
-  bool all_zero = true;
-  for (int k = 0; k < ncol; ++k) {
-    if (scal_h_[k] < kEpsRp) {
-      log_msg(kVerbHigh, nullptr, "Input guess has zero norm, generating a guess from preconditioner.");
-      gpu::launch_scale_by_alpha(1, n, d_.pol_alpha, x + k * nv, x + k * nv, st_);
-    } else {
-      log_msg(kVerbHigh, nullptr, "Using input guess as a starting point for iterative solver.");
-    }
-    if (scal_h_[k] != 0.0) all_zero = false;
-  }
-  // r = rhs - T x; an exactly zero x gives T x = 0 without the pair sum
-  if (all_zero) {
-    cudaMemcpyAsync(r_, rhs, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
-  } else {
-    matvec64(matv, ncol, x, z_, true);
-    gpu::launch_residual(ncol * nv, rhs, z_, r_, st_);
-  }
-  gpu::launch_scale_by_alpha(ncol, n, d_.pol_alpha, r_, z_, st_);
-  cudaMemcpyAsync(p_, z_, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
-  gpu::launch_dots(ncol, nv, r_, z_, partial_, st_);
-  gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-  cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
-  st = check(cudaStreamSynchronize(st_), "CG init");
-  if (st) return st;
-  for (int k = 0; k < ncol; ++k) {
-    gpu::CgCol c{};
-    c.gold = scal_h_[k];
-    c.active = 1;
-    cols_h_[k] = c;
-  }
-  cudaMemcpyAsync(cols_, cols_h_, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
-  for (int it = 1; it <= maxiter_; ++it) {
-    matvec64(matv, ncol, p_, h_, true);
-    gpu::launch_dots(ncol, nv, h_, p_, partial_, st_);
-    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-    gpu::launch_cg_alpha(ncol, dots_, cols_, kEpsRp, st_);
-    gpu::launch_cg_update(ncol, n, x, r_, p_, h_, z_, d_.pol_alpha, cols_, partial_, st_);
-    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-    gpu::launch_cg_gnew(ncol, n, dots_, cols_, tol_, hist_, maxhist_, st_);
-    gpu::launch_cg_pupdate(ncol, n, p_, z_, cols_, st_);
-    cudaMemcpyAsync(cols_h_, cols_, ncol * sizeof(gpu::CgCol), cudaMemcpyDeviceToHost, st_);
-    st = check(cudaStreamSynchronize(st_), "CG iteration");
-    if (st) return st;
-    bool any = false;
-    for (int k = 0; k < ncol; ++k) {
-      if (cols_h_[k].active) any = true;
-      if (log_level() >= kVerbHigh && cols_h_[k].iters == it)
-        log_msg(kVerbHigh, nullptr, "iter=%4d residual rms norm: %14.4E", it, cols_h_[k].rms);
-    }
-    if (!any) break;
-  }
-  std::vector<double> h(maxhist_);
-  int rc = kOk;
-  for (int k = 0; k < ncol; ++k) {
-    const gpu::CgCol &c = cols_h_[k];
-    int set = set0 + k;
-    stats_.iters[set] = c.iters;
-    int nh = std::min(c.iters, maxhist_);
-    cudaMemcpy(h.data(), hist_ + (size_t)k * maxhist_, nh * sizeof(double), cudaMemcpyDeviceToHost);
-    stats_.hist[set].assign(h.begin(), h.begin() + nh);
-    if (c.quick) log_msg(kVerbHigh, nullptr, "Direction vector with zero norm, exiting iterative solver.");
-    if (c.converged)
-      log_msg(kVerbHigh, nullptr, "Required convergence threshold reached, exiting iterative solver.");
-    if (!std::isfinite(c.rms)) {
-      set_last_error("non-finite residual in the iterative solver (coincident sites?)");
-      rc = kErrNumeric;
-    } else if (!c.converged && !c.quick && c.rms > tol_ && std::fabs(c.gama) > kEpsRp) {
-      set_last_error("Iterative solver did not converged");
-      rc = kErrNotConverged;
-    }
-  }
-  return rc;
 }
 
 // Pulay DIIS extrapolation state lives on the host (tiny B matrix).
@@ -620,129 +549,6 @@ int System::inversion64(const double *rhs, double *x) {
   cudaMemcpyAsync(x, rhs, nn * sizeof(double), cudaMemcpyDeviceToDevice, st_);
   gpu::launch_lu_solve((int)nn, tmat_, piv_, x, st_);
   return check(cudaStreamSynchronize(st_), "LU solve");
-}
-
-// FP32 preconditioned CG on r32_ (columns normalised to unit rms); result in x32_.
-int System::pcg32(int ncol, double *rms0_out, int max_it, double eta) {
-  (void)rms0_out;
-  const int n = d_.n;
-  const size_t nv = 3 * (size_t)n;
-  // x = 0; p = h = 0 so that an update step with alpha = 0 only forms
-  // z = alpha_pol r and the partial r.z
-  cudaMemsetAsync(x32_, 0, ncol * nv * sizeof(float), st_);
-  cudaMemsetAsync(p32_, 0, ncol * nv * sizeof(float), st_);
-  cudaMemsetAsync(h32_, 0, ncol * nv * sizeof(float), st_);
-  gpu::CgCol c0{};
-  for (int k = 0; k < ncol; ++k) {
-    c0.active = 1;
-    c0.alpha = 0.0;
-    cols_h_[k] = c0;
-  }
-  cudaMemcpyAsync(cols_, cols_h_, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
-  // with alpha = 0 the update kernel leaves x, r unchanged and writes
-  // z = alpha_pol r and the partial r.z
-  gpu::launch_cg_update_f32(ncol, n, x32_, r32_, p32_, h32_, z32_, alpha32_, cols_, partial_, st_);
-  gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-  cudaMemcpyAsync(p32_, z32_, ncol * nv * sizeof(float), cudaMemcpyDeviceToDevice, st_);
-  cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
-  int st = check(cudaStreamSynchronize(st_), "inner CG init");
-  if (st) return st;
-  for (int k = 0; k < ncol; ++k) {
-    gpu::CgCol c{};
-    c.gold = scal_h_[k];
-    c.active = scal_h_[k] > 0.0 ? 1 : 0;
-    cols_h_[k] = c;
-  }
-  cudaMemcpyAsync(cols_, cols_h_, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
-  int it = 0;
-  for (it = 1; it <= max_it; ++it) {
-    if (ktime_on_) {
-      KEv e = kt_begin(1, ncol);
-      gpu::launch_tmu_f32(d_, ncol, p32_, h32_, scratch32_, nsplit_tmu32_, st_);
-      kt_end(e);
-    } else {
-      gpu::launch_tmu_f32(d_, ncol, p32_, h32_, scratch32_, nsplit_tmu32_, st_);
-    }
-    stats_.f32_matvecs += 1;
-    gpu::launch_dots_f32(ncol, nv, h32_, p32_, partial_, st_);
-    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-    gpu::launch_cg_alpha(ncol, dots_, cols_, 1e-300, st_);
-    gpu::launch_cg_update_f32(ncol, n, x32_, r32_, p32_, h32_, z32_, alpha32_, cols_, partial_, st_);
-    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-    gpu::launch_cg_gnew(ncol, n, dots_, cols_, eta, nullptr, 0, st_);
-    gpu::launch_cg_pupdate_f32(ncol, n, p32_, z32_, cols_, st_);
-    cudaMemcpyAsync(cols_h_, cols_, ncol * sizeof(gpu::CgCol), cudaMemcpyDeviceToHost, st_);
-    st = check(cudaStreamSynchronize(st_), "inner CG iteration");
-    if (st) return st;
-    bool any = false;
-    for (int k = 0; k < ncol; ++k) any |= cols_h_[k].active != 0;
-    if (!any) break;
-  }
-  stats_.inner_iters += std::min(it, max_it);
-  return kOk;
-}
-
-// Iterative refinement: FP64 residual, FP32 inner PCG, FP64 accumulation.
-int System::mixed_ir(int ncol, const double *rhs, double *x, int set0, bool have_guess) {
-  const int n = d_.n;
-  const size_t nv = 3 * (size_t)n;
-  const int max_outer = 30;
-  log_msg(kVerbLow, nullptr, "Solving linear system with mixed-precision CG (FP32 inner, FP64 refinement)");
-  if (have_guess) {
-    matvec64(kMatvDirect, ncol, x, h_, true);
-    gpu::launch_residual(ncol * nv, rhs, h_, r_, st_);
-  } else {
-    cudaMemsetAsync(x, 0, ncol * nv * sizeof(double), st_);
-    cudaMemcpyAsync(r_, rhs, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
-  }
-  for (int k = 0; k < ncol; ++k) stats_.hist[set0 + k].clear();
-  std::vector<double> rms(ncol);
-  int outer = 0;
-  bool done = false;
-  while (true) {
-    gpu::launch_scale_by_alpha(ncol, n, d_.pol_alpha, r_, z_, st_);
-    gpu::launch_dots(ncol, nv, r_, z_, partial_, st_);
-    gpu::launch_reduce_partials(ncol, partial_, dots_, st_);
-    cudaMemcpyAsync(scal_h_, dots_, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
-    int st = check(cudaStreamSynchronize(st_), "refinement residual");
-    if (st) return st;
-    done = true;
-    for (int k = 0; k < ncol; ++k) {
-      rms[k] = std::sqrt(std::max(scal_h_[k], 0.0) / (double)nv);
-      stats_.hist[set0 + k].push_back(rms[k]);
-      if (!std::isfinite(rms[k])) {
-        set_last_error("non-finite residual in the refinement loop (coincident sites?)");
-        return kErrNumeric;
-      }
-      if (!(rms[k] < tol_)) done = false;
-      log_msg(kVerbHigh, nullptr, "refinement step %3d set %d residual rms norm: %14.4E", outer, set0 + k, rms[k]);
-    }
-    if (done || outer >= max_outer) break;
-    // normalise each unconverged column to unit preconditioned rms; converged
-    // columns get a zero right-hand side (the inner CG leaves them at zero)
-    double worst_eta = 1e-5;
-    for (int k = 0; k < ncol; ++k) {
-      scal_h_[8 + k] = rms[k] < tol_ ? 0.0 : 1.0 / rms[k];
-      scal_h_[16 + k] = rms[k] < tol_ ? 0.0 : rms[k];
-      if (rms[k] >= tol_) worst_eta = std::max(worst_eta, std::min(1e-2, 0.3 * tol_ / rms[k]));
-    }
-    double eta = worst_eta;
-    cudaMemcpyAsync(dots_ + 8, scal_h_ + 8, 16 * sizeof(double), cudaMemcpyHostToDevice, st_);
-    for (int k = 0; k < ncol; ++k) gpu::launch_to_f32(nv, r_ + k * nv, dots_ + 8 + k, r32_ + k * nv, st_);
-    st = pcg32(ncol, nullptr, 200, eta);
-    if (st) return st;
-    gpu::launch_ir_accumulate(ncol, n, x, x32_, dots_ + 16, st_);
-    matvec64(kMatvDirect, ncol, x, h_, true);
-    gpu::launch_residual(ncol * nv, rhs, h_, r_, st_);
-    ++outer;
-  }
-  stats_.outer += outer;
-  for (int k = 0; k < ncol; ++k) stats_.iters[set0 + k] = outer;
-  if (!done) {
-    set_last_error("Iterative solver did not converged");
-    return kErrNotConverged;
-  }
-  return kOk;
 }
 
 int System::polarization(const double *e, int solver, int matv, const bool *mask_in) {

@@ -2,7 +2,9 @@
 // inversion, and the FP32-inner / FP64-refinement solver).
 #pragma once
 
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "kernels.h"
@@ -18,6 +20,29 @@ enum Status : int {
   kErrNumeric = 4,
   kErrCuda = 5,
   kErrMemory = 6,
+};
+
+// Column buffers of one solve: a view of a system's default two-column
+// buffers, or the batch buffers (grown on demand).  Columns are [cap][n][3].
+struct Workspace {
+  int cap = 0;
+  int fcap = 0;  // batch: fields the staging buffers hold
+  double *x = nullptr, *r = nullptr, *p = nullptr, *h = nullptr, *z = nullptr, *rhs = nullptr;
+  double *fields = nullptr, *out = nullptr;  // batch staging
+  float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *h32 = nullptr, *z32 = nullptr;
+  float *scratch32 = nullptr;
+  int scratch32_nsplit = 0;  // source splits the FP32 scratch holds for cap columns
+  double *partial = nullptr;  // kRedBlocks x cap
+  double *dots = nullptr;     // 3 x cap (+ fcap)
+  double *hist = nullptr;     // cap x maxhist, or none
+  gpu::CgCol *cols = nullptr;
+  gpu::CgCol *cols_h = nullptr;  // pinned
+  double *scal_h = nullptr;      // pinned 3 x cap (+ fcap)
+  bool owned = false;
+  // captured inner FP32 iteration (CUDA graph) and what it was built for
+  cudaGraphExec_t graph = nullptr;
+  int graph_ncol = -1, graph_gmax = 0, graph_nsplit = 0;
+  long long graph_kernels = 0;
 };
 
 struct SolveStats {
@@ -43,6 +68,11 @@ class System {
   int set_default_matv(int m);
 
   // --- extensions --------------------------------------------------------------
+  // nf independent fields solved together (cold start, system state untouched):
+  // fields [nf][n][3], out [nf][n_ipd][n][3] (device or host), energies [nf] host
+  int solve_batch(int nf, const double *fields_dev, double *out_dev, double *energies);
+  int solve_batch_host(int nf, const double *fields_host, double *out_host, double *energies);
+  void set_use_graphs(bool on) { use_graphs_ = on; }
   int tmatvec(const double *x_host, double *y_host, int nrhs, bool dodiag, int matv);
   int tmatvec_f32(const double *x_host, double *y_host, int nrhs);
   int e_m2d(double *out_host);
@@ -86,11 +116,20 @@ class System {
   int ensure_tmat();
   int polarization(const double *e_dev, int solver, int matv, const bool *mask);
   int matvec64(int matv, int ncol, const double *x, double *y, bool dodiag);
-  int cg64(int matv, int ncol, const double *rhs, double *x, int set0);
+  int cg64(int matv, int ncol, const double *rhs, double *x, int set0) { return cg64_ws(ws_, matv, ncol, rhs, x, set0); }
   int diis64(int matv, const double *rhs, double *x, int set);
   int inversion64(const double *rhs, double *x);
-  int mixed_ir(int ncol, const double *rhs, double *x, int set0, bool have_guess);
-  int pcg32(int ncol, double *rms0_out, int max_it, double eta);
+  int mixed_ir(int ncol, const double *rhs, double *x, int set0, bool have_guess) {
+    return mixed_ir_ws(ws_, ncol, rhs, x, set0, have_guess);
+  }
+  // solvers.cu: the same solvers on any workspace
+  int cg64_ws(Workspace &w, int matv, int ncol, const double *rhs, double *x, int set0);
+  int pcg32_ws(Workspace &w, int ncol, int max_it, double eta);
+  int mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, int set0, bool have_guess);
+  int tune_f32(Workspace &w, int ncol, int &gmax, int &nsplit);
+  void f32_product(Workspace &w, int ncol, int gmax, int nsplit);
+  int ensure_batch_ws(int ncol, int nf);
+  void free_ws(Workspace &w);
   int check(cudaError_t e, const char *what);
   int fetch_ipd();
 
@@ -151,6 +190,10 @@ class System {
   KEv kt_begin(int kind, int cols);
   void kt_end(KEv &e);
   void kt_resolve();
+  Workspace ws_;   // view of the default two-column buffers
+  Workspace wsb_;  // batch buffers
+  std::map<int, std::pair<int, int>> f32_tune_;  // columns -> (group width, source splits)
+  bool use_graphs_ = true;
   cudaEvent_t tev_[8] = {};
   void *flush_buf_ = nullptr;
   size_t flush_bytes_ = 0;

@@ -771,7 +771,7 @@ __global__ void k_to_f32(size_t n, const double *x, const double *scale, float *
 }
 
 __global__ void k_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps) {
-  int k = threadIdx.x;
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ncol) return;
   CgCol c = cols[k];
   if (!c.active) return;
@@ -822,9 +822,8 @@ __global__ void k_cg_update(int ncol, int n, T *x, T *r, const T *p, const T *h,
   }
 }
 
-__global__ void k_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double tol, double *hist,
-                          int hist_stride) {
-  int k = threadIdx.x;
+__global__ void k_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double *hist, int hist_stride) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ncol) return;
   CgCol c = cols[k];
   if (!c.active) return;
@@ -832,7 +831,7 @@ __global__ void k_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, doub
   c.rms = sqrt(c.gnew / (3.0 * n));
   c.iters += 1;
   if (hist && c.iters <= hist_stride) hist[(size_t)k * hist_stride + c.iters - 1] = c.rms;
-  if (c.rms < tol) {
+  if (c.rms < c.tol) {
     c.converged = 1;
     c.active = 0;
   } else {
@@ -973,6 +972,7 @@ inline int blocks_for(size_t n, int tpb, int cap = 4 * 152 * 4) {
 
 static std::atomic<long long> g_launches{0};
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void add_launch_count(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 double launch_fma_peak(bool fp64, int iters, void *out, cudaStream_t st) {
   int blocks = sm_count() * 8, threads = 256;
@@ -1067,40 +1067,40 @@ static void tmu_allpairs(const DevSites &s, const typename Vec4<T>::type *pos, c
     k_tmu<T, NRHS, false, KAHAN><<<grid, TPB, 0, st>>>(s.n, pos, damp, wa, x, partial, per, thr, thr2m);
 }
 
+// Columns per launch: the widest of 8/4/2/1 not above what is left and gmax.
+inline int column_group(int left, int gmax) {
+  int g = left < gmax ? left : gmax;
+  return g >= 8 ? 8 : (g >= 4 ? 4 : (g >= 2 ? 2 : 1));
+}
+
 template <typename T, bool KAHAN>
 static void tmu_dispatch(const DevSites &s, int nrhs, const typename Vec4<T>::type *pos, const T *damp,
-                         const T *x, T *partial, int nsplit, cudaStream_t st) {
-  // process the columns in groups sharing the pair geometry
+                         const T *x, T *partial, int nsplit, int gmax, cudaStream_t st) {
+  // process the columns in groups sharing the pair geometry; every group
+  // has its own [split][g][n][3] block of partials, one after the other
   int done = 0;
   while (done < nrhs) {
-    int left = nrhs - done;
+    int g = column_group(nrhs - done, gmax);
     size_t xo = (size_t)done * s.n * 3;
-    // partial layout is [split][rhs-group][n][3] per group; groups are laid
-    // out one after the other so k_tmu_finish sees [split][nrhs][n][3]
-    // only when a single group covers all columns.  Use per-group buffers.
     T *pg = partial + (size_t)nsplit * done * s.n * 3;
-    if (left >= 4) {
-      tmu_allpairs<T, 4, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st);
-      done += 4;
-    } else if (left >= 2) {
-      tmu_allpairs<T, 2, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st);
-      done += 2;
-    } else {
-      tmu_allpairs<T, 1, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st);
-      done += 1;
+    switch (g) {
+      case 8: tmu_allpairs<T, 8, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st); break;
+      case 4: tmu_allpairs<T, 4, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st); break;
+      case 2: tmu_allpairs<T, 2, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st); break;
+      default: tmu_allpairs<T, 1, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st); break;
     }
+    done += g;
   }
 }
 
 template <typename T>
 static void tmu_finish(const DevSites &s, int nrhs, int nsplit, const T *partial,
                        const typename Vec4<T>::type *pos, const T *damp, const T *x, bool dodiag, T *y,
-                       cudaStream_t st) {
-  // groups of (4|2|1) columns have their own [split][g][n][3] block
+                       int gmax, cudaStream_t st) {
+  // the same column groups as tmu_dispatch, each with its own block
   int done = 0;
   while (done < nrhs) {
-    int left = nrhs - done;
-    int g = left >= 4 ? 4 : (left >= 2 ? 2 : 1);
+    int g = column_group(nrhs - done, gmax);
     const T *pg = partial + (size_t)nsplit * done * s.n * 3;
     g_launches.fetch_add(1, std::memory_order_relaxed);
     dim3 grid((s.n + 127) / 128, g);
@@ -1122,8 +1122,8 @@ static void tmu_finish(const DevSites &s, int nrhs, int nsplit, const T *partial
 void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
                     int nsplit, cudaStream_t st) {
   if (s.n == 0) return;
-  tmu_dispatch<double, false>(s, nrhs, s.pol_pos, s.pol_a, x, scratch, nsplit, st);
-  tmu_finish<double>(s, nrhs, nsplit, scratch, s.pol_pos, s.pol_a, x, dodiag, y, st);
+  tmu_dispatch<double, false>(s, nrhs, s.pol_pos, s.pol_a, x, scratch, nsplit, 4, st);
+  tmu_finish<double>(s, nrhs, nsplit, scratch, s.pol_pos, s.pol_a, x, dodiag, y, 4, st);
 }
 
 namespace {
@@ -1198,10 +1198,47 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
 }
 
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch, int nsplit,
-                    cudaStream_t st) {
+                    cudaStream_t st, int gmax) {
   if (s.n == 0) return;
-  tmu_dispatch<float, true>(s, nrhs, s.pol_pos32, s.pol_a32, x, scratch, nsplit, st);
-  tmu_finish<float>(s, nrhs, nsplit, scratch, s.pol_pos32, s.pol_a32, x, true, y, st);
+  tmu_dispatch<float, true>(s, nrhs, s.pol_pos32, s.pol_a32, x, scratch, nsplit, gmax, st);
+  tmu_finish<float>(s, nrhs, nsplit, scratch, s.pol_pos32, s.pol_a32, x, true, y, gmax, st);
+}
+
+// Batched right-hand sides, set-major columns: rhs[s*nf + f] = E_M2D[s] + field[f]
+__global__ void k_batch_rhs(int n, int nf, int nset, const double *__restrict__ e_m2d,
+                            const double *__restrict__ fields, double *__restrict__ rhs) {
+  size_t nv = 3 * (size_t)n;
+  size_t tot = nv * nf * nset;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    size_t col = i / nv, e = i % nv;
+    size_t set = col / nf, f = col % nf;
+    rhs[i] = e_m2d[set * nv + e] + fields[f * nv + e];
+  }
+}
+
+// out[f][s][n][3] from set-major solution columns; with nsolved == 1 the P
+// set repeats the D column (identical systems)
+__global__ void k_batch_scatter(int n, int nf, int nipd, int nsolved, const double *__restrict__ x,
+                                double *__restrict__ out) {
+  size_t nv = 3 * (size_t)n;
+  size_t tot = nv * nf * nipd;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    size_t e = i % nv, rest = i / nv;
+    size_t set = rest % nipd, f = rest / nipd;
+    size_t src_set = nsolved == 1 ? 0 : set;
+    out[i] = x[(src_set * nf + f) * nv + e];
+  }
+}
+
+void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
+                      cudaStream_t st) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_batch_rhs<<<blocks_for((size_t)3 * n * nf * nset, 256), 256, 0, st>>>(n, nf, nset, e_m2d, fields, rhs);
+}
+
+void launch_batch_scatter(int n, int nf, int nipd, int nsolved, const double *x, double *out, cudaStream_t st) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  k_batch_scatter<<<blocks_for((size_t)3 * n * nf * nipd, 256), 256, 0, st>>>(n, nf, nipd, nsolved, x, out);
 }
 
 // ---- dense T ------------------------------------------------------------------
@@ -1279,7 +1316,7 @@ void launch_to_f32(size_t n, const double *x, const double *scale, float *y, cud
 }
 void launch_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps, cudaStream_t st) {
   g_launches.fetch_add(1, std::memory_order_relaxed);
-  k_cg_alpha<<<1, 128, 0, st>>>(ncol, dots, cols, eps);
+  k_cg_alpha<<<(ncol + 127) / 128, 128, 0, st>>>(ncol, dots, cols, eps);
 }
 void launch_cg_update(int ncol, int n, double *x, double *r, const double *p, const double *h, double *z,
                       const double *alpha_pol, const CgCol *cols, double *partial, cudaStream_t st) {
@@ -1291,10 +1328,10 @@ void launch_cg_update_f32(int ncol, int n, float *x, float *r, const float *p, c
   g_launches.fetch_add(1, std::memory_order_relaxed);
   k_cg_update<float><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, x, r, p, h, z, alpha_pol, cols, partial);
 }
-void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double tol, double *hist, int hist_stride,
+void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double *hist, int hist_stride,
                     cudaStream_t st) {
   g_launches.fetch_add(1, std::memory_order_relaxed);
-  k_cg_gnew<<<1, 128, 0, st>>>(ncol, n, dots, cols, tol, hist, hist_stride);
+  k_cg_gnew<<<(ncol + 127) / 128, 128, 0, st>>>(ncol, n, dots, cols, hist, hist_stride);
 }
 void launch_cg_pupdate(int ncol, int n, double *p, const double *z, const CgCol *cols, cudaStream_t st) {
   g_launches.fetch_add(1, std::memory_order_relaxed);

@@ -67,9 +67,15 @@ void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, boo
 size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs);
 void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
                         cudaStream_t st);
-// FP32 inner operator with compensated cross-tile sums; x,y float.
+// FP32 inner operator with compensated cross-tile sums; x,y float.  Columns
+// go through the pair kernel in groups of up to gmax (8, 4, 2 or 1) sharing
+// the pair geometry; scratch holds nsplit * nrhs * n * 3 floats.
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch,
-                    int nsplit, cudaStream_t st);
+                    int nsplit, cudaStream_t st, int gmax = 4);
+// batched fields: rhs[s*nf+f] = E_M2D[s] + field[f]; solution scatter to [f][s]
+void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
+                      cudaStream_t st);
+void launch_batch_scatter(int n, int nf, int nipd, int nsolved, const double *x, double *out, cudaStream_t st);
 
 // ---- dense T (incore matvec / inversion) ---------------------------------
 void launch_build_tmat(const DevSites &s, double *tmat, cudaStream_t st);  // [3n][3n] col-major
@@ -103,6 +109,8 @@ void launch_to_f32(size_t n, const double *x, const double *scale, float *y, cud
 // Multi-column PCG state kept on the device (one entry per column).
 struct CgCol {
   double gold, gama, alpha, gnew, rms, beta;
+  double tol;     // convergence threshold of this column (kept on the device
+                  // so that a captured iteration graph stays valid)
   int active;     // column still iterating
   int quick;      // left through |p.Tp| < eps
   int converged;  // rms < tol
@@ -114,8 +122,9 @@ void launch_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps, cuda
 void launch_cg_update(int ncol, int n, double *x, double *r, const double *p, const double *h,
                       double *z, const double *alpha_pol, const CgCol *cols, double *partial,
                       cudaStream_t st);
-void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double tol, double *hist,
-                    int hist_stride, cudaStream_t st);
+// gnew = (r.z)_k, rms, convergence against cols[k].tol, beta; history
+void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double *hist, int hist_stride,
+                    cudaStream_t st);
 void launch_cg_pupdate(int ncol, int n, double *p, const double *z, const CgCol *cols,
                        cudaStream_t st);
 // FP32 vectors, FP64 scalars (inner solver of the mixed-precision path)
@@ -144,8 +153,10 @@ void launch_any_diff(size_t n, const double *a, const double *b, int *flag, cuda
 
 // Number of SMs of the current device (cached).
 int sm_count();
-// Kernels launched by this library since load (all streams).
+// Kernels launched by this library since load (all streams); graph replays
+// add the kernels of the replayed graph.
 long long launch_count();
+void add_launch_count(long long k);
 // FMA-chain kernel for the FP32 / FP64 pipe peak; returns its flop count.
 double launch_fma_peak(bool fp64, int iters, void *out, cudaStream_t st);
 

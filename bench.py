@@ -50,11 +50,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="w30k", choices=["w30k", "w10k", "w1k", "b64"])
+    ap.add_argument("--config", default="w30k", choices=["w30k", "w10k", "w1k", "b64", "c60k", "s1024"])
     ap.add_argument("--skip-cpu", action="store_true", help="leave out the CPU baseline (profiling runs)")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--requests", type=int, default=1024, help="s1024: requests in the mixed stream")
+    ap.add_argument("--fp64-requests", type=int, default=64, help="s1024: requests in the FP64 stream")
+    ap.add_argument("--slots", type=int, default=8, help="s1024: concurrent requests on the GPU")
+    ap.add_argument("--hbm-budget-gib", type=float, default=4.0, help="s1024: device memory for systems")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "ommp_gb300_bench"))
     return ap.parse_args()
 
@@ -165,15 +169,38 @@ def run_reference(args):
     orc.build()
     path, _ = workload(args.config, args.cache)
     cores = os.cpu_count() or 1
-    # matrix-vector products per plain CG solve on this workload (D + P,
-    # counting the initial residual product the reference always evaluates)
-    mv_per_solve = {"w30k": 2 * (16 + 1) + 2, "w1k": 2 * (15 + 1) + 2}[args.config]
-    rows = args.cpu_rows or (1500 if args.config == "w30k" else 3000)
-    times = []
-    for k in range(args.warmup + args.steps):
-        sec_per_mv, nrows, n = cpu_sample(path, rows, cores)
-        if k >= args.warmup:
-            times.append(sec_per_mv * mv_per_solve)
+    if args.config in ("w1k", "w10k") and not args.cpu_rows:
+        # small boxes: whole solves (D + P, CG to 1e-10) on all host cores
+        orc.set_num_threads(cores)
+        o = orc.OracleSystem(path)
+        o.set_tol(1e-10)
+        n = o.pol_atoms
+        w = workload(args.config, args.cache)[1]
+        cmm = o.cmm
+        fl = fields_for(cmm[o.polar_mm], cmm, w.box_center(), [100 + k for k in range(args.warmup + args.steps)])
+        o.e_m2d()  # cached per geometry, as on the GPU side
+        times = []
+        for k, f in enumerate(fl):
+            o.clear_guess()
+            t0 = time.perf_counter()
+            o.set_external_field(f)
+            if k >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        nrows, mv_per_solve = n, o.matvec_count()
+        sample = f"whole solves, one per step ({mv_per_solve} T.mu products each)"
+    else:
+        # T.mu products of the plain CG solve of the 90,000-site box (D: 16
+        # iterations plus residual products; P equals D and converges at once),
+        # counted by the oracle's full solve of that box
+        mv_per_solve = {"w30k": 20, "b64": 20}.get(args.config, 20)
+        rows = args.cpu_rows or 1500
+        times = []
+        for k in range(args.warmup + args.steps):
+            sec_per_mv, nrows, n = cpu_sample(path, rows, cores)
+            if k >= args.warmup:
+                times.append(sec_per_mv * mv_per_solve)
+        sample = (f"{nrows} of {n} target rows of one T.mu product per step, scaled by {n}/{nrows} rows "
+                  f"and {mv_per_solve} products per solve")
     v = 1.0 / statistics.mean(times)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
@@ -181,8 +208,7 @@ def run_reference(args):
             "config": {"workload": f"water box {args.config}: {n} AMOEBA sites, 30-charge field, "
                                    "CG tol 1e-10, direct matvec", "sites": n},
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"{nrows} of {n} target rows of one T.mu product per step, "
-                                       f"scaled by {n}/{nrows} rows and {mv_per_solve} products per solve"},
+                             "sample": sample},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -370,6 +396,61 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def run_c60k(args):
+    """Precision configuration: 60,000-site Wang-AL chain system (150 chains of
+    200 sites in 10,000 waters), mixed precision against plain FP64, with the
+    relative error of each result."""
+    import openmmpol_gb300 as og
+    from openmmpol_gb300 import build as b
+    from openmmpol_gb300 import synth
+    b.build()
+    og.set_verbose(0)
+    os.makedirs(args.cache, exist_ok=True)
+    path = os.path.join(args.cache, "chains_150x200_w10000_seed3.mmp")
+    c = synth.chain_system(seed=3)
+    if not os.path.exists(path):
+        synth.write_mmp(path + ".tmp", c)
+        os.replace(path + ".tmp", path)
+    s = og.OMMPSystem(path)
+    s.set_solver_tol(1e-10)
+    n = s.pol_atoms
+    ef = fields_for(s.cpol, s.cmm, c.box_center(), [7])[0]
+    t0 = time.perf_counter()
+    e_m2d = s.e_m2d()
+    m2d_s = time.perf_counter() - t0
+    res = {}
+    for prec in ("fp64", "mixed"):
+        s.set_precision(prec)
+        times = []
+        for k in range(args.warmup + args.steps):
+            s.clear_guess()
+            t0 = time.perf_counter()
+            s.set_external_field(ef)
+            if k >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        res[prec] = {"ipd": s.ipd, "energy": s.get_polelec_energy(), "s_per_solve": statistics.mean(times),
+                     "iterations": [s.iterations(0)], "t_mu_fp64": s.counter(0), "t_mu_fp32": s.counter(1),
+                     "residual_history": [float(x) for x in s.residual_history(0)]}
+    r64, rmx = res["fp64"], res["mixed"]
+    err_ipd = float(np.linalg.norm(rmx["ipd"] - r64["ipd"]) / np.linalg.norm(r64["ipd"]))
+    err_max = float(np.abs(rmx["ipd"] - r64["ipd"]).max() / np.abs(r64["ipd"]).max())
+    err_e = float(abs(rmx["energy"] - r64["energy"]) / abs(r64["energy"]))
+    line = {"metric": "induced-dipole solves/s, Wang-AL chain system (mixed vs FP64)",
+            "value": 1.0 / rmx["s_per_solve"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * rmx["s_per_solve"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
+            "config": {"workload": f"{n} sites: 150 self-avoiding chains x 200 sites (1.53 A bonds, "
+                                   "charges U(-0.6,0.6), alpha U(0.4,1.5) A^3, 1-2/1-3 exclusions) in 10,000 "
+                                   "waters, Wang-AL linear Thole, 30-charge field, RMS 1e-10", "sites": n},
+            "fp64_solves_per_s": 1.0 / r64["s_per_solve"], "speedup_mixed_over_fp64":
+                r64["s_per_solve"] / rmx["s_per_solve"], "m2d_s": m2d_s,
+            "errors_mixed_vs_fp64": {"field": 0.0, "field_note": "E_M2D + external field is FP64 in both modes",
+                                     "dipoles_rel_l2": err_ipd, "dipoles_rel_max": err_max, "energy_rel": err_e},
+            "fp64": {k: v for k, v in r64.items() if k != "ipd"},
+            "mixed": {k: v for k, v in rmx.items() if k != "ipd"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_b64(args):
     """64 right-hand sides on the 90,000-site box in one batched solve."""
     import ctypes as C
@@ -467,12 +548,204 @@ def run_b64(args):
     L.ommp_gpu_device_free(od)
 
 
+def serve_pool(cache, levels=32):
+    """Water clusters for the request stream: `levels` sizes spaced
+    geometrically over 300..60,000 molecules (seed = size), cached as .mmp
+    files with their coordinates; a request's log-uniform size maps to the
+    nearest level (at most 9 % away for 32 levels)."""
+    from openmmpol_gb300 import synth
+    os.makedirs(cache, exist_ok=True)
+    sizes = sorted(set(int(round(x)) for x in np.exp(np.linspace(np.log(300), np.log(60000), levels))))
+    pool = {}
+    for nw in sizes:
+        path = os.path.join(cache, f"water_{nw}_seed{nw}.mmp")
+        xyz = path + ".xyz.npy"
+        if not (os.path.exists(path) and os.path.exists(xyz)):
+            w = synth.water_cluster(nw, seed=nw)
+            synth.write_mmp(path + ".tmp", w)
+            np.save(xyz + ".tmp.npy", w.coords)
+            os.replace(path + ".tmp", path)
+            os.replace(xyz + ".tmp.npy", xyz)
+        c = np.load(xyz)
+        pool[nw] = {"path": path, "cpol": c * synth.ANG2AU,
+                    "center": 0.5 * (c.min(axis=0) + c.max(axis=0))}
+    return sizes, pool
+
+
+def serve_plan(nreq, sizes, seed=2024, followup_frac=0.3):
+    """Request k: a new cluster (log-uniform size, field of 30 fresh charges
+    with seed 10000 + k) or, with probability 0.3, a follow-up SCF iteration
+    on one of the 4 previous requests (its field times 1 + 0.01 N(0,1) per
+    component, warm start from its dipoles)."""
+    rng = np.random.default_rng(seed)
+    logs = np.log(np.array(sizes, dtype=float))
+    plan = []
+    for k in range(nreq):
+        if k > 0 and rng.random() < followup_frac:
+            plan.append({"parent": int(k - 1 - rng.integers(0, min(4, k)))})
+        else:
+            nw = float(np.exp(rng.uniform(np.log(300), np.log(60000))))
+            plan.append({"parent": None, "size": int(sizes[int(np.argmin(np.abs(logs - np.log(nw))))]),
+                         "drawn": int(round(nw))})
+    for k, p in enumerate(plan):  # resolve follow-up chains to their cluster
+        if p["parent"] is not None:
+            p["size"] = plan[p["parent"]]["size"]
+    return plan
+
+
+def serve_stream(srv, plan, pool, rate, keep, seed=77):
+    """Run the plan through the server with Poisson arrivals at `rate`
+    requests/s (None: all at t = 0).  A follow-up is submitted when both its
+    arrival time has passed and its parent is done (the next SCF iteration
+    needs the previous dipoles).  Returns per-request records and the wall
+    time from the first arrival to the last completion."""
+    import threading
+
+    from openmmpol_gb300 import OMMPError, synth
+    n = len(plan)
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n) if rate else np.zeros(n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    done = [threading.Event() for _ in range(n)]
+    out = [None] * n
+    errors = []
+    t0 = time.perf_counter() + 0.05
+
+    def one(k):
+        p = plan[k]
+        try:
+            g = pool[p["size"]]
+            nipd = 2
+            if p["parent"] is None:
+                field, _, _ = synth.point_charge_field(g["cpol"], g["center"], seed=10000 + k)
+            dt = t0 + arrivals[k] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            readmit = False
+            if p["parent"] is not None:
+                done[p["parent"]].wait()
+                par = out[p["parent"]]
+                r2 = np.random.default_rng(10000 + k)
+                field = par["field"] * (1.0 + 0.01 * r2.standard_normal(par["field"].shape))
+                try:
+                    r = srv.wait(srv.submit_followup(par["instance"], field, nipd))
+                except OMMPError as e:
+                    if e.status != 3:
+                        raise
+                    readmit = True  # the parent's system was evicted: new instance, cold start
+                    r = srv.wait(srv.submit(g["path"], field, nipd))
+            else:
+                r = srv.wait(srv.submit(g["path"], field, nipd))
+            out[k] = {"instance": r["instance"], "field": field, "latency_ms": r["latency_ms"],
+                      "energy": r["energy"], "ipd": r["ipd"] if k in keep else None,
+                      "sites": 3 * p["size"], "followup": p["parent"] is not None, "readmit": readmit,
+                      "t_done": time.perf_counter()}
+        except Exception as ex:  # recorded and reported
+            errors.append(f"request {k}: {ex!r}")
+            out[k] = {"instance": -1, "field": np.zeros((3 * p["size"], 3)), "latency_ms": float("nan"),
+                      "energy": float("nan"), "ipd": None, "sites": 3 * p["size"],
+                      "followup": p["parent"] is not None, "readmit": False, "t_done": time.perf_counter()}
+        finally:
+            done[k].set()
+
+    th = [threading.Thread(target=one, args=(k,), daemon=True) for k in range(n)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    wall = max(o["t_done"] for o in out) - t0
+    return out, wall, errors
+
+
+def run_s1024(args):
+    """Serving: a stream of requests (new water clusters of log-uniform size
+    and follow-up SCF iterations) through the request server, mixed precision
+    against plain FP64: throughput at saturation, p50/p99 latency at 70 % of
+    it, and the relative error of each common result."""
+    import openmmpol_gb300 as og
+    from openmmpol_gb300 import _lib
+    from openmmpol_gb300 import build as b
+    b.build()
+    L = _lib.load()
+    og.set_verbose(0)
+    sizes, pool = serve_pool(os.path.join(args.cache, "serve"))
+    nreq, n64 = args.requests, min(args.fp64_requests, args.requests)
+    plan = serve_plan(nreq, sizes)
+    keep = set(range(n64))
+    budget = int(args.hbm_budget_gib * (1 << 30))
+    res = {}
+    clk = Clocks(0)
+    l0 = L.ommp_gpu_kernel_launch_count()
+    for prec, nr in (("mixed", nreq), ("fp64", n64)):
+        pl = plan[:nr]
+        r = {}
+        for phase in ("saturation", "load70"):
+            rate = None if phase == "saturation" else 0.7 * r["saturation"]["requests_per_s"]
+            srv = og.Server(budget, slots=args.slots, precision=prec, tol=1e-10)
+            out, wall, errors = serve_stream(srv, pl, pool, rate, keep)
+            st = srv.stats()
+            srv.close()
+            lat = np.array([o["latency_ms"] for o in out if np.isfinite(o["latency_ms"])])
+            lat_new = np.array([o["latency_ms"] for o in out if not o["followup"] and np.isfinite(o["latency_ms"])])
+            lat_fu = np.array([o["latency_ms"] for o in out if o["followup"] and np.isfinite(o["latency_ms"])])
+            pct = lambda a, q: float(np.percentile(a, q)) if len(a) else None
+            r[phase] = {"requests": nr, "rate_offered": rate, "wall_s": wall, "requests_per_s": nr / wall,
+                        "sites_per_s": sum(o["sites"] for o in out) / wall,
+                        "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+                        "p50_new_ms": pct(lat_new, 50), "p99_new_ms": pct(lat_new, 99),
+                        "p50_followup_ms": pct(lat_fu, 50), "p99_followup_ms": pct(lat_fu, 99),
+                        "followups": int(sum(o["followup"] for o in out)),
+                        "readmitted_followups": int(sum(o["readmit"] for o in out)),
+                        "evictions": int(st["evictions"]), "peak_concurrent": int(st["peak_concurrent"]),
+                        "peak_bytes": int(st["peak_bytes"]), "errors": errors[:5], "n_errors": len(errors)}
+            if phase == "saturation":
+                r["results"] = {k: (out[k]["ipd"], out[k]["energy"]) for k in keep if k < nr}
+        res[prec] = r
+    clocks = clk.stop()
+    launches = L.ommp_gpu_kernel_launch_count() - l0
+    err_ipd, err_e = [], []
+    for k in range(n64):
+        a, ea = res["mixed"]["results"][k]
+        f, ef = res["fp64"]["results"][k]
+        if a is None or f is None:
+            continue
+        err_ipd.append(float(np.linalg.norm(a - f) / np.linalg.norm(f)))
+        err_e.append(float(abs(ea - ef) / abs(ef)))
+    for prec in res:
+        res[prec].pop("results")
+    mx, f64 = res["mixed"], res["fp64"]
+    line = {"metric": "served induced-dipole solves/s + p50/p99 latency (mixed vs FP64, <=1e-7 rel. error)",
+            "value": mx["saturation"]["requests_per_s"], "unit": "solves/s", "n_gpus": 1,
+            "steps": nreq, "warmup": 0, "ms_per_step": 1e3 / mx["saturation"]["requests_per_s"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64",
+            "data": "synthetic",
+            "config": {"workload": f"{nreq} requests: AMOEBA water clusters of log-uniform 300..60,000 molecules "
+                                   f"({len(sizes)} cached geometries), 30-charge field per new request, 30 % "
+                                   "follow-ups (field x (1 + 0.01 N(0,1)), warm start), D+P to RMS 1e-10",
+                       "hbm_budget_gib": args.hbm_budget_gib, "slots": args.slots,
+                       "fp64_requests": n64, "arrivals": "all at t=0 (saturation), then Poisson at 70 % "
+                                                         "of the saturation rate"},
+            "p50_ms": mx["load70"]["p50_ms"], "p99_ms": mx["load70"]["p99_ms"],
+            "mixed": mx, "fp64": f64,
+            "speedup_mixed_over_fp64_saturation": (mx["saturation"]["sites_per_s"] /
+                                                   f64["saturation"]["sites_per_s"]),
+            "errors_mixed_vs_fp64": {"requests_compared": len(err_ipd),
+                                     "dipoles_rel_l2_max": max(err_ipd) if err_ipd else None,
+                                     "energy_rel_max": max(err_e) if err_e else None},
+            "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.config == "b64":
         run_b64(args)
+    elif args.config == "c60k":
+        run_c60k(args)
+    elif args.config == "s1024":
+        run_s1024(args)
     else:
         run_gb300(args)
 

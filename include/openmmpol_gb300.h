@@ -64,6 +64,7 @@
 #define OMMP_GPU_ERR_NUMERIC 4
 #define OMMP_GPU_ERR_CUDA 5
 #define OMMP_GPU_ERR_MEMORY 6
+#define OMMP_GPU_ERR_CANCELLED 7
 
 typedef void *OMMP_SYSTEM_PRT;
 
@@ -215,6 +216,36 @@ int32_t ommp_gpu_copy_to_host(void *dst, const void *src, int64_t bytes);
 int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops);
 /* SM count of the current device, 0 without a GPU */
 int32_t ommp_gpu_device_sm_count(void);
+
+/* ---- request server (no counterpart in the reference) -------------------
+ * Continuous admission of solves on one GPU: `slots` worker threads each run
+ * one request at a time on its system's own CUDA stream (solves of different
+ * systems overlap on the device); a request starts as soon as a slot is free
+ * and its device memory fits `hbm_budget_bytes`, idle systems being evicted
+ * least-recently-used first.  ommp_gpu_server_submit reads a new system from
+ * a .mmp file (host setup, upload, E_M2D, solve); _submit_followup solves a
+ * new field on a resident instance warm-started from its last dipoles
+ * (follow-ups on one instance run in submission order).  _wait blocks until
+ * the request is done and returns its dipoles [n_ipd][pol_atoms][3], its
+ * polarization energy, the instance id (for follow-ups) and the latency from
+ * submission to completion.  _stats fills 7 numbers: device bytes in use,
+ * peak bytes, resident instances, evictions, peak concurrent requests,
+ * completed requests, budget.  _cancel removes a request that is still
+ * queued (its _wait then returns OMMP_GPU_ERR_CANCELLED) and returns
+ * OMMP_GPU_ERR_BAD_ARG for one that is running, done or unknown.  Destroy
+ * the server after waiting for every submitted request. */
+int32_t ommp_gpu_server_create(int64_t hbm_budget_bytes, int32_t slots, int32_t precision, double tol,
+                               void **server);
+void ommp_gpu_server_destroy(void *server);
+int32_t ommp_gpu_server_submit(void *server, const char *mmp_path, const double *field, int32_t pol_atoms,
+                               int64_t *request_id);
+int32_t ommp_gpu_server_submit_followup(void *server, int64_t instance, const double *field,
+                                        int32_t pol_atoms, int64_t *request_id);
+int32_t ommp_gpu_server_wait(void *server, int64_t request_id, double *ipd_out, double *energy,
+                             int64_t *instance, double *latency_ms);
+void ommp_gpu_server_release(void *server, int64_t instance);
+int32_t ommp_gpu_server_cancel(void *server, int64_t request_id);
+void ommp_gpu_server_stats(void *server, double *out7);
 
 /* No counterpart in the reference.  y = T x (dodiag = 1) or y = -E_dd(x)
  * (dodiag = 0) for nrhs (1|2) columns [nrhs][pol_atoms][3], with x and y in

@@ -13,7 +13,7 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ["OMMPSystem", "OMMPError", "available_solvers", "available_matrix_vector",
+__all__ = ["OMMPSystem", "Server", "OMMPError", "available_solvers", "available_matrix_vector",
            "set_verbose", "PREC_FP64", "PREC_MIXED"]
 
 # pythonapi/pyopenmmpol/pyommp_interface.cpp:9-23
@@ -22,6 +22,7 @@ available_solvers = {"none": 0, "default": 1, "conjugate gradient": 1, "cg": 1,
 available_matrix_vector = {"none": 0, "default": 2, "incore": 1, "direct": 2}
 verbosity = {"none": 0, "low": 1, "high": 2, "debug": 3}
 PREC_FP64, PREC_MIXED = 0, 1
+ERR_CANCELLED = 7
 
 
 class OMMPError(RuntimeError):
@@ -234,3 +235,67 @@ class OMMPSystem:
 
     def synchronize(self) -> None:
         _check(self._L.ommp_gpu_synchronize(self._h))
+
+
+class Server:
+    """Request server over ommp_gpu_server_* (continuous admission of solves).
+
+    ``submit(path, field)`` starts a new system; ``submit_followup(instance,
+    field)`` reuses a resident one with a warm start; ``wait(rid)`` returns a
+    dict with ``ipd``, ``energy``, ``instance`` and ``latency_ms``.
+    """
+
+    def __init__(self, hbm_budget_bytes: int, slots: int = 4, precision="mixed", tol: float = 1e-10):
+        self._L = _lib.load()
+        p = {"fp64": PREC_FP64, "mixed": PREC_MIXED}.get(precision, precision)
+        h = C.c_void_p()
+        _check(self._L.ommp_gpu_server_create(int(hbm_budget_bytes), int(slots), int(p), float(tol), C.byref(h)))
+        self._h = h
+        self._meta = {}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.ommp_gpu_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, mmp_path: str, field, n_ipd: int) -> int:
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        rid = C.c_int64(0)
+        _check(self._L.ommp_gpu_server_submit(self._h, str(mmp_path).encode(), f.ctypes.data_as(_lib._dp),
+                                              f.shape[0], C.byref(rid)))
+        self._meta[rid.value] = (f.shape[0], n_ipd)
+        return rid.value
+
+    def submit_followup(self, instance: int, field, n_ipd: int) -> int:
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        rid = C.c_int64(0)
+        _check(self._L.ommp_gpu_server_submit_followup(self._h, int(instance), f.ctypes.data_as(_lib._dp),
+                                                       f.shape[0], C.byref(rid)))
+        self._meta[rid.value] = (f.shape[0], n_ipd)
+        return rid.value
+
+    def wait(self, rid: int) -> dict:
+        npol, nipd = self._meta.pop(rid)
+        out = np.zeros((nipd, npol, 3))
+        e = C.c_double(0)
+        inst = C.c_int64(-1)
+        lat = C.c_double(0)
+        _check(self._L.ommp_gpu_server_wait(self._h, int(rid), out.ctypes.data_as(_lib._dp), C.byref(e),
+                                            C.byref(inst), C.byref(lat)))
+        return {"ipd": out, "energy": e.value, "instance": inst.value, "latency_ms": lat.value}
+
+    def release(self, instance: int) -> None:
+        self._L.ommp_gpu_server_release(self._h, int(instance))
+
+    def cancel(self, rid: int) -> bool:
+        """True when the request was still queued and is now cancelled."""
+        return self._L.ommp_gpu_server_cancel(self._h, int(rid)) == 0
+
+    def stats(self) -> dict:
+        o = np.zeros(7)
+        self._L.ommp_gpu_server_stats(self._h, o.ctypes.data_as(_lib._dp))
+        keys = ["bytes_in_use", "peak_bytes", "resident", "evictions", "peak_concurrent", "completed", "budget"]
+        return dict(zip(keys, o.tolist()))

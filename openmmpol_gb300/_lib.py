@@ -84,6 +84,14 @@ SIGNATURES = {
     "ommp_gpu_measure_pipe_peak": (C.c_int32, [C.c_int32, _dp]),
     "ommp_gpu_device_sm_count": (C.c_int32, []),
     "ommp_gpu_tmatvec_noalloc": (C.c_int32, [_vp, _vp, _vp, C.c_int32, C.c_int32]),
+    "ommp_gpu_server_create": (C.c_int32, [C.c_int64, C.c_int32, C.c_int32, C.c_double, C.POINTER(_vp)]),
+    "ommp_gpu_server_destroy": (None, [_vp]),
+    "ommp_gpu_server_submit": (C.c_int32, [_vp, C.c_char_p, _dp, C.c_int32, _i64p]),
+    "ommp_gpu_server_submit_followup": (C.c_int32, [_vp, C.c_int64, _dp, C.c_int32, _i64p]),
+    "ommp_gpu_server_wait": (C.c_int32, [_vp, C.c_int64, _dp, _dp, _i64p, _dp]),
+    "ommp_gpu_server_release": (None, [_vp, C.c_int64]),
+    "ommp_gpu_server_cancel": (C.c_int32, [_vp, C.c_int64]),
+    "ommp_gpu_server_stats": (None, [_vp, _dp]),
 }
 
 _lib = None

@@ -20,7 +20,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libommp_gb300.so")
 
 CU_SOURCES = ["kernels.cu", "engine.cu", "solvers.cu", "noalloc.cu"]
-CXX_SOURCES = ["setup.cpp", "capi.cpp", "log.cpp"]
+CXX_SOURCES = ["setup.cpp", "capi.cpp", "log.cpp", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -23,7 +23,7 @@
 namespace ommp {
 
 namespace {
-std::string g_last_error;
+thread_local std::string g_last_error;  // per host thread (the server runs workers)
 constexpr size_t kMaxDenseBytes = size_t(24) << 30;  // incore T / inversion budget
 
 template <typename T>
@@ -72,6 +72,18 @@ System::~System() {
 }
 
 System *System::from_mmp(const std::string &path, std::string &err, int &status) {
+  System *s = load_host(path, err, status);
+  if (!s) return nullptr;
+  status = s->attach_device();
+  if (status != kOk) {
+    err = last_error();
+    delete s;
+    return nullptr;
+  }
+  return s;
+}
+
+System *System::load_host(const std::string &path, std::string &err, int &status) {
   System *s = new System();
   if (!read_mmp(path, s->m_, err) || !prepare_model(s->m_, err)) {
     status = kErrInput;
@@ -84,13 +96,27 @@ System *System::from_mmp(const std::string &path, std::string &err, int &status)
     log_msg(kVerbHigh, nullptr,
             "More than 1000 MM atoms: the reference would enable FMM here; this library "
             "always evaluates the direct sums.");
-  status = s->upload_static();
-  if (status != kOk) {
-    err = last_error();
-    delete s;
-    return nullptr;
-  }
+  status = kOk;
   return s;
+}
+
+int System::attach_device() { return upload_static(); }
+
+size_t System::device_bytes_estimate() const {
+  const size_t n = m_.npol, m = m_.mm, nv = 3 * n, nipd = m_.n_ipd;
+  const size_t nm2d = m2d_pairs_.src.size(), nd2d = d2d_pairs_.src.size();
+  gpu::DevSites d;
+  d.n = (int)n;
+  d.m = (int)m;
+  int sms = gpu::sm_count();
+  size_t s32 = gpu::tmu_scratch_doubles(d, 2, 2 * gpu::tmu_pick_split(d, 2, sms, true));
+  size_t s64 = std::max(gpu::m2d_scratch_doubles(d, gpu::m2d_pick_split(d, sms)),
+                        gpu::tmu_scratch_doubles(d, 2, gpu::tmu_pick_split(d, 2, sms, false)));
+  size_t sym = n >= 2048 ? gpu::tmu_sym_scratch_doubles(d, 2) : 0;
+  size_t bytes = 8 * (6 * n + 5 * m + m * m_.ld_cart + 2 * nm2d + nd2d + nv * (2 * nipd + 3 + 10)) +
+                 4 * (9 * n + 2 * m + 10 * nv + 2 * (n + 1) + nm2d + nd2d) + 4 * s32 + 8 * s64 + 8 * sym +
+                 8 * (gpu::kRedBlocks * 32 + 64 + 2 * (size_t)maxhist_);
+  return bytes + (size_t(4) << 20);  // events, flags, rounding
 }
 
 int System::upload_static() {

@@ -20,6 +20,7 @@ enum Status : int {
   kErrNumeric = 4,
   kErrCuda = 5,
   kErrMemory = 6,
+  kErrCancelled = 7,
 };
 
 // Column buffers of one solve: a view of a system's default two-column
@@ -58,6 +59,11 @@ class System {
  public:
   ~System();
   static System *from_mmp(const std::string &path, std::string &err, int &status);
+  // two-phase creation for admission control: parse and set up on the host,
+  // then (once memory is granted) allocate and upload the device arrays
+  static System *load_host(const std::string &path, std::string &err, int &status);
+  int attach_device();
+  size_t device_bytes_estimate() const;
 
   // --- reference API semantics -------------------------------------------------
   int set_external_field(const double *ext_host, int solver, int matv, bool add_mm);

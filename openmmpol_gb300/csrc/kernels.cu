@@ -985,14 +985,16 @@ double launch_fma_peak(bool fp64, int iters, void *out, cudaStream_t st) {
 }
 
 int sm_count() {
-  static int cached = 0;
-  if (!cached) {
+  static std::atomic<int> cached{0};  // read by several server threads
+  int v = cached.load(std::memory_order_relaxed);
+  if (!v) {
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
-    if (cached <= 0) cached = 152;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    if (v <= 0) v = 152;
+    cached.store(v, std::memory_order_relaxed);
   }
-  return cached;
+  return v;
 }
 
 // ---- M2D -----------------------------------------------------------------

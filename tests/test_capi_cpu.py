@@ -61,3 +61,25 @@ def test_missing_library_fails_loudly(tmp_path):
             _lib.load(str(tmp_path / "nope.so"))
         finally:
             _lib._lib = saved
+
+
+def test_server_host_admission_without_gpu(lib_path, tmp_path, golden_mmp):
+    """Server bookkeeping that needs no device: argument checks, a file that
+    does not parse, and a system larger than the whole budget are refused
+    (host setup only; nothing is allocated on a device)."""
+    from openmmpol_gb300 import OMMPError, Server, _lib
+    _lib.load(lib_path)
+    with pytest.raises(OMMPError):
+        Server(0, slots=1)
+    with pytest.raises(OMMPError):
+        Server(1 << 20, slots=0)
+    srv = Server(4096, slots=2, precision="mixed")
+    with pytest.raises(OMMPError, match="mmp|open|read"):
+        srv.wait(srv.submit(str(tmp_path / "missing.mmp"), [[0.0, 0.0, 0.0]], 1))
+    import numpy as np
+    with pytest.raises(OMMPError, match="budget"):
+        srv.wait(srv.submit(golden_mmp["nma_amoeba"], np.zeros((18, 3)), 2))
+    assert not srv.cancel(12345)  # unknown request
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == 2 and st["resident"] == 0 and st["bytes_in_use"] == 0

@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--fp32-kernel", default="auto", choices=["auto", "pairwise", "tiled"],
+                    help="FP32 inner T.mu kernel (auto = autotuned)")
     ap.add_argument("--requests", type=int, default=1024, help="s1024: requests in the mixed stream")
     ap.add_argument("--fp64-requests", type=int, default=64, help="s1024: requests in the FP64 stream")
     ap.add_argument("--slots", type=int, default=8, help="s1024: concurrent requests on the GPU")
@@ -232,6 +234,7 @@ def run_gb300(args):
     path, w = workload(args.config, args.cache)
     sys_ = og.OMMPSystem(path)
     sys_.set_solver_tol(1e-10)
+    sys_.set_fp32_kernel(args.fp32_kernel)
     n = sys_.pol_atoms
     cpol, cmm = sys_.cpol, sys_.cmm
     center = w.box_center()

@@ -155,6 +155,10 @@ void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode);
 /* FP64 direct T.mu kernel: 0 auto (symmetric from 2048 sites), 1 all ordered
  * pairs, 2 symmetric (each unordered pair once, deterministic) */
 int32_t ommp_gpu_set_fp64_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
+/* FP32 inner T.mu kernel: 0 autotuned (default), 1 one target per thread
+ * with a per-pair damping test, 2 tile-classified (undamped inner loop for
+ * tiles beyond the damping range, two targets per thread) */
+int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
 /* forget the last dipoles as a starting guess */
 void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s);
 /* capture the inner FP32 iteration as a CUDA graph (default on) */

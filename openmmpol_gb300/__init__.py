@@ -181,6 +181,11 @@ class OMMPSystem:
         m = {"auto": 0, "ordered": 1, "symmetric": 2}.get(mode, mode)
         _check(self._L.ommp_gpu_set_fp64_kernel(self._h, int(m)))
 
+    def set_fp32_kernel(self, mode) -> None:
+        """'auto' (autotuned) | 'pairwise' (kernel 1) | 'tiled' (kernel 2)."""
+        m = {"auto": 0, "pairwise": 1, "tiled": 2}.get(mode, mode)
+        _check(self._L.ommp_gpu_set_fp32_kernel(self._h, int(m)))
+
     def clear_guess(self) -> None:
         self._L.ommp_gpu_clear_guess(self._h)
 

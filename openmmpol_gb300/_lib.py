@@ -58,6 +58,7 @@ SIGNATURES = {
     "ommp_gpu_set_solver_maxiter": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_precision": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_fp64_kernel": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_set_fp32_kernel": (C.c_int32, [_vp, C.c_int32]),
     "ommp_gpu_set_use_graphs": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_external_fields_batch": (C.c_int32, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ommp_gpu_set_external_fields_batch_device": (C.c_int32, [_vp, C.c_int32, _vp, _vp, _dp]),

@@ -19,7 +19,9 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libommp_gb300.so")
 
-CU_SOURCES = ["kernels.cu", "engine.cu", "solvers.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "engine.cu", "solvers.cu", "noalloc.cu", "tmu32.cu"]
+# per-file nvcc flags: the FP32 operator flushes subnormals (plain MUFU rsqrt)
+CU_EXTRA = {"tmu32.cu": ["-ftz=true"]}
 CXX_SOURCES = ["setup.cpp", "capi.cpp", "log.cpp", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -63,6 +65,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         if force or _stale(o, [s] + headers):
             cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                    "-Xcompiler", "-ffp-contract=off", "-c", s, "-o", o]
+            cmd[1:1] = CU_EXTRA.get(src, [])
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

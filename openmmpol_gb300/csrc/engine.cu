@@ -52,7 +52,7 @@ System::~System() {
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
                   alpha32_, scratch_, scratch32_, partial_, dots_, hist_, cols_, flag_, tmat_, piv_,
-                  info_, diis_x_, diis_e_};
+                  info_, diis_x_, diis_e_, d_.tile_box32};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (flush_buf_) cudaFree(flush_buf_);
@@ -109,7 +109,7 @@ size_t System::device_bytes_estimate() const {
   d.n = (int)n;
   d.m = (int)m;
   int sms = gpu::sm_count();
-  size_t s32 = gpu::tmu_scratch_doubles(d, 2, 2 * gpu::tmu_pick_split(d, 2, sms, true));
+  size_t s32 = gpu::tmu_scratch_doubles(d, 2, gpu::tmu32_max_split(d, sms)) + 8 * ((n + 127) / 128);
   size_t s64 = std::max(gpu::m2d_scratch_doubles(d, gpu::m2d_pick_split(d, sms)),
                         gpu::tmu_scratch_doubles(d, 2, gpu::tmu_pick_split(d, 2, sms, false)));
   size_t sym = n >= 2048 ? gpu::tmu_sym_scratch_doubles(d, 2) : 0;
@@ -133,7 +133,9 @@ int System::upload_static() {
   int sms = gpu::sm_count();
   nsplit_m2d_ = gpu::m2d_pick_split(d_, sms);
   nsplit_tmu_ = gpu::tmu_pick_split(d_, 2, sms, false);
-  nsplit_tmu32_ = gpu::tmu_pick_split(d_, 2, sms, true);
+  nsplit_tmu32_ = gpu::tmu32_pick_split(d_, sms);
+  const int f32_splits = gpu::tmu32_max_split(d_, sms);
+  d_.ntile = (n + 127) / 128;
   size_t nv = 3 * (size_t)n;
   int nipd = m.n_ipd;
   int bad = 0;
@@ -151,7 +153,8 @@ int System::upload_static() {
          dalloc(z32_, nv * 2);
   scratch_n_ = std::max(gpu::m2d_scratch_doubles(d_, nsplit_m2d_), gpu::tmu_scratch_doubles(d_, 2, nsplit_tmu_));
   // FP32 scratch for twice the default source split (the autotuner tries both)
-  bad |= dalloc(scratch_, scratch_n_) | dalloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, 2 * nsplit_tmu32_));
+  bad |= dalloc(scratch_, scratch_n_) | dalloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, f32_splits));
+  bad |= dalloc(d_.tile_box32, 2 * (size_t)d_.ntile);
   bad |= dalloc(partial_, (size_t)gpu::kRedBlocks * 32) | dalloc(dots_, 64) | dalloc(hist_, 2 * (size_t)maxhist_);
   bad |= dalloc(cols_, 2) | dalloc(flag_, 1) | dalloc(info_, 1);
   if (bad || cudaMallocHost((void **)&cols_h_, 2 * sizeof(gpu::CgCol)) != cudaSuccess ||
@@ -163,7 +166,7 @@ int System::upload_static() {
   ws_.x = x_, ws_.r = r_, ws_.p = p_, ws_.h = h_, ws_.z = z_, ws_.rhs = rhs_;
   ws_.x32 = x32_, ws_.r32 = r32_, ws_.p32 = p32_, ws_.h32 = h32_, ws_.z32 = z32_;
   ws_.scratch32 = scratch32_;
-  ws_.scratch32_nsplit = 2 * nsplit_tmu32_;
+  ws_.scratch32_nsplit = f32_splits;
   ws_.partial = partial_, ws_.dots = dots_, ws_.hist = hist_;
   ws_.cols = cols_, ws_.cols_h = cols_h_, ws_.scal_h = scal_h_;
   ws_.owned = false;
@@ -203,6 +206,11 @@ int System::upload_static() {
     mwa[i] = make_float2((float)(w * w), (float)(a * a));
   }
   up(d_.pol_wa32, pwa.data(), n * sizeof(float2));
+  {
+    std::vector<double> w(n);
+    for (int j = 0; j < n; ++j) w[j] = 1.0 / m.thole[m.polar_mm[j]];
+    d_.damp_r2max32 = gpu::damp_r2max32(m.amoeba, d_.damp_thr, w.data(), m.damping.data(), n);
+  }
   up(d_.mm_wa32, mwa.data(), mm * sizeof(float2));
   cudaStreamSynchronize(st_);  // pwa / mwa are host temporaries
   cudaMemsetAsync(ipd_, 0, nv * nipd * sizeof(double), st_);
@@ -241,6 +249,9 @@ int System::upload_geometry() {
   }
   cudaMemcpyAsync(d_.pol_pos, pp.data(), n * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.pol_pos32, pp32.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st_);
+  std::vector<float4> boxes(2 * (size_t)d_.ntile);
+  gpu::tile_boxes32(pp32.data(), n, boxes.data());
+  if (n) cudaMemcpyAsync(d_.tile_box32, boxes.data(), boxes.size() * sizeof(float4), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.mm_pos, mp.data(), mm * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.mm_a, ma.data(), mm * sizeof(double), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.mm_q, m.q.data(), m.q.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
@@ -755,6 +766,16 @@ int System::set_fp64_kernel(int mode) {
   return kOk;
 }
 
+int System::set_fp32_kernel(int mode) {
+  if (mode < 0 || mode > 2) {
+    set_last_error("FP32 kernel mode must be 0 (autotuned), 1 or 2");
+    return kErrBadArg;
+  }
+  if (mode != fp32_kernel_) f32_tune_.clear();
+  fp32_kernel_ = mode;
+  return kOk;
+}
+
 int System::set_default_solver(int s) {
   if (s != kSolverCG && s != kSolverInversion && s != kSolverDIIS) {
     set_last_error("Unrecognized setting for default solver method");
@@ -798,7 +819,9 @@ int System::tmatvec_f32(const double *xh, double *yh, int nrhs) {
   }
   cudaMemcpyAsync(p_, xh, nrhs * nv * sizeof(double), cudaMemcpyHostToDevice, st_);
   gpu::launch_to_f32(nrhs * nv, p_, nullptr, p32_, st_);
-  gpu::launch_tmu_f32(d_, nrhs, p32_, h32_, scratch32_, nsplit_tmu32_, st_);
+  const int kver = fp32_kernel_ ? fp32_kernel_ : 2;
+  const int split = kver == 2 ? nsplit_tmu32_ : gpu::tmu_pick_split(d_, nrhs, gpu::sm_count(), true);
+  gpu::launch_tmu_f32(d_, nrhs, p32_, h32_, scratch32_, split, st_, 4, kver);
   std::vector<float> tmp(nrhs * nv);
   cudaMemcpyAsync(tmp.data(), h32_, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, st_);
   int st = check(cudaStreamSynchronize(st_), "tmatvec_f32");

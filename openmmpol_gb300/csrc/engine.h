@@ -42,7 +42,7 @@ struct Workspace {
   bool owned = false;
   // captured inner FP32 iteration (CUDA graph) and what it was built for
   cudaGraphExec_t graph = nullptr;
-  int graph_ncol = -1, graph_gmax = 0, graph_nsplit = 0;
+  int graph_ncol = -1, graph_gmax = 0, graph_nsplit = 0, graph_kver = 0;
   long long graph_kernels = 0;
 };
 
@@ -89,6 +89,7 @@ class System {
   // FP64 direct product: 0 auto (symmetric from 2048 sites), 1 all ordered
   // pairs (target-outer), 2 symmetric (unordered pairs)
   int set_fp64_kernel(int mode);
+  int set_fp32_kernel(int mode);
   int precision() const { return precision_; }
   double tol() const { return tol_; }
   const SolveStats &stats() const { return stats_; }
@@ -132,8 +133,11 @@ class System {
   int cg64_ws(Workspace &w, int matv, int ncol, const double *rhs, double *x, int set0);
   int pcg32_ws(Workspace &w, int ncol, int max_it, double eta);
   int mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, int set0, bool have_guess);
-  int tune_f32(Workspace &w, int ncol, int &gmax, int &nsplit);
-  void f32_product(Workspace &w, int ncol, int gmax, int nsplit);
+  struct F32Shape {
+    int g, nsplit, kver;  // group width, source splits, kernel version
+  };
+  int tune_f32(Workspace &w, int ncol, F32Shape &shape);
+  void f32_product(Workspace &w, int ncol, const F32Shape &shape);
   int ensure_batch_ws(int ncol, int nf);
   void free_ws(Workspace &w);
   int check(cudaError_t e, const char *what);
@@ -163,6 +167,7 @@ class System {
   size_t scratch_n_ = 0;
   double *sym_scratch_ = nullptr;  // symmetric-kernel partials (allocated on first use)
   int fp64_kernel_ = 0;
+  int fp32_kernel_ = 0;  // 0 autotuned, else the forced kernel version
   float *scratch32_ = nullptr;
   double *partial_ = nullptr;  // reduction partials [kRedBlocks][8]
   double *dots_ = nullptr;     // [8]
@@ -198,7 +203,7 @@ class System {
   void kt_resolve();
   Workspace ws_;   // view of the default two-column buffers
   Workspace wsb_;  // batch buffers
-  std::map<int, std::pair<int, int>> f32_tune_;  // columns -> (group width, source splits)
+  std::map<int, F32Shape> f32_tune_;  // columns -> tuned FP32 launch shape
   bool use_graphs_ = true;
   cudaEvent_t tev_[8] = {};
   void *flush_buf_ = nullptr;

@@ -446,11 +446,39 @@ __global__ void k_tmu_finish(int n, int nrhs, int nsplit, const T *__restrict__ 
 // steps: at step t lane l meets source (l + t) mod 32, read from shared
 // memory, and the source-side accumulators travel one lane per step by
 // shuffle, so no lane ever shares an accumulator.  Source sides are summed
-// over the 4 warps in shared memory and written to jpart[I][k]; target sides
-// go to ipart[I][part].  k_tmu_sym_reduce adds them in a fixed order, so the
-// product is deterministic.
+// over the 4 warps in shared memory; they and the target sides are added to
+// per-site 128-bit fixed-point accumulators (2^-80 resolution) with integer
+// atomics.  Integer addition is exact and associative, so the product is
+// deterministic whatever the order of the CTAs, and the accumulators take
+// O(n) memory.
 // ---------------------------------------------------------------------------
 constexpr int SYM_TILE = 128;
+
+// v added exactly into the two-word fixed-point value hi * 2^-16 + lo * 2^-80
+// (hi two's complement, lo unsigned).  A value that is not finite or not
+// below 2^36 in magnitude sets *bad instead (the whole product is then NaN).
+__device__ __forceinline__ void fixed_add(unsigned long long *lo, unsigned long long *hi, double v,
+                                          unsigned long long *bad) {
+  if (!(fabs(v) < 68719476736.0)) {
+    atomicOr(bad, 1ull);
+    return;
+  }
+  const double s = v * 65536.0;  // exact
+  double fl = floor(s);
+  double fr = s - fl;  // exact, in [0, 1]
+  if (fr >= 1.0) {     // s - floor(s) rounded up to 1 for tiny negative s
+    fr = 0.0;
+    fl += 1.0;
+  }
+  const unsigned long long h = (unsigned long long)(long long)fl;
+  const unsigned long long l = (unsigned long long)(fr * 18446744073709551616.0);
+  const unsigned long long old = atomicAdd(lo, l);
+  atomicAdd(hi, h + (old + l < old ? 1ull : 0ull));
+}
+
+__device__ __forceinline__ double fixed_value(unsigned long long lo, unsigned long long hi) {
+  return ((double)(long long)hi + (double)lo * 5.421010862427522e-20) * 1.52587890625e-05;
+}
 
 template <int NRHS, bool AMOEBA>
 __global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, int nparts, int per_part,
@@ -458,8 +486,10 @@ __global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, i
                                                        const double *__restrict__ damp,
                                                        const float2 *__restrict__ wa,
                                                        const double *__restrict__ x,
-                                                       double *__restrict__ jpart, double *__restrict__ ipart,
-                                                       double thr, float thr2m) {
+                                                       unsigned long long *__restrict__ acc_lo,
+                                                       unsigned long long *__restrict__ acc_hi,
+                                                       unsigned long long *__restrict__ bad, double thr,
+                                                       float thr2m) {
   constexpr int C = 3 * NRHS;
   __shared__ double s_x[SYM_TILE], s_y[SYM_TILE], s_z[SYM_TILE], s_w[SYM_TILE], s_a[SYM_TILE];
   __shared__ float2 s_wa[SYM_TILE];
@@ -483,12 +513,7 @@ __global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, i
   for (int k = k0; k < k1; ++k) {
     int J = I + k;
     if (J >= ntile) J -= ntile;
-    double *jp = jpart + ((size_t)I * (K + 1) + k) * SYM_TILE * C;
-    if (k > 0 && 2 * k == ntile && I >= ntile / 2) {  // the other tile of the pair owns it
-#pragma unroll
-      for (int c = 0; c < C; ++c) jp[(size_t)c * SYM_TILE + tid] = 0.0;
-      continue;
-    }
+    if (k > 0 && 2 * k == ntile && I >= ntile / 2) continue;  // the other tile of the pair owns it
     const bool diag = (k == 0);
     __syncthreads();
     {
@@ -546,34 +571,33 @@ __global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, i
     }
     if (!diag) {
       __syncthreads();
+      const int sj = J * SYM_TILE + tid;
+      if (sj < n) {
 #pragma unroll
-      for (int c = 0; c < C; ++c)
-        jp[(size_t)c * SYM_TILE + tid] = ((s_accj[0][c][tid] + s_accj[1][c][tid]) + s_accj[2][c][tid]) +
-                                         s_accj[3][c][tid];
+        for (int c = 0; c < C; ++c) {
+          const double v = ((s_accj[0][c][tid] + s_accj[1][c][tid]) + s_accj[2][c][tid]) + s_accj[3][c][tid];
+          const size_t o = ((size_t)(c / 3) * n + sj) * 3 + (c % 3);
+          fixed_add(acc_lo + o, acc_hi + o, v, bad);
+        }
+      }
     }
   }
-  double *ip = ipart + ((size_t)I * nparts + part) * SYM_TILE * C;
+  if (vi) {
 #pragma unroll
-  for (int c = 0; c < C; ++c) ip[(size_t)c * SYM_TILE + tid] = acci[c];
+    for (int c = 0; c < C; ++c) {
+      const size_t o = ((size_t)(c / 3) * n + ti) * 3 + (c % 3);
+      fixed_add(acc_lo + o, acc_hi + o, acci[c], bad);
+    }
+  }
 }
 
-// out[r][t][c] = sum_part ipart[J][part] + sum_{k=1..K} jpart[(J - k) mod ntile][k]
-__global__ void k_tmu_sym_reduce(int n, int nrhs, int ntile, int K, int nparts, const double *__restrict__ jpart,
-                                 const double *__restrict__ ipart, double *__restrict__ out) {
-  const int C = 3 * nrhs;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  int J = t / SYM_TILE, l = t % SYM_TILE;
-  for (int c = 0; c < C; ++c) {
-    double e = 0.0;
-    for (int p = 0; p < nparts; ++p) e += ipart[(((size_t)J * nparts + p) * C + c) * SYM_TILE + l];
-    for (int k = 1; k <= K; ++k) {
-      int I = J - k;
-      if (I < 0) I += ntile;
-      e += jpart[(((size_t)I * (K + 1) + k) * C + c) * SYM_TILE + l];
-    }
-    out[((size_t)(c / 3) * n + t) * 3 + (c % 3)] = e;
-  }
+// out[k] = the fixed-point accumulator k as a double (NaN when flagged)
+__global__ void k_fixed_to_double(size_t total, const unsigned long long *__restrict__ lo,
+                                  const unsigned long long *__restrict__ hi, const unsigned long long *bad,
+                                  double *__restrict__ out) {
+  const bool nan = *bad != 0ull;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = nan ? __longlong_as_double(0x7ff8000000000000ll) : fixed_value(lo[k], hi[k]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1049,6 +1073,14 @@ int tmu_pick_split(const DevSites &s, int nrhs, int sms, bool fp32) {
   return split;
 }
 
+int tmu32_max_split(const DevSites &s, int sms) {
+  int a = tmu_pick_split(s, 2, sms, true), b = tmu32_pick_split(s, sms);
+  int tiles = (s.n + TILE - 1) / TILE;
+  int m = 2 * (a > b ? a : b);
+  if (m > tiles) m = tiles;
+  return m < 1 ? 1 : m;
+}
+
 size_t tmu_scratch_doubles(const DevSites &s, int nrhs, int nsplit) {
   return (size_t)nsplit * nrhs * s.n * 3;
 }
@@ -1077,7 +1109,7 @@ inline int column_group(int left, int gmax) {
 
 template <typename T, bool KAHAN>
 static void tmu_dispatch(const DevSites &s, int nrhs, const typename Vec4<T>::type *pos, const T *damp,
-                         const T *x, T *partial, int nsplit, int gmax, cudaStream_t st) {
+                         const T *x, T *partial, int nsplit, int gmax, cudaStream_t st, int kver = 1) {
   // process the columns in groups sharing the pair geometry; every group
   // has its own [split][g][n][3] block of partials, one after the other
   int done = 0;
@@ -1085,6 +1117,14 @@ static void tmu_dispatch(const DevSites &s, int nrhs, const typename Vec4<T>::ty
     int g = column_group(nrhs - done, gmax);
     size_t xo = (size_t)done * s.n * 3;
     T *pg = partial + (size_t)nsplit * done * s.n * 3;
+    if constexpr (std::is_same<T, float>::value) {
+      if (kver == 2) {
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        launch_tmu32_pairs(s, g, x + xo, pg, nsplit, st);
+        done += g;
+        continue;
+      }
+    }
     switch (g) {
       case 8: tmu_allpairs<T, 8, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st); break;
       case 4: tmu_allpairs<T, 4, KAHAN>(s, pos, damp, x + xo, pg, nsplit, st); break;
@@ -1147,10 +1187,10 @@ SymPlan sym_plan(int n) {
 
 size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs) {
   if (s.n == 0) return 0;
-  SymPlan p = sym_plan(s.n);
-  size_t C = 3 * (size_t)nrhs;
-  return (size_t)p.ntile * (p.K + 1) * SYM_TILE * C + (size_t)p.ntile * p.nparts * SYM_TILE * C +
-         (size_t)nrhs * s.n * 3;
+  // two 64-bit accumulator words and one double per value of a column group
+  // (at most two columns)
+  size_t C = 3 * (size_t)(nrhs < 2 ? nrhs : 2);
+  return 3 * C * (size_t)s.n + 1;
 }
 
 void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
@@ -1163,28 +1203,31 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
   while (done < nrhs) {
     int g = (nrhs - done) >= 2 ? 2 : 1;
     size_t C = 3 * (size_t)g;
-    double *jpart = scratch;
-    double *ipart = jpart + (size_t)p.ntile * (p.K + 1) * SYM_TILE * C;
-    double *e = ipart + (size_t)p.ntile * p.nparts * SYM_TILE * C;
+    unsigned long long *lo = reinterpret_cast<unsigned long long *>(scratch);
+    unsigned long long *hi = lo + C * s.n;
+    double *e = scratch + 2 * C * s.n;
+    unsigned long long *bad = reinterpret_cast<unsigned long long *>(scratch + 3 * C * s.n);
     const double *xg = x + (size_t)done * s.n * 3;
     dim3 grid(p.ntile, p.nparts);
     g_launches.fetch_add(3, std::memory_order_relaxed);
+    cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
+    cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st);
     if (g == 2) {
       if (s.amoeba)
         k_tmu_sym<2, true><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos, s.pol_a,
-                                                      s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+                                                      s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
       else
         k_tmu_sym<2, false><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos,
-                                                       s.pol_a, s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+                                                       s.pol_a, s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
     } else {
       if (s.amoeba)
         k_tmu_sym<1, true><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos, s.pol_a,
-                                                      s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+                                                      s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
       else
         k_tmu_sym<1, false><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos,
-                                                       s.pol_a, s.pol_wa32, xg, jpart, ipart, s.damp_thr, thr2m);
+                                                       s.pol_a, s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
     }
-    k_tmu_sym_reduce<<<(s.n + 127) / 128, 128, 0, st>>>(s.n, g, p.ntile, p.K, p.nparts, jpart, ipart, e);
+    k_fixed_to_double<<<blocks_for(C * s.n, 256), 256, 0, st>>>(C * s.n, lo, hi, bad, e);
     const float2 *wa = s.pol_wa32;
     dim3 fgrid((s.n + 127) / 128, g);
     if (s.amoeba)
@@ -1200,9 +1243,9 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
 }
 
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch, int nsplit,
-                    cudaStream_t st, int gmax) {
+                    cudaStream_t st, int gmax, int kver) {
   if (s.n == 0) return;
-  tmu_dispatch<float, true>(s, nrhs, s.pol_pos32, s.pol_a32, x, scratch, nsplit, gmax, st);
+  tmu_dispatch<float, true>(s, nrhs, s.pol_pos32, s.pol_a32, x, scratch, nsplit, gmax, st, kver);
   tmu_finish<float>(s, nrhs, nsplit, scratch, s.pol_pos32, s.pol_a32, x, true, y, gmax, st);
 }
 

@@ -47,6 +47,11 @@ struct DevSites {
   double *d2d_s = nullptr;
   int d2d_nnz = 0;
   double damp_thr = 50.0;       // AMOEBA: damping applied when a u^3 < 50
+  // FP32 operator: per 128-site tile the bounding box of pol_pos32 (lo, hi
+  // pairs, [2*ntile]) and the squared distance beyond which no pair is damped
+  float4 *tile_box32 = nullptr;
+  int ntile = 0;
+  float damp_r2max32 = 0.f;
 };
 
 // ---- pair kernels ---------------------------------------------------------
@@ -70,8 +75,19 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
 // FP32 inner operator with compensated cross-tile sums; x,y float.  Columns
 // go through the pair kernel in groups of up to gmax (8, 4, 2 or 1) sharing
 // the pair geometry; scratch holds nsplit * nrhs * n * 3 floats.
+// kver 1: one target per thread, per-pair damping test (kernels.cu);
+// kver 2: the tile-classified kernel of tmu32.cu.
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch,
-                    int nsplit, cudaStream_t st, int gmax = 4);
+                    int nsplit, cudaStream_t st, int gmax = 4, int kver = 2);
+void launch_tmu32_pairs(const DevSites &s, int g, const float *x, float *partial, int nsplit, cudaStream_t st);
+// source splits an FP32 scratch must hold (per column) for every shape the
+// autotuner may pick
+int tmu32_max_split(const DevSites &s, int sm_count);
+// Split of the source range for the FP32 operator (tmu32.cu) and its tile
+// boxes / undamped distance, computed on the host from the FP32 positions.
+int tmu32_pick_split(const DevSites &s, int sm_count);
+void tile_boxes32(const float4 *pos32, int n, float4 *boxes /*[2*ceil(n/128)]*/);
+float damp_r2max32(bool amoeba, double damp_thr, const double *inv_thole, const double *a, int n);
 // batched fields: rhs[s*nf+f] = E_M2D[s] + field[f]; solution scatter to [f][s]
 void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
                       cudaStream_t st);

@@ -53,14 +53,14 @@ int System::ensure_batch_ws(int ncol, int nf) {
   Workspace &w = wsb_;
   const size_t nv = 3 * (size_t)d_.n;
   const int nipd = m_.n_ipd;
-  int s0 = gpu::tmu_pick_split(d_, ncol, gpu::sm_count(), true);
+  int s0 = gpu::tmu32_max_split(d_, gpu::sm_count());
   int bad = 0;
   bad |= walloc(w.x, ncol * nv) | walloc(w.r, ncol * nv) | walloc(w.p, ncol * nv) | walloc(w.h, ncol * nv) |
          walloc(w.z, ncol * nv) | walloc(w.rhs, ncol * nv);
   bad |= walloc(w.fields, nf * nv) | walloc(w.out, (size_t)nf * nipd * nv);
   bad |= walloc(w.x32, ncol * nv) | walloc(w.r32, ncol * nv) | walloc(w.p32, ncol * nv) |
          walloc(w.h32, ncol * nv) | walloc(w.z32, ncol * nv);
-  bad |= walloc(w.scratch32, 2 * (size_t)s0 * ncol * nv);
+  bad |= walloc(w.scratch32, (size_t)s0 * ncol * nv);
   bad |= walloc(w.partial, (size_t)gpu::kRedBlocks * std::max(ncol, nf)) |
          walloc(w.dots, 3 * (size_t)ncol + nf) | walloc(w.cols, ncol);
   if (bad || cudaMallocHost((void **)&w.cols_h, ncol * sizeof(gpu::CgCol)) != cudaSuccess ||
@@ -72,7 +72,7 @@ int System::ensure_batch_ws(int ncol, int nf) {
   }
   w.cap = ncol;
   w.fcap = nf;
-  w.scratch32_nsplit = 2 * s0;
+  w.scratch32_nsplit = s0;
   w.owned = true;
   return kOk;
 }
@@ -173,52 +173,62 @@ int System::cg64_ws(Workspace &w, int matv, int ncol, const double *rhs, double 
 // ---------------------------------------------------------------------------
 // FP32 product with the tuned launch shape
 // ---------------------------------------------------------------------------
-void System::f32_product(Workspace &w, int ncol, int gmax, int nsplit) {
-  gpu::launch_tmu_f32(d_, ncol, w.p32, w.h32, w.scratch32, nsplit, st_, gmax);
+void System::f32_product(Workspace &w, int ncol, const F32Shape &sh) {
+  gpu::launch_tmu_f32(d_, ncol, w.p32, w.h32, w.scratch32, sh.nsplit, st_, sh.g, sh.kver);
 }
 
-int System::tune_f32(Workspace &w, int ncol, int &gmax, int &nsplit) {
+int System::tune_f32(Workspace &w, int ncol, F32Shape &shape) {
   auto it = f32_tune_.find(ncol);
-  const int s0 = gpu::tmu_pick_split(d_, ncol, gpu::sm_count(), true);
-  if (it != f32_tune_.end() && it->second.second <= w.scratch32_nsplit) {
-    gmax = it->second.first;
-    nsplit = it->second.second;
+  if (it != f32_tune_.end() && it->second.nsplit <= w.scratch32_nsplit) {
+    shape = it->second;
     return kOk;
   }
+  const int sms = gpu::sm_count();
   const int tiles = (d_.n + 127) / 128;
+  const int cap = std::min(w.scratch32_nsplit, tiles);
+  std::vector<F32Shape> cands;
   std::vector<int> widths = {1};
   for (int g : {2, 4, 8})
     if (g <= ncol) widths.push_back(g);
-  std::vector<int> splits = {s0};
-  if (2 * s0 <= std::min(w.scratch32_nsplit, tiles)) splits.push_back(2 * s0);
+  // kernel 1: one target per thread; kernel 2: tile-classified, two
+  // targets per thread for one or two columns
+  const int s1 = gpu::tmu_pick_split(d_, ncol, sms, true), s2 = gpu::tmu32_pick_split(d_, sms);
+  for (int g : widths) {
+    if (fp32_kernel_ != 2)
+      for (int s : {s1, 2 * s1})
+        if (s <= cap) cands.push_back({g, s, 1});
+    if (fp32_kernel_ != 1)
+      for (int s : {std::max(1, s2 / 2), s2, 2 * s2})
+        if (s <= cap) cands.push_back({g, s, 2});
+  }
+  if (cands.empty()) cands.push_back({1, 1, fp32_kernel_ ? fp32_kernel_ : 2});
   const size_t nv = 3 * (size_t)d_.n;
   cudaMemsetAsync(w.p32, 0, ncol * nv * sizeof(float), st_);
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   float best = 1e30f;
-  int bg = 1, bs = s0;
-  for (int g : widths)
-    for (int s : splits) {
-      f32_product(w, ncol, g, s);  // warm-up
-      cudaEventRecord(a, st_);
-      f32_product(w, ncol, g, s);
-      f32_product(w, ncol, g, s);
-      cudaEventRecord(b, st_);
-      cudaEventSynchronize(b);
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, a, b);
-      if (ms < best) best = ms, bg = g, bs = s;
-    }
+  F32Shape pick = cands.front();
+  for (const F32Shape &c : cands) {
+    f32_product(w, ncol, c);  // warm-up
+    cudaEventRecord(a, st_);
+    f32_product(w, ncol, c);
+    f32_product(w, ncol, c);
+    cudaEventRecord(b, st_);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) best = ms, pick = c;
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   int st = check(cudaGetLastError(), "FP32 autotune");
   if (st) return st;
-  f32_tune_[ncol] = {bg, bs};
-  gmax = bg;
-  nsplit = bs;
-  log_msg(kVerbHigh, nullptr, "autotuned FP32 T.mu for %d columns: %d per launch, %d source splits (%.3f ms)", ncol,
-          bg, bs, best / 2);
+  f32_tune_[ncol] = pick;
+  shape = pick;
+  log_msg(kVerbHigh, nullptr,
+          "autotuned FP32 T.mu for %d columns: kernel %d, %d per launch, %d source splits (%.3f ms)", ncol,
+          pick.kver, pick.g, pick.nsplit, best / 2);
   return kOk;
 }
 
@@ -228,8 +238,8 @@ int System::tune_f32(Workspace &w, int ncol, int &gmax, int &nsplit) {
 int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
   const int n = d_.n;
   const size_t nv = 3 * (size_t)n;
-  int gmax = 1, nsplit = 1;
-  int st = tune_f32(w, ncol, gmax, nsplit);
+  F32Shape shape{1, 1, 2};
+  int st = tune_f32(w, ncol, shape);
   if (st) return st;
   // x = 0; p = h = 0 so that an update step with alpha = 0 only forms
   // z = alpha_pol r and the partial r.z
@@ -258,7 +268,7 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
   }
   cudaMemcpyAsync(w.cols, w.cols_h, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
   auto iteration = [&]() {
-    f32_product(w, ncol, gmax, nsplit);
+    f32_product(w, ncol, shape);
     gpu::launch_dots_f32(ncol, nv, w.h32, w.p32, w.partial, st_);
     gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
     gpu::launch_cg_alpha(ncol, w.dots, w.cols, 1e-300, st_);
@@ -270,7 +280,8 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
   };
   // capture one iteration as a graph (kernel arguments and buffers are fixed
   // per workspace, width and launch shape; the tolerance lives in w.cols)
-  if (use_graphs_ && (w.graph_ncol != ncol || w.graph_gmax != gmax || w.graph_nsplit != nsplit)) {
+  if (use_graphs_ && (w.graph_ncol != ncol || w.graph_gmax != shape.g || w.graph_nsplit != shape.nsplit ||
+                     w.graph_kver != shape.kver)) {
     if (w.graph) cudaGraphExecDestroy(w.graph);
     w.graph = nullptr;
     w.graph_ncol = -1;
@@ -283,8 +294,9 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
       gpu::add_launch_count(-kernels);  // captured, not launched
       if (e == cudaSuccess && g && cudaGraphInstantiate(&w.graph, g, 0) == cudaSuccess) {
         w.graph_ncol = ncol;
-        w.graph_gmax = gmax;
-        w.graph_nsplit = nsplit;
+        w.graph_gmax = shape.g;
+        w.graph_nsplit = shape.nsplit;
+        w.graph_kver = shape.kver;
         w.graph_kernels = kernels;
       } else {
         w.graph = nullptr;

@@ -232,13 +232,32 @@ def test_w1k_mixed_precision_within_1e7(w1k):
     assert hist[-1] < 1e-10
 
 
-def test_fp32_operator_accuracy(w1k):
-    p, _ = w1k
+@pytest.mark.parametrize("kernel", ["pairwise", "tiled"])
+@pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba"])
+def test_fp32_operator_accuracy(case, kernel, w1k, chains, golden_mmp):
+    """Both FP32 kernels against the FP64 operator: relative 1e-5 overall and
+    at every site (damped near pairs and scaled pairs included)."""
+    p = {"w1k": w1k[0], "chains": chains[0]}.get(case) or golden_mmp[case]
     g = OMMPSystem(p)
+    g.set_fp32_kernel(kernel)
     x = np.random.default_rng(2).standard_normal((g.pol_atoms, 3)) * 0.05
     y64 = g.tmatvec(x)
     y32 = g.tmatvec_fp32(x)
     assert rel(y32, y64) < 1e-5
+    site = np.linalg.norm(y32 - y64, axis=1) / np.maximum(np.linalg.norm(y64, axis=1), 1e-3 * np.abs(y64).max())
+    assert site.max() < 1e-4
+
+
+@pytest.mark.parametrize("kernel", ["pairwise", "tiled"])
+def test_mixed_solve_with_each_fp32_kernel(kernel, chains):
+    p, ef = chains
+    ref = converged_reference(p, ef).ipd
+    g = OMMPSystem(p)
+    g.set_fp32_kernel(kernel)
+    g.set_solver_tol(1e-10)
+    g.set_precision("mixed")
+    g.set_external_field(ef)
+    assert rel(g.ipd, ref) < 1e-7
 
 
 def test_chain_system_wang_exclusions(chains):

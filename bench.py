@@ -42,6 +42,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "induced-dipole solves/s (mixed FP32/FP64 at <=1e-7 rel. error vs FP64)"
 FLOP_PER_PAIR = 45.0  # per ordered T.mu pair and right-hand side
+# FP32 operations (an FMA counts once) per undamped ordered pair of the
+# double-single kernel, counted in csrc/tmu_ds.cu: 3 coordinate differences
+# (33), r^2 (31), reciprocal square root (17 + 1 MUFU), r^-2 / r^-3 / 3 r^-5
+# (27), mu.d (31), the field factor (7), six accumulations (72) and three
+# renormalisations (9)
+DS_OPS_PER_PAIR = 227.0
 
 
 def parse():
@@ -55,6 +61,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-ds"],
+                    help="mixed: FP64 refinement residual products; mixed-ds: double-single ones")
     ap.add_argument("--fp32-kernel", default="auto", choices=["auto", "pairwise", "tiled"],
                     help="FP32 inner T.mu kernel (auto = autotuned)")
     ap.add_argument("--requests", type=int, default=1024, help="s1024: requests in the mixed stream")
@@ -255,7 +263,7 @@ def run_gb300(args):
     st = L.ommp_gpu_get_e_m2d(h, np.zeros((sys_.n_ipd, n, 3)).ctypes.data_as(_lib._dp))
     m2d_s = time.perf_counter() - t0
     assert st == 0, L.ommp_gpu_last_error()
-    sys_.set_precision("mixed")
+    sys_.set_precision(args.precision)
     flush = 256 << 20
 
     def one_step(k, timed):
@@ -284,7 +292,7 @@ def run_gb300(args):
     wall0 = time.perf_counter()
     for k in range(W, W + K):
         step_ms.append(one_step(k, True))
-        counters.append((sys_.counter(0), sys_.counter(1), sys_.counter(2), sys_.counter(3)))
+        counters.append((sys_.counter(0), sys_.counter(1), sys_.counter(2), sys_.counter(3), sys_.counter(4)))
     sys_.synchronize()
     wall = time.perf_counter() - wall0
     clocks = clk.stop()
@@ -292,6 +300,7 @@ def run_gb300(args):
     sys_.enable_kernel_timing(False)
     k64 = sys_.kernel_stats(0)
     k32 = sys_.kernel_stats(1)
+    kds = sys_.kernel_stats(2)
     total_ms = sum(step_ms)
     if dist:
         import torch
@@ -342,24 +351,36 @@ def run_gb300(args):
     L.ommp_gpu_measure_pipe_peak(0, C.byref(peak32))
     pairs = float(n) * (n - 1)
     kstats = {}
-    for name, (cnt, ms, cols), pk in (("tmu_fp64", k64, peak64.value), ("tmu_fp32", k32, peak32.value)):
+    for name, (cnt, ms, cols), pk in (("tmu_fp64", k64, peak64.value), ("tmu_fp32", k32, peak32.value),
+                                      ("tmu_ds", kds, peak32.value)):
         if cnt:
             # algorithmic flop of all timed launches: 45 per ordered pair per column
             avg = ms / cnt
             ach = FLOP_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
             kstats[name] = {"launches": cnt, "columns": cols, "total_ms": ms, "avg_ms": avg,
                             "achieved_tflops": ach, "peak_tflops": pk, "frac": ach / pk if pk else None}
+            if name == "tmu_ds":
+                # FP32 pipe: double-single operations issued per second against
+                # the FMA-pipe instruction rate (peak flop / 2)
+                ops = DS_OPS_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
+                kstats[name].update({"fp64_equivalent_tflops": ach, "achieved_tops": ops,
+                                     "peak_tops": pk / 2, "frac": ops / (pk / 2) if pk else None})
     dom = max(kstats, key=lambda k: kstats[k]["total_ms"]) if kstats else None
     roof = None
     if dom:
         d = kstats[dom]
+        ds = dom == "tmu_ds"
         roof = {"bound": "fp64" if dom == "tmu_fp64" else "fp32", "kernel": dom,
-                "achieved": d["achieved_tflops"], "peak": d["peak_tflops"], "unit": "TFLOP/s",
+                "achieved": d["achieved_tops"] if ds else d["achieved_tflops"],
+                "peak": d["peak_tops"] if ds else d["peak_tflops"],
+                "unit": "Tops/s (FP32 instructions)" if ds else "TFLOP/s",
                 "frac": d["frac"], "traffic": None,
                 "peak_source": "FMA-chain kernel measured in this run (pipe peak; "
                                "MEASURED_PEAKS.json has no FP32/FP64 CUDA-core figure)",
-                "algorithmic": f"{FLOP_PER_PAIR:.0f} flop per ordered pair x N(N-1) pairs x right-hand sides "
-                               f"({d['columns']} columns over {d['launches']} launches)",
+                "algorithmic": (f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair" if ds else
+                                f"{FLOP_PER_PAIR:.0f} flop per ordered pair") +
+                               f" x N(N-1) pairs x right-hand sides ({d['columns']} columns over "
+                               f"{d['launches']} launches)",
                 "share_of_timed": d["total_ms"] / total_ms}
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -55,6 +55,8 @@
 /* precision modes of ommp_gpu_set_precision */
 #define OMMP_GPU_PREC_FP64 0  /* plain FP64 solver (default) */
 #define OMMP_GPU_PREC_MIXED 1 /* FP32 inner CG + FP64 iterative refinement */
+#define OMMP_GPU_PREC_MIXED_DS 2 /* as MIXED, refinement residual products in  \
+                                    double-single arithmetic (~1e-13 relative) */
 
 /* status codes of the ommp_gpu_* calls */
 #define OMMP_GPU_OK 0
@@ -195,8 +197,11 @@ int32_t ommp_gpu_get_e_m2d(OMMP_SYSTEM_PRT s, double *out);
 int32_t ommp_gpu_tmatvec(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs, int32_t dodiag,
                          int32_t matv);
 int32_t ommp_gpu_tmatvec_fp32(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs);
+/* the double-single product of OMMP_GPU_PREC_MIXED_DS (diagonal included) */
+int32_t ommp_gpu_tmatvec_ds(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs);
 
-/* CUDA-event timing of the pair kernels: which 0 = FP64 T.mu, 1 = FP32 T.mu;
+/* CUDA-event timing of the pair kernels: which 0 = FP64 T.mu, 1 = FP32 T.mu,
+ * 2 = double-single T.mu;
  * columns = right-hand sides summed over the timed launches (may be NULL) */
 void ommp_gpu_enable_kernel_timing(OMMP_SYSTEM_PRT s, int32_t on);
 void ommp_gpu_kernel_stats(OMMP_SYSTEM_PRT s, int32_t which, int64_t *launches, double *total_ms,

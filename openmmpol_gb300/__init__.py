@@ -14,14 +14,16 @@ import numpy as np
 from . import _lib
 
 __all__ = ["OMMPSystem", "Server", "OMMPError", "available_solvers", "available_matrix_vector",
-           "set_verbose", "PREC_FP64", "PREC_MIXED"]
+           "set_verbose", "PREC_FP64", "PREC_MIXED", "PREC_MIXED_DS", "PRECISIONS"]
 
 # pythonapi/pyopenmmpol/pyommp_interface.cpp:9-23
 available_solvers = {"none": 0, "default": 1, "conjugate gradient": 1, "cg": 1,
                      "inversion": 3, "diis": 2}
 available_matrix_vector = {"none": 0, "default": 2, "incore": 1, "direct": 2}
 verbosity = {"none": 0, "low": 1, "high": 2, "debug": 3}
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_DS = 0, 1, 2
+# 'mixed-ds': the refinement residual products in double-single arithmetic
+PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "mixed-ds": PREC_MIXED_DS}
 ERR_CANCELLED = 7
 
 
@@ -173,7 +175,7 @@ class OMMPSystem:
         self._L.ommp_gpu_set_solver_maxiter(self._h, int(n))
 
     def set_precision(self, mode) -> None:
-        m = {"fp64": PREC_FP64, "mixed": PREC_MIXED}.get(mode, mode)
+        m = PRECISIONS.get(mode, mode)
         self._L.ommp_gpu_set_precision(self._h, int(m))
 
     def set_fp64_kernel(self, mode) -> None:
@@ -218,12 +220,18 @@ class OMMPSystem:
         return y[0] if nrhs == 1 else y
 
     def tmatvec_fp32(self, x) -> np.ndarray:
+        return self._tmatvec_alt(self._L.ommp_gpu_tmatvec_fp32, x)
+
+    def tmatvec_ds(self, x) -> np.ndarray:
+        """y = T x with the double-single kernel of the 'mixed-ds' mode."""
+        return self._tmatvec_alt(self._L.ommp_gpu_tmatvec_ds, x)
+
+    def _tmatvec_alt(self, fn, x) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float64)
         nrhs = 1 if x.ndim == 2 else x.shape[0]
         x = x.reshape(nrhs, self.pol_atoms, 3)
         y = np.zeros_like(x)
-        _check(self._L.ommp_gpu_tmatvec_fp32(self._h, x.ctypes.data_as(_lib._dp),
-                                             y.ctypes.data_as(_lib._dp), nrhs))
+        _check(fn(self._h, x.ctypes.data_as(_lib._dp), y.ctypes.data_as(_lib._dp), nrhs))
         return y[0] if nrhs == 1 else y
 
     def enable_kernel_timing(self, on: bool = True) -> None:
@@ -231,7 +239,7 @@ class OMMPSystem:
 
     def kernel_stats(self, which: int):
         """(launches, total ms, right-hand-side columns) of the timed pair
-        kernel: which 0 = FP64 T.mu, 1 = FP32 T.mu."""
+        kernel: which 0 = FP64 T.mu, 1 = FP32 T.mu, 2 = double-single T.mu."""
         n = C.c_int64(0)
         ms = C.c_double(0.0)
         cols = C.c_int64(0)
@@ -252,7 +260,7 @@ class Server:
 
     def __init__(self, hbm_budget_bytes: int, slots: int = 4, precision="mixed", tol: float = 1e-10):
         self._L = _lib.load()
-        p = {"fp64": PREC_FP64, "mixed": PREC_MIXED}.get(precision, precision)
+        p = PRECISIONS.get(precision, precision)
         h = C.c_void_p()
         _check(self._L.ommp_gpu_server_create(int(hbm_budget_bytes), int(slots), int(p), float(tol), C.byref(h)))
         self._h = h

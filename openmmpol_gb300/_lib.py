@@ -70,6 +70,7 @@ SIGNATURES = {
     "ommp_gpu_get_e_m2d": (C.c_int32, [_vp, _dp]),
     "ommp_gpu_tmatvec": (C.c_int32, [_vp, _dp, _dp, C.c_int32, C.c_int32, C.c_int32]),
     "ommp_gpu_tmatvec_fp32": (C.c_int32, [_vp, _dp, _dp, C.c_int32]),
+    "ommp_gpu_tmatvec_ds": (C.c_int32, [_vp, _dp, _dp, C.c_int32]),
     "ommp_gpu_enable_kernel_timing": (None, [_vp, C.c_int32]),
     "ommp_gpu_kernel_stats": (None, [_vp, C.c_int32, _i64p, _dp, _i64p]),
     "ommp_gpu_synchronize": (C.c_int32, [_vp]),

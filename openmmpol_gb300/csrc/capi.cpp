@@ -157,6 +157,7 @@ int64_t ommp_gpu_get_counter(OMMP_SYSTEM_PRT s, int32_t which) {
     case 1: return st.f32_matvecs;
     case 2: return st.outer;
     case 3: return st.inner_iters;
+    case 4: return st.ds_matvecs;
     default: return -1;
   }
 }
@@ -165,6 +166,9 @@ double ommp_gpu_last_solve_ms(OMMP_SYSTEM_PRT s) { return S(s)->last_solve_ms();
 int32_t ommp_gpu_get_e_m2d(OMMP_SYSTEM_PRT s, double *out) { return S(s)->e_m2d(out); }
 int32_t ommp_gpu_tmatvec(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs, int32_t dodiag, int32_t matv) {
   return S(s)->tmatvec(x, y, nrhs, dodiag != 0, matv);
+}
+int32_t ommp_gpu_tmatvec_ds(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs) {
+  return S(s)->tmatvec_ds(x, y, nrhs);
 }
 int32_t ommp_gpu_tmatvec_fp32(OMMP_SYSTEM_PRT s, const double *x, double *y, int32_t nrhs) {
   return S(s)->tmatvec_f32(x, y, nrhs);

@@ -47,7 +47,8 @@ System::~System() {
   if (st_) cudaStreamSynchronize(st_);
   free_ws(ws_);
   free_ws(wsb_);
-  void *bufs[] = {d_.pol_pos, d_.pol_a, d_.pol_alpha, d_.polar_mm, d_.pol_pos32, d_.pol_a32, d_.pol_wa32,
+  void *bufs[] = {d_.pol_pos, d_.pol_a, d_.pol_alpha, d_.polar_mm, d_.pol_pos32, d_.pol_pos32lo, d_.pol_a32,
+                  d_.pol_wa32, ds_scratch_,
                   d_.mm_wa32, d_.mm_pos,
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
@@ -140,7 +141,7 @@ int System::upload_static() {
   int nipd = m.n_ipd;
   int bad = 0;
   bad |= dalloc(d_.pol_pos, n) | dalloc(d_.pol_a, n) | dalloc(d_.pol_alpha, n) | dalloc(d_.polar_mm, n);
-  bad |= dalloc(d_.pol_pos32, n) | dalloc(d_.pol_a32, n) | dalloc(alpha32_, n);
+  bad |= dalloc(d_.pol_pos32, n) | dalloc(d_.pol_pos32lo, n) | dalloc(d_.pol_a32, n) | dalloc(alpha32_, n);
   bad |= dalloc(d_.pol_wa32, n) | dalloc(d_.mm_wa32, mm);
   bad |= dalloc(d_.mm_pos, mm) | dalloc(d_.mm_a, mm) | dalloc(d_.mm_q, (size_t)mm * m.ld_cart);
   bad |= dalloc(d_.m2d_ri, n + 1) | dalloc(d_.m2d_src, m2d_pairs_.src.size()) |
@@ -227,7 +228,7 @@ int System::upload_geometry() {
   int n = m.npol, mm = m.mm;
   const double inf = std::numeric_limits<double>::infinity();
   std::vector<gpu::Pos64> pp(n), mp(mm);
-  std::vector<float4> pp32(n);
+  std::vector<float4> pp32(n), pp32lo(n);
   std::vector<double> ma(mm, 0.0);
   double c[3] = {0, 0, 0};
   for (int i = 0; i < mm; ++i)
@@ -238,7 +239,10 @@ int System::upload_geometry() {
     const double *x = &m.cmm[3 * (size_t)a];
     double w = 1.0 / m.thole[a];
     pp[j] = gpu::Pos64{x[0], x[1], x[2], w};
-    pp32[j] = make_float4((float)(x[0] - c[0]), (float)(x[1] - c[1]), (float)(x[2] - c[2]), (float)w);
+    const double xc[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+    pp32[j] = make_float4((float)xc[0], (float)xc[1], (float)xc[2], (float)w);
+    pp32lo[j] = make_float4((float)(xc[0] - (double)pp32[j].x), (float)(xc[1] - (double)pp32[j].y),
+                            (float)(xc[2] - (double)pp32[j].z), 0.f);
     for (int k = 0; k < 3; ++k) cpol_h_[3 * (size_t)j + k] = x[k];
   }
   for (int i = 0; i < mm; ++i) {
@@ -249,6 +253,7 @@ int System::upload_geometry() {
   }
   cudaMemcpyAsync(d_.pol_pos, pp.data(), n * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.pol_pos32, pp32.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st_);
+  cudaMemcpyAsync(d_.pol_pos32lo, pp32lo.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st_);
   std::vector<float4> boxes(2 * (size_t)d_.ntile);
   gpu::tile_boxes32(pp32.data(), n, boxes.data());
   if (n) cudaMemcpyAsync(d_.tile_box32, boxes.data(), boxes.size() * sizeof(float4), cudaMemcpyHostToDevice, st_);
@@ -300,16 +305,19 @@ void System::kt_resolve() {
 
 void System::kernel_stats(int which, long long &launches, double &ms, long long &columns) {
   kt_resolve();
-  launches = klaunch_[which & 1];
-  ms = kms_[which & 1];
-  columns = kcols_[which & 1];
+  const int k = which >= 0 && which < 3 ? which : 0;
+  launches = klaunch_[k];
+  ms = kms_[k];
+  columns = kcols_[k];
 }
 
 void System::reset_kernel_stats() {
   kt_resolve();
-  klaunch_[0] = klaunch_[1] = 0;
-  kcols_[0] = kcols_[1] = 0;
-  kms_[0] = kms_[1] = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    klaunch_[k] = 0;
+    kcols_[k] = 0;
+    kms_[k] = 0.0;
+  }
 }
 
 int System::timer_record(int slot) {
@@ -419,6 +427,26 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
     if (ktime_on_) kt_end(e);
     stats_.f64_matvecs += 1;
   }
+  return kOk;
+}
+
+// FP64-accurate product for the refinement residual: the FP64 kernel, or in
+// the double-single mode the double-single kernel (one column at a time)
+int System::matvec_residual(int ncol, const double *x, double *y) {
+  if (precision_ != kPrecMixedDS) return matvec64(kMatvDirect, ncol, x, y, true);
+  if (!ds_scratch_) {
+    nsplit_ds_ = gpu::tmu_ds_pick_split(d_, gpu::sm_count());
+    if (dalloc(ds_scratch_, (size_t)nsplit_ds_ * 3 * d_.n)) {
+      ds_scratch_ = nullptr;
+      set_last_error("out of device memory for the double-single product");
+      return kErrMemory;
+    }
+  }
+  KEv e;
+  if (ktime_on_) e = kt_begin(2, ncol);
+  gpu::launch_tmu_ds(d_, ncol, x, y, true, ds_scratch_, nsplit_ds_, st_);
+  if (ktime_on_) kt_end(e);
+  stats_.ds_matvecs += 1;
   return kOk;
 }
 
@@ -628,7 +656,7 @@ int System::polarization(const double *e, int solver, int matv, const bool *mask
   }
   int st = kOk;
   if (solver == kSolverCG || solver == kSolverDIIS) {
-    bool mixed = solver == kSolverCG && precision_ == kPrecMixed && matv == kMatvDirect;
+    bool mixed = solver == kSolverCG && precision_ != kPrecFP64 && matv == kMatvDirect;
     if (mixed) {
       if (nipd == 2 && mask[0] && mask[1]) {
         // Identical D and P systems (right-hand sides and starting guesses
@@ -809,6 +837,22 @@ int System::tmatvec(const double *xh, double *yh, int nrhs, bool dodiag, int mat
   matvec64(matv, nrhs, p_, h_, dodiag);
   cudaMemcpyAsync(yh, h_, nrhs * nv * sizeof(double), cudaMemcpyDeviceToHost, st_);
   return check(cudaStreamSynchronize(st_), "tmatvec");
+}
+
+int System::tmatvec_ds(const double *xh, double *yh, int nrhs) {
+  const size_t nv = 3 * (size_t)d_.n;
+  if (nrhs < 1 || nrhs > 2) {
+    set_last_error("tmatvec_ds: nrhs must be 1 or 2");
+    return kErrBadArg;
+  }
+  cudaMemcpyAsync(p_, xh, nrhs * nv * sizeof(double), cudaMemcpyHostToDevice, st_);
+  const int keep = precision_;
+  precision_ = kPrecMixedDS;
+  int st = matvec_residual(nrhs, p_, h_);
+  precision_ = keep;
+  if (st) return st;
+  cudaMemcpyAsync(yh, h_, nrhs * nv * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  return check(cudaStreamSynchronize(st_), "tmatvec_ds");
 }
 
 int System::tmatvec_f32(const double *xh, double *yh, int nrhs) {

@@ -53,6 +53,7 @@ struct SolveStats {
   int inner_iters = 0;    // FP32 iterations summed over outer steps
   int f64_matvecs = 0;
   int f32_matvecs = 0;
+  int ds_matvecs = 0;     // double-single residual products
 };
 
 class System {
@@ -81,15 +82,19 @@ class System {
   void set_use_graphs(bool on) { use_graphs_ = on; }
   int tmatvec(const double *x_host, double *y_host, int nrhs, bool dodiag, int matv);
   int tmatvec_f32(const double *x_host, double *y_host, int nrhs);
+  int tmatvec_ds(const double *x_host, double *y_host, int nrhs);
   int e_m2d(double *out_host);
   void clear_guess() { ipd_use_guess_ = false; }
   void set_tol(double t) { tol_ = t; }
   void set_maxiter(int n) { maxiter_ = n; }
-  void set_precision(int p) { precision_ = p; }
+  void set_precision(int p) {
+    if (p >= kPrecFP64 && p <= kPrecMixedDS) precision_ = p;
+  }
   // FP64 direct product: 0 auto (symmetric from 2048 sites), 1 all ordered
   // pairs (target-outer), 2 symmetric (unordered pairs)
   int set_fp64_kernel(int mode);
   int set_fp32_kernel(int mode);
+  int matvec_residual(int ncol, const double *x, double *y);
   int precision() const { return precision_; }
   double tol() const { return tol_; }
   const SolveStats &stats() const { return stats_; }
@@ -167,6 +172,8 @@ class System {
   size_t scratch_n_ = 0;
   double *sym_scratch_ = nullptr;  // symmetric-kernel partials (allocated on first use)
   int fp64_kernel_ = 0;
+  double *ds_scratch_ = nullptr;  // split partials of the double-single product
+  int nsplit_ds_ = 1;
   int fp32_kernel_ = 0;  // 0 autotuned, else the forced kernel version
   float *scratch32_ = nullptr;
   double *partial_ = nullptr;  // reduction partials [kRedBlocks][8]
@@ -189,9 +196,9 @@ class System {
   SolveStats stats_;
   float last_ms_ = 0.f;
   bool ktime_on_ = false;
-  long long klaunch_[2] = {0, 0};
-  long long kcols_[2] = {0, 0};
-  double kms_[2] = {0, 0};
+  long long klaunch_[3] = {0, 0, 0};  // kernel timing: 0 FP64, 1 FP32, 2 double-single T.mu
+  long long kcols_[3] = {0, 0, 0};
+  double kms_[3] = {0, 0, 0};
   struct KEv {
     cudaEvent_t a, b;
     int kind;

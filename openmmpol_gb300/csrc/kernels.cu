@@ -25,6 +25,7 @@
 #include <type_traits>
 
 #include "kernels.h"
+#include "pair_math.cuh"
 
 namespace ommp {
 namespace gpu {
@@ -32,31 +33,6 @@ namespace gpu {
 namespace {
 constexpr int TPB = 128;   // targets per CTA
 constexpr int TILE = 128;  // sources per shared-memory tile
-
-// 1/sqrt(r2) in FP64 from the FP32 hardware estimate and one Newton-Raphson
-// step y <- y + y (1 - r2 y^2) / 2 (quadratic convergence: the ~2^-23
-// relative error of the seed becomes ~2e-14).  GB300 runs FP64 at 1/64 of
-// the FP32 rate, so the seed and the conversions cost less than a full-
-// precision FP64 reciprocal square root.
-__device__ __forceinline__ double rinv_f64(double r2, float r2f) {
-  double y = (double)rsqrtf(r2f);
-  double e = fma(-r2, y * y, 1.0);
-  return fma(0.5 * y, e, y);
-}
-
-// Damping pre-test in FP32 for the FP64 kernels.  AMOEBA damps when
-// a u^3 < thr with u = r / (thole_t thole_s); squared: a^2 q^3 < thr^2 with
-// q = r^2 (1/thole_t)^2 (1/thole_s)^2.  The FP32 test carries a relative
-// margin of 1e-5 (FP32 rounding of q is ~1e-7), so every pair that the exact
-// FP64 test damps enters the branch, where the FP64 test decides.
-__device__ __forceinline__ bool maybe_damped_amoeba(float r2f, float2 wat, float2 was, float thr2m) {
-  float q = r2f * wat.x * was.x;
-  return fminf(wat.y, was.y) * (q * q * q) < thr2m;
-}
-// Wang-AL damps when r < thole_t thole_s, i.e. q < 1.
-__device__ __forceinline__ bool maybe_damped_wang(float r2f, float2 wat, float2 was) {
-  return r2f * wat.x * was.x < 1.00001f;
-}
 
 // Field at target (position pt, 1/thole wt, damping at) of source s.
 template <bool AMOEBA>
@@ -218,91 +194,6 @@ __global__ void k_m2d_finish(int n, int nsplit, const double *__restrict__ parti
     }
   } else {
     for (int c = 0; c < 3; ++c) out[(size_t)j * 3 + c] = eP[c];
-  }
-}
-
-// ---------------------------------------------------------------------------
-// dipole-dipole field
-// ---------------------------------------------------------------------------
-template <typename T>
-struct Vec4;
-template <>
-struct Vec4<double> {
-  using type = Pos64;
-};
-template <>
-struct Vec4<float> {
-  using type = float4;
-};
-
-__device__ __forceinline__ double fast_rsqrt(double x) { return rsqrt(x); }
-__device__ __forceinline__ float fast_rsqrt(float x) { return rsqrtf(x); }
-__device__ __forceinline__ double fast_exp(double x) { return exp(x); }
-__device__ __forceinline__ float fast_exp(float x) { return __expf(x); }
-
-// Damped r^-3 and 3 r^-5 factors of the dipole field for one pair.
-template <typename T, bool AMOEBA>
-__device__ __forceinline__ void dd_kernel(T r2, T wt, T ws, T at, T as, T thr, T &k3, T &k5x3) {
-  T rinv = fast_rsqrt(r2);
-  T ir2 = rinv * rinv;
-  k3 = rinv * ir2;
-  T k5 = k3 * ir2;
-  T u = r2 * rinv * (wt * ws);
-  if (AMOEBA) {
-    T au3 = fmin(at, as) * u * u * u;
-    if (au3 < thr) {
-      T e = fast_exp(-au3);
-      k3 *= T(1) - e;
-      k5 *= T(1) - (T(1) + au3) * e;
-    }
-  } else {
-    if (u < T(1)) {
-      T u3 = u * u * u;
-      T u4 = u3 * u;
-      k3 *= T(4) * u3 - T(3) * u4;
-      k5 *= u4;
-    }
-  }
-  k5x3 = T(3) * k5;
-}
-
-// The pair factors in the precision of the kernel.  FP64: reciprocal square
-// root from the FP32 seed plus one Newton step and the FP32 damping
-// pre-test, so that only the arithmetic that needs FP64 runs on GB300's
-// FP64 pipe.  FP32: the plain formulas.
-template <typename T, bool AMOEBA>
-__device__ __forceinline__ void dd_pair(T r2, T wt, T ws, T at, T as, float2 wat, float2 was, T thr,
-                                        float thr2m, T &k3, T &k5x3) {
-  if constexpr (std::is_same<T, double>::value) {
-    float r2f = (float)r2;
-    double rinv = rinv_f64(r2, r2f);
-    double ir2 = rinv * rinv;
-    k3 = rinv * ir2;
-    double k5 = k3 * ir2;
-    if (AMOEBA) {
-      if (maybe_damped_amoeba(r2f, wat, was, thr2m)) {
-        double u = r2 * rinv * (wt * ws);
-        double au3 = fmin(at, as) * u * u * u;
-        if (au3 < thr) {
-          double e = exp(-au3);
-          k3 *= 1.0 - e;
-          k5 *= 1.0 - (1.0 + au3) * e;
-        }
-      }
-    } else {
-      if (maybe_damped_wang(r2f, wat, was)) {
-        double u = r2 * rinv * (wt * ws);
-        if (u < 1.0) {
-          double u3 = u * u * u;
-          double u4 = u3 * u;
-          k3 *= 4.0 * u3 - 3.0 * u4;
-          k5 *= u4;
-        }
-      }
-    }
-    k5x3 = 3.0 * k5;
-  } else {
-    dd_kernel<T, AMOEBA>(r2, wt, ws, at, as, thr, k3, k5x3);
   }
 }
 
@@ -1166,6 +1057,17 @@ void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, boo
   if (s.n == 0) return;
   tmu_dispatch<double, false>(s, nrhs, s.pol_pos, s.pol_a, x, scratch, nsplit, 4, st);
   tmu_finish<double>(s, nrhs, nsplit, scratch, s.pol_pos, s.pol_a, x, dodiag, y, 4, st);
+}
+
+void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
+                   int nsplit, cudaStream_t st) {
+  if (s.n == 0) return;
+  const size_t nv = 3 * (size_t)s.n;
+  for (int c = 0; c < nrhs; ++c) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    launch_tmu_ds_pairs(s, x + c * nv, scratch, nsplit, st);
+    tmu_finish<double>(s, 1, nsplit, scratch, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 1, st);
+  }
 }
 
 namespace {

@@ -31,6 +31,7 @@ struct DevSites {
   double *pol_alpha = nullptr;  // polarizability
   int *polar_mm = nullptr;      // mm index of each polarizable site
   float4 *pol_pos32 = nullptr;  // centred FP32 copy: x, y, z, 1/thole
+  float4 *pol_pos32lo = nullptr;  // x, y, z - pol_pos32 (double-single low parts), w = 0
   float *pol_a32 = nullptr;
   float2 *pol_wa32 = nullptr;   // (1/thole)^2, a^2 in FP32: damping pre-test of the FP64 kernels
   float2 *mm_wa32 = nullptr;    // same for the static sites (inf when not polarizable)
@@ -88,6 +89,12 @@ int tmu32_max_split(const DevSites &s, int sm_count);
 int tmu32_pick_split(const DevSites &s, int sm_count);
 void tile_boxes32(const float4 *pos32, int n, float4 *boxes /*[2*ceil(n/128)]*/);
 float damp_r2max32(bool amoeba, double damp_thr, const double *inv_thole, const double *a, int n);
+// Double-single product (tmu_ds.cu): y = T x for one column at a time with
+// ~1e-13 relative accuracy on the FP32 pipes; scratch of nsplit * n * 3.
+int tmu_ds_pick_split(const DevSites &s, int sm_count);
+void launch_tmu_ds_pairs(const DevSites &s, const double *x, double *partial, int nsplit, cudaStream_t st);
+void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
+                   int nsplit, cudaStream_t st);
 // batched fields: rhs[s*nf+f] = E_M2D[s] + field[f]; solution scatter to [f][s]
 void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
                       cudaStream_t st);

@@ -19,7 +19,7 @@ constexpr double kAng2Au = 1.8897261245650;
 constexpr double kEpsRp = 2.220446049250313e-16 * 100.0;
 constexpr int kSolverNone = 0, kSolverCG = 1, kSolverDIIS = 2, kSolverInversion = 3;
 constexpr int kMatvNone = 0, kMatvIncore = 1, kMatvDirect = 2;
-constexpr int kPrecFP64 = 0, kPrecMixed = 1;
+constexpr int kPrecFP64 = 0, kPrecMixed = 1, kPrecMixedDS = 2;
 
 // Compressed sparse rows, 0-based.
 struct Csr {

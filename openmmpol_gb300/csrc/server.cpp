@@ -350,8 +350,8 @@ extern "C" {
 int32_t ommp_gpu_server_create(int64_t hbm_budget_bytes, int32_t slots, int32_t precision, double tol,
                                void **server) {
   *server = nullptr;
-  if (hbm_budget_bytes <= 0 || slots < 1 || slots > 64) {
-    ommp::set_last_error("server: budget must be positive and slots 1..64");
+  if (hbm_budget_bytes <= 0 || slots < 1 || slots > 64 || precision < 0 || precision > 2) {
+    ommp::set_last_error("server: budget must be positive, slots 1..64 and precision 0..2");
     return ommp::kErrBadArg;
   }
   *server = new Server((size_t)hbm_budget_bytes, slots, precision, tol);

@@ -341,7 +341,8 @@ int System::mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, in
   const int cap = w.cap;
   log_msg(kVerbLow, nullptr, "Solving linear system with mixed-precision CG (FP32 inner, FP64 refinement)");
   if (have_guess) {
-    matvec64(kMatvDirect, ncol, x, w.h, true);
+    int st0 = matvec_residual(ncol, x, w.h);
+    if (st0) return st0;
     gpu::launch_residual(ncol * nv, rhs, w.h, w.r, st_);
   } else {
     cudaMemsetAsync(x, 0, ncol * nv * sizeof(double), st_);
@@ -385,7 +386,8 @@ int System::mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, in
     st = pcg32_ws(w, ncol, 200, eta);
     if (st) return st;
     gpu::launch_ir_accumulate(ncol, n, x, w.x32, w.dots + 2 * cap, st_);
-    matvec64(kMatvDirect, ncol, x, w.h, true);
+    st = matvec_residual(ncol, x, w.h);
+    if (st) return st;
     gpu::launch_residual(ncol * nv, rhs, w.h, w.r, st_);
     ++outer;
   }
@@ -436,7 +438,7 @@ int System::solve_batch(int nf, const double *fields, double *out, double *energ
   cudaEventRecord(ev0_, st_);
   gpu::launch_batch_rhs(n, nf, nsets, e_m2d_, fields, w.rhs, st_);
   cudaMemsetAsync(w.x, 0, ncol * nv * sizeof(double), st_);
-  if (precision_ == kPrecMixed) {
+  if (precision_ != kPrecFP64) {
     st = mixed_ir_ws(w, ncol, w.rhs, w.x, -1, false);
   } else {
     int matv = def_matv_ == kMatvIncore ? kMatvIncore : kMatvDirect;

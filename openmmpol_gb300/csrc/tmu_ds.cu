@@ -1,0 +1,281 @@
+// Double-single T.mu: FP64-accurate dipole field on GB300's FP32 pipes.
+//
+// The refinement residual E - T mu of the mixed-precision solver needs the
+// product to ~1e-12 relative; GB300 executes FP64 at 1/64 of its FP32 rate.
+// This kernel carries every quantity of an undamped pair as an unevaluated
+// sum of two floats (hi + lo, ~48-bit significand) built from error-free
+// transformations (Knuth's TwoSum, Dekker's FastTwoSum, FMA-based TwoProd;
+// double-word algorithms as analysed by Joldes, Muller and Popescu, ACM TOMS
+// 44(4), 2017), so each pair costs ~230 FP32 instructions instead of ~34 FP64
+// ones (~2,200 FP32 issue slots).  The few source tiles whose bounding box
+// comes within the Thole damping range of the CTA's targets run the FP64 pair
+// code of the FP64 kernels (damped factors need exp).  Per tile and target
+// the double-single sum is added to an FP64 accumulator; the split partials
+// [split][n][3] go through the same scaled-pair / diagonal pass
+// (k_tmu_finish<double>) as the FP64 product.
+//
+// Same product as TMatVec_otf / field_extD2D (src/mod_polarization.F90:459-481,
+// src/mod_electrostatics.F90:1954-2111).  Built with --fmad=false so that no
+// product is fused into a later addition behind the error-free
+// transformations' back (every intended FMA is an explicit fmaf), and with
+// -ftz=true (the reciprocal-square-root seed is the plain MUFU estimate).
+#include <cmath>
+
+#include "kernels.h"
+#include "pair_math.cuh"
+
+namespace ommp {
+namespace gpu {
+
+namespace {
+
+constexpr int DS_TPB = 128;
+constexpr int DS_TILE = 128;
+constexpr int DS_TPT = 2;  // targets per thread
+
+struct dsf {
+  float h, l;
+};
+
+// s + e = a + b exactly (Knuth)
+__device__ __forceinline__ dsf two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+// s + e = a + b exactly when |a| >= |b| or a = 0 (Dekker)
+__device__ __forceinline__ dsf fast_two_sum(float a, float b) {
+  float s = a + b;
+  float e = b - (s - a);
+  return {s, e};
+}
+// x * y, double-single operands
+__device__ __forceinline__ dsf ds_mul(dsf x, dsf y) {
+  float p = x.h * y.h;
+  float e = fmaf(x.h, y.h, -p);
+  e = fmaf(x.h, y.l, e);
+  e = fmaf(x.l, y.h, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ dsf ds_sqr(dsf x) {
+  float p = x.h * x.h;
+  float e = fmaf(x.h, x.h, -p);
+  e = fmaf(x.h + x.h, x.l, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ dsf ds_mulf(dsf x, float y) {
+  float p = x.h * y;
+  float e = fmaf(x.h, y, -p);
+  e = fmaf(x.l, y, e);
+  return fast_two_sum(p, e);
+}
+// (ah + al) - (bh + bl): the hi difference is exact, the lo difference
+// rounds once; absolute error ~2^-48 of the operands (coordinates)
+__device__ __forceinline__ dsf ds_diff(float ah, float al, float bh, float bl) {
+  dsf s = two_sum(ah, -bh);
+  return fast_two_sum(s.h, s.l + (al - bl));
+}
+// 1/sqrt(a): FP32 estimate y, one Newton step y (1 + (1 - a y^2) / 2) with
+// 1 - a y^2 formed in double-single (the estimate's 2^-22 error squares)
+__device__ __forceinline__ dsf ds_rsqrt(dsf a) {
+  float y = rsqrtf(a.h);
+  float p = y * y;
+  dsf y2{p, fmaf(y, y, -p)};
+  dsf t = ds_mul(a, y2);
+  float e = (1.0f - t.h) - t.l;  // 1 - t.h is exact: t.h is within 2^-21 of 1
+  float c = (0.5f * y) * e;
+  return fast_two_sum(y, c);
+}
+// acc += p_exact(x * y) with x, y double-single, lazily (acc.l collects the
+// low-order parts; the caller renormalises)
+__device__ __forceinline__ void acc_mul(float &ah, float &al, dsf x, dsf y) {
+  float p = x.h * y.h;
+  float q = fmaf(x.h, y.h, -p);
+  q = fmaf(x.h, y.l, q);
+  q = fmaf(x.l, y.h, q);
+  dsf s = two_sum(ah, p);
+  ah = s.h;
+  al += s.l + q;
+}
+
+template <bool AMOEBA>
+__global__ void __launch_bounds__(DS_TPB) k_tmu_ds(int n, const float4 *__restrict__ ph, const float4 *__restrict__ pl,
+                                                   const Pos64 *__restrict__ p64, const double *__restrict__ damp,
+                                                   const float2 *__restrict__ wa, const float4 *__restrict__ boxes,
+                                                   const double *__restrict__ x, double *__restrict__ partial,
+                                                   int per_split, double thr, float thr2m, float r2max) {
+  __shared__ float4 s_ph[DS_TILE], s_pl[DS_TILE], s_mh[DS_TILE], s_ml[DS_TILE];
+  __shared__ Pos64 s_p64[DS_TILE];
+  __shared__ double s_a[DS_TILE];
+  __shared__ float2 s_wa[DS_TILE];
+  __shared__ double s_mu[3][DS_TILE];
+  const int jb = blockIdx.x * (DS_TPB * DS_TPT);
+  float4 th[DS_TPT], tl[DS_TPT];
+  bool valid[DS_TPT];
+  double sum[DS_TPT][3];
+#pragma unroll
+  for (int t = 0; t < DS_TPT; ++t) {
+    const int j = jb + t * DS_TPB + threadIdx.x;
+    valid[t] = j < n;
+    th[t] = valid[t] ? ph[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    tl[t] = valid[t] ? pl[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    sum[t][0] = sum[t][1] = sum[t][2] = 0.0;
+  }
+  const int ntile = (n + DS_TILE - 1) / DS_TILE;
+  const int tb0 = jb / DS_TILE;
+  const int tb1 = min(ntile - 1, (jb + DS_TPB * DS_TPT - 1) / DS_TILE);
+  float4 blo = boxes[2 * tb0], bhi = boxes[2 * tb0 + 1];
+  for (int tb = tb0 + 1; tb <= tb1; ++tb) {
+    float4 lo = boxes[2 * tb], hi = boxes[2 * tb + 1];
+    blo.x = fminf(blo.x, lo.x), blo.y = fminf(blo.y, lo.y), blo.z = fminf(blo.z, lo.z);
+    bhi.x = fmaxf(bhi.x, hi.x), bhi.y = fmaxf(bhi.y, hi.y), bhi.z = fmaxf(bhi.z, hi.z);
+  }
+
+  const int s0 = blockIdx.y * per_split;
+  const int s1 = min(n, s0 + per_split);
+  for (int t0 = s0; t0 < s1; t0 += DS_TILE) {
+    __syncthreads();
+    {
+      const int k = threadIdx.x;
+      const int i = t0 + k;
+      if (i < s1) {
+        s_ph[k] = ph[i];
+        s_pl[k] = pl[i];
+        s_p64[k] = p64[i];
+        s_a[k] = AMOEBA ? damp[i] : 0.0;
+        s_wa[k] = wa[i];
+        double m[3];
+        float mh[3], ml[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          m[c] = x[(size_t)i * 3 + c];
+          s_mu[c][k] = m[c];
+          mh[c] = (float)m[c];
+          ml[c] = (float)(m[c] - (double)mh[c]);
+        }
+        s_mh[k] = make_float4(mh[0], mh[1], mh[2], 0.f);
+        s_ml[k] = make_float4(ml[0], ml[1], ml[2], 0.f);
+      }
+    }
+    __syncthreads();
+    const int cnt = min(DS_TILE, s1 - t0);
+    const float4 slo = boxes[2 * (t0 / DS_TILE)], shi = boxes[2 * (t0 / DS_TILE) + 1];
+    const float gx = fmaxf(0.f, fmaxf(slo.x - bhi.x, blo.x - shi.x));
+    const float gy = fmaxf(0.f, fmaxf(slo.y - bhi.y, blo.y - shi.y));
+    const float gz = fmaxf(0.f, fmaxf(slo.z - bhi.z, blo.z - shi.z));
+    const bool far_tile = gx * gx + gy * gy + gz * gz > r2max;
+    if (far_tile) {
+      float ah[DS_TPT][3], al[DS_TPT][3];
+#pragma unroll
+      for (int t = 0; t < DS_TPT; ++t)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ah[t][c] = al[t][c] = 0.f;
+#pragma unroll 1
+      for (int k = 0; k < cnt; ++k) {
+        const float4 sh = s_ph[k], sl = s_pl[k], mh = s_mh[k], ml = s_ml[k];
+#pragma unroll
+        for (int t = 0; t < DS_TPT; ++t) {
+          const dsf dx = ds_diff(th[t].x, tl[t].x, sh.x, sl.x);
+          const dsf dy = ds_diff(th[t].y, tl[t].y, sh.y, sl.y);
+          const dsf dz = ds_diff(th[t].z, tl[t].z, sh.z, sl.z);
+          // r^2
+          float px = dx.h * dx.h, py = dy.h * dy.h, pz = dz.h * dz.h;
+          float ex = fmaf(dx.h + dx.h, dx.l, fmaf(dx.h, dx.h, -px));
+          float ey = fmaf(dy.h + dy.h, dy.l, fmaf(dy.h, dy.h, -py));
+          float ez = fmaf(dz.h + dz.h, dz.l, fmaf(dz.h, dz.h, -pz));
+          const dsf sa = two_sum(px, py);
+          const dsf sb = two_sum(sa.h, pz);
+          const dsf r2 = fast_two_sum(sb.h, ((ex + ey) + ez) + (sa.l + sb.l));
+          const dsf rinv = ds_rsqrt(r2);
+          const dsf ir2 = ds_sqr(rinv);
+          const dsf k3 = ds_mul(rinv, ir2);
+          const dsf k5x3 = ds_mulf(ds_mul(k3, ir2), 3.0f);
+          // mu . d
+          float qx = mh.x * dx.h, qy = mh.y * dy.h, qz = mh.z * dz.h;
+          float fx = fmaf(ml.x, dx.h, fmaf(mh.x, dx.l, fmaf(mh.x, dx.h, -qx)));
+          float fy = fmaf(ml.y, dy.h, fmaf(mh.y, dy.l, fmaf(mh.y, dy.h, -qy)));
+          float fz = fmaf(ml.z, dz.h, fmaf(mh.z, dz.l, fmaf(mh.z, dz.h, -qz)));
+          dsf u1 = two_sum(qx, qy);
+          dsf u2 = two_sum(u1.h, qz);
+          const dsf dot = fast_two_sum(u2.h, ((fx + fy) + fz) + (u1.l + u2.l));
+          const dsf f = ds_mul(k5x3, dot);
+          const dsf nk3{-k3.h, -k3.l};
+          // field += f d - k3 mu
+          acc_mul(ah[t][0], al[t][0], f, dx);
+          acc_mul(ah[t][0], al[t][0], nk3, dsf{mh.x, ml.x});
+          acc_mul(ah[t][1], al[t][1], f, dy);
+          acc_mul(ah[t][1], al[t][1], nk3, dsf{mh.y, ml.y});
+          acc_mul(ah[t][2], al[t][2], f, dz);
+          acc_mul(ah[t][2], al[t][2], nk3, dsf{mh.z, ml.z});
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            dsf r = fast_two_sum(ah[t][c], al[t][c]);
+            ah[t][c] = r.h;
+            al[t][c] = r.l;
+          }
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < DS_TPT; ++t)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sum[t][c] += (double)ah[t][c] + (double)al[t][c];
+    } else {
+      // tiles within the damping range: the FP64 pair code
+#pragma unroll
+      for (int t = 0; t < DS_TPT; ++t) {
+        const int j = jb + t * DS_TPB + threadIdx.x;
+        if (!valid[t]) continue;
+        const Pos64 pt = p64[j];
+        const double at = AMOEBA ? damp[j] : 0.0;
+        const float2 wat = wa[j];
+        for (int k = 0; k < cnt; ++k) {
+          if (t0 + k == j) continue;
+          const Pos64 ps = s_p64[k];
+          double dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
+          double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+          double k3, k5x3;
+          dd_pair<double, AMOEBA>(r2, pt.w, ps.w, at, s_a[k], wat, s_wa[k], thr, thr2m, k3, k5x3);
+          const double mx = s_mu[0][k], my = s_mu[1][k], mz = s_mu[2][k];
+          const double f = k5x3 * fma(mx, dx, fma(my, dy, mz * dz));
+          sum[t][0] += fma(f, dx, -k3 * mx);
+          sum[t][1] += fma(f, dy, -k3 * my);
+          sum[t][2] += fma(f, dz, -k3 * mz);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < DS_TPT; ++t) {
+    const int j = jb + t * DS_TPB + threadIdx.x;
+    if (!valid[t]) continue;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) partial[((size_t)blockIdx.y * n + j) * 3 + c] = sum[t][c];
+  }
+}
+
+}  // namespace
+
+int tmu_ds_pick_split(const DevSites &s, int sms) {
+  const int tblocks = (s.n + DS_TPB * DS_TPT - 1) / (DS_TPB * DS_TPT);
+  const int tiles = (s.n + DS_TILE - 1) / DS_TILE;
+  int split = (4 * sms + tblocks - 1) / tblocks;
+  if (split > tiles) split = tiles;
+  return split < 1 ? 1 : split;
+}
+
+void launch_tmu_ds_pairs(const DevSites &s, const double *x, double *partial, int nsplit, cudaStream_t st) {
+  const int tiles = (s.n + DS_TILE - 1) / DS_TILE;
+  const int per = ((tiles + nsplit - 1) / nsplit) * DS_TILE;
+  dim3 grid((s.n + DS_TPB * DS_TPT - 1) / (DS_TPB * DS_TPT), nsplit);
+  const float thr2m = (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));
+  if (s.amoeba)
+    k_tmu_ds<true><<<grid, DS_TPB, 0, st>>>(s.n, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32,
+                                            s.tile_box32, x, partial, per, s.damp_thr, thr2m, s.damp_r2max32);
+  else
+    k_tmu_ds<false><<<grid, DS_TPB, 0, st>>>(s.n, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32,
+                                             s.tile_box32, x, partial, per, s.damp_thr, thr2m, s.damp_r2max32);
+}
+
+}  // namespace gpu
+}  // namespace ommp

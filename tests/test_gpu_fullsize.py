@@ -75,3 +75,17 @@ def test_w30k_mixed_precision_matches_oracle_fixture(w30k):
     _check_against_fixture(g, ref, 1e-7)
     assert g.residual_history(0)[-1] < 1e-10
     assert _sampled_residual(p, g, ef) < 1e-7
+
+
+def test_w30k_mixed_ds_matches_oracle_fixture(w30k):
+    p, g, ef = w30k
+    ref = np.load(FIX)
+    g.set_precision("mixed-ds")
+    g.set_solver_tol(1e-10)
+    g.clear_guess()
+    g.set_external_field(ef)
+    _check_against_fixture(g, ref, 1e-7)
+    assert g.residual_history(0)[-1] < 1e-10
+    assert g.counter(0) == 0 and g.counter(4) >= 1
+    assert _sampled_residual(p, g, ef) < 1e-7
+    g.set_precision("fp64")

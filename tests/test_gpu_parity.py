@@ -248,6 +248,35 @@ def test_fp32_operator_accuracy(case, kernel, w1k, chains, golden_mmp):
     assert site.max() < 1e-4
 
 
+@pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba", "nma_wang"])
+def test_double_single_operator_accuracy(case, w1k, chains, golden_mmp):
+    """The double-single product against the FP64 one: 1e-11 relative overall
+    and 1e-9 at every site (the refinement residual needs ~1e-10)."""
+    p = {"w1k": w1k[0], "chains": chains[0]}.get(case) or golden_mmp[case]
+    g = OMMPSystem(p)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((2, g.pol_atoms, 3)) * 0.05
+    y64 = g.tmatvec(x)
+    yds = g.tmatvec_ds(x)
+    assert rel(yds, y64) < 1e-11
+    site = np.linalg.norm(yds - y64, axis=2) / np.maximum(np.linalg.norm(y64, axis=2), 1e-3 * np.abs(y64).max())
+    assert site.max() < 1e-9
+
+
+@pytest.mark.parametrize("case", ["w1k", "chains"])
+def test_mixed_ds_solve(case, w1k, chains):
+    p, ef = {"w1k": w1k, "chains": chains}[case]
+    ref = converged_reference(p, ef)
+    g = OMMPSystem(p)
+    g.set_solver_tol(1e-10)
+    g.set_precision("mixed-ds")
+    g.set_external_field(ef)
+    assert rel(g.ipd, ref.ipd) < 1e-7
+    assert abs(g.get_polelec_energy() - ref.get_polelec_energy()) <= 1e-7 * abs(ref.get_polelec_energy())
+    assert g.counter(4) >= 1 and g.counter(0) == 0  # residual products in double-single, none in FP64
+    assert g.residual_history(0)[-1] < 1e-10
+
+
 @pytest.mark.parametrize("kernel", ["pairwise", "tiled"])
 def test_mixed_solve_with_each_fp32_kernel(kernel, chains):
     p, ef = chains

@@ -8,8 +8,9 @@
 // double-word algorithms as analysed by Joldes, Muller and Popescu, ACM TOMS
 // 44(4), 2017), so each pair costs ~230 FP32 instructions instead of ~34 FP64
 // ones (~2,200 FP32 issue slots).  The few source tiles whose bounding box
-// comes within the Thole damping range of the CTA's targets run the FP64 pair
-// code of the FP64 kernels (damped factors need exp).  Per tile and target
+// comes within the Thole damping range of the CTA's targets test each pair in
+// FP32 and form the Thole factors of the (few) damped ones in FP64, applied
+// in double-single.  Per tile and target
 // the double-single sum is added to an FP64 accumulator; the split partials
 // [split][n][3] go through the same scaled-pair / diagonal pass
 // (k_tmu_finish<double>) as the FP64 product.
@@ -99,8 +100,84 @@ __device__ __forceinline__ void acc_mul(float &ah, float &al, dsf x, dsf y) {
   al += s.l + q;
 }
 
+__device__ __forceinline__ dsf to_ds(double v) {
+  float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+
+// One ordered pair in double-single: acc += 3 r^-5 (mu.d) d - r^-3 mu.
+// NEAR: the pair may be damped; an FP32 pre-test (1e-5 margin) selects the
+// pairs whose Thole factors are then formed in FP64 (exp) and applied in
+// double-single.  Far pairs (tile boxes beyond the damping range) skip it.
+template <bool NEAR, bool AMOEBA>
+__device__ __forceinline__ void ds_pair(const float4 &th, const float4 &tl, const float4 &sh, const float4 &sl,
+                                        const float4 &mh, const float4 &ml, float (&ah)[3], float (&al)[3],
+                                        double wt, double ws, double at, double as, float2 wat, float2 was,
+                                        double thr, float thr2m) {
+  const dsf dx = ds_diff(th.x, tl.x, sh.x, sl.x);
+  const dsf dy = ds_diff(th.y, tl.y, sh.y, sl.y);
+  const dsf dz = ds_diff(th.z, tl.z, sh.z, sl.z);
+  // r^2
+  float px = dx.h * dx.h, py = dy.h * dy.h, pz = dz.h * dz.h;
+  float ex = fmaf(dx.h + dx.h, dx.l, fmaf(dx.h, dx.h, -px));
+  float ey = fmaf(dy.h + dy.h, dy.l, fmaf(dy.h, dy.h, -py));
+  float ez = fmaf(dz.h + dz.h, dz.l, fmaf(dz.h, dz.h, -pz));
+  const dsf sa = two_sum(px, py);
+  const dsf sb = two_sum(sa.h, pz);
+  const dsf r2 = fast_two_sum(sb.h, ((ex + ey) + ez) + (sa.l + sb.l));
+  const dsf rinv = ds_rsqrt(r2);
+  const dsf ir2 = ds_sqr(rinv);
+  dsf k3 = ds_mul(rinv, ir2);
+  dsf k5 = ds_mul(k3, ir2);
+  if (NEAR) {
+    const bool maybe = AMOEBA ? maybe_damped_amoeba(r2.h, wat, was, thr2m) : maybe_damped_wang(r2.h, wat, was);
+    if (maybe) {
+      const double u = sqrt((double)r2.h + (double)r2.l) * (wt * ws);  // r / (thole_t thole_s)
+      double f3 = 1.0, f5 = 1.0;
+      if (AMOEBA) {
+        const double au3 = fmin(at, as) * u * u * u;
+        if (au3 < thr) {
+          const double e = exp(-au3);
+          f3 = 1.0 - e;
+          f5 = 1.0 - (1.0 + au3) * e;
+        }
+      } else if (u < 1.0) {
+        const double u3 = u * u * u;
+        const double u4 = u3 * u;
+        f3 = 4.0 * u3 - 3.0 * u4;
+        f5 = u4;
+      }
+      k3 = ds_mul(k3, to_ds(f3));
+      k5 = ds_mul(k5, to_ds(f5));
+    }
+  }
+  const dsf k5x3 = ds_mulf(k5, 3.0f);
+  // mu . d
+  float qx = mh.x * dx.h, qy = mh.y * dy.h, qz = mh.z * dz.h;
+  float fx = fmaf(ml.x, dx.h, fmaf(mh.x, dx.l, fmaf(mh.x, dx.h, -qx)));
+  float fy = fmaf(ml.y, dy.h, fmaf(mh.y, dy.l, fmaf(mh.y, dy.h, -qy)));
+  float fz = fmaf(ml.z, dz.h, fmaf(mh.z, dz.l, fmaf(mh.z, dz.h, -qz)));
+  const dsf u1 = two_sum(qx, qy);
+  const dsf u2 = two_sum(u1.h, qz);
+  const dsf dot = fast_two_sum(u2.h, ((fx + fy) + fz) + (u1.l + u2.l));
+  const dsf f = ds_mul(k5x3, dot);
+  const dsf nk3{-k3.h, -k3.l};
+  acc_mul(ah[0], al[0], f, dx);
+  acc_mul(ah[0], al[0], nk3, dsf{mh.x, ml.x});
+  acc_mul(ah[1], al[1], f, dy);
+  acc_mul(ah[1], al[1], nk3, dsf{mh.y, ml.y});
+  acc_mul(ah[2], al[2], f, dz);
+  acc_mul(ah[2], al[2], nk3, dsf{mh.z, ml.z});
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const dsf r = fast_two_sum(ah[c], al[c]);
+    ah[c] = r.h;
+    al[c] = r.l;
+  }
+}
+
 template <bool AMOEBA>
-__global__ void __launch_bounds__(DS_TPB) k_tmu_ds(int n, const float4 *__restrict__ ph, const float4 *__restrict__ pl,
+__global__ void __launch_bounds__(DS_TPB, 5) k_tmu_ds(int n, const float4 *__restrict__ ph, const float4 *__restrict__ pl,
                                                    const Pos64 *__restrict__ p64, const double *__restrict__ damp,
                                                    const float2 *__restrict__ wa, const float4 *__restrict__ boxes,
                                                    const double *__restrict__ x, double *__restrict__ partial,
@@ -109,7 +186,6 @@ __global__ void __launch_bounds__(DS_TPB) k_tmu_ds(int n, const float4 *__restri
   __shared__ Pos64 s_p64[DS_TILE];
   __shared__ double s_a[DS_TILE];
   __shared__ float2 s_wa[DS_TILE];
-  __shared__ double s_mu[3][DS_TILE];
   const int jb = blockIdx.x * (DS_TPB * DS_TPT);
   float4 th[DS_TPT], tl[DS_TPT];
   bool valid[DS_TPT];
@@ -150,7 +226,6 @@ __global__ void __launch_bounds__(DS_TPB) k_tmu_ds(int n, const float4 *__restri
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           m[c] = x[(size_t)i * 3 + c];
-          s_mu[c][k] = m[c];
           mh[c] = (float)m[c];
           ml[c] = (float)(m[c] - (double)mh[c]);
         }
@@ -165,85 +240,48 @@ __global__ void __launch_bounds__(DS_TPB) k_tmu_ds(int n, const float4 *__restri
     const float gy = fmaxf(0.f, fmaxf(slo.y - bhi.y, blo.y - shi.y));
     const float gz = fmaxf(0.f, fmaxf(slo.z - bhi.z, blo.z - shi.z));
     const bool far_tile = gx * gx + gy * gy + gz * gz > r2max;
+    float ah[DS_TPT][3], al[DS_TPT][3];
+#pragma unroll
+    for (int t = 0; t < DS_TPT; ++t)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ah[t][c] = al[t][c] = 0.f;
     if (far_tile) {
-      float ah[DS_TPT][3], al[DS_TPT][3];
-#pragma unroll
-      for (int t = 0; t < DS_TPT; ++t)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) ah[t][c] = al[t][c] = 0.f;
 #pragma unroll 1
       for (int k = 0; k < cnt; ++k) {
         const float4 sh = s_ph[k], sl = s_pl[k], mh = s_mh[k], ml = s_ml[k];
 #pragma unroll
-        for (int t = 0; t < DS_TPT; ++t) {
-          const dsf dx = ds_diff(th[t].x, tl[t].x, sh.x, sl.x);
-          const dsf dy = ds_diff(th[t].y, tl[t].y, sh.y, sl.y);
-          const dsf dz = ds_diff(th[t].z, tl[t].z, sh.z, sl.z);
-          // r^2
-          float px = dx.h * dx.h, py = dy.h * dy.h, pz = dz.h * dz.h;
-          float ex = fmaf(dx.h + dx.h, dx.l, fmaf(dx.h, dx.h, -px));
-          float ey = fmaf(dy.h + dy.h, dy.l, fmaf(dy.h, dy.h, -py));
-          float ez = fmaf(dz.h + dz.h, dz.l, fmaf(dz.h, dz.h, -pz));
-          const dsf sa = two_sum(px, py);
-          const dsf sb = two_sum(sa.h, pz);
-          const dsf r2 = fast_two_sum(sb.h, ((ex + ey) + ez) + (sa.l + sb.l));
-          const dsf rinv = ds_rsqrt(r2);
-          const dsf ir2 = ds_sqr(rinv);
-          const dsf k3 = ds_mul(rinv, ir2);
-          const dsf k5x3 = ds_mulf(ds_mul(k3, ir2), 3.0f);
-          // mu . d
-          float qx = mh.x * dx.h, qy = mh.y * dy.h, qz = mh.z * dz.h;
-          float fx = fmaf(ml.x, dx.h, fmaf(mh.x, dx.l, fmaf(mh.x, dx.h, -qx)));
-          float fy = fmaf(ml.y, dy.h, fmaf(mh.y, dy.l, fmaf(mh.y, dy.h, -qy)));
-          float fz = fmaf(ml.z, dz.h, fmaf(mh.z, dz.l, fmaf(mh.z, dz.h, -qz)));
-          dsf u1 = two_sum(qx, qy);
-          dsf u2 = two_sum(u1.h, qz);
-          const dsf dot = fast_two_sum(u2.h, ((fx + fy) + fz) + (u1.l + u2.l));
-          const dsf f = ds_mul(k5x3, dot);
-          const dsf nk3{-k3.h, -k3.l};
-          // field += f d - k3 mu
-          acc_mul(ah[t][0], al[t][0], f, dx);
-          acc_mul(ah[t][0], al[t][0], nk3, dsf{mh.x, ml.x});
-          acc_mul(ah[t][1], al[t][1], f, dy);
-          acc_mul(ah[t][1], al[t][1], nk3, dsf{mh.y, ml.y});
-          acc_mul(ah[t][2], al[t][2], f, dz);
-          acc_mul(ah[t][2], al[t][2], nk3, dsf{mh.z, ml.z});
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            dsf r = fast_two_sum(ah[t][c], al[t][c]);
-            ah[t][c] = r.h;
-            al[t][c] = r.l;
-          }
-        }
+        for (int t = 0; t < DS_TPT; ++t)
+          ds_pair<false, AMOEBA>(th[t], tl[t], sh, sl, mh, ml, ah[t], al[t], 0.0, 0.0, 0.0, 0.0, make_float2(0.f, 0.f),
+                                 make_float2(0.f, 0.f), thr, thr2m);
       }
-#pragma unroll
-      for (int t = 0; t < DS_TPT; ++t)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) sum[t][c] += (double)ah[t][c] + (double)al[t][c];
     } else {
-      // tiles within the damping range: the FP64 pair code
+      // tiles within the damping range: per-pair pre-test, FP64 Thole factors
+      double wt[DS_TPT], at[DS_TPT];
+      float2 wat[DS_TPT];
 #pragma unroll
       for (int t = 0; t < DS_TPT; ++t) {
-        const int j = jb + t * DS_TPB + threadIdx.x;
-        if (!valid[t]) continue;
-        const Pos64 pt = p64[j];
-        const double at = AMOEBA ? damp[j] : 0.0;
-        const float2 wat = wa[j];
-        for (int k = 0; k < cnt; ++k) {
-          if (t0 + k == j) continue;
-          const Pos64 ps = s_p64[k];
-          double dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
-          double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-          double k3, k5x3;
-          dd_pair<double, AMOEBA>(r2, pt.w, ps.w, at, s_a[k], wat, s_wa[k], thr, thr2m, k3, k5x3);
-          const double mx = s_mu[0][k], my = s_mu[1][k], mz = s_mu[2][k];
-          const double f = k5x3 * fma(mx, dx, fma(my, dy, mz * dz));
-          sum[t][0] += fma(f, dx, -k3 * mx);
-          sum[t][1] += fma(f, dy, -k3 * my);
-          sum[t][2] += fma(f, dz, -k3 * mz);
+        const int j = valid[t] ? jb + t * DS_TPB + threadIdx.x : 0;
+        wt[t] = p64[j].w;
+        at[t] = AMOEBA ? damp[j] : 0.0;
+        wat[t] = wa[j];
+      }
+#pragma unroll 1
+      for (int k = 0; k < cnt; ++k) {
+        const float4 sh = s_ph[k], sl = s_pl[k], mh = s_mh[k], ml = s_ml[k];
+        const double ws = s_p64[k].w, as = s_a[k];
+        const float2 was = s_wa[k];
+#pragma unroll
+        for (int t = 0; t < DS_TPT; ++t) {
+          if (!valid[t] || t0 + k == jb + t * DS_TPB + (int)threadIdx.x) continue;
+          ds_pair<true, AMOEBA>(th[t], tl[t], sh, sl, mh, ml, ah[t], al[t], wt[t], ws, at[t], as, wat[t], was, thr,
+                                thr2m);
         }
       }
     }
+#pragma unroll
+    for (int t = 0; t < DS_TPT; ++t)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) sum[t][c] += (double)ah[t][c] + (double)al[t][c];
   }
 #pragma unroll
   for (int t = 0; t < DS_TPT; ++t) {

@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 METRIC = "induced-dipole solves/s (mixed FP32/FP64 at <=1e-7 rel. error vs FP64)"
 FLOP_PER_PAIR = 45.0  # per ordered T.mu pair and right-hand side
 # FP32 operations (an FMA counts once) per undamped ordered pair of the
-# double-single kernel, counted in csrc/tmu_ds.cu: 3 coordinate differences
+# double-single kernel, counted in openmmpol_gb300/csrc/ds_kernels.cu: 3 coordinate differences
 # (33), r^2 (31), reciprocal square root (17 + 1 MUFU), r^-2 / r^-3 / 3 r^-5
 # (27), mu.d (31), the field factor (7), six accumulations (72) and three
 # renormalisations (9)
@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-ds", action="store_true", help="leave out the double-single pass")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-ds"],
                     help="mixed: FP64 refinement residual products; mixed-ds: double-single ones")
     ap.add_argument("--fp32-kernel", default="auto", choices=["auto", "pairwise", "tiled"],
@@ -223,6 +224,51 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def kernel_table(kst, n, peak64, peak32):
+    """Per pair kernel: launches, columns, time and the rate against its pipe."""
+    pairs = float(n) * (n - 1)
+    out = {}
+    for name, (cnt, ms, cols), pk in (("tmu_fp64", kst[0], peak64), ("tmu_fp32", kst[1], peak32),
+                                      ("tmu_ds", kst[2], peak32)):
+        if not cnt:
+            continue
+        # algorithmic flop of all timed launches: 45 per ordered pair per column
+        ach = FLOP_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
+        out[name] = {"launches": cnt, "columns": cols, "total_ms": ms, "avg_ms": ms / cnt,
+                     "achieved_tflops": ach, "peak_tflops": pk, "frac": ach / pk if pk else None}
+        if name == "tmu_ds":
+            # FP32 pipe: double-single operations issued per second against
+            # the FMA-pipe instruction rate (peak flop / 2)
+            ops = DS_OPS_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
+            out[name].update({"fp64_equivalent_tflops": ach, "achieved_tops": ops, "peak_tops": pk / 2,
+                              "frac": ops / (pk / 2) if pk else None})
+    return out
+
+
+def roofline_of(kstats, total_ms):
+    if not kstats:
+        return None
+    dom = max(kstats, key=lambda k: kstats[k]["total_ms"])
+    d = kstats[dom]
+    ds = dom == "tmu_ds"
+    return {"bound": "fp64" if dom == "tmu_fp64" else "fp32", "kernel": dom,
+            "achieved": d["achieved_tops"] if ds else d["achieved_tflops"],
+            "peak": d["peak_tops"] if ds else d["peak_tflops"],
+            "unit": "Tops/s (FP32 instructions)" if ds else "TFLOP/s",
+            "frac": d["frac"], "traffic": None,
+            "peak_source": "FMA-chain kernel measured in this run (pipe peak; "
+                           "MEASURED_PEAKS.json has no FP32/FP64 CUDA-core figure)",
+            "algorithmic": (f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair" if ds else
+                            f"{FLOP_PER_PAIR:.0f} flop per ordered pair") +
+                           f" x N(N-1) pairs x right-hand sides ({d['columns']} columns over "
+                           f"{d['launches']} launches)",
+            "share_of_timed": d["total_ms"] / total_ms}
+
+
+def rel_err(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
 def run_gb300(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -243,6 +289,7 @@ def run_gb300(args):
     sys_ = og.OMMPSystem(path)
     sys_.set_solver_tol(1e-10)
     sys_.set_fp32_kernel(args.fp32_kernel)
+    sys_.set_precision(args.precision)
     n = sys_.pol_atoms
     cpol, cmm = sys_.cpol, sys_.cmm
     center = w.box_center()
@@ -257,17 +304,19 @@ def run_gb300(args):
         assert L.ommp_gpu_device_alloc(nv * 8, C.byref(p)) == 0
         assert L.ommp_gpu_copy_to_device(p, f.ctypes.data, nv * 8) == 0
         dev.append(p)
-    h = sys_._h
     # first solve on this geometry computes E_M2D (timed separately)
     t0 = time.perf_counter()
-    st = L.ommp_gpu_get_e_m2d(h, np.zeros((sys_.n_ipd, n, 3)).ctypes.data_as(_lib._dp))
+    e_main = sys_.e_m2d()
     m2d_s = time.perf_counter() - t0
-    assert st == 0, L.ommp_gpu_last_error()
-    sys_.set_precision(args.precision)
     flush = 256 << 20
+    peak64 = C.c_double(0)
+    peak32 = C.c_double(0)
+    L.ommp_gpu_measure_pipe_peak(1, C.byref(peak64))
+    L.ommp_gpu_measure_pipe_peak(0, C.byref(peak32))
 
-    def one_step(k, timed):
-        sys_.clear_guess()
+    def one_step(g, k):
+        h = g._h
+        g.clear_guess()
         L.ommp_gpu_flush_l2(h, flush)
         L.ommp_gpu_timer_record(h, 0)
         st = L.ommp_gpu_set_external_field_device(h, dev[k], 0, 0, 1)
@@ -278,61 +327,78 @@ def run_gb300(args):
         L.ommp_gpu_timer_elapsed(h, 0, 1, C.byref(ms))
         return ms.value
 
-    for k in range(W):
-        one_step(k, False)
-    if dist:
-        dist.barrier()
-    sys_.synchronize()
-    L.ommp_gpu_reset_kernel_stats(h)
-    sys_.enable_kernel_timing(True)
-    launches0 = L.ommp_gpu_kernel_launch_count()
-    clk = Clocks(local if ws > 1 else 0)
-    step_ms = []
-    counters = []
-    wall0 = time.perf_counter()
-    for k in range(W, W + K):
-        step_ms.append(one_step(k, True))
-        counters.append((sys_.counter(0), sys_.counter(1), sys_.counter(2), sys_.counter(3), sys_.counter(4)))
-    sys_.synchronize()
-    wall = time.perf_counter() - wall0
-    clocks = clk.stop()
-    launches = L.ommp_gpu_kernel_launch_count() - launches0
-    sys_.enable_kernel_timing(False)
-    k64 = sys_.kernel_stats(0)
-    k32 = sys_.kernel_stats(1)
-    kds = sys_.kernel_stats(2)
-    total_ms = sum(step_ms)
-    if dist:
-        import torch
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = ws * K / (total_ms * 1e-3)
-    mixed_ipd = sys_.ipd.copy()
-    mixed_ep = sys_.get_polelec_energy()
-
-    # e2e through the reference-facing call with host buffers
-    e2e_ms = []
-    ipd_ptr = None
-    for k in range(e2e_k):
-        f = fields[W + K + k]
-        sys_.clear_guess()
-        L.ommp_gpu_flush_l2(h, flush)
+    def timed_pass(sys_):
+        h = sys_._h
+        for k in range(W):
+            one_step(sys_, k)
+        if dist:
+            dist.barrier()
         sys_.synchronize()
-        t0 = time.perf_counter()
-        L.ommp_set_external_field(h, f.ctypes.data_as(_lib._dp), 0, 0)
-        ipd_ptr = L.ommp_get_ipd(h)
-        out = np.ctypeslib.as_array(ipd_ptr, shape=(sys_.n_ipd * nv,)).copy()
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_value = ws * e2e_k / (sum(e2e_ms) * 1e-3)
+        L.ommp_gpu_reset_kernel_stats(h)
+        sys_.enable_kernel_timing(True)
+        launches0 = L.ommp_gpu_kernel_launch_count()
+        clk = Clocks(local if ws > 1 else 0)
+        step_ms, counters = [], []
+        wall0 = time.perf_counter()
+        for k in range(W, W + K):
+            step_ms.append(one_step(sys_, k))
+            counters.append([sys_.counter(c) for c in range(5)])
+        sys_.synchronize()
+        wall = time.perf_counter() - wall0
+        clocks = clk.stop()
+        launches = L.ommp_gpu_kernel_launch_count() - launches0
+        sys_.enable_kernel_timing(False)
+        kst = [sys_.kernel_stats(c) for c in range(3)]
+        total_ms = sum(step_ms)
+        if dist:
+            import torch
+            t = torch.tensor([total_ms], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+        kstats = kernel_table(kst, n, peak64.value, peak32.value)
+        res = {"value": ws * K / (total_ms * 1e-3), "ms_per_step": total_ms / K, "steps_ms": step_ms,
+               "solver_counters_per_step": counters, "gpu_launches": int(launches), "wall_s_timed": wall,
+               "clocks": clocks, "kernels": kstats, "roofline": roofline_of(kstats, total_ms),
+               "ipd": sys_.ipd.copy(), "energy": sys_.get_polelec_energy()}
+        # e2e through the reference-facing call with host buffers
+        e2e_ms = []
+        for k in range(e2e_k):
+            f = fields[W + K + k]
+            sys_.clear_guess()
+            L.ommp_gpu_flush_l2(h, flush)
+            sys_.synchronize()
+            t0 = time.perf_counter()
+            L.ommp_set_external_field(h, f.ctypes.data_as(_lib._dp), 0, 0)
+            np.ctypeslib.as_array(L.ommp_get_ipd(h), shape=(sys_.n_ipd * nv,)).copy()
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        res["e2e"] = {"value": ws * e2e_k / (sum(e2e_ms) * 1e-3), "unit": "solves/s",
+                      "h2d_bytes_per_step": nv * 8, "d2h_bytes_per_step": sys_.n_ipd * nv * 8, "ms": e2e_ms}
+        return res
 
-    # plain FP64 solve of the last timed field, and the mixed error against it
+    main = timed_pass(sys_)
+    # the double-single variant alongside the strict mixed mode, on its own
+    # system: refinement residual products and E_M2D in double-single
+    ds = None
+    if args.precision == "mixed" and not args.no_ds:
+        g2 = og.OMMPSystem(path)
+        g2.set_solver_tol(1e-10)
+        g2.set_fp32_kernel(args.fp32_kernel)
+        g2.set_precision("mixed-ds")
+        t0 = time.perf_counter()
+        e_ds = g2.e_m2d()
+        m2d_ds_s = time.perf_counter() - t0
+        ds = timed_pass(g2)
+        ds["m2d_first_solve_s"] = m2d_ds_s
+        ds["e_m2d"] = e_ds
+        g2.close()
+    # plain FP64 solve of the last timed field, and the errors against it
     fp64 = None
     if not args.no_fp64:
         sys_.set_precision("fp64")
+        e64 = sys_.e_m2d()  # recomputed in FP64 if the cached field is double-single
         sys_.clear_guess()
         t0 = time.perf_counter()
-        st = L.ommp_gpu_set_external_field_device(h, dev[W + K - 1], 0, 0, 1)
+        st = L.ommp_gpu_set_external_field_device(sys_._h, dev[W + K - 1], 0, 0, 1)
         fp64_s = time.perf_counter() - t0
         assert st == 0, L.ommp_gpu_last_error()
         ref = sys_.ipd
@@ -341,60 +407,32 @@ def run_gb300(args):
                 "t_mu_products": sys_.counter(0), "cg_iterations": [sys_.iterations(0), sys_.iterations(1)],
                 "residual_history_D": [float(x) for x in sys_.residual_history(0)],
                 "residual_history_P": [float(x) for x in sys_.residual_history(1)],
-                "mixed_rel_err_ipd": float(np.linalg.norm(mixed_ipd - ref) / np.linalg.norm(ref)),
-                "mixed_rel_err_energy": float(abs(mixed_ep - ref_ep) / abs(ref_ep)),
-                "energy": ref_ep, "speedup_mixed_over_fp64": value / ws * fp64_s}
-    # roofline of the dominant pair kernel
-    peak64 = C.c_double(0)
-    peak32 = C.c_double(0)
-    L.ommp_gpu_measure_pipe_peak(1, C.byref(peak64))
-    L.ommp_gpu_measure_pipe_peak(0, C.byref(peak32))
-    pairs = float(n) * (n - 1)
-    kstats = {}
-    for name, (cnt, ms, cols), pk in (("tmu_fp64", k64, peak64.value), ("tmu_fp32", k32, peak32.value),
-                                      ("tmu_ds", kds, peak32.value)):
-        if cnt:
-            # algorithmic flop of all timed launches: 45 per ordered pair per column
-            avg = ms / cnt
-            ach = FLOP_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
-            kstats[name] = {"launches": cnt, "columns": cols, "total_ms": ms, "avg_ms": avg,
-                            "achieved_tflops": ach, "peak_tflops": pk, "frac": ach / pk if pk else None}
-            if name == "tmu_ds":
-                # FP32 pipe: double-single operations issued per second against
-                # the FMA-pipe instruction rate (peak flop / 2)
-                ops = DS_OPS_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
-                kstats[name].update({"fp64_equivalent_tflops": ach, "achieved_tops": ops,
-                                     "peak_tops": pk / 2, "frac": ops / (pk / 2) if pk else None})
-    dom = max(kstats, key=lambda k: kstats[k]["total_ms"]) if kstats else None
-    roof = None
-    if dom:
-        d = kstats[dom]
-        ds = dom == "tmu_ds"
-        roof = {"bound": "fp64" if dom == "tmu_fp64" else "fp32", "kernel": dom,
-                "achieved": d["achieved_tops"] if ds else d["achieved_tflops"],
-                "peak": d["peak_tops"] if ds else d["peak_tflops"],
-                "unit": "Tops/s (FP32 instructions)" if ds else "TFLOP/s",
-                "frac": d["frac"], "traffic": None,
-                "peak_source": "FMA-chain kernel measured in this run (pipe peak; "
-                               "MEASURED_PEAKS.json has no FP32/FP64 CUDA-core figure)",
-                "algorithmic": (f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair" if ds else
-                                f"{FLOP_PER_PAIR:.0f} flop per ordered pair") +
-                               f" x N(N-1) pairs x right-hand sides ({d['columns']} columns over "
-                               f"{d['launches']} launches)",
-                "share_of_timed": d["total_ms"] / total_ms}
-    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": K, "warmup": W,
-            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "energy": ref_ep}
+        for label, r, e_field in (("mixed", main, e_main), ("mixed_ds", ds, ds["e_m2d"] if ds else None)):
+            if r is None:
+                continue
+            fp64[f"{label}_rel_err_ipd"] = rel_err(r["ipd"], ref)
+            fp64[f"{label}_rel_err_energy"] = float(abs(r["energy"] - ref_ep) / abs(ref_ep))
+            fp64[f"{label}_rel_err_field"] = rel_err(e_field, e64)
+            fp64[f"speedup_{label}_over_fp64"] = r["value"] / ws * fp64_s
+    for r in (main, ds):
+        if r:
+            r.pop("ipd")
+            r.pop("e_m2d", None)
+    line = {"metric": METRIC, "value": main["value"], "unit": "solves/s", "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": main["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32+f64", "data": "synthetic",
             "config": {"workload": f"AMOEBA water box, {n} polarizable sites "
                                    f"({n // 3} molecules, seed 1), fresh 30-charge field per step, "
                                    "D+P solved to RMS residual 1e-10, cold start, E_M2D cached per geometry",
-                       "sites": n, "l2": "flushed (256 MiB write) between steps",
+                       "sites": n, "precision": args.precision, "l2": "flushed (256 MiB write) between steps",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": nv * 8,
-                    "d2h_bytes_per_step": sys_.n_ipd * nv * 8, "ms": e2e_ms},
-            "gpu_launches": int(launches), "wall_s_timed": wall, "m2d_first_solve_s": m2d_s,
-            "steps_ms": step_ms, "solver_counters_per_step": counters, "kernels": kstats,
-            "roofline": roof, "clocks": clocks, "fp64": fp64}
+            "e2e": main["e2e"], "gpu_launches": main["gpu_launches"], "wall_s_timed": main["wall_s_timed"],
+            "m2d_first_solve_s": m2d_s, "steps_ms": main["steps_ms"],
+            "solver_counters_per_step": main["solver_counters_per_step"], "kernels": main["kernels"],
+            "roofline": main["roofline"], "clocks": main["clocks"], "energy": main["energy"], "fp64": fp64}
+    if ds:
+        line["mixed_ds"] = ds
     if rank == 0 and args.skip_cpu:
         line["cpu_baseline"] = {"value": None, "skipped": "--skip-cpu"}
         print(json.dumps(line), flush=True)
@@ -422,8 +460,8 @@ def run_gb300(args):
 
 def run_c60k(args):
     """Precision configuration: 60,000-site Wang-AL chain system (150 chains of
-    200 sites in 10,000 waters), mixed precision against plain FP64, with the
-    relative error of each result."""
+    200 sites in 10,000 waters), the mixed modes against plain FP64, with the
+    relative error of each result (field, dipoles, energy)."""
     import openmmpol_gb300 as og
     from openmmpol_gb300 import build as b
     from openmmpol_gb300 import synth
@@ -435,16 +473,18 @@ def run_c60k(args):
     if not os.path.exists(path):
         synth.write_mmp(path + ".tmp", c)
         os.replace(path + ".tmp", path)
-    s = og.OMMPSystem(path)
-    s.set_solver_tol(1e-10)
-    n = s.pol_atoms
-    ef = fields_for(s.cpol, s.cmm, c.box_center(), [7])[0]
-    t0 = time.perf_counter()
-    e_m2d = s.e_m2d()
-    m2d_s = time.perf_counter() - t0
     res = {}
-    for prec in ("fp64", "mixed"):
+    ef = None
+    for prec in ("fp64", "mixed", "mixed-ds"):
+        s = og.OMMPSystem(path)
+        s.set_solver_tol(1e-10)
         s.set_precision(prec)
+        n = s.pol_atoms
+        if ef is None:
+            ef = fields_for(s.cpol, s.cmm, c.box_center(), [7])[0]
+        t0 = time.perf_counter()
+        e_m2d = s.e_m2d()
+        m2d_s = time.perf_counter() - t0
         times = []
         for k in range(args.warmup + args.steps):
             s.clear_guess()
@@ -452,13 +492,18 @@ def run_c60k(args):
             s.set_external_field(ef)
             if k >= args.warmup:
                 times.append(time.perf_counter() - t0)
-        res[prec] = {"ipd": s.ipd, "energy": s.get_polelec_energy(), "s_per_solve": statistics.mean(times),
-                     "iterations": [s.iterations(0)], "t_mu_fp64": s.counter(0), "t_mu_fp32": s.counter(1),
+        res[prec] = {"ipd": s.ipd, "field": e_m2d, "energy": s.get_polelec_energy(),
+                     "s_per_solve": statistics.mean(times), "m2d_s": m2d_s, "iterations": [s.iterations(0)],
+                     "t_mu_fp64": s.counter(0), "t_mu_fp32": s.counter(1), "t_mu_ds": s.counter(4),
                      "residual_history": [float(x) for x in s.residual_history(0)]}
-    r64, rmx = res["fp64"], res["mixed"]
-    err_ipd = float(np.linalg.norm(rmx["ipd"] - r64["ipd"]) / np.linalg.norm(r64["ipd"]))
-    err_max = float(np.abs(rmx["ipd"] - r64["ipd"]).max() / np.abs(r64["ipd"]).max())
-    err_e = float(abs(rmx["energy"] - r64["energy"]) / abs(r64["energy"]))
+        s.close()
+    r64 = res["fp64"]
+
+    def errors(r):
+        return {"field_rel_l2": rel_err(r["field"], r64["field"]), "dipoles_rel_l2": rel_err(r["ipd"], r64["ipd"]),
+                "dipoles_rel_max": float(np.abs(r["ipd"] - r64["ipd"]).max() / np.abs(r64["ipd"]).max()),
+                "energy_rel": float(abs(r["energy"] - r64["energy"]) / abs(r64["energy"]))}
+    rmx, rds = res["mixed"], res["mixed-ds"]
     line = {"metric": "induced-dipole solves/s, Wang-AL chain system (mixed vs FP64)",
             "value": 1.0 / rmx["s_per_solve"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * rmx["s_per_solve"], "higher_is_better": True,
@@ -466,12 +511,13 @@ def run_c60k(args):
             "config": {"workload": f"{n} sites: 150 self-avoiding chains x 200 sites (1.53 A bonds, "
                                    "charges U(-0.6,0.6), alpha U(0.4,1.5) A^3, 1-2/1-3 exclusions) in 10,000 "
                                    "waters, Wang-AL linear Thole, 30-charge field, RMS 1e-10", "sites": n},
-            "fp64_solves_per_s": 1.0 / r64["s_per_solve"], "speedup_mixed_over_fp64":
-                r64["s_per_solve"] / rmx["s_per_solve"], "m2d_s": m2d_s,
-            "errors_mixed_vs_fp64": {"field": 0.0, "field_note": "E_M2D + external field is FP64 in both modes",
-                                     "dipoles_rel_l2": err_ipd, "dipoles_rel_max": err_max, "energy_rel": err_e},
-            "fp64": {k: v for k, v in r64.items() if k != "ipd"},
-            "mixed": {k: v for k, v in rmx.items() if k != "ipd"}}
+            "fp64_solves_per_s": 1.0 / r64["s_per_solve"],
+            "speedup_mixed_over_fp64": r64["s_per_solve"] / rmx["s_per_solve"],
+            "mixed_ds_solves_per_s": 1.0 / rds["s_per_solve"],
+            "speedup_mixed_ds_over_fp64": r64["s_per_solve"] / rds["s_per_solve"],
+            "errors_mixed_vs_fp64": errors(rmx), "errors_mixed_ds_vs_fp64": errors(rds)}
+    for k, r in res.items():
+        line[k.replace("-", "_")] = {kk: vv for kk, vv in r.items() if kk not in ("ipd", "field")}
     print(json.dumps(line), flush=True)
 
 
@@ -700,7 +746,7 @@ def run_s1024(args):
     res = {}
     clk = Clocks(0)
     l0 = L.ommp_gpu_kernel_launch_count()
-    for prec, nr in (("mixed", nreq), ("fp64", n64)):
+    for label, prec, nr in (("mixed", args.precision, nreq), ("fp64", "fp64", n64)):
         pl = plan[:nr]
         r = {}
         for phase in ("saturation", "load70"):
@@ -724,7 +770,7 @@ def run_s1024(args):
                         "peak_bytes": int(st["peak_bytes"]), "errors": errors[:5], "n_errors": len(errors)}
             if phase == "saturation":
                 r["results"] = {k: (out[k]["ipd"], out[k]["energy"]) for k in keep if k < nr}
-        res[prec] = r
+        res[label] = r
     clocks = clk.stop()
     launches = L.ommp_gpu_kernel_launch_count() - l0
     err_ipd, err_e = [], []
@@ -746,7 +792,7 @@ def run_s1024(args):
             "config": {"workload": f"{nreq} requests: AMOEBA water clusters of log-uniform 300..60,000 molecules "
                                    f"({len(sizes)} cached geometries), 30-charge field per new request, 30 % "
                                    "follow-ups (field x (1 + 0.01 N(0,1)), warm start), D+P to RMS 1e-10",
-                       "hbm_budget_gib": args.hbm_budget_gib, "slots": args.slots,
+                       "hbm_budget_gib": args.hbm_budget_gib, "slots": args.slots, "precision": args.precision,
                        "fp64_requests": n64, "arrivals": "all at t=0 (saturation), then Poisson at 70 % "
                                                          "of the saturation rate"},
             "p50_ms": mx["load70"]["p50_ms"], "p99_ms": mx["load70"]["p99_ms"],

@@ -292,6 +292,235 @@ __global__ void __launch_bounds__(DS_TPB, 5) k_tmu_ds(int n, const float4 *__res
   }
 }
 
+// ---------------------------------------------------------------------------
+// E_M2D in double-single: field of the static multipoles (charge, dipole,
+// quadrupole for AMOEBA; charge for Wang-AL) at the polarizable sites, the
+// all-pairs part of elec_prop_M2D (src/mod_electrostatics.F90:2579-2731) at
+// scale 1; the scaled pairs are corrected in FP64 by k_m2d_finish.
+// ---------------------------------------------------------------------------
+// sum of three double-single products a.b (a, b given as hi/lo floats)
+__device__ __forceinline__ dsf ds_dot3(float ah0, float al0, float ah1, float al1, float ah2, float al2, dsf b0,
+                                       dsf b1, dsf b2) {
+  float q0 = ah0 * b0.h, q1 = ah1 * b1.h, q2 = ah2 * b2.h;
+  float f0 = fmaf(al0, b0.h, fmaf(ah0, b0.l, fmaf(ah0, b0.h, -q0)));
+  float f1 = fmaf(al1, b1.h, fmaf(ah1, b1.l, fmaf(ah1, b1.h, -q1)));
+  float f2 = fmaf(al2, b2.h, fmaf(ah2, b2.l, fmaf(ah2, b2.h, -q2)));
+  const dsf u1 = two_sum(q0, q1);
+  const dsf u2 = two_sum(u1.h, q2);
+  return fast_two_sum(u2.h, ((f0 + f1) + f2) + (u1.l + u2.l));
+}
+__device__ __forceinline__ dsf ds_add(dsf x, dsf y) {
+  const dsf s = two_sum(x.h, y.h);
+  return fast_two_sum(s.h, s.l + (x.l + y.l));
+}
+
+constexpr int M2D_LD = 10;  // q, mu (3), theta xx xy yy xz yz zz
+
+// One target-source pair; q hi/lo in smem rows of M2D_LD floats.
+template <bool NEAR, bool AMOEBA>
+__device__ __forceinline__ void ds_m2d_pair(const float4 &th, const float4 &tl, const float4 &sh, const float4 &sl,
+                                            const float *qh, const float *ql, float (&ah)[3], float (&al)[3],
+                                            double wt, double ws, double at, double as, float2 wat, float2 was,
+                                            double thr, float thr2m, int &bad) {
+  const dsf dx = ds_diff(th.x, tl.x, sh.x, sl.x);
+  const dsf dy = ds_diff(th.y, tl.y, sh.y, sl.y);
+  const dsf dz = ds_diff(th.z, tl.z, sh.z, sl.z);
+  float px = dx.h * dx.h, py = dy.h * dy.h, pz = dz.h * dz.h;
+  float ex = fmaf(dx.h + dx.h, dx.l, fmaf(dx.h, dx.h, -px));
+  float ey = fmaf(dy.h + dy.h, dy.l, fmaf(dy.h, dy.h, -py));
+  float ez = fmaf(dz.h + dz.h, dz.l, fmaf(dz.h, dz.h, -pz));
+  const dsf sa = two_sum(px, py);
+  const dsf sb = two_sum(sa.h, pz);
+  const dsf r2 = fast_two_sum(sb.h, ((ex + ey) + ez) + (sa.l + sb.l));
+  if (NEAR && r2.h < 4.9e-28f) {  // |r| < 100 eps: coincident sites
+    bad = 1;
+    return;
+  }
+  const dsf rinv = ds_rsqrt(r2);
+  const dsf ir2 = ds_sqr(rinv);
+  dsf k3 = ds_mul(rinv, ir2);
+  dsf k5 = ds_mul(k3, ir2), k7 = ds_mul(k5, ir2);
+  if (NEAR) {
+    const bool maybe = AMOEBA ? maybe_damped_amoeba(r2.h, wat, was, thr2m) : maybe_damped_wang(r2.h, wat, was);
+    if (maybe) {
+      const double u = sqrt((double)r2.h + (double)r2.l) * (wt * ws);
+      double f3 = 1.0, f5 = 1.0, f7 = 1.0;
+      if (AMOEBA) {
+        const double au3 = fmin(at, as) * u * u * u;
+        if (au3 < thr) {
+          const double e = exp(-au3);
+          f3 = 1.0 - e;
+          f5 = 1.0 - (1.0 + au3) * e;
+          f7 = 1.0 - (1.0 + au3 + 0.6 * au3 * au3) * e;
+        }
+      } else if (u < 1.0) {
+        const double u3 = u * u * u;
+        f3 = 4.0 * u3 - 3.0 * u3 * u;
+      }
+      k3 = ds_mul(k3, to_ds(f3));
+      if (AMOEBA) {
+        k5 = ds_mul(k5, to_ds(f5));
+        k7 = ds_mul(k7, to_ds(f7));
+      }
+    }
+  }
+  if (AMOEBA) {
+    // mu.d, theta d, d.theta.d
+    const dsf mdr = ds_dot3(qh[1], ql[1], qh[2], ql[2], qh[3], ql[3], dx, dy, dz);
+    const dsf tx = ds_dot3(qh[4], ql[4], qh[5], ql[5], qh[7], ql[7], dx, dy, dz);
+    const dsf ty = ds_dot3(qh[5], ql[5], qh[6], ql[6], qh[8], ql[8], dx, dy, dz);
+    const dsf tz = ds_dot3(qh[7], ql[7], qh[8], ql[8], qh[9], ql[9], dx, dy, dz);
+    const dsf txr = ds_add(ds_add(ds_mul(tx, dx), ds_mul(ty, dy)), ds_mul(tz, dz));
+    // c = q k3 + 3 mu.d k5 + 15 d.theta.d k7
+    const dsf c = ds_add(ds_add(ds_mul(k3, dsf{qh[0], ql[0]}), ds_mulf(ds_mul(mdr, k5), 3.0f)),
+                         ds_mulf(ds_mul(txr, k7), 15.0f));
+    const dsf nk3{-k3.h, -k3.l};
+    const dsf k5x6 = ds_mulf(k5, -6.0f);
+    acc_mul(ah[0], al[0], c, dx);
+    acc_mul(ah[0], al[0], nk3, dsf{qh[1], ql[1]});
+    acc_mul(ah[0], al[0], k5x6, tx);
+    acc_mul(ah[1], al[1], c, dy);
+    acc_mul(ah[1], al[1], nk3, dsf{qh[2], ql[2]});
+    acc_mul(ah[1], al[1], k5x6, ty);
+    acc_mul(ah[2], al[2], c, dz);
+    acc_mul(ah[2], al[2], nk3, dsf{qh[3], ql[3]});
+    acc_mul(ah[2], al[2], k5x6, tz);
+  } else {
+    const dsf c = ds_mul(k3, dsf{qh[0], ql[0]});
+    acc_mul(ah[0], al[0], c, dx);
+    acc_mul(ah[1], al[1], c, dy);
+    acc_mul(ah[2], al[2], c, dz);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const dsf r = fast_two_sum(ah[k], al[k]);
+    ah[k] = r.h;
+    al[k] = r.l;
+  }
+}
+
+// partial[split][j][3] over the split's static sources (the target's own
+// site excluded; coincident sites set *err_flag)
+template <bool AMOEBA>
+__global__ void __launch_bounds__(DS_TPB, 4) k_m2d_ds(int n, int m, const float4 *__restrict__ ph,
+                                                      const float4 *__restrict__ pl, const Pos64 *__restrict__ p64,
+                                                      const double *__restrict__ pol_a, const float2 *__restrict__ pol_wa,
+                                                      const int *__restrict__ polar_mm, const float4 *__restrict__ pbox,
+                                                      const float4 *__restrict__ mh, const float4 *__restrict__ ml,
+                                                      const Pos64 *__restrict__ m64, const double *__restrict__ mm_a,
+                                                      const float2 *__restrict__ mm_wa, const double *__restrict__ mm_q,
+                                                      const float4 *__restrict__ mbox, double *__restrict__ partial,
+                                                      int per_split, double thr, float thr2m, float r2max, int *err_flag) {
+  constexpr int LD = AMOEBA ? M2D_LD : 1;
+  __shared__ float4 s_ph[DS_TILE], s_pl[DS_TILE];
+  __shared__ float s_qh[DS_TILE * LD], s_ql[DS_TILE * LD];
+  __shared__ double s_w[DS_TILE], s_a[DS_TILE];
+  __shared__ float2 s_wa[DS_TILE];
+  const int jb = blockIdx.x * (DS_TPB * DS_TPT);
+  float4 th[DS_TPT], tl[DS_TPT];
+  bool valid[DS_TPT];
+  double sum[DS_TPT][3];
+#pragma unroll
+  for (int t = 0; t < DS_TPT; ++t) {
+    const int j = jb + t * DS_TPB + threadIdx.x;
+    valid[t] = j < n;
+    th[t] = valid[t] ? ph[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    tl[t] = valid[t] ? pl[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    sum[t][0] = sum[t][1] = sum[t][2] = 0.0;
+  }
+  const int ntile = (n + DS_TILE - 1) / DS_TILE;
+  const int tb0 = jb / DS_TILE;
+  const int tb1 = min(ntile - 1, (jb + DS_TPB * DS_TPT - 1) / DS_TILE);
+  float4 blo = pbox[2 * tb0], bhi = pbox[2 * tb0 + 1];
+  for (int tb = tb0 + 1; tb <= tb1; ++tb) {
+    float4 lo = pbox[2 * tb], hi = pbox[2 * tb + 1];
+    blo.x = fminf(blo.x, lo.x), blo.y = fminf(blo.y, lo.y), blo.z = fminf(blo.z, lo.z);
+    bhi.x = fmaxf(bhi.x, hi.x), bhi.y = fmaxf(bhi.y, hi.y), bhi.z = fmaxf(bhi.z, hi.z);
+  }
+  int bad = 0;
+  const int s0 = blockIdx.y * per_split;
+  const int s1 = min(m, s0 + per_split);
+  for (int t0 = s0; t0 < s1; t0 += DS_TILE) {
+    __syncthreads();
+    {
+      const int k = threadIdx.x;
+      const int i = t0 + k;
+      if (i < s1) {
+        s_ph[k] = mh[i];
+        s_pl[k] = ml[i];
+        s_w[k] = m64[i].w;
+        s_a[k] = AMOEBA ? mm_a[i] : 0.0;
+        s_wa[k] = mm_wa[i];
+#pragma unroll
+        for (int c = 0; c < LD; ++c) {
+          const double v = mm_q[(size_t)i * LD + c];
+          const float h = (float)v;
+          s_qh[k * LD + c] = h;
+          s_ql[k * LD + c] = (float)(v - (double)h);
+        }
+      }
+    }
+    __syncthreads();
+    const int cnt = min(DS_TILE, s1 - t0);
+    const float4 slo = mbox[2 * (t0 / DS_TILE)], shi = mbox[2 * (t0 / DS_TILE) + 1];
+    const float gx = fmaxf(0.f, fmaxf(slo.x - bhi.x, blo.x - shi.x));
+    const float gy = fmaxf(0.f, fmaxf(slo.y - bhi.y, blo.y - shi.y));
+    const float gz = fmaxf(0.f, fmaxf(slo.z - bhi.z, blo.z - shi.z));
+    const bool far_tile = gx * gx + gy * gy + gz * gz > r2max;
+    float ah[DS_TPT][3], al[DS_TPT][3];
+#pragma unroll
+    for (int t = 0; t < DS_TPT; ++t)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ah[t][c] = al[t][c] = 0.f;
+    if (far_tile) {
+#pragma unroll 1
+      for (int k = 0; k < cnt; ++k) {
+        const float4 sh = s_ph[k], sl = s_pl[k];
+#pragma unroll
+        for (int t = 0; t < DS_TPT; ++t)
+          ds_m2d_pair<false, AMOEBA>(th[t], tl[t], sh, sl, &s_qh[k * LD], &s_ql[k * LD], ah[t], al[t], 0.0, 0.0,
+                                     0.0, 0.0, make_float2(0.f, 0.f), make_float2(0.f, 0.f), thr, thr2m, bad);
+      }
+    } else {
+      double wt[DS_TPT], at[DS_TPT];
+      float2 wat[DS_TPT];
+      int tm[DS_TPT];
+#pragma unroll
+      for (int t = 0; t < DS_TPT; ++t) {
+        const int j = valid[t] ? jb + t * DS_TPB + threadIdx.x : 0;
+        wt[t] = p64[j].w;
+        at[t] = AMOEBA ? pol_a[j] : 0.0;
+        wat[t] = pol_wa[j];
+        tm[t] = valid[t] ? polar_mm[j] : -1;
+      }
+#pragma unroll 1
+      for (int k = 0; k < cnt; ++k) {
+        const float4 sh = s_ph[k], sl = s_pl[k];
+        const double ws = s_w[k], as = s_a[k];
+        const float2 was = s_wa[k];
+#pragma unroll
+        for (int t = 0; t < DS_TPT; ++t) {
+          if (!valid[t] || t0 + k == tm[t]) continue;
+          ds_m2d_pair<true, AMOEBA>(th[t], tl[t], sh, sl, &s_qh[k * LD], &s_ql[k * LD], ah[t], al[t], wt[t], ws,
+                                    at[t], as, wat[t], was, thr, thr2m, bad);
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < DS_TPT; ++t)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) sum[t][c] += (double)ah[t][c] + (double)al[t][c];
+  }
+  if (bad) atomicOr(err_flag, 1);
+#pragma unroll
+  for (int t = 0; t < DS_TPT; ++t) {
+    const int j = jb + t * DS_TPB + threadIdx.x;
+    if (!valid[t]) continue;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) partial[((size_t)blockIdx.y * n + j) * 3 + c] = sum[t][c];
+  }
+}
+
 }  // namespace
 
 int tmu_ds_pick_split(const DevSites &s, int sms) {
@@ -313,6 +542,37 @@ void launch_tmu_ds_pairs(const DevSites &s, const double *x, double *partial, in
   else
     k_tmu_ds<false><<<grid, DS_TPB, 0, st>>>(s.n, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32,
                                              s.tile_box32, x, partial, per, s.damp_thr, thr2m, s.damp_r2max32);
+}
+
+}  // namespace gpu
+}  // namespace ommp
+
+namespace ommp {
+namespace gpu {
+
+int m2d_ds_pick_split(const DevSites &s, int sms) {
+  const int tblocks = (s.n + DS_TPB * DS_TPT - 1) / (DS_TPB * DS_TPT);
+  const int tiles = (s.m + DS_TILE - 1) / DS_TILE;
+  int split = (4 * sms + tblocks - 1) / tblocks;
+  if (split > tiles) split = tiles;
+  return split < 1 ? 1 : split;
+}
+
+void launch_m2d_ds_pairs(const DevSites &s, double *partial, int nsplit, int *err_flag, cudaStream_t st) {
+  const int tiles = (s.m + DS_TILE - 1) / DS_TILE;
+  const int per = ((tiles + nsplit - 1) / nsplit) * DS_TILE;
+  dim3 grid((s.n + DS_TPB * DS_TPT - 1) / (DS_TPB * DS_TPT), nsplit);
+  const float thr2m = (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));
+  if (s.amoeba)
+    k_m2d_ds<true><<<grid, DS_TPB, 0, st>>>(s.n, s.m, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32,
+                                            s.polar_mm, s.tile_box32, s.mm_pos32, s.mm_pos32lo, s.mm_pos, s.mm_a,
+                                            s.mm_wa32, s.mm_q, s.mm_tile_box32, partial, per, s.damp_thr, thr2m,
+                                            s.m2d_r2max32, err_flag);
+  else
+    k_m2d_ds<false><<<grid, DS_TPB, 0, st>>>(s.n, s.m, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32,
+                                             s.polar_mm, s.tile_box32, s.mm_pos32, s.mm_pos32lo, s.mm_pos, s.mm_a,
+                                             s.mm_wa32, s.mm_q, s.mm_tile_box32, partial, per, s.damp_thr, thr2m,
+                                             s.m2d_r2max32, err_flag);
 }
 
 }  // namespace gpu

@@ -48,7 +48,7 @@ System::~System() {
   free_ws(ws_);
   free_ws(wsb_);
   void *bufs[] = {d_.pol_pos, d_.pol_a, d_.pol_alpha, d_.polar_mm, d_.pol_pos32, d_.pol_pos32lo, d_.pol_a32,
-                  d_.pol_wa32, ds_scratch_,
+                  d_.pol_wa32, ds_scratch_, d_.mm_pos32, d_.mm_pos32lo, d_.mm_tile_box32,
                   d_.mm_wa32, d_.mm_pos,
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
@@ -117,6 +117,10 @@ size_t System::device_bytes_estimate() const {
   size_t bytes = 8 * (6 * n + 5 * m + m * m_.ld_cart + 2 * nm2d + nd2d + nv * (2 * nipd + 3 + 10)) +
                  4 * (9 * n + 2 * m + 10 * nv + 2 * (n + 1) + nm2d + nd2d) + 4 * s32 + 8 * s64 + 8 * sym +
                  8 * (gpu::kRedBlocks * 32 + 64 + 2 * (size_t)maxhist_);
+  // double-single copies of the positions, static-site tile boxes, and the
+  // double-single kernels' split partials (allocated in that mode only)
+  const size_t ds_split = std::max(gpu::tmu_ds_pick_split(d, sms), gpu::m2d_ds_pick_split(d, sms));
+  bytes += 16 * (n + 2 * m + 2 * ((m + 127) / 128)) + 8 * ds_split * nv;
   return bytes + (size_t(4) << 20);  // events, flags, rounding
 }
 
@@ -156,6 +160,7 @@ int System::upload_static() {
   // FP32 scratch for twice the default source split (the autotuner tries both)
   bad |= dalloc(scratch_, scratch_n_) | dalloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, f32_splits));
   bad |= dalloc(d_.tile_box32, 2 * (size_t)d_.ntile);
+  bad |= dalloc(d_.mm_pos32, mm) | dalloc(d_.mm_pos32lo, mm) | dalloc(d_.mm_tile_box32, 2 * (size_t)((mm + 127) / 128));
   bad |= dalloc(partial_, (size_t)gpu::kRedBlocks * 32) | dalloc(dots_, 64) | dalloc(hist_, 2 * (size_t)maxhist_);
   bad |= dalloc(cols_, 2) | dalloc(flag_, 1) | dalloc(info_, 1);
   if (bad || cudaMallocHost((void **)&cols_h_, 2 * sizeof(gpu::CgCol)) != cudaSuccess ||
@@ -211,6 +216,12 @@ int System::upload_static() {
     std::vector<double> w(n);
     for (int j = 0; j < n; ++j) w[j] = 1.0 / m.thole[m.polar_mm[j]];
     d_.damp_r2max32 = gpu::damp_r2max32(m.amoeba, d_.damp_thr, w.data(), m.damping.data(), n);
+    std::vector<double> mw(mm), ma(mm, 0.0);
+    for (int i = 0; i < mm; ++i) {
+      mw[i] = m.thole[i] > 0.0 ? 1.0 / m.thole[i] : std::numeric_limits<double>::infinity();
+      if (m.mm_polar[i] >= 0) ma[i] = m.damping[m.mm_polar[i]];
+    }
+    d_.m2d_r2max32 = gpu::m2d_r2max32(m.amoeba, d_.damp_thr, w.data(), m.damping.data(), n, mw.data(), ma.data(), mm);
   }
   up(d_.mm_wa32, mwa.data(), mm * sizeof(float2));
   cudaStreamSynchronize(st_);  // pwa / mwa are host temporaries
@@ -257,6 +268,22 @@ int System::upload_geometry() {
   std::vector<float4> boxes(2 * (size_t)d_.ntile);
   gpu::tile_boxes32(pp32.data(), n, boxes.data());
   if (n) cudaMemcpyAsync(d_.tile_box32, boxes.data(), boxes.size() * sizeof(float4), cudaMemcpyHostToDevice, st_);
+  // static sites in double-single for the double-single E_M2D
+  std::vector<float4> mp32(mm), mp32lo(mm);
+  for (int i = 0; i < mm; ++i) {
+    const double *x = &m.cmm[3 * (size_t)i];
+    const double xc[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+    mp32[i] = make_float4((float)xc[0], (float)xc[1], (float)xc[2], 0.f);
+    mp32lo[i] = make_float4((float)(xc[0] - (double)mp32[i].x), (float)(xc[1] - (double)mp32[i].y),
+                            (float)(xc[2] - (double)mp32[i].z), 0.f);
+  }
+  std::vector<float4> mboxes(2 * (size_t)((mm + 127) / 128));
+  gpu::tile_boxes32(mp32.data(), mm, mboxes.data());
+  if (mm) {
+    cudaMemcpyAsync(d_.mm_pos32, mp32.data(), mm * sizeof(float4), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(d_.mm_pos32lo, mp32lo.data(), mm * sizeof(float4), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(d_.mm_tile_box32, mboxes.data(), mboxes.size() * sizeof(float4), cudaMemcpyHostToDevice, st_);
+  }
   cudaMemcpyAsync(d_.mm_pos, mp.data(), mm * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.mm_a, ma.data(), mm * sizeof(double), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.mm_q, m.q.data(), m.q.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
@@ -357,9 +384,18 @@ int System::flush_l2(size_t bytes) {
 }
 
 int System::ensure_m2d() {
-  if (m2d_done_) return kOk;
+  // a field computed in double-single serves only the double-single mode
+  if (m2d_done_ && !(m2d_ds_ && precision_ != kPrecMixedDS)) return kOk;
   cudaMemsetAsync(flag_, 0, sizeof(int), st_);
-  gpu::launch_m2d(d_, e_m2d_, scratch_, nsplit_m2d_, flag_, st_);
+  const bool ds = precision_ == kPrecMixedDS;
+  if (ds) {
+    int st = ensure_ds_scratch();
+    if (st) return st;
+    gpu::launch_m2d_ds(d_, e_m2d_, ds_scratch_, nsplit_m2d_ds_, flag_, st_);
+  } else {
+    gpu::launch_m2d(d_, e_m2d_, scratch_, nsplit_m2d_, flag_, st_);
+  }
+  m2d_ds_ = ds;
   int flag = 0;
   cudaMemcpyAsync(&flag, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);
   int st = check(cudaStreamSynchronize(st_), "M2D field");
@@ -432,16 +468,22 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
 
 // FP64-accurate product for the refinement residual: the FP64 kernel, or in
 // the double-single mode the double-single kernel (one column at a time)
+int System::ensure_ds_scratch() {
+  if (ds_scratch_) return kOk;
+  nsplit_ds_ = gpu::tmu_ds_pick_split(d_, gpu::sm_count());
+  nsplit_m2d_ds_ = gpu::m2d_ds_pick_split(d_, gpu::sm_count());
+  if (dalloc(ds_scratch_, (size_t)std::max(nsplit_ds_, nsplit_m2d_ds_) * 3 * d_.n)) {
+    ds_scratch_ = nullptr;
+    set_last_error("out of device memory for the double-single kernels");
+    return kErrMemory;
+  }
+  return kOk;
+}
+
 int System::matvec_residual(int ncol, const double *x, double *y) {
   if (precision_ != kPrecMixedDS) return matvec64(kMatvDirect, ncol, x, y, true);
-  if (!ds_scratch_) {
-    nsplit_ds_ = gpu::tmu_ds_pick_split(d_, gpu::sm_count());
-    if (dalloc(ds_scratch_, (size_t)nsplit_ds_ * 3 * d_.n)) {
-      ds_scratch_ = nullptr;
-      set_last_error("out of device memory for the double-single product");
-      return kErrMemory;
-    }
-  }
+  int st = ensure_ds_scratch();
+  if (st) return st;
   KEv e;
   if (ktime_on_) e = kt_begin(2, ncol);
   gpu::launch_tmu_ds(d_, ncol, x, y, true, ds_scratch_, nsplit_ds_, st_);

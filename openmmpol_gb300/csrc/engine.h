@@ -95,6 +95,7 @@ class System {
   int set_fp64_kernel(int mode);
   int set_fp32_kernel(int mode);
   int matvec_residual(int ncol, const double *x, double *y);
+  int ensure_ds_scratch();
   int precision() const { return precision_; }
   double tol() const { return tol_; }
   const SolveStats &stats() const { return stats_; }
@@ -172,8 +173,9 @@ class System {
   size_t scratch_n_ = 0;
   double *sym_scratch_ = nullptr;  // symmetric-kernel partials (allocated on first use)
   int fp64_kernel_ = 0;
-  double *ds_scratch_ = nullptr;  // split partials of the double-single product
-  int nsplit_ds_ = 1;
+  double *ds_scratch_ = nullptr;  // split partials of the double-single kernels
+  int nsplit_ds_ = 1, nsplit_m2d_ds_ = 1;
+  bool m2d_ds_ = false;  // the cached E_M2D was computed in double-single
   int fp32_kernel_ = 0;  // 0 autotuned, else the forced kernel version
   float *scratch32_ = nullptr;
   double *partial_ = nullptr;  // reduction partials [kRedBlocks][8]

@@ -925,6 +925,19 @@ int m2d_pick_split(const DevSites &s, int sms) {
 
 size_t m2d_scratch_doubles(const DevSites &s, int nsplit) { return (size_t)nsplit * s.n * 3; }
 
+// split partials -> FP64 scaled-pair corrections -> D and P sets
+static void m2d_finish(const DevSites &s, double *out, const double *scratch, int nsplit, cudaStream_t st) {
+  int fb = (s.n + 127) / 128;
+  if (s.amoeba)
+    k_m2d_finish<true><<<fb, 128, 0, st>>>(s.n, nsplit, scratch, s.pol_pos, s.pol_a, s.mm_pos, s.mm_a, s.mm_q,
+                                           s.pol_wa32, s.mm_wa32, s.m2d_ri, s.m2d_src, s.m2d_sP, s.m2d_sD,
+                                           s.damp_thr, damp_thr2_margin(s), out);
+  else
+    k_m2d_finish<false><<<fb, 128, 0, st>>>(s.n, nsplit, scratch, s.pol_pos, s.pol_a, s.mm_pos, s.mm_a,
+                                            s.mm_q, s.pol_wa32, s.mm_wa32, s.m2d_ri, s.m2d_src, s.m2d_sP,
+                                            s.m2d_sD, s.damp_thr, damp_thr2_margin(s), out);
+}
+
 void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag,
                 cudaStream_t st) {
   if (s.n == 0) return;
@@ -940,15 +953,14 @@ void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int
     k_m2d_allpairs<false><<<grid, TPB, 0, st>>>(s.n, s.m, s.pol_pos, s.pol_a, s.polar_mm, s.mm_pos, s.mm_a,
                                                 s.mm_q, s.ld, s.pol_wa32, s.mm_wa32, scratch, per, s.damp_thr,
                                                 damp_thr2_margin(s), err_flag);
-  int fb = (s.n + 127) / 128;
-  if (s.amoeba)
-    k_m2d_finish<true><<<fb, 128, 0, st>>>(s.n, nsplit, scratch, s.pol_pos, s.pol_a, s.mm_pos, s.mm_a, s.mm_q,
-                                           s.pol_wa32, s.mm_wa32, s.m2d_ri, s.m2d_src, s.m2d_sP, s.m2d_sD,
-                                           s.damp_thr, damp_thr2_margin(s), out);
-  else
-    k_m2d_finish<false><<<fb, 128, 0, st>>>(s.n, nsplit, scratch, s.pol_pos, s.pol_a, s.mm_pos, s.mm_a,
-                                            s.mm_q, s.pol_wa32, s.mm_wa32, s.m2d_ri, s.m2d_src, s.m2d_sP,
-                                            s.m2d_sD, s.damp_thr, damp_thr2_margin(s), out);
+  m2d_finish(s, out, scratch, nsplit, st);
+}
+
+void launch_m2d_ds(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag, cudaStream_t st) {
+  if (s.n == 0) return;
+  g_launches.fetch_add(2, std::memory_order_relaxed);
+  launch_m2d_ds_pairs(s, scratch, nsplit, err_flag, st);
+  m2d_finish(s, out, scratch, nsplit, st);
 }
 
 // ---- T.mu -----------------------------------------------------------------

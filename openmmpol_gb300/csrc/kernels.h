@@ -53,6 +53,10 @@ struct DevSites {
   float4 *tile_box32 = nullptr;
   int ntile = 0;
   float damp_r2max32 = 0.f;
+  // double-single E_M2D: static-site positions (hi with w = 0, lo), their
+  // tile boxes and the squared distance beyond which no M2D pair is damped
+  float4 *mm_pos32 = nullptr, *mm_pos32lo = nullptr, *mm_tile_box32 = nullptr;
+  float m2d_r2max32 = 0.f;
 };
 
 // ---- pair kernels ---------------------------------------------------------
@@ -89,12 +93,18 @@ int tmu32_max_split(const DevSites &s, int sm_count);
 int tmu32_pick_split(const DevSites &s, int sm_count);
 void tile_boxes32(const float4 *pos32, int n, float4 *boxes /*[2*ceil(n/128)]*/);
 float damp_r2max32(bool amoeba, double damp_thr, const double *inv_thole, const double *a, int n);
-// Double-single product (tmu_ds.cu): y = T x for one column at a time with
+// Double-single product (ds_kernels.cu): y = T x for one column at a time with
 // ~1e-13 relative accuracy on the FP32 pipes; scratch of nsplit * n * 3.
 int tmu_ds_pick_split(const DevSites &s, int sm_count);
 void launch_tmu_ds_pairs(const DevSites &s, const double *x, double *partial, int nsplit, cudaStream_t st);
 void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
                    int nsplit, cudaStream_t st);
+// E_M2D with the all-pairs part in double-single (scratch nsplit * n * 3)
+int m2d_ds_pick_split(const DevSites &s, int sm_count);
+void launch_m2d_ds_pairs(const DevSites &s, double *partial, int nsplit, int *err_flag, cudaStream_t st);
+void launch_m2d_ds(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag, cudaStream_t st);
+float m2d_r2max32(bool amoeba, double damp_thr, const double *pol_w, const double *pol_a, int n, const double *mm_w,
+                  const double *mm_a, int m);
 // batched fields: rhs[s*nf+f] = E_M2D[s] + field[f]; solution scatter to [f][s]
 void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
                       cudaStream_t st);

@@ -1,5 +1,5 @@
 // Pair arithmetic shared by the FP64/FP32 pair kernels (kernels.cu) and
-// the double-single kernel (tmu_ds.cu): FP64 reciprocal square root from an
+// the double-single kernels (ds_kernels.cu): FP64 reciprocal square root from an
 // FP32 seed, the FP32 damping pre-tests, and the damped dipole-field factors
 // (Thole damping of the reference, src/mod_electrostatics.F90:978-1095).
 #pragma once

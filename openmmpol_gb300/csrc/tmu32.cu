@@ -256,5 +256,31 @@ float damp_r2max32(bool amoeba, double damp_thr, const double *inv_thole, const 
   return (float)(rmax * rmax);
 }
 
+float m2d_r2max32(bool amoeba, double damp_thr, const double *pol_w, const double *pol_a, int n, const double *mm_w,
+                  const double *mm_a, int m) {
+  // a pair (polarizable target t, static source s) is damped only if
+  // min(a_t, a_s) (r w_t w_s)^3 < thr (AMOEBA) or r w_t w_s < 1 (Wang-AL);
+  // sources with w = inf (no Thole factor) or a = 0 (AMOEBA) never are
+  if (n == 0 || m == 0) return 0.f;
+  double wt = INFINITY, ws = INFINITY, amin = INFINITY;
+  for (int i = 0; i < n; ++i) {
+    wt = std::fmin(wt, pol_w[i]);
+    if (amoeba) amin = std::fmin(amin, pol_a[i]);
+  }
+  bool any = false;
+  for (int i = 0; i < m; ++i) {
+    if (!std::isfinite(mm_w[i])) continue;
+    if (amoeba && !(mm_a[i] > 0.0)) continue;
+    any = true;
+    ws = std::fmin(ws, mm_w[i]);
+    if (amoeba) amin = std::fmin(amin, mm_a[i]);
+  }
+  if (!any) return 0.f;  // no source can be damped
+  if (!(wt > 0.0) || !(ws > 0.0) || (amoeba && !(amin > 0.0))) return INFINITY;
+  double rmax = amoeba ? std::cbrt(damp_thr / amin) / (wt * ws) : 1.0 / (wt * ws);
+  rmax = rmax * 1.001 + 1e-3;
+  return (float)(rmax * rmax);
+}
+
 }  // namespace gpu
 }  // namespace ommp

@@ -263,6 +263,24 @@ def test_double_single_operator_accuracy(case, w1k, chains, golden_mmp):
     assert site.max() < 1e-9
 
 
+@pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba", "nma_wang_cut",
+                                  "1ubq_amoeba"])
+def test_double_single_m2d_accuracy(case, w1k, chains, golden_mmp):
+    """E_M2D of the mixed-ds mode (all pairs in double-single, scaled pairs
+    in FP64) against the FP64 field: 1e-11 relative, 1e-9 per site; back in
+    FP64 mode the field is recomputed in FP64."""
+    p = {"w1k": w1k[0], "chains": chains[0]}.get(case) or golden_mmp[case]
+    e64 = OMMPSystem(p).e_m2d()
+    g = OMMPSystem(p)
+    g.set_precision("mixed-ds")
+    eds = g.e_m2d()
+    assert rel(eds, e64) < 1e-11
+    site = np.linalg.norm(eds - e64, axis=2) / np.maximum(np.linalg.norm(e64, axis=2), 1e-3 * np.abs(e64).max())
+    assert site.max() < 1e-9
+    g.set_precision("fp64")
+    assert rel(g.e_m2d(), e64) < 1e-13
+
+
 @pytest.mark.parametrize("case", ["w1k", "chains"])
 def test_mixed_ds_solve(case, w1k, chains):
     p, ef = {"w1k": w1k, "chains": chains}[case]

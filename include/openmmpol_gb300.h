@@ -126,6 +126,18 @@ double *ommp_get_ipd(OMMP_SYSTEM_PRT s);
 int32_t *ommp_get_polar_mm(OMMP_SYSTEM_PRT s);
 /* include/openmmpol.h:86 : new coordinates [mm_atoms][3] */
 void ommp_update_coordinates(OMMP_SYSTEM_PRT s, const double *cmm);
+/* include/openmmpol.h:43-48 ; src/mod_c_interface.F90:327-376,1123-1176 ;
+ * src/mod_interface.F90:250-330.  Potential v [n] or field E [n][3] at n
+ * points cext [n][3] (bohr) of the static multipoles (mm), the induced
+ * dipoles (pol: D set for the potential, (P + D)/2 for the AMOEBA field) or
+ * both (mmpol); undamped, no screening.  The result is ADDED into v / E.
+ * The induced part needs a solved system. */
+void ommp_potential_mmpol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *v);
+void ommp_potential_mm2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *v);
+void ommp_potential_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *v);
+void ommp_field_mmpol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *E);
+void ommp_field_mm2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *E);
+void ommp_field_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *E);
 /* include/openmmpol.h:153-155 ; src/mod_c_interface.F90:1843-1879.  The fast
  * multipole method is not part of this library: enabling it logs a warning
  * and the direct sums are kept; ommp_use_fmm always returns false. */
@@ -139,6 +151,9 @@ bool ommp_use_fmm(OMMP_SYSTEM_PRT s);
 int32_t ommp_gpu_init_mmp(const char *filename, OMMP_SYSTEM_PRT *out);
 int32_t ommp_gpu_set_external_field(OMMP_SYSTEM_PRT s, const double *ext_field, int32_t solver,
                                     int32_t matv, int32_t add_mm_field);
+/* the same call, named for hosts that look for an explicit status variant */
+int32_t ommp_gpu_set_external_field_status(OMMP_SYSTEM_PRT s, const double *ext_field, int32_t solver,
+                                           int32_t matv, int32_t add_mm_field);
 /* same with a device pointer ext_field [pol_atoms][3] (no host copy) */
 int32_t ommp_gpu_set_external_field_device(OMMP_SYSTEM_PRT s, const double *ext_field_dev,
                                            int32_t solver, int32_t matv, int32_t add_mm_field);
@@ -157,6 +172,13 @@ void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode);
 /* FP64 direct T.mu kernel: 0 auto (symmetric from 2048 sites), 1 all ordered
  * pairs, 2 symmetric (each unordered pair once, deterministic) */
 int32_t ommp_gpu_set_fp64_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
+/* status-returning forms of ommp_{potential,field}_*2ext; which:
+ * OMMP_GPU_EXT_MMPOL, OMMP_GPU_EXT_MM or OMMP_GPU_EXT_POL */
+#define OMMP_GPU_EXT_MMPOL 0
+#define OMMP_GPU_EXT_MM 1
+#define OMMP_GPU_EXT_POL 2
+int32_t ommp_gpu_potential_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, const double *cext, double *v);
+int32_t ommp_gpu_field_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, const double *cext, double *E);
 /* FP32 inner T.mu kernel: 0 autotuned (default), 1 one target per thread
  * with a per-pair damping test, 2 tile-classified (undamped inner loop for
  * tiles beyond the damping range, two targets per thread) */

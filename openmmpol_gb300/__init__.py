@@ -167,6 +167,34 @@ class OMMPSystem:
     def use_fmm(self) -> bool:
         return bool(self._L.ommp_use_fmm(self._h))
 
+    # --- potential and field at external points (pyopenmmpol names) -------------
+    def _ext(self, field: bool, which: int, cext) -> np.ndarray:
+        c = np.ascontiguousarray(cext, dtype=np.float64)
+        if c.ndim != 2 or c.shape[1] != 3:
+            raise ValueError("cext should be shaped [:, 3]")
+        out = np.zeros((len(c), 3) if field else len(c))
+        fn = self._L.ommp_gpu_field_ext if field else self._L.ommp_gpu_potential_ext
+        _check(fn(self._h, which, len(c), c.ctypes.data_as(_lib._dp), out.ctypes.data_as(_lib._dp)))
+        return out
+
+    def potential_mmpol2ext(self, cext) -> np.ndarray:
+        return self._ext(False, 0, cext)
+
+    def potential_mm2ext(self, cext) -> np.ndarray:
+        return self._ext(False, 1, cext)
+
+    def potential_pol2ext(self, cext) -> np.ndarray:
+        return self._ext(False, 2, cext)
+
+    def field_mmpol2ext(self, cext) -> np.ndarray:
+        return self._ext(True, 0, cext)
+
+    def field_mm2ext(self, cext) -> np.ndarray:
+        return self._ext(True, 1, cext)
+
+    def field_pol2ext(self, cext) -> np.ndarray:
+        return self._ext(True, 2, cext)
+
     # --- extensions ---------------------------------------------------------------
     def set_solver_tol(self, tol: float) -> None:
         self._L.ommp_gpu_set_solver_tol(self._h, float(tol))

@@ -48,6 +48,7 @@ SIGNATURES = {
     "ommp_use_fmm": (C.c_bool, [_vp]),
     "ommp_gpu_init_mmp": (C.c_int32, [C.c_char_p, C.POINTER(_vp)]),
     "ommp_gpu_set_external_field": (C.c_int32, [_vp, _dp, C.c_int32, C.c_int32, C.c_int32]),
+    "ommp_gpu_set_external_field_status": (C.c_int32, [_vp, _dp, C.c_int32, C.c_int32, C.c_int32]),
     "ommp_gpu_set_external_field_device": (C.c_int32, [_vp, _vp, C.c_int32, C.c_int32, C.c_int32]),
     "ommp_gpu_get_polelec_energy": (C.c_int32, [_vp, _dp]),
     "ommp_gpu_update_coordinates": (C.c_int32, [_vp, _dp]),
@@ -59,6 +60,14 @@ SIGNATURES = {
     "ommp_gpu_set_precision": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_fp64_kernel": (C.c_int32, [_vp, C.c_int32]),
     "ommp_gpu_set_fp32_kernel": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_potential_ext": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp, _dp]),
+    "ommp_gpu_field_ext": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp, _dp]),
+    "ommp_potential_mmpol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
+    "ommp_potential_mm2ext": (None, [_vp, C.c_int32, _dp, _dp]),
+    "ommp_potential_pol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
+    "ommp_field_mmpol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
+    "ommp_field_mm2ext": (None, [_vp, C.c_int32, _dp, _dp]),
+    "ommp_field_pol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
     "ommp_gpu_set_use_graphs": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_external_fields_batch": (C.c_int32, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ommp_gpu_set_external_fields_batch_device": (C.c_int32, [_vp, C.c_int32, _vp, _vp, _dp]),

@@ -77,6 +77,10 @@ int32_t ommp_gpu_set_external_field(OMMP_SYSTEM_PRT s, const double *ef, int32_t
                                     int32_t add_mm) {
   return S(s)->set_external_field(ef, solver, matv, add_mm != 0);
 }
+int32_t ommp_gpu_set_external_field_status(OMMP_SYSTEM_PRT s, const double *ef, int32_t solver, int32_t matv,
+                                           int32_t add_mm) {
+  return ommp_gpu_set_external_field(s, ef, solver, matv, add_mm);
+}
 int32_t ommp_gpu_set_external_field_device(OMMP_SYSTEM_PRT s, const double *ef, int32_t solver, int32_t matv,
                                            int32_t add_mm) {
   return S(s)->set_external_field_device(ef, solver, matv, add_mm != 0);
@@ -114,6 +118,31 @@ int32_t *ommp_get_polar_mm(OMMP_SYSTEM_PRT s) { return S(s)->polar_mm_host(); }
 
 int32_t ommp_gpu_update_coordinates(OMMP_SYSTEM_PRT s, const double *c) { return S(s)->update_coordinates(c); }
 void ommp_update_coordinates(OMMP_SYSTEM_PRT s, const double *c) { fatal_if(ommp_gpu_update_coordinates(s, c)); }
+
+int32_t ommp_gpu_potential_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, const double *cext, double *v) {
+  return S(s)->ext_props(which, false, n, cext, v);
+}
+int32_t ommp_gpu_field_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, const double *cext, double *e) {
+  return S(s)->ext_props(which, true, n, cext, e);
+}
+void ommp_potential_mmpol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *v) {
+  fatal_if(S(s)->ext_props(0, false, n, c, v));
+}
+void ommp_potential_mm2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *v) {
+  fatal_if(S(s)->ext_props(1, false, n, c, v));
+}
+void ommp_potential_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *v) {
+  fatal_if(S(s)->ext_props(2, false, n, c, v));
+}
+void ommp_field_mmpol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *e) {
+  fatal_if(S(s)->ext_props(0, true, n, c, e));
+}
+void ommp_field_mm2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *e) {
+  fatal_if(S(s)->ext_props(1, true, n, c, e));
+}
+void ommp_field_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *e) {
+  fatal_if(S(s)->ext_props(2, true, n, c, e));
+}
 
 void ommp_enable_fmm(OMMP_SYSTEM_PRT s) {
   (void)s;

@@ -53,7 +53,7 @@ System::~System() {
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
                   alpha32_, scratch_, scratch32_, partial_, dots_, hist_, cols_, flag_, tmat_, piv_,
-                  info_, diis_x_, diis_e_, d_.tile_box32};
+                  info_, diis_x_, diis_e_, d_.tile_box32, ext_buf_};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (flush_buf_) cudaFree(flush_buf_);

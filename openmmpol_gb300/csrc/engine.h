@@ -83,6 +83,9 @@ class System {
   int tmatvec(const double *x_host, double *y_host, int nrhs, bool dodiag, int matv);
   int tmatvec_f32(const double *x_host, double *y_host, int nrhs);
   int tmatvec_ds(const double *x_host, double *y_host, int nrhs);
+  // potential (field = false, out [n]) or field (out [n][3]) at the points
+  // cext [n][3], added into out; which 0 all, 1 static, 2 induced
+  int ext_props(int which, bool field, int n, const double *cext_host, double *out_host);
   int e_m2d(double *out_host);
   void clear_guess() { ipd_use_guess_ = false; }
   void set_tol(double t) { tol_ = t; }
@@ -173,6 +176,8 @@ class System {
   size_t scratch_n_ = 0;
   double *sym_scratch_ = nullptr;  // symmetric-kernel partials (allocated on first use)
   int fp64_kernel_ = 0;
+  double *ext_buf_ = nullptr;  // external points: coordinates, partials, output, dipoles
+  size_t ext_cap_ = 0;
   double *ds_scratch_ = nullptr;  // split partials of the double-single kernels
   int nsplit_ds_ = 1, nsplit_m2d_ds_ = 1;
   bool m2d_ds_ = false;  // the cached E_M2D was computed in double-single

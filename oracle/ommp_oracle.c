@@ -1535,3 +1535,113 @@ int orc_update_coordinates(orc_sys *s, const double *c) {
     if (s->amoeba) return rotate_multipoles(s);
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* potential and field at arbitrary points (QM coupling)               */
+/* potential_M2E / potential_D2E / field_M2E / field_D2E,              */
+/* src/mod_electrostatics.F90:3067-3336, with the undamped             */
+/* coulomb_kernel :978-1016 and q/mu/quad_elec_prop :1097-1405; the    */
+/* ABI wrappers ommp_{potential,field}_{mmpol,mm,pol}2ext              */
+/* (src/mod_interface.F90:250-330) add into the caller's array.         */
+/* ------------------------------------------------------------------ */
+static int coulomb_kernel(const double *dr, int maxder, double *res) {
+    double nr = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+    if (nr < EPS_RP) {
+        set_err("Requesting Coulomb kernel for two atoms placed in the same point, this could be an internal "
+                "bug or a problem in your input file, please check.");
+        return 1;
+    }
+    res[0] = 1.0 / nr;
+    double inv2 = res[0] * res[0];
+    for (int k = 1; k <= maxder; k++) res[k] = res[k - 1] * inv2;
+    return 0;
+}
+
+/* which: 0 = static multipoles + induced dipoles, 1 = static only,
+   2 = induced dipoles only; field != 0 selects the field (3 per point) */
+static int ext_props(orc_sys *s, int32_t which, int32_t n, const double *cext, double *out, int field) {
+    const int do_mm = which == 0 || which == 1, do_pol = which == 0 || which == 2;
+    if (do_pol && s->npol > 0 && !s->ipd_done) {
+        set_err(field ? "IPD should be computed before computing D2E field."
+                      : "IPD should be computed before D2E potential.");
+        return ORC_ERR_INPUT;
+    }
+    const int C = field ? 3 : 1;
+    int bad = 0;
+    /* the dipoles seen from outside: D (potential) or (P + D) / 2 (field)
+       for AMOEBA, the single set otherwise (:3100-3120, :3240-3250) */
+    double *mu = NULL;
+    if (do_pol && s->npol > 0) {
+        mu = xcalloc(3 * (size_t)s->npol, sizeof(double));
+        for (int k = 0; k < 3 * s->npol; k++)
+            mu[k] = (s->amoeba && field) ? 0.5 * (s->ipd[3 * (size_t)s->npol + k] + s->ipd[k]) : s->ipd[k];
+    }
+#pragma omp parallel for schedule(dynamic) reduction(| : bad)
+    for (int j = 0; j < n; j++) {
+        double acc[3] = {0, 0, 0};
+        const double *p = &cext[3 * (size_t)j];
+        if (do_mm) {
+            for (int i = 0; i < s->mm; i++) {
+                double dr[3] = {p[0] - s->cmm[3 * i], p[1] - s->cmm[3 * i + 1], p[2] - s->cmm[3 * i + 2]};
+                double k[5];
+                if (coulomb_kernel(dr, s->amoeba ? (field ? 4 : 2) : (field ? 2 : 1), k)) {
+                    bad = 1;
+                    continue;
+                }
+                const double *q = &s->q[(size_t)i * s->ld_cart];
+                if (!field) {
+                    double v = k[0] * q[0];
+                    if (s->amoeba) {
+                        double mdr = q[1] * dr[0] + q[2] * dr[1] + q[3] * dr[2];
+                        double qx = q[4] * dr[0] + q[5] * dr[1] + q[7] * dr[2];
+                        double qy = q[5] * dr[0] + q[6] * dr[1] + q[8] * dr[2];
+                        double qz = q[7] * dr[0] + q[8] * dr[1] + q[9] * dr[2];
+                        v += mdr * k[1] + 3.0 * (qx * dr[0] + qy * dr[1] + qz * dr[2]) * k[2];
+                    }
+                    acc[0] += v;
+                } else {
+                    for (int c = 0; c < 3; c++) acc[c] += q[0] * k[1] * dr[c];
+                    if (s->amoeba) {
+                        double mdr = q[1] * dr[0] + q[2] * dr[1] + q[3] * dr[2];
+                        double qv[3] = {q[4] * dr[0] + q[5] * dr[1] + q[7] * dr[2],
+                                        q[5] * dr[0] + q[6] * dr[1] + q[8] * dr[2],
+                                        q[7] * dr[0] + q[8] * dr[1] + q[9] * dr[2]};
+                        double qxr = qv[0] * dr[0] + qv[1] * dr[1] + qv[2] * dr[2];
+                        for (int c = 0; c < 3; c++) {
+                            acc[c] += 3.0 * mdr * dr[c] * k[2] - q[1 + c] * k[1];
+                            acc[c] += 15.0 * qxr * dr[c] * k[3] - 6.0 * qv[c] * k[2];
+                        }
+                    }
+                }
+            }
+        }
+        if (do_pol) {
+            for (int i = 0; i < s->npol; i++) {
+                const double *c0 = &s->cmm[3 * (size_t)s->polar_mm[i]];
+                double dr[3] = {p[0] - c0[0], p[1] - c0[1], p[2] - c0[2]};
+                double k[4];
+                if (coulomb_kernel(dr, field ? 2 : 1, k)) {
+                    bad = 1;
+                    continue;
+                }
+                const double *m = &mu[3 * (size_t)i];
+                double mdr = m[0] * dr[0] + m[1] * dr[1] + m[2] * dr[2];
+                if (!field)
+                    acc[0] += mdr * k[1];
+                else
+                    for (int c = 0; c < 3; c++) acc[c] += 3.0 * mdr * dr[c] * k[2] - m[c] * k[1];
+            }
+        }
+        for (int c = 0; c < C; c++) out[(size_t)j * C + c] += acc[c];
+    }
+    free(mu);
+    return bad ? ORC_ERR_NUMERIC : ORC_OK;
+}
+
+int orc_potential_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, double *v) {
+    return ext_props(s, which, n, cext, v, 0);
+}
+
+int orc_field_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, double *e) {
+    return ext_props(s, which, n, cext, e, 1);
+}

@@ -25,6 +25,9 @@
  *   set_external_field      src/mod_interface.F90:184-233
  *   get_polelec_energy      src/mod_interface.F90:343-370, energy_MM_pol
  *                           src/mod_electrostatics.F90:943-976
+ *   potential/field at external points (QM coupling)
+ *                           src/mod_electrostatics.F90:3067-3336,
+ *                           src/mod_interface.F90:250-330
  *
  * Parity of this restatement is pinned against the reference's own golden
  * files (tests/N-methylacetamide, tests/1crn, tests/1ao6, tests/1ubq IPD_* and
@@ -98,6 +101,11 @@ int32_t orc_residual_history(const orc_sys *s, int32_t set, double *out, int32_t
 int orc_update_coordinates(orc_sys *s, const double *c);
 /* drop the warm-start guess (ipd_use_guess = false) */
 void orc_clear_guess(orc_sys *s);
+/* potential [n] / field [n][3] at points cext [n][3] (bohr), ADDED into the
+   output like the reference's ommp_{potential,field}_*2ext; which: 0 static
+   multipoles + induced dipoles, 1 static multipoles, 2 induced dipoles */
+int orc_potential_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, double *v);
+int orc_field_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, double *e);
 
 #ifdef __cplusplus
 }

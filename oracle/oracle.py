@@ -59,6 +59,8 @@ def lib():
             "orc_get_screening": (None, [vp, C.c_int32, ip, ip, dp]),
             "orc_tmatvec": (C.c_int, [vp, dp, dp, C.c_int32, C.c_int32]),
             "orc_tmatvec_rows": (C.c_int, [vp, dp, ip, C.c_int32, dp]),
+            "orc_potential_ext": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp]),
+            "orc_field_ext": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp]),
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
             "orc_last_iterations": (C.c_int32, [vp, C.c_int32]),
@@ -193,6 +195,20 @@ class OracleSystem:
         y = np.zeros((len(rows), 3))
         self._check(lib().orc_tmatvec_rows(self._h, _dp(x), _ip(rows), len(rows), _dp(y)))
         return y
+
+    def potential_ext(self, which, cext, v=None):
+        """Potential at points cext [n][3] added into v (zeros if None);
+        which: 0 static + induced, 1 static, 2 induced."""
+        cext = np.ascontiguousarray(cext, dtype=np.float64).reshape(-1, 3)
+        v = np.zeros(len(cext)) if v is None else np.array(v, dtype=np.float64)
+        self._check(lib().orc_potential_ext(self._h, int(which), len(cext), _dp(cext), _dp(v)))
+        return v
+
+    def field_ext(self, which, cext, e=None):
+        cext = np.ascontiguousarray(cext, dtype=np.float64).reshape(-1, 3)
+        e = np.zeros((len(cext), 3)) if e is None else np.array(e, dtype=np.float64).reshape(-1, 3)
+        self._check(lib().orc_field_ext(self._h, int(which), len(cext), _dp(cext), _dp(e)))
+        return e
 
     def set_external_field(self, ef, nomm=False, solver=SOLVER_NONE, matv=MATV_NONE):
         ef = np.ascontiguousarray(ef, dtype=np.float64).reshape(self.pol_atoms, 3)

@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--fp64-requests", type=int, default=64, help="s1024: requests in the FP64 stream")
     ap.add_argument("--slots", type=int, default=8, help="s1024: concurrent requests on the GPU")
     ap.add_argument("--hbm-budget-gib", type=float, default=4.0, help="s1024: device memory for systems")
+    ap.add_argument("--loads", default="0.5,0.7,0.9", help="s1024: offered loads, fractions of saturation")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "ommp_gb300_bench"))
     return ap.parse_args()
 
@@ -269,6 +270,12 @@ def rel_err(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
 
 
+def max_err(a, b):
+    """max_i |a_i - b_i| / max_i |b_i| over sites (3-vectors)"""
+    a, b = np.asarray(a).reshape(-1, 3), np.asarray(b).reshape(-1, 3)
+    return float(np.linalg.norm(a - b, axis=1).max() / np.linalg.norm(b, axis=1).max())
+
+
 def run_gb300(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -414,6 +421,8 @@ def run_gb300(args):
             fp64[f"{label}_rel_err_ipd"] = rel_err(r["ipd"], ref)
             fp64[f"{label}_rel_err_energy"] = float(abs(r["energy"] - ref_ep) / abs(ref_ep))
             fp64[f"{label}_rel_err_field"] = rel_err(e_field, e64)
+            fp64[f"{label}_max_err_ipd"] = max_err(r["ipd"], ref)
+            fp64[f"{label}_max_err_field"] = max_err(e_field, e64)
             fp64[f"speedup_{label}_over_fp64"] = r["value"] / ws * fp64_s
     for r in (main, ds):
         if r:
@@ -534,7 +543,7 @@ def run_b64(args):
     path, w = workload("b64", args.cache)
     s = og.OMMPSystem(path)
     s.set_solver_tol(1e-10)
-    s.set_precision("mixed")
+    s.set_precision(args.precision)
     n = s.pol_atoms
     nv = 3 * n
     nf = 64
@@ -568,8 +577,8 @@ def run_b64(args):
     clocks = clk.stop()
     launches = L.ommp_gpu_kernel_launch_count() - l0
     s.enable_kernel_timing(False)
-    counters = [s.counter(k) for k in range(4)]
-    k64, k32 = s.kernel_stats(0), s.kernel_stats(1)
+    counters = [s.counter(k) for k in range(5)]
+    k64, k32, kds = s.kernel_stats(0), s.kernel_stats(1), s.kernel_stats(2)
     value = nf * args.steps / (sum(times) * 1e-3)
     ipd_b = np.zeros((nf, s.n_ipd, n, 3))
     L.ommp_gpu_copy_to_host(ipd_b.ctypes.data, od, ipd_b.nbytes)
@@ -585,6 +594,7 @@ def run_b64(args):
         s.set_external_field(fields[k])
         seq.append(time.perf_counter() - t0)
     s.set_precision("fp64")
+    s.e_m2d()  # recomputed in FP64 if the cached field is double-single
     s.clear_guess()
     t0 = time.perf_counter()
     s.set_external_field(fields[0])
@@ -593,7 +603,7 @@ def run_b64(args):
     err = float(np.linalg.norm(ipd_b[0] - ref) / np.linalg.norm(ref))
     pairs = float(n) * (n - 1)
     kst = {}
-    for name, (cnt, ms, cols) in (("tmu_fp64", k64), ("tmu_fp32", k32)):
+    for name, (cnt, ms, cols) in (("tmu_fp64", k64), ("tmu_fp32", k32), ("tmu_ds", kds)):
         if cnt:
             kst[name] = {"launches": cnt, "columns": cols, "total_ms": ms,
                          "achieved_tflops": FLOP_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12}
@@ -603,7 +613,8 @@ def run_b64(args):
             "vs_baseline": None, "dtype": "fp32+f64", "data": "synthetic",
             "config": {"workload": f"AMOEBA water box {n} sites, 64 fields of 30 point charges "
                                    "(seeds 1000..1063), mixed-precision block solve to RMS 1e-10",
-                       "sites": n, "fields": nf, "l2": "flushed (256 MiB write) between batches"},
+                       "sites": n, "fields": nf, "precision": args.precision,
+                       "l2": "flushed (256 MiB write) between batches"},
             "e2e": {"value": nf / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": nf * nv * 8,
                     "d2h_bytes_per_step": nf * s.n_ipd * nv * 8},
             "gpu_launches": int(launches), "batch_ms": times, "counters_last_batch": counters,
@@ -746,11 +757,18 @@ def run_s1024(args):
     res = {}
     clk = Clocks(0)
     l0 = L.ommp_gpu_kernel_launch_count()
+    loads = [float(x) for x in args.loads.split(",") if x.strip()]
+    if 0.7 not in loads:
+        loads.append(0.7)
     for label, prec, nr in (("mixed", args.precision, nreq), ("fp64", "fp64", n64)):
         pl = plan[:nr]
         r = {}
-        for phase in ("saturation", "load70"):
-            rate = None if phase == "saturation" else 0.7 * r["saturation"]["requests_per_s"]
+        # saturation first (all requests at t = 0), then Poisson arrivals at
+        # fractions of the saturation rate: the mixed stream sweeps the load,
+        # the FP64 one is measured at 70 % only
+        phases = ["saturation"] + [f"load{int(round(100 * f))}" for f in (loads if label == "mixed" else [0.7])]
+        for phase in phases:
+            rate = None if phase == "saturation" else float(phase[4:]) / 100 * r["saturation"]["requests_per_s"]
             srv = og.Server(budget, slots=args.slots, precision=prec, tol=1e-10)
             out, wall, errors = serve_stream(srv, pl, pool, rate, keep)
             st = srv.stats()
@@ -784,6 +802,15 @@ def run_s1024(args):
     for prec in res:
         res[prec].pop("results")
     mx, f64 = res["mixed"], res["fp64"]
+    # the knee: the highest offered load whose stream is still served at the
+    # offered rate (>= 95 %) with p99 within 3x of the lightest load's
+    sweep = sorted([(float(k[4:]) / 100, v) for k, v in mx.items() if k.startswith("load")], key=lambda t: t[0])
+    knee = None
+    if sweep:
+        p99_0 = sweep[0][1]["p99_ms"]
+        for f, v in sweep:
+            if v["requests_per_s"] >= 0.95 * v["rate_offered"] and v["p99_ms"] <= 3 * p99_0:
+                knee = f
     line = {"metric": "served induced-dipole solves/s + p50/p99 latency (mixed vs FP64, <=1e-7 rel. error)",
             "value": mx["saturation"]["requests_per_s"], "unit": "solves/s", "n_gpus": 1,
             "steps": nreq, "warmup": 0, "ms_per_step": 1e3 / mx["saturation"]["requests_per_s"],
@@ -793,9 +820,12 @@ def run_s1024(args):
                                    f"({len(sizes)} cached geometries), 30-charge field per new request, 30 % "
                                    "follow-ups (field x (1 + 0.01 N(0,1)), warm start), D+P to RMS 1e-10",
                        "hbm_budget_gib": args.hbm_budget_gib, "slots": args.slots, "precision": args.precision,
-                       "fp64_requests": n64, "arrivals": "all at t=0 (saturation), then Poisson at 70 % "
-                                                         "of the saturation rate"},
+                       "fp64_requests": n64, "arrivals": "all at t=0 (saturation), then Poisson at the "
+                                                         "listed fractions of the saturation rate"},
             "p50_ms": mx["load70"]["p50_ms"], "p99_ms": mx["load70"]["p99_ms"],
+            "load_sweep": [{"load": f, "offered_rps": v["rate_offered"], "served_rps": v["requests_per_s"],
+                            "p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"]} for f, v in sweep],
+            "knee_load_fraction": knee,
             "mixed": mx, "fp64": f64,
             "speedup_mixed_over_fp64_saturation": (mx["saturation"]["sites_per_s"] /
                                                    f64["saturation"]["sites_per_s"]),

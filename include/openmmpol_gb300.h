@@ -183,6 +183,11 @@ int32_t ommp_gpu_field_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, const do
  * with a per-pair damping test, 2 tile-classified (undamped inner loop for
  * tiles beyond the damping range, two targets per thread) */
 int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
+/* preconditioner of the FP32 inner solver of the mixed modes: 0 the
+ * reference's diagonal (alpha), 1 block Jacobi over runs of bonded sites
+ * (default).  The FP64 solver and the outer convergence test always use the
+ * reference's diagonal. */
+int32_t ommp_gpu_set_inner_preconditioner(OMMP_SYSTEM_PRT s, int32_t mode);
 /* forget the last dipoles as a starting guess */
 void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s);
 /* capture the inner FP32 iteration as a CUDA graph (default on) */

@@ -211,6 +211,12 @@ class OMMPSystem:
         m = {"auto": 0, "ordered": 1, "symmetric": 2}.get(mode, mode)
         _check(self._L.ommp_gpu_set_fp64_kernel(self._h, int(m)))
 
+    def set_inner_preconditioner(self, mode) -> None:
+        """'diagonal' (the reference's alpha) | 'block' (block Jacobi, default)
+        for the FP32 inner solver of the mixed modes."""
+        m = {"diagonal": 0, "block": 1}.get(mode, mode)
+        _check(self._L.ommp_gpu_set_inner_preconditioner(self._h, int(m)))
+
     def set_fp32_kernel(self, mode) -> None:
         """'auto' (autotuned) | 'pairwise' (kernel 1) | 'tiled' (kernel 2)."""
         m = {"auto": 0, "pairwise": 1, "tiled": 2}.get(mode, mode)

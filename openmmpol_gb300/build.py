@@ -23,7 +23,7 @@ CU_SOURCES = ["kernels.cu", "engine.cu", "solvers.cu", "noalloc.cu", "tmu32.cu",
 # per-file nvcc flags: the FP32 operators flush subnormals (plain MUFU rsqrt);
 # the double-single kernel fuses nothing implicitly (its FMAs are explicit)
 CU_EXTRA = {"tmu32.cu": ["-ftz=true"], "ds_kernels.cu": ["-ftz=true", "--fmad=false"]}
-CXX_SOURCES = ["setup.cpp", "capi.cpp", "log.cpp", "server.cpp"]
+CXX_SOURCES = ["setup.cpp", "capi.cpp", "log.cpp", "server.cpp", "precond.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -161,6 +161,9 @@ void ommp_gpu_set_solver_maxiter(OMMP_SYSTEM_PRT s, int32_t n) { S(s)->set_maxit
 void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode) { S(s)->set_precision(mode); }
 int32_t ommp_gpu_set_fp64_kernel(OMMP_SYSTEM_PRT s, int32_t mode) { return S(s)->set_fp64_kernel(mode); }
 int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode) { return S(s)->set_fp32_kernel(mode); }
+int32_t ommp_gpu_set_inner_preconditioner(OMMP_SYSTEM_PRT s, int32_t mode) {
+  return S(s)->set_inner_preconditioner(mode);
+}
 void ommp_gpu_set_use_graphs(OMMP_SYSTEM_PRT s, int32_t on) { S(s)->set_use_graphs(on != 0); }
 int32_t ommp_gpu_set_external_fields_batch(OMMP_SYSTEM_PRT s, int32_t nfields, const double *fields, double *ipd_out,
                                            double *energies) {

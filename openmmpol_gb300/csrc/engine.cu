@@ -53,7 +53,7 @@ System::~System() {
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
                   alpha32_, scratch_, scratch32_, partial_, dots_, hist_, cols_, flag_, tmat_, piv_,
-                  info_, diis_x_, diis_e_, d_.tile_box32, ext_buf_};
+                  info_, diis_x_, diis_e_, d_.tile_box32, ext_buf_, blk_info_, blk_minv_};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (flush_buf_) cudaFree(flush_buf_);
@@ -288,6 +288,26 @@ int System::upload_geometry() {
   cudaMemcpyAsync(d_.mm_a, ma.data(), mm * sizeof(double), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.mm_q, m.q.data(), m.q.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
   // the host vectors above die at return: wait for the copies
+  // block-Jacobi preconditioner of the FP32 inner solver (geometry-dependent)
+  {
+    std::vector<int> info;
+    std::vector<float> minv;
+    build_block_jacobi(m, d2d_pairs_, d_.damp_thr, info, minv);
+    cudaStreamSynchronize(st_);
+    if (blk_info_) cudaFree(blk_info_);
+    if (blk_minv_) cudaFree(blk_minv_);
+    blk_info_ = nullptr;
+    blk_minv_ = nullptr;
+    if (n > 0) {
+      if (dalloc(blk_info_, (size_t)n) || dalloc(blk_minv_, minv.size())) {
+        set_last_error("out of device memory for the block preconditioner");
+        return kErrMemory;
+      }
+      cudaMemcpyAsync(blk_info_, info.data(), info.size() * sizeof(int), cudaMemcpyHostToDevice, st_);
+      cudaMemcpyAsync(blk_minv_, minv.data(), minv.size() * sizeof(float), cudaMemcpyHostToDevice, st_);
+    }
+    // the host vectors die at return: the synchronisation below covers the copies
+  }
   return check(cudaStreamSynchronize(st_), "geometry upload");
 }
 
@@ -833,6 +853,15 @@ int System::set_fp64_kernel(int mode) {
     return kErrBadArg;
   }
   fp64_kernel_ = mode;
+  return kOk;
+}
+
+int System::set_inner_preconditioner(int mode) {
+  if (mode < 0 || mode > 1) {
+    set_last_error("inner preconditioner must be 0 (diagonal) or 1 (block Jacobi)");
+    return kErrBadArg;
+  }
+  inner_precond_ = mode;
   return kOk;
 }
 

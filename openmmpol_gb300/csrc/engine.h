@@ -42,7 +42,7 @@ struct Workspace {
   bool owned = false;
   // captured inner FP32 iteration (CUDA graph) and what it was built for
   cudaGraphExec_t graph = nullptr;
-  int graph_ncol = -1, graph_gmax = 0, graph_nsplit = 0, graph_kver = 0;
+  int graph_ncol = -1, graph_gmax = 0, graph_nsplit = 0, graph_kver = 0, graph_prec = -1;
   long long graph_kernels = 0;
 };
 
@@ -97,6 +97,7 @@ class System {
   // pairs (target-outer), 2 symmetric (unordered pairs)
   int set_fp64_kernel(int mode);
   int set_fp32_kernel(int mode);
+  int set_inner_preconditioner(int mode);
   int matvec_residual(int ncol, const double *x, double *y);
   int ensure_ds_scratch();
   int precision() const { return precision_; }
@@ -176,6 +177,9 @@ class System {
   size_t scratch_n_ = 0;
   double *sym_scratch_ = nullptr;  // symmetric-kernel partials (allocated on first use)
   int fp64_kernel_ = 0;
+  int4 *blk_info_ = nullptr;   // block-Jacobi preconditioner (build_block_jacobi)
+  float *blk_minv_ = nullptr;
+  int inner_precond_ = 1;       // FP32 inner solver: 0 diagonal, 1 block Jacobi
   double *ext_buf_ = nullptr;  // external points: coordinates, partials, output, dipoles
   size_t ext_cap_ = 0;
   double *ds_scratch_ = nullptr;  // split partials of the double-single kernels

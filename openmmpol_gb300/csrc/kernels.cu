@@ -1163,6 +1163,39 @@ void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float
   tmu_finish<float>(s, nrhs, nsplit, scratch, s.pol_pos32, s.pol_a32, x, true, y, gmax, st);
 }
 
+// z = M^-1 r, one thread per site and column: the three rows of the site's
+// block times the run's slice of r
+__global__ void k_block_apply(int n, const int4 *__restrict__ info, const float *__restrict__ minv,
+                              const float *__restrict__ r, float *__restrict__ z) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const size_t co = (size_t)blockIdx.y * 3 * n;
+  const int4 b = info[j];
+  const int w = 3 * b.y;
+  const float *rr = r + co + 3 * (size_t)b.x;
+  const float *m0 = minv + b.z + (size_t)(3 * b.w) * w;
+  const float *m1 = m0 + w, *m2 = m1 + w;
+  float z0 = 0.f, z1 = 0.f, z2 = 0.f;
+  for (int l = 0; l < w; ++l) {
+    const float v = rr[l];
+    z0 = fmaf(m0[l], v, z0);
+    z1 = fmaf(m1[l], v, z1);
+    z2 = fmaf(m2[l], v, z2);
+  }
+  float *zz = z + co + 3 * (size_t)j;
+  zz[0] = z0;
+  zz[1] = z1;
+  zz[2] = z2;
+}
+
+void launch_block_apply(int ncol, int n, const int4 *info, const float *minv, const float *r, float *z,
+                        cudaStream_t st) {
+  if (n == 0) return;
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  dim3 grid((n + 127) / 128, ncol);
+  k_block_apply<<<grid, 128, 0, st>>>(n, info, minv, r, z);
+}
+
 // Batched right-hand sides, set-major columns: rhs[s*nf + f] = E_M2D[s] + field[f]
 __global__ void k_batch_rhs(int n, int nf, int nset, const double *__restrict__ e_m2d,
                             const double *__restrict__ fields, double *__restrict__ rhs) {

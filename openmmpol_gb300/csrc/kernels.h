@@ -105,6 +105,10 @@ void launch_m2d_ds_pairs(const DevSites &s, double *partial, int nsplit, int *er
 void launch_m2d_ds(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag, cudaStream_t st);
 float m2d_r2max32(bool amoeba, double damp_thr, const double *pol_w, const double *pol_a, int n, const double *mm_w,
                   const double *mm_a, int m);
+// z = M^-1 r for the block-Jacobi preconditioner (info / minv as built by
+// build_block_jacobi), columns [ncol][n][3], FP32
+void launch_block_apply(int ncol, int n, const int4 *info, const float *minv, const float *r, float *z,
+                        cudaStream_t st);
 // batched fields: rhs[s*nf+f] = E_M2D[s] + field[f]; solution scatter to [f][s]
 void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
                       cudaStream_t st);

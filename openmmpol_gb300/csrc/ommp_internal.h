@@ -75,4 +75,14 @@ bool rotate_multipoles(HostModel &m, std::string &err);
 void build_m2d_pairs(const HostModel &m, ScaledPairs &out);
 void build_d2d_pairs(const HostModel &m, ScaledPairs &out);
 
+// Block-Jacobi preconditioner of the FP32 inner solver (precond.cpp): runs of
+// at most kMaxBlock consecutive polarizable sites, each within kBlockLinkBohr
+// of an earlier site of its run; per site {run start, run size, offset of the
+// run's inverse block in minv, index in the run}; minv holds the FP32
+// inverse of each run's diagonal block of T, (3 size) x (3 size) row-major.
+constexpr int kMaxBlock = 8;
+constexpr double kBlockLinkBohr = 3.0;
+void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_thr, std::vector<int> &info,
+                        std::vector<float> &minv);
+
 }  // namespace ommp

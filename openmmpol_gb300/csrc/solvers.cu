@@ -253,7 +253,15 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
     w.cols_h[k] = c;
   }
   cudaMemcpyAsync(w.cols, w.cols_h, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
+  // z = M^-1 r: the diagonal (fused in the update) or the block-Jacobi blocks
+  const bool blocks = inner_precond_ == 1 && blk_info_;
+  auto precondition = [&]() {
+    if (!blocks) return;
+    gpu::launch_block_apply(ncol, n, blk_info_, blk_minv_, w.r32, w.z32, st_);
+    gpu::launch_dots_f32(ncol, nv, w.r32, w.z32, w.partial, st_);
+  };
   gpu::launch_cg_update_f32(ncol, n, w.x32, w.r32, w.p32, w.h32, w.z32, alpha32_, w.cols, w.partial, st_);
+  precondition();
   gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
   cudaMemcpyAsync(w.p32, w.z32, ncol * nv * sizeof(float), cudaMemcpyDeviceToDevice, st_);
   cudaMemcpyAsync(w.scal_h, w.dots, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
@@ -273,6 +281,7 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
     gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
     gpu::launch_cg_alpha(ncol, w.dots, w.cols, 1e-300, st_);
     gpu::launch_cg_update_f32(ncol, n, w.x32, w.r32, w.p32, w.h32, w.z32, alpha32_, w.cols, w.partial, st_);
+    precondition();
     gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
     gpu::launch_cg_gnew(ncol, n, w.dots, w.cols, nullptr, 0, st_);
     gpu::launch_cg_pupdate_f32(ncol, n, w.p32, w.z32, w.cols, st_);
@@ -281,7 +290,7 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
   // capture one iteration as a graph (kernel arguments and buffers are fixed
   // per workspace, width and launch shape; the tolerance lives in w.cols)
   if (use_graphs_ && (w.graph_ncol != ncol || w.graph_gmax != shape.g || w.graph_nsplit != shape.nsplit ||
-                     w.graph_kver != shape.kver)) {
+                     w.graph_kver != shape.kver || w.graph_prec != (blocks ? 1 : 0))) {
     if (w.graph) cudaGraphExecDestroy(w.graph);
     w.graph = nullptr;
     w.graph_ncol = -1;
@@ -297,6 +306,7 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
         w.graph_gmax = shape.g;
         w.graph_nsplit = shape.nsplit;
         w.graph_kver = shape.kver;
+        w.graph_prec = blocks ? 1 : 0;
         w.graph_kernels = kernels;
       } else {
         w.graph = nullptr;

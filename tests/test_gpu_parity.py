@@ -295,6 +295,38 @@ def test_mixed_ds_solve(case, w1k, chains):
     assert g.residual_history(0)[-1] < 1e-10
 
 
+@pytest.mark.parametrize("precond", ["diagonal", "block"])
+@pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba"])
+def test_mixed_solve_with_each_inner_preconditioner(case, precond, w1k, chains, golden, golden_mmp):
+    """The inner preconditioner changes only the FP32 inner iterations: both
+    reach the converged reference within the mixed-precision tolerance."""
+    if case in ("w1k", "chains"):
+        p, ef = {"w1k": w1k, "chains": chains}[case]
+    else:
+        p, ef = golden_mmp[case], golden[case + "_ef1"]
+    ref = converged_reference(p, ef)
+    g = OMMPSystem(p)
+    g.set_solver_tol(1e-10)
+    g.set_precision("mixed")
+    g.set_inner_preconditioner(precond)
+    g.set_external_field(ef)
+    assert rel(g.ipd, ref.ipd) < 1e-7
+    assert g.residual_history(0)[-1] < 1e-10
+
+
+def test_block_preconditioner_saves_inner_iterations(w1k):
+    p, ef = w1k
+    counts = {}
+    for precond in ("diagonal", "block"):
+        g = OMMPSystem(p)
+        g.set_solver_tol(1e-10)
+        g.set_precision("mixed")
+        g.set_inner_preconditioner(precond)
+        g.set_external_field(ef)
+        counts[precond] = g.counter(1)
+    assert counts["block"] < counts["diagonal"]
+
+
 @pytest.mark.parametrize("kernel", ["pairwise", "tiled"])
 def test_mixed_solve_with_each_fp32_kernel(kernel, chains):
     p, ef = chains

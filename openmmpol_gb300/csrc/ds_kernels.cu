@@ -109,14 +109,23 @@ __device__ __forceinline__ dsf to_ds(double v) {
 // NEAR: the pair may be damped; an FP32 pre-test (1e-5 margin) selects the
 // pairs whose Thole factors are then formed in FP64 (exp) and applied in
 // double-single.  Far pairs (tile boxes beyond the damping range) skip it.
+// Geometry of one ordered pair: d and the (damped) factors r^-3, 3 r^-5.
+// NEAR: the pair may be damped; an FP32 pre-test (1e-5 margin) selects the
+// pairs whose Thole factors are then formed in FP64 (exp) and applied in
+// double-single.  Far pairs (tile boxes beyond the damping range) skip it.
+struct DsGeom {
+  dsf dx, dy, dz, k3, k5x3;
+};
+
 template <bool NEAR, bool AMOEBA>
-__device__ __forceinline__ void ds_pair(const float4 &th, const float4 &tl, const float4 &sh, const float4 &sl,
-                                        const float4 &mh, const float4 &ml, float (&ah)[3], float (&al)[3],
-                                        double wt, double ws, double at, double as, float2 wat, float2 was,
-                                        double thr, float thr2m) {
-  const dsf dx = ds_diff(th.x, tl.x, sh.x, sl.x);
-  const dsf dy = ds_diff(th.y, tl.y, sh.y, sl.y);
-  const dsf dz = ds_diff(th.z, tl.z, sh.z, sl.z);
+__device__ __forceinline__ DsGeom ds_geometry(const float4 &th, const float4 &tl, const float4 &sh,
+                                              const float4 &sl, double wt, double ws, double at, double as,
+                                              float2 wat, float2 was, double thr, float thr2m) {
+  DsGeom g;
+  g.dx = ds_diff(th.x, tl.x, sh.x, sl.x);
+  g.dy = ds_diff(th.y, tl.y, sh.y, sl.y);
+  g.dz = ds_diff(th.z, tl.z, sh.z, sl.z);
+  const dsf dx = g.dx, dy = g.dy, dz = g.dz;
   // r^2
   float px = dx.h * dx.h, py = dy.h * dy.h, pz = dz.h * dz.h;
   float ex = fmaf(dx.h + dx.h, dx.l, fmaf(dx.h, dx.h, -px));
@@ -151,8 +160,15 @@ __device__ __forceinline__ void ds_pair(const float4 &th, const float4 &tl, cons
       k5 = ds_mul(k5, to_ds(f5));
     }
   }
-  const dsf k5x3 = ds_mulf(k5, 3.0f);
-  // mu . d
+  g.k3 = k3;
+  g.k5x3 = ds_mulf(k5, 3.0f);
+  return g;
+}
+
+// acc += 3 r^-5 (mu.d) d - r^-3 mu for one column (mu as hi / lo floats)
+__device__ __forceinline__ void ds_column(const DsGeom &g, const float4 &mh, const float4 &ml, float (&ah)[3],
+                                          float (&al)[3]) {
+  const dsf dx = g.dx, dy = g.dy, dz = g.dz;
   float qx = mh.x * dx.h, qy = mh.y * dy.h, qz = mh.z * dz.h;
   float fx = fmaf(ml.x, dx.h, fmaf(mh.x, dx.l, fmaf(mh.x, dx.h, -qx)));
   float fy = fmaf(ml.y, dy.h, fmaf(mh.y, dy.l, fmaf(mh.y, dy.h, -qy)));
@@ -160,8 +176,8 @@ __device__ __forceinline__ void ds_pair(const float4 &th, const float4 &tl, cons
   const dsf u1 = two_sum(qx, qy);
   const dsf u2 = two_sum(u1.h, qz);
   const dsf dot = fast_two_sum(u2.h, ((fx + fy) + fz) + (u1.l + u2.l));
-  const dsf f = ds_mul(k5x3, dot);
-  const dsf nk3{-k3.h, -k3.l};
+  const dsf f = ds_mul(g.k5x3, dot);
+  const dsf nk3{-g.k3.h, -g.k3.l};
   acc_mul(ah[0], al[0], f, dx);
   acc_mul(ah[0], al[0], nk3, dsf{mh.x, ml.x});
   acc_mul(ah[1], al[1], f, dy);
@@ -176,31 +192,35 @@ __device__ __forceinline__ void ds_pair(const float4 &th, const float4 &tl, cons
   }
 }
 
-template <bool AMOEBA>
+// partial[split][g][n][3]: G columns sharing each pair's geometry, TPT
+// targets per thread (target t of thread x is blockIdx.x * TPB * TPT + t *
+// TPB + x)
+template <bool AMOEBA, int G, int TPT>
 __global__ void __launch_bounds__(DS_TPB, 5) k_tmu_ds(int n, const float4 *__restrict__ ph, const float4 *__restrict__ pl,
                                                    const Pos64 *__restrict__ p64, const double *__restrict__ damp,
                                                    const float2 *__restrict__ wa, const float4 *__restrict__ boxes,
                                                    const double *__restrict__ x, double *__restrict__ partial,
                                                    int per_split, double thr, float thr2m, float r2max) {
-  __shared__ float4 s_ph[DS_TILE], s_pl[DS_TILE], s_mh[DS_TILE], s_ml[DS_TILE];
+  __shared__ float4 s_ph[DS_TILE], s_pl[DS_TILE], s_mh[G][DS_TILE], s_ml[G][DS_TILE];
   __shared__ Pos64 s_p64[DS_TILE];
   __shared__ double s_a[DS_TILE];
   __shared__ float2 s_wa[DS_TILE];
-  const int jb = blockIdx.x * (DS_TPB * DS_TPT);
-  float4 th[DS_TPT], tl[DS_TPT];
-  bool valid[DS_TPT];
-  double sum[DS_TPT][3];
+  const int jb = blockIdx.x * (DS_TPB * TPT);
+  float4 th[TPT], tl[TPT];
+  bool valid[TPT];
+  double sum[TPT][G][3];
 #pragma unroll
-  for (int t = 0; t < DS_TPT; ++t) {
+  for (int t = 0; t < TPT; ++t) {
     const int j = jb + t * DS_TPB + threadIdx.x;
     valid[t] = j < n;
     th[t] = valid[t] ? ph[j] : make_float4(0.f, 0.f, 0.f, 0.f);
     tl[t] = valid[t] ? pl[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-    sum[t][0] = sum[t][1] = sum[t][2] = 0.0;
+#pragma unroll
+    for (int c = 0; c < G; ++c) sum[t][c][0] = sum[t][c][1] = sum[t][c][2] = 0.0;
   }
   const int ntile = (n + DS_TILE - 1) / DS_TILE;
   const int tb0 = jb / DS_TILE;
-  const int tb1 = min(ntile - 1, (jb + DS_TPB * DS_TPT - 1) / DS_TILE);
+  const int tb1 = min(ntile - 1, (jb + DS_TPB * TPT - 1) / DS_TILE);
   float4 blo = boxes[2 * tb0], bhi = boxes[2 * tb0 + 1];
   for (int tb = tb0 + 1; tb <= tb1; ++tb) {
     float4 lo = boxes[2 * tb], hi = boxes[2 * tb + 1];
@@ -221,16 +241,18 @@ __global__ void __launch_bounds__(DS_TPB, 5) k_tmu_ds(int n, const float4 *__res
         s_p64[k] = p64[i];
         s_a[k] = AMOEBA ? damp[i] : 0.0;
         s_wa[k] = wa[i];
-        double m[3];
-        float mh[3], ml[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          m[c] = x[(size_t)i * 3 + c];
-          mh[c] = (float)m[c];
-          ml[c] = (float)(m[c] - (double)mh[c]);
+        for (int col = 0; col < G; ++col) {
+          float mh[3], ml[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const double m = x[((size_t)col * n + i) * 3 + c];
+            mh[c] = (float)m;
+            ml[c] = (float)(m - (double)mh[c]);
+          }
+          s_mh[col][k] = make_float4(mh[0], mh[1], mh[2], 0.f);
+          s_ml[col][k] = make_float4(ml[0], ml[1], ml[2], 0.f);
         }
-        s_mh[k] = make_float4(mh[0], mh[1], mh[2], 0.f);
-        s_ml[k] = make_float4(ml[0], ml[1], ml[2], 0.f);
       }
     }
     __syncthreads();
@@ -240,26 +262,31 @@ __global__ void __launch_bounds__(DS_TPB, 5) k_tmu_ds(int n, const float4 *__res
     const float gy = fmaxf(0.f, fmaxf(slo.y - bhi.y, blo.y - shi.y));
     const float gz = fmaxf(0.f, fmaxf(slo.z - bhi.z, blo.z - shi.z));
     const bool far_tile = gx * gx + gy * gy + gz * gz > r2max;
-    float ah[DS_TPT][3], al[DS_TPT][3];
+    float ah[TPT][G][3], al[TPT][G][3];
 #pragma unroll
-    for (int t = 0; t < DS_TPT; ++t)
+    for (int t = 0; t < TPT; ++t)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) ah[t][c] = al[t][c] = 0.f;
+      for (int col = 0; col < G; ++col)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ah[t][col][c] = al[t][col][c] = 0.f;
     if (far_tile) {
 #pragma unroll 1
       for (int k = 0; k < cnt; ++k) {
-        const float4 sh = s_ph[k], sl = s_pl[k], mh = s_mh[k], ml = s_ml[k];
+        const float4 sh = s_ph[k], sl = s_pl[k];
 #pragma unroll
-        for (int t = 0; t < DS_TPT; ++t)
-          ds_pair<false, AMOEBA>(th[t], tl[t], sh, sl, mh, ml, ah[t], al[t], 0.0, 0.0, 0.0, 0.0, make_float2(0.f, 0.f),
-                                 make_float2(0.f, 0.f), thr, thr2m);
+        for (int t = 0; t < TPT; ++t) {
+          const DsGeom g = ds_geometry<false, AMOEBA>(th[t], tl[t], sh, sl, 0.0, 0.0, 0.0, 0.0,
+                                                      make_float2(0.f, 0.f), make_float2(0.f, 0.f), thr, thr2m);
+#pragma unroll
+          for (int col = 0; col < G; ++col) ds_column(g, s_mh[col][k], s_ml[col][k], ah[t][col], al[t][col]);
+        }
       }
     } else {
       // tiles within the damping range: per-pair pre-test, FP64 Thole factors
-      double wt[DS_TPT], at[DS_TPT];
-      float2 wat[DS_TPT];
+      double wt[TPT], at[TPT];
+      float2 wat[TPT];
 #pragma unroll
-      for (int t = 0; t < DS_TPT; ++t) {
+      for (int t = 0; t < TPT; ++t) {
         const int j = valid[t] ? jb + t * DS_TPB + threadIdx.x : 0;
         wt[t] = p64[j].w;
         at[t] = AMOEBA ? damp[j] : 0.0;
@@ -267,28 +294,34 @@ __global__ void __launch_bounds__(DS_TPB, 5) k_tmu_ds(int n, const float4 *__res
       }
 #pragma unroll 1
       for (int k = 0; k < cnt; ++k) {
-        const float4 sh = s_ph[k], sl = s_pl[k], mh = s_mh[k], ml = s_ml[k];
+        const float4 sh = s_ph[k], sl = s_pl[k];
         const double ws = s_p64[k].w, as = s_a[k];
         const float2 was = s_wa[k];
 #pragma unroll
-        for (int t = 0; t < DS_TPT; ++t) {
+        for (int t = 0; t < TPT; ++t) {
           if (!valid[t] || t0 + k == jb + t * DS_TPB + (int)threadIdx.x) continue;
-          ds_pair<true, AMOEBA>(th[t], tl[t], sh, sl, mh, ml, ah[t], al[t], wt[t], ws, at[t], as, wat[t], was, thr,
-                                thr2m);
+          const DsGeom g =
+              ds_geometry<true, AMOEBA>(th[t], tl[t], sh, sl, wt[t], ws, at[t], as, wat[t], was, thr, thr2m);
+#pragma unroll
+          for (int col = 0; col < G; ++col) ds_column(g, s_mh[col][k], s_ml[col][k], ah[t][col], al[t][col]);
         }
       }
     }
 #pragma unroll
-    for (int t = 0; t < DS_TPT; ++t)
+    for (int t = 0; t < TPT; ++t)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) sum[t][c] += (double)ah[t][c] + (double)al[t][c];
+      for (int col = 0; col < G; ++col)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sum[t][col][c] += (double)ah[t][col][c] + (double)al[t][col][c];
   }
 #pragma unroll
-  for (int t = 0; t < DS_TPT; ++t) {
+  for (int t = 0; t < TPT; ++t) {
     const int j = jb + t * DS_TPB + threadIdx.x;
     if (!valid[t]) continue;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) partial[((size_t)blockIdx.y * n + j) * 3 + c] = sum[t][c];
+    for (int col = 0; col < G; ++col)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) partial[(((size_t)blockIdx.y * G + col) * n + j) * 3 + c] = sum[t][col][c];
   }
 }
 
@@ -531,17 +564,33 @@ int tmu_ds_pick_split(const DevSites &s, int sms) {
   return split < 1 ? 1 : split;
 }
 
-void launch_tmu_ds_pairs(const DevSites &s, const double *x, double *partial, int nsplit, cudaStream_t st) {
+namespace {
+template <bool AMOEBA, int G, int TPT>
+void launch_ds_shape(const DevSites &s, const double *x, double *partial, int nsplit, cudaStream_t st) {
   const int tiles = (s.n + DS_TILE - 1) / DS_TILE;
   const int per = ((tiles + nsplit - 1) / nsplit) * DS_TILE;
-  dim3 grid((s.n + DS_TPB * DS_TPT - 1) / (DS_TPB * DS_TPT), nsplit);
+  dim3 grid((s.n + DS_TPB * TPT - 1) / (DS_TPB * TPT), nsplit);
   const float thr2m = (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));
-  if (s.amoeba)
-    k_tmu_ds<true><<<grid, DS_TPB, 0, st>>>(s.n, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32,
-                                            s.tile_box32, x, partial, per, s.damp_thr, thr2m, s.damp_r2max32);
-  else
-    k_tmu_ds<false><<<grid, DS_TPB, 0, st>>>(s.n, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32,
-                                             s.tile_box32, x, partial, per, s.damp_thr, thr2m, s.damp_r2max32);
+  k_tmu_ds<AMOEBA, G, TPT><<<grid, DS_TPB, 0, st>>>(s.n, s.pol_pos32, s.pol_pos32lo, s.pol_pos, s.pol_a,
+                                                    s.pol_wa32, s.tile_box32, x, partial, per, s.damp_thr, thr2m,
+                                                    s.damp_r2max32);
+}
+}  // namespace
+
+// g = 1: two targets per thread; g = 2: one target per thread, two columns
+// sharing the pair geometry (the same split keeps the grid size)
+void launch_tmu_ds_pairs(const DevSites &s, int g, const double *x, double *partial, int nsplit, cudaStream_t st) {
+  if (g == 2) {
+    if (s.amoeba)
+      launch_ds_shape<true, 2, 1>(s, x, partial, nsplit, st);
+    else
+      launch_ds_shape<false, 2, 1>(s, x, partial, nsplit, st);
+  } else {
+    if (s.amoeba)
+      launch_ds_shape<true, 1, DS_TPT>(s, x, partial, nsplit, st);
+    else
+      launch_ds_shape<false, 1, DS_TPT>(s, x, partial, nsplit, st);
+  }
 }
 
 }  // namespace gpu

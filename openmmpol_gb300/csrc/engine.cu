@@ -119,7 +119,7 @@ size_t System::device_bytes_estimate() const {
                  8 * (gpu::kRedBlocks * 32 + 64 + 2 * (size_t)maxhist_);
   // double-single copies of the positions, static-site tile boxes, and the
   // double-single kernels' split partials (allocated in that mode only)
-  const size_t ds_split = std::max(gpu::tmu_ds_pick_split(d, sms), gpu::m2d_ds_pick_split(d, sms));
+  const size_t ds_split = std::max(2 * gpu::tmu_ds_pick_split(d, sms), gpu::m2d_ds_pick_split(d, sms));
   bytes += 16 * (n + 2 * m + 2 * ((m + 127) / 128)) + 8 * ds_split * nv;
   return bytes + (size_t(4) << 20);  // events, flags, rounding
 }
@@ -492,7 +492,7 @@ int System::ensure_ds_scratch() {
   if (ds_scratch_) return kOk;
   nsplit_ds_ = gpu::tmu_ds_pick_split(d_, gpu::sm_count());
   nsplit_m2d_ds_ = gpu::m2d_ds_pick_split(d_, gpu::sm_count());
-  if (dalloc(ds_scratch_, (size_t)std::max(nsplit_ds_, nsplit_m2d_ds_) * 3 * d_.n)) {
+  if (dalloc(ds_scratch_, (size_t)std::max(2 * nsplit_ds_, nsplit_m2d_ds_) * 3 * d_.n)) {
     ds_scratch_ = nullptr;
     set_last_error("out of device memory for the double-single kernels");
     return kErrMemory;

@@ -1075,10 +1075,12 @@ void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool
                    int nsplit, cudaStream_t st) {
   if (s.n == 0) return;
   const size_t nv = 3 * (size_t)s.n;
-  for (int c = 0; c < nrhs; ++c) {
+  for (int c = 0; c < nrhs;) {
+    const int g = nrhs - c >= 2 ? 2 : 1;
     g_launches.fetch_add(1, std::memory_order_relaxed);
-    launch_tmu_ds_pairs(s, x + c * nv, scratch, nsplit, st);
-    tmu_finish<double>(s, 1, nsplit, scratch, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 1, st);
+    launch_tmu_ds_pairs(s, g, x + c * nv, scratch, nsplit, st);
+    tmu_finish<double>(s, g, nsplit, scratch, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 2, st);
+    c += g;
   }
 }
 

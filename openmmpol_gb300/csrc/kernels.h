@@ -93,10 +93,11 @@ int tmu32_max_split(const DevSites &s, int sm_count);
 int tmu32_pick_split(const DevSites &s, int sm_count);
 void tile_boxes32(const float4 *pos32, int n, float4 *boxes /*[2*ceil(n/128)]*/);
 float damp_r2max32(bool amoeba, double damp_thr, const double *inv_thole, const double *a, int n);
-// Double-single product (ds_kernels.cu): y = T x for one column at a time with
-// ~1e-13 relative accuracy on the FP32 pipes; scratch of nsplit * n * 3.
+// Double-single product (ds_kernels.cu): y = T x, columns in groups of two
+// sharing the pair geometry, ~1e-13 relative accuracy on the FP32 pipes;
+// scratch of nsplit * 2 * n * 3.
 int tmu_ds_pick_split(const DevSites &s, int sm_count);
-void launch_tmu_ds_pairs(const DevSites &s, const double *x, double *partial, int nsplit, cudaStream_t st);
+void launch_tmu_ds_pairs(const DevSites &s, int g, const double *x, double *partial, int nsplit, cudaStream_t st);
 void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
                    int nsplit, cudaStream_t st);
 // E_M2D with the all-pairs part in double-single (scratch nsplit * n * 3)

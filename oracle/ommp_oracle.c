@@ -923,6 +923,8 @@ static int damped_kernel(const orc_sys *s, int i, int j, int maxder, double *res
         if (maxder >= 1) res[1] *= 1.0 - eexp;
         if (maxder >= 2) res[2] *= 1.0 - (1.0 - fexp) * eexp;
         if (maxder >= 3) res[3] *= 1.0 - (1.0 - fexp + 0.6 * fexp * fexp) * eexp;
+        if (maxder >= 4)
+            res[4] *= 1.0 - (1.0 - fexp + 18.0 / 35.0 * fexp * fexp - 9.0 / 35.0 * fexp * fexp * fexp) * eexp;
     } else if (!s->amoeba && res[0] > 1.0 / sij) {
         double u4 = u3 * u;
         if (maxder >= 1) res[1] *= 4.0 * u3 - 3.0 * u4;
@@ -1644,4 +1646,412 @@ int orc_potential_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, 
 
 int orc_field_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, double *e) {
     return ext_props(s, which, n, cext, e, 1);
+}
+
+/* ------------------------------------------------------------------ */
+/* geometric gradients of the polarization energy                       */
+/* polelec_geomgrad, src/mod_geomgrad.F90:113-277; prepare_polelec with  */
+/* gradients, src/mod_electrostatics.F90:1487-1596; elec_prop_M2D /     */
+/* D2D / D2M with field gradients and Hessians :2113-3065; the          */
+/* q/mu/quad_elec_prop derivative formulas :1097-1405; rotation_geomgrad */
+/* and rotation_matrix(doder), src/rotate_multipoles.F90:3-230,298-643.  */
+/* Component orders: gradient xx,xy,yy,xz,yz,zz; Hessian xxx,xxy,xxz,    */
+/* xyy,xyz,xzz,yyy,yyz,yzz,zzz (include/f_cart_components.h).           */
+/* ------------------------------------------------------------------ */
+static const int G6[3][3] = {{0, 1, 3}, {1, 2, 4}, {3, 4, 5}};
+static const int H10[3][3][3] = {{{0, 1, 2}, {1, 3, 4}, {2, 4, 5}},
+                                 {{1, 3, 4}, {3, 6, 7}, {4, 7, 8}},
+                                 {{2, 4, 5}, {4, 7, 8}, {5, 8, 9}}};
+static const int G6A[6] = {0, 0, 1, 0, 1, 2}, G6B[6] = {0, 1, 1, 2, 2, 2};
+static const int H10A[10] = {0, 0, 0, 0, 0, 0, 1, 1, 1, 2}, H10B[10] = {0, 0, 0, 1, 1, 2, 1, 1, 2, 2},
+                 H10C[10] = {0, 1, 2, 1, 2, 2, 1, 2, 2, 2};
+static inline double kd(int a, int b) { return a == b ? 1.0 : 0.0; }
+
+/* field gradient of a charge q (kernel k: 1/r, r^-3, r^-5, ...) */
+static void q_grad(double q, const double *d, const double *k, double *g) {
+    for (int c = 0; c < 6; c++) {
+        int a = G6A[c], b = G6B[c];
+        g[c] += q * (3.0 * k[2] * d[a] * d[b] - k[1] * kd(a, b));
+    }
+}
+/* field gradient and Hessian of a point dipole */
+static void mu_grad(const double *mu, const double *d, const double *k, double *g, double *h) {
+    double md = mu[0] * d[0] + mu[1] * d[1] + mu[2] * d[2];
+    if (g)
+        for (int c = 0; c < 6; c++) {
+            int a = G6A[c], b = G6B[c];
+            g[c] += md * k[3] * 15.0 * d[a] * d[b] - (md * kd(a, b) + mu[a] * d[b] + mu[b] * d[a]) * 3.0 * k[2];
+        }
+    if (h)
+        for (int c = 0; c < 10; c++) {
+            int a = H10A[c], b = H10B[c], e = H10C[c];
+            h[c] += 105.0 * md * k[4] * d[a] * d[b] * d[e] -
+                    15.0 * k[3] * (mu[a] * d[b] * d[e] + mu[b] * d[a] * d[e] + mu[e] * d[a] * d[b] +
+                                   md * (kd(a, b) * d[e] + kd(a, e) * d[b] + kd(b, e) * d[a])) +
+                    3.0 * k[2] * (mu[a] * kd(b, e) + mu[b] * kd(a, e) + mu[e] * kd(a, b));
+        }
+}
+/* field gradient of a point quadrupole stored xx,xy,yy,xz,yz,zz */
+static void quad_grad(const double *q6, const double *d, const double *k, double *g) {
+    double Q[3][3] = {{q6[0], q6[1], q6[3]}, {q6[1], q6[2], q6[4]}, {q6[3], q6[4], q6[5]}};
+    double t[3];
+    for (int a = 0; a < 3; a++) t[a] = Q[a][0] * d[0] + Q[a][1] * d[1] + Q[a][2] * d[2];
+    double sdr = t[0] * d[0] + t[1] * d[1] + t[2] * d[2];
+    for (int c = 0; c < 6; c++) {
+        int a = G6A[c], b = G6B[c];
+        g[c] += 105.0 * k[4] * sdr * d[a] * d[b] + 6.0 * k[2] * Q[a][b] -
+                15.0 * k[3] * (sdr * kd(a, b) + 2.0 * (t[a] * d[b] + t[b] * d[a]));
+    }
+}
+/* field of a point dipole */
+static void mu_field(const double *mu, const double *d, const double *k, double *e) {
+    double md = mu[0] * d[0] + mu[1] * d[1] + mu[2] * d[2];
+    for (int c = 0; c < 3; c++) e[c] += 3.0 * md * d[c] * k[2] - mu[c] * k[1];
+}
+
+/* rotation_matrix with derivatives: dr*[a][b][c] = d R[b][c] / d (coordinate a
+   of the atom); R columns are ex, ey, ez */
+static void m3mul(double a[3][3], double b[3][3], double o[3][3]) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            o[i][j] = 0.0;
+            for (int k = 0; k < 3; k++) o[i][j] += a[i][k] * b[k][j];
+        }
+}
+static int rotation_derivatives(const double *c, const double *cx, const double *cy, const double *cz, int frame,
+                                double r[3][3], double dri[3][3][3], double driz[3][3][3], double drix[3][3][3],
+                                double driy[3][3][3]) {
+    memset(dri, 0, 27 * sizeof(double));
+    memset(driz, 0, 27 * sizeof(double));
+    memset(drix, 0, 27 * sizeof(double));
+    memset(driy, 0, 27 * sizeof(double));
+    int st = rotation_matrix(c, cx, cy, cz, frame, r);
+    if (st || frame == 0) return st;
+    double xi[3], eta[3], zeta[3], u[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+    for (int k = 0; k < 3; k++) {
+        xi[k] = cz[k] - c[k];
+        eta[k] = cx[k] - c[k];
+        zeta[k] = cy[k] - c[k];
+    }
+    double xin = sqrt(xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2]);
+    double etan = sqrt(eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
+    double zetan = sqrt(zeta[0] * zeta[0] + zeta[1] * zeta[1] + zeta[2] * zeta[2]);
+    if (frame == 1) {
+        for (int k = 0; k < 3; k++) u[k] = xi[k], v[k] = eta[k];
+    } else if (frame == 2) {
+        for (int k = 0; k < 3; k++) u[k] = etan * xi[k] + xin * eta[k], v[k] = eta[k];
+    } else if (frame == 3) {
+        for (int k = 0; k < 3; k++) u[k] = xi[k];
+        if (u[2] / xin <= 0.866 && fabs(u[1]) > EPS_RP)
+            v[0] = 1.0;
+        else
+            v[1] = 1.0;
+    } else if (frame == 4) {
+        for (int k = 0; k < 3; k++) u[k] = xi[k], v[k] = zetan * eta[k] + etan * zeta[k];
+    } else if (frame == 5) {
+        for (int k = 0; k < 3; k++)
+            u[k] = etan * zetan * xi[k] + xin * zetan * eta[k] + xin * etan * zeta[k], v[k] = eta[k];
+    }
+    double ex[3], ey[3], ez[3];
+    for (int k = 0; k < 3; k++) ex[k] = r[k][0], ey[k] = r[k][1], ez[k] = r[k][2];
+    (void)ey;
+    double usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2], un = sqrt(usq), ucube = usq * un;
+    double vez = v[0] * ez[0] + v[1] * ez[1] + v[2] * ez[2];
+    double exr[3];
+    for (int k = 0; k < 3; k++) exr[k] = v[k] - vez * ez[k];
+    double exsq = exr[0] * exr[0] + exr[1] * exr[1] + exr[2] * exr[2], exn = sqrt(exsq);
+    double ez_u[3][3] = {{0}}, ex_v[3][3] = {{0}}, ex_ez[3][3] = {{0}}, ey_ez[3][3], ey_ex[3][3];
+    double u_ri[3][3] = {{0}}, u_riz[3][3] = {{0}}, u_rix[3][3] = {{0}}, u_riy[3][3] = {{0}};
+    double v_ri[3][3] = {{0}}, v_rix[3][3] = {{0}}, v_riy[3][3] = {{0}};
+    for (int k = 0; k < 3; k++) {
+        ez_u[k][k] = 1.0 / un;
+        ex_v[k][k] = 1.0 / exn;
+        ex_ez[k][k] = -vez / exn;
+    }
+    for (int k = 0; k < 3; k++)
+        for (int a = 0; a < 3; a++) {
+            ez_u[a][k] -= u[a] * u[k] / ucube;
+            ex_v[a][k] -= ez[a] * ez[k] / exn + ex[a] * ex[k] / exn;
+            ex_ez[a][k] += ex[a] * vez * v[k] / exsq - ez[a] * v[k] / exn;
+        }
+    double ey_ez_[3][3] = {{0, ex[2], -ex[1]}, {-ex[2], 0, ex[0]}, {ex[1], -ex[0], 0}};
+    double ey_ex_[3][3] = {{0, -ez[2], ez[1]}, {ez[2], 0, -ez[0]}, {-ez[1], ez[0], 0}};
+    memcpy(ey_ez, ey_ez_, sizeof(ey_ez));
+    memcpy(ey_ex, ey_ex_, sizeof(ey_ex));
+    if (frame == 1) {
+        for (int k = 0; k < 3; k++) u_ri[k][k] = -1.0, u_riz[k][k] = 1.0, v_ri[k][k] = -1.0, v_rix[k][k] = 1.0;
+    } else if (frame == 2) {
+        for (int k = 0; k < 3; k++)
+            u_ri[k][k] = -xin - etan, u_riz[k][k] = etan, u_rix[k][k] = xin, v_ri[k][k] = -1.0, v_rix[k][k] = 1.0;
+        for (int k = 0; k < 3; k++)
+            for (int a = 0; a < 3; a++) {
+                u_ri[a][k] += -eta[a] * xi[k] / xin - xi[a] * eta[k] / etan;
+                u_riz[a][k] += eta[a] * xi[k] / xin;
+                u_rix[a][k] += xi[a] * eta[k] / etan;
+            }
+    } else if (frame == 3) {
+        for (int k = 0; k < 3; k++) u_ri[k][k] = -1.0, u_riz[k][k] = 1.0;
+    } else if (frame == 4) {
+        for (int k = 0; k < 3; k++)
+            u_ri[k][k] = -1.0, u_riz[k][k] = 1.0, v_ri[k][k] = -etan - zetan, v_rix[k][k] = zetan,
+            u_riy[k][k] = etan;
+        for (int k = 0; k < 3; k++)
+            for (int a = 0; a < 3; a++) {
+                v_ri[a][k] += -eta[a] * zeta[k] / zetan - zeta[a] * eta[k] / etan;
+                v_rix[a][k] += zeta[a] * eta[k] / etan;
+                v_riy[a][k] += eta[a] * zeta[k] / zetan;
+            }
+    } else if (frame == 5) {
+        for (int k = 0; k < 3; k++)
+            u_ri[k][k] = -xin * etan - xin * zetan - etan * zetan, u_riz[k][k] = etan * zetan,
+            u_rix[k][k] = xin * zetan, u_riy[k][k] = xin * etan, v_ri[k][k] = -1.0, v_rix[k][k] = 1.0;
+        for (int k = 0; k < 3; k++)
+            for (int a = 0; a < 3; a++) {
+                double A = eta[a] * zetan + zeta[a] * etan, B = xi[a] * zetan + zeta[a] * xin,
+                       Cc = xi[a] * etan + eta[a] * xin;
+                u_ri[a][k] += -A * xi[k] / xin - B * eta[k] / etan - Cc * zeta[k] / zetan;
+                u_riz[a][k] += A * xi[k] / xin;
+                u_rix[a][k] += B * eta[k] / etan;
+                u_riy[a][k] += Cc * zeta[k] / zetan;
+            }
+    }
+    double ez_ri[3][3], ez_riz[3][3], ez_rix[3][3], ez_riy[3][3];
+    m3mul(ez_u, u_ri, ez_ri);
+    m3mul(ez_u, u_riz, ez_riz);
+    m3mul(ez_u, u_rix, ez_rix);
+    m3mul(ez_u, u_riy, ez_riy);
+    double t1[3][3], t2[3][3], ex_ri[3][3], ex_riz[3][3], ex_rix[3][3], ex_riy[3][3];
+    m3mul(ex_v, v_ri, t1);
+    m3mul(ex_ez, ez_ri, t2);
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) ex_ri[a][b] = t1[a][b] + t2[a][b];
+    m3mul(ex_ez, ez_riz, ex_riz);
+    m3mul(ex_v, v_rix, t1);
+    m3mul(ex_ez, ez_rix, t2);
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) ex_rix[a][b] = t1[a][b] + t2[a][b];
+    m3mul(ex_v, v_riy, t1);
+    m3mul(ex_ez, ez_riy, t2);
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) ex_riy[a][b] = t1[a][b] + t2[a][b];
+    double ey_ri[3][3], ey_riz[3][3], ey_rix[3][3], ey_riy[3][3];
+    double (*exs[4])[3] = {ex_ri, ex_riz, ex_rix, ex_riy};
+    double (*ezs[4])[3] = {ez_ri, ez_riz, ez_rix, ez_riy};
+    double (*eys[4])[3] = {ey_ri, ey_riz, ey_rix, ey_riy};
+    for (int w = 0; w < 4; w++) {
+        m3mul(ey_ex, exs[w], t1);
+        m3mul(ey_ez, ezs[w], t2);
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) eys[w][a][b] = t1[a][b] + t2[a][b];
+    }
+    /* d[a][b][col] = d e_col(b) / d r_a  (the transposes of the reference) */
+    double (*outs[4])[3][3] = {dri, driz, drix, driy};
+    for (int w = 0; w < 4; w++)
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                outs[w][a][b][0] = exs[w][b][a];
+                outs[w][a][b][1] = eys[w][b][a];
+                outs[w][a][b][2] = ezs[w][b][a];
+            }
+    return 0;
+}
+
+/* rotation_geomgrad: forces from the frame dependence of the rotated dipoles
+   and quadrupoles in the field E / field gradient G at each static site */
+static int rotation_geomgrad(orc_sys *s, const double *E, const double *G, double *grad) {
+    for (int j = 0; j < s->mm; j++) {
+        int jz = s->iz[j] >= 0 ? s->iz[j] : j;
+        int jx = s->ix[j] >= 0 ? s->ix[j] : j;
+        int jy = s->iy[j] >= 0 ? s->iy[j] : j;
+        double r[3][3], d[4][3][3][3];
+        int st = rotation_derivatives(&s->cmm[3 * j], &s->cmm[3 * jx], &s->cmm[3 * jy], &s->cmm[3 * jz],
+                                      s->frame[j], r, d[0], d[1], d[2], d[3]);
+        if (st) return st;
+        const double *q0 = &s->q0[10 * j], *q = &s->q[10 * j];
+        double dip[3] = {q0[1], q0[2], q0[3]};
+        double qua[3][3] = {{q0[4], q0[5], q0[7]}, {q0[5], q0[6], q0[8]}, {q0[7], q0[8], q0[9]}};
+        double rqua[3][3] = {{q[4], q[5], q[7]}, {q[5], q[6], q[8]}, {q[7], q[8], q[9]}};
+        const int atoms[4] = {j, jz, jx, jy};
+        const double *Ej = &E[3 * j], *Gj = &G[6 * j];
+        for (int w = 0; w < 4; w++) {
+            double ddip[3][3] = {{0}}, dqua[3][3][3] = {{{0}}};
+            for (int a = 0; a < 3; a++)
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) ddip[a][k] += d[w][a][k][l] * dip[l];
+            for (int a = 0; a < 3; a++)
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++)
+                        for (int m = 0; m < 3; m++)
+                            for (int n = 0; n < 3; n++)
+                                dqua[a][k][l] += (d[w][a][k][m] * qua[m][n] - rqua[k][m] * d[w][a][m][n]) * r[l][n];
+            double *g = &grad[3 * atoms[w]];
+            for (int a = 0; a < 3; a++) {
+                g[a] -= ddip[a][0] * Ej[0] + ddip[a][1] * Ej[1] + ddip[a][2] * Ej[2];
+                g[a] += dqua[a][0][0] * Gj[0] + dqua[a][1][1] * Gj[2] + dqua[a][2][2] * Gj[5] +
+                        2.0 * (dqua[a][0][1] * Gj[1] + dqua[a][0][2] * Gj[3] + dqua[a][1][2] * Gj[4]);
+            }
+        }
+    }
+    return 0;
+}
+
+/* the scale of the (static site i, polarizable site j) pair in one list */
+static inline void pair_scale(const slist_t *l, int i, int j, int *todo, double *sc) {
+    int k = list_find(l, i, j);
+    *todo = 1;
+    *sc = 1.0;
+    if (k >= 0) {
+        *todo = l->todo[k];
+        *sc = l->scale[k];
+    }
+}
+
+int orc_polelec_geomgrad(orc_sys *s, double *grad) {
+    const int np = s->npol, mm = s->mm, amoeba = s->amoeba, nset = s->n_ipd;
+    if (np == 0) return 0;
+    int st = 0;
+    if (!s->ipd_done) {
+        st = prepare_polelec(s);
+        if (!st) st = polarization(s, s->e_m2d, SOLVER_NONE, MATV_NONE, NULL);
+        if (st) return st;
+    }
+    double *gm2d = xcalloc(6 * (size_t)np * nset, sizeof(double));
+    double *gd2d = xcalloc(6 * (size_t)np * nset, sizeof(double));
+    double *ed2m = xcalloc(3 * (size_t)mm, sizeof(double));
+    double *gd2m = xcalloc(6 * (size_t)mm, sizeof(double));
+    double *hd2m = xcalloc(10 * (size_t)mm, sizeof(double));
+    int bad = 0;
+    /* Egrd_M2D: set 0 (D, S_P_D scales) and set 1 (P, S_P_P scales) for AMOEBA */
+#pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
+    for (int j = 0; j < np; j++) {
+        int jm = s->polar_mm[j];
+        for (int i = 0; i < mm; i++) {
+            if (i == jm) continue;
+            int tp, td = 0;
+            double sp, sd = 1.0;
+            pair_scale(&s->sPP, i, j, &tp, &sp);
+            if (amoeba) pair_scale(&s->sPD, i, j, &td, &sd);
+            if (!tp && !td) continue;
+            double k[5], dr[3], g[6] = {0, 0, 0, 0, 0, 0};
+            if (damped_kernel(s, i, jm, amoeba ? 4 : 2, k, dr)) {
+                bad = 1;
+                continue;
+            }
+            const double *q = &s->q[(size_t)s->ld_cart * i];
+            q_grad(q[0], dr, k, g);
+            if (amoeba) {
+                mu_grad(&q[1], dr, k, g, NULL);
+                quad_grad(&q[4], dr, k, g);
+            }
+            if (amoeba) {
+                for (int c = 0; c < 6; c++) {
+                    if (tp) gm2d[6 * ((size_t)np + j) + c] += g[c] * sp;
+                    if (td) gm2d[6 * (size_t)j + c] += g[c] * sd;
+                }
+            } else if (tp) {
+                for (int c = 0; c < 6; c++) gm2d[6 * (size_t)j + c] += g[c] * sp;
+            }
+        }
+    }
+    /* Egrd_D2D per set, list_P_P scales */
+#pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
+    for (int j = 0; j < np; j++) {
+        for (int i = 0; i < np; i++) {
+            if (i == j) continue;
+            int todo = 1;
+            double sc = 1.0;
+            int kk = list_find(&s->PP, i, j);
+            if (kk >= 0) {
+                todo = s->PP.todo[kk];
+                sc = s->PP.scale[kk];
+            }
+            if (!todo) continue;
+            double k[4], dr[3];
+            if (damped_kernel(s, s->polar_mm[i], s->polar_mm[j], 3, k, dr)) {
+                bad = 1;
+                continue;
+            }
+            for (int set = 0; set < nset; set++) {
+                double g[6] = {0, 0, 0, 0, 0, 0};
+                mu_grad(&s->ipd[3 * ((size_t)set * np + i)], dr, k, g, NULL);
+                for (int c = 0; c < 6; c++) gd2d[6 * ((size_t)set * np + j) + c] += g[c] * sc;
+            }
+        }
+    }
+    /* E / Egrd / EHes of the induced dipoles at the static sites: AMOEBA
+       averages the P dipoles with S_P_D scales and the D dipoles with S_P_P
+       scales; Wang-AL uses its one set with S_P_P */
+#pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
+    for (int j = 0; j < mm; j++) {
+        for (int i = 0; i < np; i++) {
+            if (s->polar_mm[i] == j) continue;
+            double k[5], dr[3];
+            int have = 0;
+            for (int kind = 0; kind < (amoeba ? 2 : 1); kind++) {
+                /* kind 0: D dipoles (S_P_P); kind 1: P dipoles (S_P_D) */
+                int todo;
+                double sc;
+                pair_scale(kind == 0 ? &s->sPP : &s->sPD, j, i, &todo, &sc);
+                if (!todo) continue;
+                if (!have) {
+                    if (damped_kernel(s, s->polar_mm[i], j, amoeba ? 4 : 2, k, dr)) {
+                        bad = 1;
+                        break;
+                    }
+                    have = 1;
+                }
+                const double *mu = &s->ipd[3 * ((size_t)(kind == 0 ? 0 : 1) * np + i)];
+                double e[3] = {0, 0, 0}, g[6] = {0, 0, 0, 0, 0, 0}, h[10] = {0};
+                mu_field(mu, dr, k, e);
+                if (amoeba) mu_grad(mu, dr, k, g, h);
+                const double w = (amoeba ? 0.5 : 1.0) * sc;
+                for (int c = 0; c < 3; c++) ed2m[3 * (size_t)j + c] += e[c] * w;
+                if (amoeba) {
+                    for (int c = 0; c < 6; c++) gd2m[6 * (size_t)j + c] += g[c] * w;
+                    for (int c = 0; c < 10; c++) hd2m[10 * (size_t)j + c] += h[c] * w;
+                }
+            }
+        }
+    }
+    if (bad) {
+        set_err("Requesting Coulomb kernel for two atoms placed in the same point");
+        free(gm2d), free(gd2d), free(ed2m), free(gd2m), free(hd2m);
+        return ORC_ERR_NUMERIC;
+    }
+    /* assembly (mod_geomgrad.F90:132-271) */
+    for (int i = 0; i < mm; i++) {
+        const double *q = &s->q[(size_t)s->ld_cart * i];
+        for (int a = 0; a < 3; a++) grad[3 * i + a] -= q[0] * ed2m[3 * i + a];
+        if (!amoeba) continue;
+        const double *G = &gd2m[6 * (size_t)i], *H = &hd2m[10 * (size_t)i];
+        for (int a = 0; a < 3; a++) {
+            grad[3 * i + a] += q[1] * G[G6[a][0]] + q[2] * G[G6[a][1]] + q[3] * G[G6[a][2]];
+            double Q[3][3] = {{q[4], q[5], q[7]}, {q[5], q[6], q[8]}, {q[7], q[8], q[9]}};
+            double acc = 0.0;
+            for (int b = 0; b < 3; b++)
+                for (int c = 0; c < 3; c++) acc += Q[b][c] * H[H10[b][c][a]];
+            grad[3 * i + a] -= acc;
+        }
+    }
+    for (int j = 0; j < np; j++) {
+        double *g = &grad[3 * (size_t)s->polar_mm[j]];
+        if (amoeba) {
+            const double *mD = &s->ipd[3 * (size_t)j], *mP = &s->ipd[3 * ((size_t)np + j)];
+            const double *GP = &gm2d[6 * ((size_t)np + j)], *GD = &gm2d[6 * (size_t)j];
+            const double *HP = &gd2d[6 * ((size_t)np + j)], *HD = &gd2d[6 * (size_t)j];
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) {
+                    int c = G6[a][b];
+                    g[a] += 0.5 * mD[b] * (GP[c] + HP[c]) + 0.5 * mP[b] * (GD[c] + HD[c]);
+                }
+        } else {
+            const double *m = &s->ipd[3 * (size_t)j];
+            const double *GM = &gm2d[6 * (size_t)j], *HM = &gd2d[6 * (size_t)j];
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) g[a] += m[b] * (GM[G6[a][b]] + HM[G6[a][b]]);
+        }
+    }
+    if (amoeba) st = rotation_geomgrad(s, ed2m, gd2m, grad);
+    free(gm2d), free(gd2d), free(ed2m), free(gd2m), free(hd2m);
+    return st;
 }

@@ -25,6 +25,8 @@
  *   set_external_field      src/mod_interface.F90:184-233
  *   get_polelec_energy      src/mod_interface.F90:343-370, energy_MM_pol
  *                           src/mod_electrostatics.F90:943-976
+ *   polelec_geomgrad        src/mod_geomgrad.F90:113-277, rotation_geomgrad
+ *                           src/rotate_multipoles.F90:3-230, 298-643
  *   potential/field at external points (QM coupling)
  *                           src/mod_electrostatics.F90:3067-3336,
  *                           src/mod_interface.F90:250-330
@@ -106,6 +108,10 @@ void orc_clear_guess(orc_sys *s);
    multipoles + induced dipoles, 1 static multipoles, 2 induced dipoles */
 int orc_potential_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, double *v);
 int orc_field_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, double *e);
+/* polelec_geomgrad: gradient of the polarization energy with respect to the
+   static-site coordinates, ADDED into grad [mm][3] (solves with the
+   permanent field alone first if no dipoles are available) */
+int orc_polelec_geomgrad(orc_sys *s, double *grad);
 
 #ifdef __cplusplus
 }

@@ -61,6 +61,7 @@ def lib():
             "orc_tmatvec_rows": (C.c_int, [vp, dp, ip, C.c_int32, dp]),
             "orc_potential_ext": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp]),
             "orc_field_ext": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp]),
+            "orc_polelec_geomgrad": (C.c_int, [vp, dp]),
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
             "orc_last_iterations": (C.c_int32, [vp, C.c_int32]),
@@ -203,6 +204,13 @@ class OracleSystem:
         v = np.zeros(len(cext)) if v is None else np.array(v, dtype=np.float64)
         self._check(lib().orc_potential_ext(self._h, int(which), len(cext), _dp(cext), _dp(v)))
         return v
+
+    def polelec_geomgrad(self):
+        """Gradient of the polarization energy w.r.t. the static-site
+        coordinates, [mm][3] (a.u.)."""
+        g = np.zeros((self.mm_atoms, 3))
+        self._check(lib().orc_polelec_geomgrad(self._h, _dp(g)))
+        return g
 
     def field_ext(self, which, cext, e=None):
         cext = np.ascontiguousarray(cext, dtype=np.float64).reshape(-1, 3)

@@ -138,6 +138,12 @@ void ommp_potential_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, do
 void ommp_field_mmpol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *E);
 void ommp_field_mm2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *E);
 void ommp_field_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double *E);
+/* include/openmmpol.h:91 ; src/mod_c_interface.F90:833-846, polelec_geomgrad
+ * src/mod_geomgrad.F90:113-277.  Geometric gradient of the polarization
+ * energy, grd [mm_atoms][3] (hartree/bohr), overwritten; the induced dipoles
+ * are solved first (default solver) when the system has none.  FP64 on the
+ * GPU whatever the precision mode. */
+void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
 /* include/openmmpol.h:153-155 ; src/mod_c_interface.F90:1843-1879.  The fast
  * multipole method is not part of this library: enabling it logs a warning
  * and the direct sums are kept; ommp_use_fmm always returns false. */
@@ -158,6 +164,8 @@ int32_t ommp_gpu_set_external_field_status(OMMP_SYSTEM_PRT s, const double *ext_
 int32_t ommp_gpu_set_external_field_device(OMMP_SYSTEM_PRT s, const double *ext_field_dev,
                                            int32_t solver, int32_t matv, int32_t add_mm_field);
 int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *energy);
+/* ommp_polelec_geomgrad returning a status instead of stopping the process */
+int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
 int32_t ommp_gpu_update_coordinates(OMMP_SYSTEM_PRT s, const double *cmm);
 int32_t ommp_gpu_set_default_solver(OMMP_SYSTEM_PRT s, int32_t solver);
 int32_t ommp_gpu_set_default_matv(OMMP_SYSTEM_PRT s, int32_t matv);

@@ -69,6 +69,8 @@ SIGNATURES = {
     "ommp_field_mmpol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
     "ommp_field_mm2ext": (None, [_vp, C.c_int32, _dp, _dp]),
     "ommp_field_pol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
+    "ommp_polelec_geomgrad": (None, [_vp, _dp]),
+    "ommp_gpu_polelec_geomgrad": (C.c_int32, [_vp, _dp]),
     "ommp_gpu_set_use_graphs": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_external_fields_batch": (C.c_int32, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ommp_gpu_set_external_fields_batch_device": (C.c_int32, [_vp, C.c_int32, _vp, _vp, _dp]),

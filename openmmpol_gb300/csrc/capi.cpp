@@ -143,6 +143,13 @@ void ommp_field_mm2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *e)
 void ommp_field_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *c, double *e) {
   fatal_if(S(s)->ext_props(2, true, n, c, e));
 }
+int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) {
+  ommp_time_push();
+  int st = S(s)->polelec_geomgrad(grd);
+  if (st == ommp::kOk) ommp_time_pull("Polarizable Elctrostatic grad");
+  return st;
+}
+void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) { fatal_if(ommp_gpu_polelec_geomgrad(s, grd)); }
 
 void ommp_enable_fmm(OMMP_SYSTEM_PRT s) {
   (void)s;

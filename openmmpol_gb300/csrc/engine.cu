@@ -58,6 +58,7 @@ System::~System() {
     if (b) cudaFree(b);
   if (flush_buf_) cudaFree(flush_buf_);
   if (sym_scratch_) cudaFree(sym_scratch_);
+  free_grad_state(grad_);
   kt_resolve();
   for (auto &e : kfree_) {
     cudaEventDestroy(e.a);
@@ -352,7 +353,7 @@ void System::kt_resolve() {
 
 void System::kernel_stats(int which, long long &launches, double &ms, long long &columns) {
   kt_resolve();
-  const int k = which >= 0 && which < 3 ? which : 0;
+  const int k = which >= 0 && which < 4 ? which : 0;
   launches = klaunch_[k];
   ms = kms_[k];
   columns = kcols_[k];
@@ -360,7 +361,7 @@ void System::kernel_stats(int which, long long &launches, double &ms, long long 
 
 void System::reset_kernel_stats() {
   kt_resolve();
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 4; ++k) {
     klaunch_[k] = 0;
     kcols_[k] = 0;
     kms_[k] = 0.0;

@@ -46,6 +46,10 @@ struct Workspace {
   long long graph_kernels = 0;
 };
 
+// device data of the polarization gradient (grad.cu)
+struct GradState;
+void free_grad_state(GradState *g);
+
 struct SolveStats {
   int iters[2] = {0, 0};
   std::vector<double> hist[2];
@@ -87,6 +91,8 @@ class System {
   // cext [n][3], added into out; which 0 all, 1 static, 2 induced
   int ext_props(int which, bool field, int n, const double *cext_host, double *out_host);
   int e_m2d(double *out_host);
+  // geometric gradient of the polarization energy, out [mm][3] (overwritten)
+  int polelec_geomgrad(double *grad_host);
   void clear_guess() { ipd_use_guess_ = false; }
   void set_tol(double t) { tol_ = t; }
   void set_maxiter(int n) { maxiter_ = n; }
@@ -207,9 +213,10 @@ class System {
   SolveStats stats_;
   float last_ms_ = 0.f;
   bool ktime_on_ = false;
-  long long klaunch_[3] = {0, 0, 0};  // kernel timing: 0 FP64, 1 FP32, 2 double-single T.mu
-  long long kcols_[3] = {0, 0, 0};
-  double kms_[3] = {0, 0, 0};
+  // kernel timing: 0 FP64, 1 FP32, 2 double-single T.mu, 3 gradient pair pass
+  long long klaunch_[4] = {0, 0, 0, 0};
+  long long kcols_[4] = {0, 0, 0, 0};
+  double kms_[4] = {0, 0, 0, 0};
   struct KEv {
     cudaEvent_t a, b;
     int kind;
@@ -219,6 +226,7 @@ class System {
   KEv kt_begin(int kind, int cols);
   void kt_end(KEv &e);
   void kt_resolve();
+  GradState *grad_ = nullptr;
   Workspace ws_;   // view of the default two-column buffers
   Workspace wsb_;  // batch buffers
   std::map<int, F32Shape> f32_tune_;  // columns -> tuned FP32 launch shape

@@ -1858,8 +1858,10 @@ static int rotation_derivatives(const double *c, const double *cx, const double 
 
 /* rotation_geomgrad: forces from the frame dependence of the rotated dipoles
    and quadrupoles in the field E / field gradient G at each static site */
-static int rotation_geomgrad(orc_sys *s, const double *E, const double *G, double *grad) {
+static int rotation_geomgrad(orc_sys *s, const double *E, const double *G, double *grad,
+                             const unsigned char *fmask) {
     for (int j = 0; j < s->mm; j++) {
+        if (fmask && !fmask[j]) continue;
         int jz = s->iz[j] >= 0 ? s->iz[j] : j;
         int jx = s->ix[j] >= 0 ? s->ix[j] : j;
         int jy = s->iy[j] >= 0 ? s->iy[j] : j;
@@ -1906,7 +1908,11 @@ static inline void pair_scale(const slist_t *l, int i, int j, int *todo, double 
     }
 }
 
-int orc_polelec_geomgrad(orc_sys *s, double *grad) {
+/* fmask [mm]: static sites whose field, field gradient and Hessian are
+   needed; pmask [npol]: polarizable sites whose field gradients are needed
+   (NULL: all).  The gradient is exact on every atom whose own site is in
+   both masks (when polarizable) and whose frame dependents are in fmask. */
+static int geomgrad_impl(orc_sys *s, double *grad, const unsigned char *fmask, const unsigned char *pmask) {
     const int np = s->npol, mm = s->mm, amoeba = s->amoeba, nset = s->n_ipd;
     if (np == 0) return 0;
     int st = 0;
@@ -1925,6 +1931,7 @@ int orc_polelec_geomgrad(orc_sys *s, double *grad) {
 #pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
     for (int j = 0; j < np; j++) {
         int jm = s->polar_mm[j];
+        if (pmask && !pmask[j]) continue;
         for (int i = 0; i < mm; i++) {
             if (i == jm) continue;
             int tp, td = 0;
@@ -1956,6 +1963,7 @@ int orc_polelec_geomgrad(orc_sys *s, double *grad) {
     /* Egrd_D2D per set, list_P_P scales */
 #pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
     for (int j = 0; j < np; j++) {
+        if (pmask && !pmask[j]) continue;
         for (int i = 0; i < np; i++) {
             if (i == j) continue;
             int todo = 1;
@@ -1983,6 +1991,7 @@ int orc_polelec_geomgrad(orc_sys *s, double *grad) {
        scales; Wang-AL uses its one set with S_P_P */
 #pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
     for (int j = 0; j < mm; j++) {
+        if (fmask && !fmask[j]) continue;
         for (int i = 0; i < np; i++) {
             if (s->polar_mm[i] == j) continue;
             double k[5], dr[3];
@@ -2051,7 +2060,41 @@ int orc_polelec_geomgrad(orc_sys *s, double *grad) {
                 for (int b = 0; b < 3; b++) g[a] += m[b] * (GM[G6[a][b]] + HM[G6[a][b]]);
         }
     }
-    if (amoeba) st = rotation_geomgrad(s, ed2m, gd2m, grad);
+    if (amoeba) st = rotation_geomgrad(s, ed2m, gd2m, grad, fmask);
     free(gm2d), free(gd2d), free(ed2m), free(gd2m), free(hd2m);
     return st;
+}
+
+int orc_polelec_geomgrad(orc_sys *s, double *grad) { return geomgrad_impl(s, grad, NULL, NULL); }
+
+int orc_polelec_geomgrad_atoms(orc_sys *s, int32_t na, const int32_t *atoms, double *out) {
+    const int mm = s->mm;
+    unsigned char *want = xcalloc(mm, 1), *fmask = xcalloc(mm, 1), *pmask = xcalloc(s->npol > 0 ? s->npol : 1, 1);
+    for (int k = 0; k < na; k++) {
+        if (atoms[k] < 0 || atoms[k] >= mm) {
+            free(want), free(fmask), free(pmask);
+            set_err("atom index out of range");
+            return ORC_ERR_BAD_ARG;
+        }
+        want[atoms[k]] = 1;
+    }
+    for (int j = 0; j < mm; j++) {
+        int jz = s->iz[j] >= 0 ? s->iz[j] : j, jx = s->ix[j] >= 0 ? s->ix[j] : j;
+        int jy = s->iy[j] >= 0 ? s->iy[j] : j;
+        if (want[j] || (s->amoeba && s->frame[j] != 0 && (want[jz] || want[jx] || want[jy]))) fmask[j] = 1;
+        if (want[j] && s->mm_polar[j] >= 0) pmask[s->mm_polar[j]] = 1;
+    }
+    double *g = xcalloc(3 * (size_t)mm, sizeof(double));
+    int st = geomgrad_impl(s, g, fmask, pmask);
+    for (int k = 0; k < na; k++)
+        for (int c = 0; c < 3; c++) out[3 * k + c] = g[3 * (size_t)atoms[k] + c];
+    free(g), free(want), free(fmask), free(pmask);
+    return st;
+}
+
+int orc_set_ipd(orc_sys *s, const double *ipd) {
+    if (s->npol == 0) return 0;
+    memcpy(s->ipd, ipd, sizeof(double) * 3 * (size_t)s->npol * s->n_ipd);
+    s->ipd_done = 1;
+    return 0;
 }

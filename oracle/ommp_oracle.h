@@ -112,6 +112,12 @@ int orc_field_ext(orc_sys *s, int32_t which, int32_t n, const double *cext, doub
    static-site coordinates, ADDED into grad [mm][3] (solves with the
    permanent field alone first if no dipoles are available) */
 int orc_polelec_geomgrad(orc_sys *s, double *grad);
+/* the same gradient on the listed atoms only, out [na][3] (overwritten);
+   fields are evaluated only where those atoms need them */
+int orc_polelec_geomgrad_atoms(orc_sys *s, int32_t na, const int32_t *atoms, double *out);
+/* install induced dipoles ipd [n_ipd][npol][3] as the solved state (so that
+   the gradient can be evaluated on dipoles solved elsewhere) */
+int orc_set_ipd(orc_sys *s, const double *ipd);
 
 #ifdef __cplusplus
 }

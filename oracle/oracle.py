@@ -62,6 +62,8 @@ def lib():
             "orc_potential_ext": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp]),
             "orc_field_ext": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp]),
             "orc_polelec_geomgrad": (C.c_int, [vp, dp]),
+            "orc_polelec_geomgrad_atoms": (C.c_int, [vp, C.c_int32, ip, dp]),
+            "orc_set_ipd": (C.c_int, [vp, dp]),
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
             "orc_last_iterations": (C.c_int32, [vp, C.c_int32]),
@@ -211,6 +213,18 @@ class OracleSystem:
         g = np.zeros((self.mm_atoms, 3))
         self._check(lib().orc_polelec_geomgrad(self._h, _dp(g)))
         return g
+
+    def polelec_geomgrad_atoms(self, atoms):
+        """The gradient on the listed atoms only, [len(atoms)][3]."""
+        atoms = np.ascontiguousarray(atoms, dtype=np.int32)
+        g = np.zeros((len(atoms), 3))
+        self._check(lib().orc_polelec_geomgrad_atoms(self._h, len(atoms), _ip(atoms), _dp(g)))
+        return g
+
+    def set_ipd(self, ipd):
+        """Install dipoles [n_ipd][npol][3] solved elsewhere as the solved state."""
+        ipd = np.ascontiguousarray(ipd, dtype=np.float64).reshape(self.n_ipd, self.pol_atoms, 3)
+        self._check(lib().orc_set_ipd(self._h, _dp(ipd)))
 
     def field_ext(self, which, cext, e=None):
         cext = np.ascontiguousarray(cext, dtype=np.float64).reshape(-1, 3)

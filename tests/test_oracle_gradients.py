@@ -75,3 +75,18 @@ def test_gradient_is_translation_invariant(case, tol, golden_mmp):
     o.set_external_field(np.zeros((o.pol_atoms, 3)))
     g = o.polelec_geomgrad()
     assert np.abs(g.sum(0)).max() < tol * np.abs(g).max()
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "1crn_amoeba", "1crn_wang"])
+def test_gradient_rows_and_installed_dipoles(case, golden_mmp):
+    # the per-atom restriction (used on the full-size water box) and dipoles
+    # installed from elsewhere reproduce the full gradient exactly
+    o = OracleSystem(golden_mmp[case])
+    o.set_tol(1e-12)
+    o.set_external_field(np.zeros((o.pol_atoms, 3)))
+    g = o.polelec_geomgrad()
+    atoms = np.array([0, 3, 5, 7, 11]) if case.startswith("nma") else np.array([0, 73, 101, 153, 250, 377, 640])
+    assert np.array_equal(o.polelec_geomgrad_atoms(atoms), g[atoms])
+    o2 = OracleSystem(golden_mmp[case])
+    o2.set_ipd(o.ipd)
+    assert np.array_equal(o2.polelec_geomgrad(), g)

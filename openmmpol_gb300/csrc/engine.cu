@@ -295,6 +295,13 @@ int System::upload_geometry() {
     std::vector<float> minv;
     build_block_jacobi(m, d2d_pairs_, d_.damp_thr, info, minv);
     cudaStreamSynchronize(st_);
+    // a captured inner iteration holds the preconditioner's device pointers:
+    // drop it before the buffers are replaced (it is captured again)
+    for (Workspace *w : {&ws_, &wsb_}) {
+      if (w->graph) cudaGraphExecDestroy(w->graph);
+      w->graph = nullptr;
+      w->graph_ncol = -1;
+    }
     if (blk_info_) cudaFree(blk_info_);
     if (blk_minv_) cudaFree(blk_minv_);
     blk_info_ = nullptr;

@@ -198,6 +198,31 @@ def test_gpu_warm_start_and_update_coordinates(golden, golden_mmp):
     assert abs(g.get_polelec_energy() - o.get_polelec_energy()) <= 1e-9 * abs(o.get_polelec_energy())
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed-ds"])
+def test_mixed_solves_across_coordinate_updates(precision, golden, golden_mmp):
+    # the captured inner iteration (CUDA graph) and the block preconditioner
+    # rebuilt for each geometry: solves on successive geometries match the
+    # oracle at each one
+    case = "1ubq_amoeba"
+    ef = golden[case + "_ef1"]
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    g.set_precision(precision)
+    g.set_solver_tol(1e-10)
+    o.set_tol(1e-12)
+    o.set_default_solver(SOLVER_DIIS)
+    rng = np.random.default_rng(4)
+    c0 = o.cmm.copy()
+    for step in range(3):
+        if step:
+            c = c0 + rng.normal(0, 0.02, c0.shape)
+            g.update_coordinates(c)
+            o.update_coordinates(c)
+        g.set_external_field(ef)
+        o.set_external_field(ef)
+        assert rel(g.ipd, o.ipd) < 1e-7
+
+
 def test_w1k_fp64_parity_and_energy(w1k):
     p, ef = w1k
     g = OMMPSystem(p)

@@ -49,7 +49,9 @@ struct GradState {
   double *t_sP = nullptr, *t_sD = nullptr;
   int *r_ri = nullptr, *r_src = nullptr;  // frame atom -> (site, slot) entries
   double *mu = nullptr;        // [mm][2*3] dipoles per static site
-  double *partial = nullptr;   // [nsplit][nacc][mm]
+  double *partial = nullptr;   // [nsplit][nacc][mm] (FP64 pass)
+  int ns_mp = 0, ns_dip = 0;   // double-single passes: splits and partials
+  double *part_mp = nullptr, *part_dip = nullptr;
   double *base = nullptr;      // [mm][3]
   double *rot = nullptr;       // [mm][4][3]
   double *grad = nullptr;      // [mm][3]
@@ -58,7 +60,7 @@ struct GradState {
 void free_grad_state(GradState *g) {
   if (!g) return;
   void *bufs[] = {g->q0, g->frame, g->mm_polar, g->t_ri, g->t_src, g->t_sP, g->t_sD, g->r_ri, g->r_src,
-                  g->mu, g->partial, g->base, g->rot, g->grad};
+                  g->mu, g->partial, g->base, g->rot, g->grad, g->part_mp, g->part_dip};
   for (void *b : bufs)
     if (b) cudaFree(b);
   delete g;
@@ -93,6 +95,10 @@ struct GradArgs {
   const int4 *frame;
   const int *r_ri, *r_src;
   double *partial, *base, *rot, *grad;
+  // partial sums read by k_grad_finish: components [0, 6) from pa (splits
+  // na, component stride sa), components [6, nacc) from pb (nb, sb)
+  const double *pa, *pb;
+  int na, sa, nb, sb;
   double thr;
   float thr2m;
   int *err;
@@ -222,9 +228,14 @@ __global__ void k_grad_finish(GradArgs g) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= g.mm) return;
   double acc[NA];
-  for (int c = 0; c < NA; ++c) {
+  for (int c = 0; c < 6; ++c) {
     double s = 0.0;
-    for (int p = 0; p < g.nsplit; ++p) s += g.partial[((size_t)p * NA + c) * g.mm + t];
+    for (int p = 0; p < g.na; ++p) s += g.pa[((size_t)p * g.sa + c) * g.mm + t];
+    acc[c] = s;
+  }
+  for (int c = 6; c < NA; ++c) {
+    double s = 0.0;
+    for (int p = 0; p < g.nb; ++p) s += g.pb[((size_t)p * g.sb + c - 6) * g.mm + t];
     acc[c] = s;
   }
   double *g0 = acc, *hd = acc + 6, *hp = acc + 12;
@@ -491,6 +502,10 @@ int System::polelec_geomgrad(double *grad_h) {
   a.r_ri = gs.r_ri;
   a.r_src = gs.r_src;
   a.partial = gs.partial;
+  a.pa = gs.partial;
+  a.pb = gs.partial + 6 * (size_t)mm;
+  a.na = a.nb = gs.nsplit;
+  a.sa = a.sb = nacc;
   a.base = gs.base;
   a.rot = gs.rot;
   a.grad = gs.grad;
@@ -499,23 +514,52 @@ int System::polelec_geomgrad(double *grad_h) {
   a.err = flag_;
   cudaMemsetAsync(flag_, 0, sizeof(int), st_);
   const int tb = (mm + gpu::GTPB - 1) / gpu::GTPB;
-  const int tiles = (mm + gpu::GTILE - 1) / gpu::GTILE;
-  const int per = ((tiles + gs.nsplit - 1) / gs.nsplit) * gpu::GTILE;
-  const dim3 grid(tb, gs.nsplit);
-  gpu::k_grad_mu<<<(mm + 255) / 256, 256, 0, st_>>>(mm, n, nset, gs.mm_polar, ipd_, gs.mu);
+  // the mixed modes evaluate the pair sums in double-single (FP32 pipes)
+  const bool ds = precision_ != kPrecFP64;
+  if (ds && !gs.part_mp) {
+    const int sms = gpu::sm_count();
+    gs.ns_mp = gpu::grad_ds_pick_split(d_, 0, sms);
+    gs.ns_dip = gpu::grad_ds_pick_split(d_, 1, sms);
+    if (cudaMalloc((void **)&gs.part_mp, (size_t)gs.ns_mp * 6 * mm * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void **)&gs.part_dip, (size_t)gs.ns_dip * (nacc - 6) * mm * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      if (gs.part_mp) cudaFree(gs.part_mp);
+      gs.part_mp = nullptr;
+      set_last_error("out of device memory for the polarization gradient");
+      return kErrMemory;
+    }
+    // the first pass writes only the polarizable sites' rows
+    cudaMemsetAsync(gs.part_mp, 0, (size_t)gs.ns_mp * 6 * mm * sizeof(double), st_);
+  }
   KEv ev{};
   if (ktime_on_) ev = kt_begin(3, 1);
-  if (amoeba)
-    gpu::k_grad_pairs<true><<<grid, gpu::GTPB, 0, st_>>>(a, per);
-  else
-    gpu::k_grad_pairs<false><<<grid, gpu::GTPB, 0, st_>>>(a, per);
+  if (ds) {
+    gpu::launch_grad_ds_mp(d_, gs.part_mp, gs.ns_mp, flag_, st_);
+    gpu::launch_grad_ds_dip(d_, ipd_, gs.part_dip, gs.ns_dip, flag_, st_);
+    a.pa = gs.part_mp;
+    a.na = gs.ns_mp;
+    a.sa = 6;
+    a.pb = gs.part_dip;
+    a.nb = gs.ns_dip;
+    a.sb = nacc - 6;
+  } else {
+    const int tiles = (mm + gpu::GTILE - 1) / gpu::GTILE;
+    const int per = ((tiles + gs.nsplit - 1) / gs.nsplit) * gpu::GTILE;
+    const dim3 grid(tb, gs.nsplit);
+    gpu::k_grad_mu<<<(mm + 255) / 256, 256, 0, st_>>>(mm, n, nset, gs.mm_polar, ipd_, gs.mu);
+    if (amoeba)
+      gpu::k_grad_pairs<true><<<grid, gpu::GTPB, 0, st_>>>(a, per);
+    else
+      gpu::k_grad_pairs<false><<<grid, gpu::GTPB, 0, st_>>>(a, per);
+    gpu::add_launch_count(2);
+  }
   if (ktime_on_) kt_end(ev);
   if (amoeba)
     gpu::k_grad_finish<true><<<tb, gpu::GTPB, 0, st_>>>(a);
   else
     gpu::k_grad_finish<false><<<tb, gpu::GTPB, 0, st_>>>(a);
   gpu::k_grad_gather<<<(mm + 255) / 256, 256, 0, st_>>>(mm, amoeba, gs.base, gs.rot, gs.r_ri, gs.r_src, gs.grad);
-  gpu::add_launch_count(4);
+  gpu::add_launch_count(2);
   int flag = 0;
   cudaMemcpyAsync(grad_h, gs.grad, 3 * (size_t)mm * sizeof(double), cudaMemcpyDeviceToHost, st_);
   cudaMemcpyAsync(&flag, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);

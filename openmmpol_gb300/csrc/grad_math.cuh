@@ -63,10 +63,20 @@ OMMP_HD void damped_k(double r2, double rinv, double ww, double a, double thr, b
   }
 }
 
+// The tensor formulas below are templates over the scalar type T (double,
+// or the double-single type of the FP32-pipe kernels) and the weight type W
+// (a scalar, or One for a unit weight that costs nothing).  Constants are
+// written as floats: all are exact in single precision.
+struct One {};
+template <typename T>
+OMMP_HD T operator*(One, T x) {
+  return x;
+}
+
 // g += w * (A d d^T + B I + v d^T + d v^T)
-OMMP_HD void sym_add(double A, double B, double vx, double vy, double vz, double dx, double dy, double dz, double w,
-                     double *g) {
-  const double px = A * dx + vx, py = A * dy + vy, pz = A * dz + vz;
+template <typename T, typename W>
+OMMP_HD void sym_add(T A, T B, T vx, T vy, T vz, T dx, T dy, T dz, W w, T *g) {
+  const T px = A * dx + vx, py = A * dy + vy, pz = A * dz + vz;
   g[0] += w * (px * dx + vx * dx + B);
   g[1] += w * (px * dy + vy * dx);
   g[2] += w * (py * dy + vy * dy + B);
@@ -77,42 +87,42 @@ OMMP_HD void sym_add(double A, double B, double vx, double vy, double vz, double
 
 // field gradient of a static multipole q[0..ld-1] (charge; + dipole and
 // quadrupole when AMOEBA), added with weight w
-template <bool AMOEBA>
-OMMP_HD void multipole_grad(const double *q, double dx, double dy, double dz, double k3, double k5, double k7,
-                            double k9, double w, double *g) {
+template <bool AMOEBA, typename T, typename W>
+OMMP_HD void multipole_grad(const T *q, T dx, T dy, T dz, T k3, T k5, T k7, T k9, W w, T *g) {
   if (!AMOEBA) {
-    sym_add(3.0 * q[0] * k5, -q[0] * k3, 0.0, 0.0, 0.0, dx, dy, dz, w, g);
+    const T z = 0.0f * dx;
+    sym_add(3.0f * q[0] * k5, -(q[0] * k3), z, z, z, dx, dy, dz, w, g);
     return;
   }
-  const double md = q[1] * dx + q[2] * dy + q[3] * dz;
-  const double tx = q[4] * dx + q[5] * dy + q[7] * dz;
-  const double ty = q[5] * dx + q[6] * dy + q[8] * dz;
-  const double tz = q[7] * dx + q[8] * dy + q[9] * dz;
-  const double s = tx * dx + ty * dy + tz * dz;
-  const double A = 3.0 * q[0] * k5 + 15.0 * k7 * md + 105.0 * k9 * s;
-  const double B = -(q[0] * k3 + 3.0 * k5 * md + 15.0 * k7 * s);
-  const double c5 = -3.0 * k5, c7 = -30.0 * k7;
+  const T md = q[1] * dx + q[2] * dy + q[3] * dz;
+  const T tx = q[4] * dx + q[5] * dy + q[7] * dz;
+  const T ty = q[5] * dx + q[6] * dy + q[8] * dz;
+  const T tz = q[7] * dx + q[8] * dy + q[9] * dz;
+  const T s = tx * dx + ty * dy + tz * dz;
+  const T A = 3.0f * q[0] * k5 + 15.0f * k7 * md + 105.0f * k9 * s;
+  const T B = -(q[0] * k3 + 3.0f * k5 * md + 15.0f * k7 * s);
+  const T c5 = -3.0f * k5, c7 = -30.0f * k7;
   sym_add(A, B, c5 * q[1] + c7 * tx, c5 * q[2] + c7 * ty, c5 * q[3] + c7 * tz, dx, dy, dz, w, g);
-  const double C = 6.0 * k5 * w;
-  g[0] += C * q[4];
-  g[1] += C * q[5];
-  g[2] += C * q[6];
-  g[3] += C * q[7];
-  g[4] += C * q[8];
-  g[5] += C * q[9];
+  const T C = 6.0f * k5;
+  g[0] += w * (C * q[4]);
+  g[1] += w * (C * q[5]);
+  g[2] += w * (C * q[6]);
+  g[3] += w * (C * q[7]);
+  g[4] += w * (C * q[8]);
+  g[5] += w * (C * q[9]);
 }
 
 // field gradient of a point dipole mu (md = mu.d), weight w
-OMMP_HD void dipole_grad(const double *mu, double md, double dx, double dy, double dz, double k5, double k7, double w,
-                         double *g) {
-  const double c = -3.0 * k5;
-  sym_add(15.0 * k7 * md, c * md, c * mu[0], c * mu[1], c * mu[2], dx, dy, dz, w, g);
+template <typename T, typename W>
+OMMP_HD void dipole_grad(const T *mu, T md, T dx, T dy, T dz, T k5, T k7, W w, T *g) {
+  const T c = -3.0f * k5;
+  sym_add(15.0f * k7 * md, c * md, c * mu[0], c * mu[1], c * mu[2], dx, dy, dz, w, g);
 }
 
 // field of a point dipole, weight w
-OMMP_HD void dipole_field(const double *mu, double md, double dx, double dy, double dz, double k3, double k5, double w,
-                          double *e) {
-  const double c = 3.0 * md * k5;
+template <typename T, typename W>
+OMMP_HD void dipole_field(const T *mu, T md, T dx, T dy, T dz, T k3, T k5, W w, T *e) {
+  const T c = 3.0f * md * k5;
   e[0] += w * (c * dx - k3 * mu[0]);
   e[1] += w * (c * dy - k3 * mu[1]);
   e[2] += w * (c * dz - k3 * mu[2]);
@@ -120,20 +130,20 @@ OMMP_HD void dipole_field(const double *mu, double md, double dx, double dy, dou
 
 // h_a += w * sum_bc Q_bc H_abc, H the field Hessian of the dipole mu and Q
 // (6 components, trace trq) the target's quadrupole
-OMMP_HD void dipole_hess_q(const double *mu, double md, double dx, double dy, double dz, const double *Q, double trq,
-                           double k5, double k7, double k9, double w, double *h) {
-  const double tx = Q[0] * dx + Q[1] * dy + Q[3] * dz;
-  const double ty = Q[1] * dx + Q[2] * dy + Q[4] * dz;
-  const double tz = Q[3] * dx + Q[4] * dy + Q[5] * dz;
-  const double s = tx * dx + ty * dy + tz * dz;
-  const double wx = Q[0] * mu[0] + Q[1] * mu[1] + Q[3] * mu[2];
-  const double wy = Q[1] * mu[0] + Q[2] * mu[1] + Q[4] * mu[2];
-  const double wz = Q[3] * mu[0] + Q[4] * mu[1] + Q[5] * mu[2];
-  const double mt = mu[0] * tx + mu[1] * ty + mu[2] * tz;
-  const double cd = 105.0 * k9 * md * s - 30.0 * k7 * mt - 15.0 * k7 * md * trq;
-  const double cm = 3.0 * k5 * trq - 15.0 * k7 * s;
-  const double ct = -30.0 * k7 * md;
-  const double cw = 6.0 * k5;
+template <typename T, typename W>
+OMMP_HD void dipole_hess_q(const T *mu, T md, T dx, T dy, T dz, const T *Q, T trq, T k5, T k7, T k9, W w, T *h) {
+  const T tx = Q[0] * dx + Q[1] * dy + Q[3] * dz;
+  const T ty = Q[1] * dx + Q[2] * dy + Q[4] * dz;
+  const T tz = Q[3] * dx + Q[4] * dy + Q[5] * dz;
+  const T s = tx * dx + ty * dy + tz * dz;
+  const T wx = Q[0] * mu[0] + Q[1] * mu[1] + Q[3] * mu[2];
+  const T wy = Q[1] * mu[0] + Q[2] * mu[1] + Q[4] * mu[2];
+  const T wz = Q[3] * mu[0] + Q[4] * mu[1] + Q[5] * mu[2];
+  const T mt = mu[0] * tx + mu[1] * ty + mu[2] * tz;
+  const T cd = 105.0f * k9 * md * s - 30.0f * k7 * mt - 15.0f * k7 * md * trq;
+  const T cm = 3.0f * k5 * trq - 15.0f * k7 * s;
+  const T ct = -30.0f * k7 * md;
+  const T cw = 6.0f * k5;
   h[0] += w * (cd * dx + cm * mu[0] + ct * tx + cw * wx);
   h[1] += w * (cd * dy + cm * mu[1] + ct * ty + cw * wy);
   h[2] += w * (cd * dz + cm * mu[2] + ct * tz + cw * wz);

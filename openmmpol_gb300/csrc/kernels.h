@@ -106,6 +106,15 @@ void launch_m2d_ds_pairs(const DevSites &s, double *partial, int nsplit, int *er
 void launch_m2d_ds(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag, cudaStream_t st);
 float m2d_r2max32(bool amoeba, double damp_thr, const double *pol_w, const double *pol_a, int n, const double *mm_w,
                   const double *mm_a, int m);
+// Polarization-gradient pair sums in double-single (grad_ds.cu): the static
+// multipoles' field gradient at the polarizable sites (partial [nsplit][6]
+// [m], at each site's static index; which 0) and the induced dipoles' field
+// gradients, field and quadrupole-contracted Hessian at the static sites
+// (partial [nsplit][18 or 9][m]; which 1), unscaled
+int grad_ds_pick_split(const DevSites &s, int which, int sm_count);
+void launch_grad_ds_mp(const DevSites &s, double *partial, int nsplit, int *err, cudaStream_t st);
+void launch_grad_ds_dip(const DevSites &s, const double *ipd, double *partial, int nsplit, int *err,
+                        cudaStream_t st);
 // z = M^-1 r for the block-Jacobi preconditioner (info / minv as built by
 // build_block_jacobi), columns [ncol][n][3], FP32
 void launch_block_apply(int ncol, int n, const int4 *info, const float *minv, const float *r, float *z,

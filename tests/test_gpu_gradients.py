@@ -3,7 +3,8 @@ the oracle's restatement of polelec_geomgrad (src/mod_geomgrad.F90:113-277).
 
 The oracle evaluates the gradient on the GPU's own dipoles (installed with
 set_ipd), so the comparison isolates the gradient arithmetic: FP64 pair sums
-in a different order, tolerance 1e-11 relative (max over atoms and
+in a different order (fp64 mode) or double-single pair sums (mixed modes),
+tolerance 1e-11 relative (max over atoms and
 components, normalised by the largest component).  Against an independent
 oracle solve (both converged to 1e-12) the tolerance is 1e-9.  The water box
 at benchmark size (90,000 sites) is checked on sampled atoms through the
@@ -40,9 +41,11 @@ def solved(path, tol=1e-12, precision="fp64"):
     return g
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("case", CASES)
-def test_gradient_matches_oracle_on_same_dipoles(case, golden_mmp):
-    g = solved(golden_mmp[case])
+def test_gradient_matches_oracle_on_same_dipoles(case, precision, golden_mmp):
+    # fp64: the FP64 pair pass; mixed modes: the double-single pair passes
+    g = solved(golden_mmp[case], precision=precision)
     gg = g.polelec_geomgrad()
     o = OracleSystem(golden_mmp[case])
     o.set_ipd(g.ipd)
@@ -120,12 +123,13 @@ def test_coincident_sites_are_reported(golden_mmp):
         g.polelec_geomgrad()
 
 
-def test_water_box_gradient_sampled(tmp_path):
+@pytest.mark.parametrize("precision", ["fp64", "mixed-ds"])
+def test_water_box_gradient_sampled(precision, tmp_path):
     # benchmark geometry: 30,000 AMOEBA waters (90,000 sites)
     w = synth.water_cluster(30000, seed=1)
     p = synth.write_mmp(str(tmp_path / "w30k.mmp"), w)
     g = OMMPSystem(p)
-    g.set_precision("mixed")
+    g.set_precision(precision)
     g.set_solver_tol(1e-10)
     g.set_external_field(np.zeros((g.pol_atoms, 3)))
     gg = g.polelec_geomgrad()

@@ -18,7 +18,8 @@ in the reference (src/mod_electrostatics.F90:1487-1596, M2D_done cache).
   pair per right-hand side) over its CUDA-event time, against the FMA pipe
   peak measured in the same run.
 * ``geomgrad``: the polarization-energy gradient (ommp_polelec_geomgrad) on
-  the solved system: calls/s, its FP64 pair kernel against the FP64 pipe, and
+  the solved system: calls/s with the double-single pair passes of the mixed
+  modes and with the FP64 pass, each against its pipe, their difference, and
   the oracle's gradient on the host cores (3,000-molecule sample scaled).
 * ``cpu_baseline``: the C/OpenMP oracle (restatement of the reference's
   OpenMP path) timed on a bounded sample of target rows of one matrix-vector
@@ -57,6 +58,10 @@ DS_OPS_PER_PAIR = 227.0
 # 30,000-site box (undamped pairs dominate); flop counts an FMA twice
 GRAD_F64_INST_PER_PAIR = 207.0
 GRAD_F64_FLOP_PER_PAIR = 302.0
+# FP32 arithmetic instructions (FADD + FMUL + FFMA) per ordered pair of the
+# double-single gradient passes (grad_ds.cu), same counters and box: 945 in
+# the static-multipole pass + 1,758 in the induced-dipole pass
+GRAD_DS_OPS_PER_PAIR = 2703.0
 
 
 def parse():
@@ -310,38 +315,54 @@ def grad_cpu_sample(cache, threads):
     return dt, o.mm_atoms, err
 
 
-def grad_pass(g, L, peak64, cache, reps=2, cpu=True):
+def grad_pass(g, L, peak64, peak32, cache, restore, reps=2, cpu=True):
     """Polarization-energy gradient on the solved system through the public
-    call (ommp_gpu_polelec_geomgrad: gradient D2H included), its pair kernel
-    against the FP64 pipe, and the oracle's gradient on the host cores."""
+    call (ommp_gpu_polelec_geomgrad: gradient D2H included): the
+    double-single pair passes of the mixed modes and the FP64 pass of the
+    fp64 mode, each pair kernel against its pipe; the oracle's gradient on
+    the host cores."""
     h = g._h
     mm = g.mm_atoms
-    g.polelec_geomgrad()  # first call builds the gradient's device lists
-    g.synchronize()
-    L.ommp_gpu_reset_kernel_stats(h)
-    g.enable_kernel_timing(True)
-    launches0 = L.ommp_gpu_kernel_launch_count()
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        grad = g.polelec_geomgrad()
-    wall = (time.perf_counter() - t0) / reps
-    launches = L.ommp_gpu_kernel_launch_count() - launches0
-    g.enable_kernel_timing(False)
-    cnt, ms, _ = g.kernel_stats(3)
-    kms = ms / max(cnt, 1)
     pairs = float(mm) * (mm - 1)
-    inst = GRAD_F64_INST_PER_PAIR * pairs / (kms * 1e-3) / 1e12
-    flop = GRAD_F64_FLOP_PER_PAIR * pairs / (kms * 1e-3) / 1e12
-    res = {"gradients_per_s": 1.0 / wall, "ms_per_gradient": wall * 1e3, "pair_kernel_ms": kms,
-           "pairs_per_s": pairs / (kms * 1e-3), "gpu_launches_per_gradient": launches / reps,
-           "net_force_rel": float(np.abs(grad.sum(0)).max() / np.abs(grad).max()),
-           "roofline": {"bound": "fp64", "kernel": "k_grad_pairs", "achieved": inst, "peak": peak64 / 2,
-                        "unit": "T FP64 instructions/s", "frac": inst / (peak64 / 2) if peak64 else None,
-                        "achieved_tflops": flop, "peak_tflops": peak64,
-                        "algorithmic": f"{GRAD_F64_INST_PER_PAIR:.0f} FP64 instructions "
-                                       f"({GRAD_F64_FLOP_PER_PAIR:.0f} flop) per ordered pair x N(N-1)",
-                        "peak_source": "FMA-chain kernel measured in this run (FP64 pipe)"},
-           "d2h_bytes_per_call": mm * 3 * 8}
+
+    def timed(precision):
+        g.set_precision(precision)
+        g.polelec_geomgrad()  # first call builds the gradient's device lists
+        g.synchronize()
+        L.ommp_gpu_reset_kernel_stats(h)
+        g.enable_kernel_timing(True)
+        launches0 = L.ommp_gpu_kernel_launch_count()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            grad = g.polelec_geomgrad()
+        wall = (time.perf_counter() - t0) / reps
+        launches = L.ommp_gpu_kernel_launch_count() - launches0
+        g.enable_kernel_timing(False)
+        cnt, ms, _ = g.kernel_stats(3)
+        kms = ms / max(cnt, 1)
+        if precision == "fp64":
+            inst, peak, unit = GRAD_F64_INST_PER_PAIR, peak64 / 2, "T FP64 instructions/s"
+            alg = (f"{GRAD_F64_INST_PER_PAIR:.0f} FP64 instructions ({GRAD_F64_FLOP_PER_PAIR:.0f} flop) "
+                   "per ordered pair x N(N-1)")
+        else:
+            inst, peak, unit = GRAD_DS_OPS_PER_PAIR, peak32 / 2, "T FP32 instructions/s"
+            alg = f"{GRAD_DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair (both passes) x N(N-1)"
+        ach = inst * pairs / (kms * 1e-3) / 1e12
+        return grad, {"gradients_per_s": 1.0 / wall, "ms_per_gradient": wall * 1e3, "pair_kernels_ms": kms,
+                      "pairs_per_s": pairs / (kms * 1e-3), "gpu_launches_per_gradient": launches / reps,
+                      "net_force_rel": float(np.abs(grad.sum(0)).max() / np.abs(grad).max()),
+                      "roofline": {"bound": "fp64" if precision == "fp64" else "fp32", "achieved": ach,
+                                   "peak": peak, "unit": unit, "frac": ach / peak if peak else None,
+                                   "algorithmic": alg,
+                                   "peak_source": "FMA-chain kernel measured in this run (pipe instruction rate)"}}
+
+    g_ds, res = timed("mixed-ds")
+    g_64, res64 = timed("fp64")
+    g.set_precision(restore)
+    res["precision"] = "double-single pair sums (mixed modes)"
+    res["fp64"] = res64
+    res["max_rel_diff_vs_fp64"] = float(np.abs(g_ds - g_64).max() / np.abs(g_64).max())
+    res["d2h_bytes_per_call"] = mm * 3 * 8
     if cpu:
         try:
             cores = os.cpu_count() or 1
@@ -351,7 +372,7 @@ def grad_pass(g, L, peak64, cache, reps=2, cpu=True):
                                    "kind": "port", "s_per_gradient_sample": dt,
                                    "sample": f"full oracle gradient of the {m_s}-site box (3,000 molecules) "
                                              f"on GPU-solved dipoles, scaled by the pair count to {mm} sites",
-                                   "gpu_vs_oracle_max_rel_err_on_sample": err}
+                                   "gpu_fp64_vs_oracle_max_rel_err_on_sample": err}
         except Exception as ex:  # report, do not hide
             res["cpu_baseline"] = {"value": None, "error": repr(ex)}
     return res
@@ -466,7 +487,8 @@ def run_gb300(args):
     main = timed_pass(sys_)
     grad = None
     if not args.no_grad:
-        grad = grad_pass(sys_, L, peak64.value, args.cache, cpu=rank == 0 and not args.skip_cpu)
+        grad = grad_pass(sys_, L, peak64.value, peak32.value, args.cache, args.precision,
+                         cpu=rank == 0 and not args.skip_cpu)
     # the double-single variant alongside the strict mixed mode, on its own
     # system: refinement residual products and E_M2D in double-single
     ds = None

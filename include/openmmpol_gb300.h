@@ -69,6 +69,7 @@
 #define OMMP_GPU_ERR_CANCELLED 7
 
 typedef void *OMMP_SYSTEM_PRT;
+typedef void *OMMP_QM_HELPER_PRT;
 
 #ifdef __cplusplus
 extern "C" {
@@ -144,6 +145,41 @@ void ommp_field_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double
  * are solved first (default solver) when the system has none.  FP64 on the
  * GPU whatever the precision mode. */
 void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
+/* QM helper, include/openmmpol.h:106-127 ; src/mod_c_interface.F90:1179-1196,
+ * 1374-1660 ; src/mod_qm_helper.F90:80-161,356-520.  A helper holds n QM
+ * nuclei (coordinates cqm [n][3] bohr, charges qqm [n], atomic numbers zqm
+ * [n]).  ommp_prepare_qm_ele_ene computes, once until the next
+ * ommp_qm_helper_update_coord, the field of the nuclei at the polarizable
+ * sites (E_n2p [pol_atoms][3]) and the potential of the static multipoles at
+ * the nuclei (V_m2n [n]), and, once the system holds dipoles, that of the
+ * induced dipoles (V_p2n [n]; like the reference, update_coord keeps it).
+ * ommp_prepare_qm_ele_grd recomputes at every call the field, field gradient
+ * and field Hessian of the nuclei at every static site (E_n2m [mm][3], G_n2m
+ * [mm][6] xx,xy,yy,xz,yz,zz, H_n2m [mm][10] xxx,xxy,xxz,xyy,xyz,xzz,yyy,yyz,
+ * yzz,zzz), G_n2p (G_n2m at the polarizable sites) and the field of the
+ * static multipoles / induced dipoles at the nuclei (E_m2n, E_p2n [n][3];
+ * E_p2n needs dipoles).  The getters return the helper's arrays, or NULL
+ * before they are computed; get_npol / get_nmm return 0 until E_n2p / E_n2m
+ * exist.  The QM-MM van der Waals terms, link atoms and frozen atoms of the
+ * reference's helper are not part of this library. */
+OMMP_QM_HELPER_PRT ommp_init_qm_helper(int32_t n, const double *cqm, const double *qqm, const int32_t *zqm);
+void ommp_terminate_qm_helper(OMMP_QM_HELPER_PRT qm);
+void ommp_qm_helper_update_coord(OMMP_QM_HELPER_PRT qm, const double *cqm);
+void ommp_prepare_qm_ele_ene(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm);
+void ommp_prepare_qm_ele_grd(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_V_m2n(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_V_p2n(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_E_m2n(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_E_p2n(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_E_n2p(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_G_n2p(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_E_n2m(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_G_n2m(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_H_n2m(OMMP_QM_HELPER_PRT qm);
+double *ommp_qm_helper_get_cqm(OMMP_QM_HELPER_PRT qm);
+int32_t ommp_qm_helper_get_npol(OMMP_QM_HELPER_PRT qm);
+int32_t ommp_qm_helper_get_nmm(OMMP_QM_HELPER_PRT qm);
+int32_t ommp_qm_helper_get_qm_atoms(OMMP_QM_HELPER_PRT qm);
 /* include/openmmpol.h:153-155 ; src/mod_c_interface.F90:1843-1879.  The fast
  * multipole method is not part of this library: enabling it logs a warning
  * and the direct sums are kept; ommp_use_fmm always returns false. */
@@ -166,6 +202,11 @@ int32_t ommp_gpu_set_external_field_device(OMMP_SYSTEM_PRT s, const double *ext_
 int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *energy);
 /* ommp_polelec_geomgrad returning a status instead of stopping the process */
 int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
+/* QM helper calls returning a status instead of stopping the process */
+int32_t ommp_gpu_init_qm_helper(int32_t n, const double *cqm, const double *qqm, const int32_t *zqm,
+                                OMMP_QM_HELPER_PRT *out);
+int32_t ommp_gpu_prepare_qm_ele_ene(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm);
+int32_t ommp_gpu_prepare_qm_ele_grd(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm);
 int32_t ommp_gpu_update_coordinates(OMMP_SYSTEM_PRT s, const double *cmm);
 int32_t ommp_gpu_set_default_solver(OMMP_SYSTEM_PRT s, int32_t solver);
 int32_t ommp_gpu_set_default_matv(OMMP_SYSTEM_PRT s, int32_t matv);

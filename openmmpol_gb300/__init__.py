@@ -13,7 +13,7 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ["OMMPSystem", "Server", "OMMPError", "available_solvers", "available_matrix_vector",
+__all__ = ["OMMPSystem", "OMMPQmHelper", "Server", "OMMPError", "available_solvers", "available_matrix_vector",
            "set_verbose", "PREC_FP64", "PREC_MIXED", "PREC_MIXED_DS", "PRECISIONS"]
 
 # pythonapi/pyopenmmpol/pyommp_interface.cpp:9-23
@@ -307,6 +307,79 @@ class OMMPSystem:
 
     def synchronize(self) -> None:
         _check(self._L.ommp_gpu_synchronize(self._h))
+
+
+class OMMPQmHelper:
+    """QM nuclei and their electrostatics with one system, as pyopenmmpol's
+    OMMPQmHelper (pythonapi/pyopenmmpol/pyommp_interface.cpp:946-1285):
+    ``OMMPQmHelper(cqm [n, 3], qqm [n], zqm [n])``, ``prepare_qm_ele_ene(s)``,
+    ``prepare_qm_ele_grd(s)``, ``update_coord(cqm)`` and the read-only arrays
+    ``E_n2p``, ``G_n2p``, ``E_n2m``, ``G_n2m``, ``H_n2m``, ``V_m2n``,
+    ``V_p2n``, ``E_m2n``, ``E_p2n`` (AttributeError before they are
+    computed, like the reference's)."""
+
+    _SHAPES = {"E_n2p": ("npol", 3), "G_n2p": ("npol", 6), "E_n2m": ("nmm", 3), "G_n2m": ("nmm", 6),
+               "H_n2m": ("nmm", 10), "V_m2n": ("qm", None), "V_p2n": ("qm", None), "E_m2n": ("qm", 3),
+               "E_p2n": ("qm", 3)}
+    _WHEN = {"E_n2p": "prepare_qm_ele_ene", "V_m2n": "prepare_qm_ele_ene", "V_p2n": "prepare_qm_ele_ene"}
+
+    def __init__(self, cqm, qqm, zqm):
+        self._L = _lib.load()
+        cqm = np.ascontiguousarray(cqm, dtype=np.float64).reshape(-1, 3)
+        n = cqm.shape[0]
+        qqm = _as_c(qqm, (n,))
+        zqm = _as_c(zqm, (n,), np.int32)
+        h = C.c_void_p()
+        _check(self._L.ommp_gpu_init_qm_helper(n, cqm.ctypes.data_as(_lib._dp), qqm.ctypes.data_as(_lib._dp),
+                                               zqm.ctypes.data_as(_lib._ip), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.ommp_terminate_qm_helper(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def qm_atoms(self) -> int:
+        return self._L.ommp_qm_helper_get_qm_atoms(self._h)
+
+    @property
+    def npol(self) -> int:
+        return self._L.ommp_qm_helper_get_npol(self._h)
+
+    @property
+    def nmm(self) -> int:
+        return self._L.ommp_qm_helper_get_nmm(self._h)
+
+    @property
+    def cqm(self) -> np.ndarray:
+        p = self._L.ommp_qm_helper_get_cqm(self._h)
+        return np.ctypeslib.as_array(p, shape=(self.qm_atoms, 3)).copy()
+
+    def update_coord(self, cqm) -> None:
+        c = _as_c(cqm, (self.qm_atoms, 3))
+        self._L.ommp_qm_helper_update_coord(self._h, c.ctypes.data_as(_lib._dp))
+
+    def prepare_qm_ele_ene(self, system: "OMMPSystem") -> None:
+        _check(self._L.ommp_gpu_prepare_qm_ele_ene(system._h, self._h))
+
+    def prepare_qm_ele_grd(self, system: "OMMPSystem") -> None:
+        _check(self._L.ommp_gpu_prepare_qm_ele_grd(system._h, self._h))
+
+    def __getattr__(self, name):
+        shape = OMMPQmHelper._SHAPES.get(name)
+        if shape is None:
+            raise AttributeError(name)
+        p = getattr(self._L, "ommp_qm_helper_get_" + name)(self._h)
+        if not p:
+            when = OMMPQmHelper._WHEN.get(name, "prepare_qm_ele_grd")
+            raise AttributeError(f"{name} is not available. OMMPQmHelper.{when}() should be called before!")
+        rows = {"npol": self.npol, "nmm": self.nmm, "qm": self.qm_atoms}[shape[0]]
+        full = (rows,) if shape[1] is None else (rows, shape[1])
+        return np.ctypeslib.as_array(p, shape=full).copy()
 
 
 class Server:

@@ -71,6 +71,27 @@ SIGNATURES = {
     "ommp_field_pol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
     "ommp_polelec_geomgrad": (None, [_vp, _dp]),
     "ommp_gpu_polelec_geomgrad": (C.c_int32, [_vp, _dp]),
+    "ommp_init_qm_helper": (_vp, [C.c_int32, _dp, _dp, _ip]),
+    "ommp_gpu_init_qm_helper": (C.c_int32, [C.c_int32, _dp, _dp, _ip, C.POINTER(_vp)]),
+    "ommp_terminate_qm_helper": (None, [_vp]),
+    "ommp_qm_helper_update_coord": (None, [_vp, _dp]),
+    "ommp_prepare_qm_ele_ene": (None, [_vp, _vp]),
+    "ommp_prepare_qm_ele_grd": (None, [_vp, _vp]),
+    "ommp_gpu_prepare_qm_ele_ene": (C.c_int32, [_vp, _vp]),
+    "ommp_gpu_prepare_qm_ele_grd": (C.c_int32, [_vp, _vp]),
+    "ommp_qm_helper_get_V_m2n": (_dp, [_vp]),
+    "ommp_qm_helper_get_V_p2n": (_dp, [_vp]),
+    "ommp_qm_helper_get_E_m2n": (_dp, [_vp]),
+    "ommp_qm_helper_get_E_p2n": (_dp, [_vp]),
+    "ommp_qm_helper_get_E_n2p": (_dp, [_vp]),
+    "ommp_qm_helper_get_G_n2p": (_dp, [_vp]),
+    "ommp_qm_helper_get_E_n2m": (_dp, [_vp]),
+    "ommp_qm_helper_get_G_n2m": (_dp, [_vp]),
+    "ommp_qm_helper_get_H_n2m": (_dp, [_vp]),
+    "ommp_qm_helper_get_cqm": (_dp, [_vp]),
+    "ommp_qm_helper_get_npol": (C.c_int32, [_vp]),
+    "ommp_qm_helper_get_nmm": (C.c_int32, [_vp]),
+    "ommp_qm_helper_get_qm_atoms": (C.c_int32, [_vp]),
     "ommp_gpu_set_use_graphs": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_external_fields_batch": (C.c_int32, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ommp_gpu_set_external_fields_batch_device": (C.c_int32, [_vp, C.c_int32, _vp, _vp, _dp]),

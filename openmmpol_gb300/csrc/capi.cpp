@@ -12,11 +12,14 @@
 #include "../../include/openmmpol_gb300.h"
 #include "engine.h"
 #include "log.h"
+#include "qm_helper.h"
 
+using ommp::QMHelper;
 using ommp::System;
 
 namespace {
 System *S(OMMP_SYSTEM_PRT p) { return static_cast<System *>(p); }
+QMHelper *Q(OMMP_QM_HELPER_PRT p) { return static_cast<QMHelper *>(p); }
 
 void fatal_if(int st) {
   if (st != ommp::kOk) ommp::log_fatal(ommp::last_error());
@@ -150,6 +153,41 @@ int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) {
   return st;
 }
 void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) { fatal_if(ommp_gpu_polelec_geomgrad(s, grd)); }
+
+int32_t ommp_gpu_init_qm_helper(int32_t n, const double *cqm, const double *qqm, const int32_t *zqm,
+                                OMMP_QM_HELPER_PRT *out) {
+  *out = nullptr;
+  if (n < 0 || (n > 0 && (!cqm || !qqm || !zqm))) {
+    ommp::set_last_error("QM helper: n >= 0 and coordinates, charges and atomic numbers are required");
+    return ommp::kErrBadArg;
+  }
+  *out = new QMHelper(n, cqm, qqm, zqm);
+  return ommp::kOk;
+}
+OMMP_QM_HELPER_PRT ommp_init_qm_helper(int32_t n, const double *cqm, const double *qqm, const int32_t *zqm) {
+  OMMP_QM_HELPER_PRT h = nullptr;
+  fatal_if(ommp_gpu_init_qm_helper(n, cqm, qqm, zqm, &h));
+  return h;
+}
+void ommp_terminate_qm_helper(OMMP_QM_HELPER_PRT qm) { delete Q(qm); }
+void ommp_qm_helper_update_coord(OMMP_QM_HELPER_PRT qm, const double *c) { Q(qm)->update_coord(c); }
+int32_t ommp_gpu_prepare_qm_ele_ene(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm) { return Q(qm)->prepare_ene(*S(s)); }
+int32_t ommp_gpu_prepare_qm_ele_grd(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm) { return Q(qm)->prepare_grd(*S(s)); }
+void ommp_prepare_qm_ele_ene(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm) { fatal_if(ommp_gpu_prepare_qm_ele_ene(s, qm)); }
+void ommp_prepare_qm_ele_grd(OMMP_SYSTEM_PRT s, OMMP_QM_HELPER_PRT qm) { fatal_if(ommp_gpu_prepare_qm_ele_grd(s, qm)); }
+double *ommp_qm_helper_get_V_m2n(OMMP_QM_HELPER_PRT qm) { return Q(qm)->V_m2n(); }
+double *ommp_qm_helper_get_V_p2n(OMMP_QM_HELPER_PRT qm) { return Q(qm)->V_p2n(); }
+double *ommp_qm_helper_get_E_m2n(OMMP_QM_HELPER_PRT qm) { return Q(qm)->E_m2n(); }
+double *ommp_qm_helper_get_E_p2n(OMMP_QM_HELPER_PRT qm) { return Q(qm)->E_p2n(); }
+double *ommp_qm_helper_get_E_n2p(OMMP_QM_HELPER_PRT qm) { return Q(qm)->E_n2p(); }
+double *ommp_qm_helper_get_G_n2p(OMMP_QM_HELPER_PRT qm) { return Q(qm)->G_n2p(); }
+double *ommp_qm_helper_get_E_n2m(OMMP_QM_HELPER_PRT qm) { return Q(qm)->E_n2m(); }
+double *ommp_qm_helper_get_G_n2m(OMMP_QM_HELPER_PRT qm) { return Q(qm)->G_n2m(); }
+double *ommp_qm_helper_get_H_n2m(OMMP_QM_HELPER_PRT qm) { return Q(qm)->H_n2m(); }
+double *ommp_qm_helper_get_cqm(OMMP_QM_HELPER_PRT qm) { return Q(qm)->cqm(); }
+int32_t ommp_qm_helper_get_npol(OMMP_QM_HELPER_PRT qm) { return Q(qm)->npol(); }
+int32_t ommp_qm_helper_get_nmm(OMMP_QM_HELPER_PRT qm) { return Q(qm)->nmm(); }
+int32_t ommp_qm_helper_get_qm_atoms(OMMP_QM_HELPER_PRT qm) { return Q(qm)->qm_atoms(); }
 
 void ommp_enable_fmm(OMMP_SYSTEM_PRT s) {
   (void)s;

@@ -130,6 +130,8 @@ class System {
   double *q_host() { return m_.q.data(); }
   cudaStream_t stream() const { return st_; }
   const gpu::DevSites &dev() const { return d_; }
+  bool ipd_done() const { return ipd_done_; }
+  int *flag_dev() { return flag_; }  // device error flag of the system's stream
 
  private:
   System() = default;

@@ -2098,3 +2098,56 @@ int orc_set_ipd(orc_sys *s, const double *ipd) {
     s->ipd_done = 1;
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* QM helper electrostatics: fields of the QM nuclei (point charges,   */
+/* undamped coulomb_kernel) at the MM sites, electrostatic_for_ene /   */
+/* electrostatic_for_grad (src/mod_qm_helper.F90:356-520) with         */
+/* q_elec_prop (src/mod_electrostatics.F90:1097-1176).  The MM side    */
+/* (V_m2n, V_p2n, E_m2n, E_p2n) is orc_potential_ext / orc_field_ext.  */
+/* which 0: E_n2p [npol][3] only; 1: E_n2m [mm][3], G_n2m [mm][6],     */
+/* H_n2m [mm][10] (outputs overwritten).                               */
+/* ------------------------------------------------------------------ */
+int orc_nuclei_fields(orc_sys *s, int32_t which, int32_t nq, const double *cqm, const double *qqm, double *E,
+                      double *G, double *H) {
+    const int nt = which == 0 ? s->npol : s->mm;
+    int bad = 0;
+    memset(E, 0, sizeof(double) * 3 * (size_t)nt);
+    if (which) {
+        memset(G, 0, sizeof(double) * 6 * (size_t)nt);
+        memset(H, 0, sizeof(double) * 10 * (size_t)nt);
+    }
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int j = 0; j < nt; j++) {
+        const double *c = &s->cmm[3 * (size_t)(which == 0 ? s->polar_mm[j] : j)];
+        for (int i = 0; i < nq; i++) {
+            double d[3] = {c[0] - cqm[3 * i], c[1] - cqm[3 * i + 1], c[2] - cqm[3 * i + 2]};
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (r < EPS_RP) {
+                bad = 1;
+                continue;
+            }
+            double k[4];
+            k[0] = 1.0 / r;
+            for (int l = 1; l < 4; l++) k[l] = k[l - 1] / (r * r);
+            const double q = qqm[i];
+            for (int a = 0; a < 3; a++) E[3 * (size_t)j + a] += q * k[1] * d[a];
+            if (!which) continue;
+            for (int c6 = 0; c6 < 6; c6++) {
+                int a = G6A[c6], b = G6B[c6];
+                G[6 * (size_t)j + c6] += q * (3.0 * k[2] * d[a] * d[b] - k[1] * kd(a, b));
+            }
+            for (int c10 = 0; c10 < 10; c10++) {
+                int a = H10A[c10], b = H10B[c10], e = H10C[c10];
+                H[10 * (size_t)j + c10] +=
+                    q * (15.0 * k[3] * d[a] * d[b] * d[e] - 3.0 * k[2] * (kd(a, b) * d[e] + kd(a, e) * d[b] + kd(b, e) * d[a]));
+            }
+        }
+    }
+    if (bad) {
+        set_err("Requesting Coulomb kernel for two atoms placed in the same point, this could be an internal bug or "
+                "a problem in your input file, please check.");
+        return ORC_ERR_NUMERIC;
+    }
+    return 0;
+}

@@ -118,6 +118,11 @@ int orc_polelec_geomgrad_atoms(orc_sys *s, int32_t na, const int32_t *atoms, dou
 /* install induced dipoles ipd [n_ipd][npol][3] as the solved state (so that
    the gradient can be evaluated on dipoles solved elsewhere) */
 int orc_set_ipd(orc_sys *s, const double *ipd);
+/* fields of QM nuclei (charges qqm at cqm [nq][3]) at the MM sites, the QM
+   helper's E_n2p (which 0: E [npol][3]) or E_n2m / G_n2m / H_n2m (which 1:
+   E [mm][3], G [mm][6], H [mm][10]); outputs overwritten */
+int orc_nuclei_fields(orc_sys *s, int32_t which, int32_t nq, const double *cqm, const double *qqm, double *E,
+                      double *G, double *H);
 
 #ifdef __cplusplus
 }

@@ -64,6 +64,7 @@ def lib():
             "orc_polelec_geomgrad": (C.c_int, [vp, dp]),
             "orc_polelec_geomgrad_atoms": (C.c_int, [vp, C.c_int32, ip, dp]),
             "orc_set_ipd": (C.c_int, [vp, dp]),
+            "orc_nuclei_fields": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp, dp, dp, dp]),
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
             "orc_last_iterations": (C.c_int32, [vp, C.c_int32]),
@@ -225,6 +226,17 @@ class OracleSystem:
         """Install dipoles [n_ipd][npol][3] solved elsewhere as the solved state."""
         ipd = np.ascontiguousarray(ipd, dtype=np.float64).reshape(self.n_ipd, self.pol_atoms, 3)
         self._check(lib().orc_set_ipd(self._h, _dp(ipd)))
+
+    def nuclei_fields(self, cqm, qqm, grad=False):
+        """QM-helper fields of point nuclei at the MM sites: E_n2p [npol][3]
+        (grad False) or (E_n2m [mm][3], G_n2m [mm][6], H_n2m [mm][10])."""
+        cqm = np.ascontiguousarray(cqm, dtype=np.float64).reshape(-1, 3)
+        qqm = np.ascontiguousarray(qqm, dtype=np.float64)
+        nt = self.mm_atoms if grad else self.pol_atoms
+        E, G, H = np.zeros((nt, 3)), np.zeros((nt, 6)), np.zeros((nt, 10))
+        self._check(lib().orc_nuclei_fields(self._h, int(grad), len(cqm), _dp(cqm), _dp(qqm), _dp(E), _dp(G),
+                                            _dp(H)))
+        return (E, G, H) if grad else E
 
     def field_ext(self, which, cext, e=None):
         cext = np.ascontiguousarray(cext, dtype=np.float64).reshape(-1, 3)

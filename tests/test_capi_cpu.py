@@ -14,7 +14,7 @@ HEADER = os.path.join(ROOT, "include", "openmmpol_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"\b(ommp_[a-z0-9_]+)\s*\(", text)
+    names = re.findall(r"\b(ommp_[A-Za-z0-9_]+)\s*\(", text)
     return sorted(set(names))
 
 

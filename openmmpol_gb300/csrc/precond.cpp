@@ -15,6 +15,7 @@
 // water it cuts the CG iterations by about a quarter.
 #include <algorithm>
 #include <cmath>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -93,9 +94,10 @@ void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_
     const double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
     return dx * dx + dy * dy + dz * dz;
   };
-  int start = 0;
-  while (start < n) {
-    // grow the run while the next site is close to one already in it
+  // runs: grow while the next site is close to one already in the run
+  std::vector<int> run_start, run_off;
+  size_t total = 0;
+  for (int start = 0; start < n;) {
     int end = start + 1;
     while (end < n && end - start < kMaxBlock) {
       bool linked = false;
@@ -103,52 +105,68 @@ void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_
       if (!linked) break;
       ++end;
     }
-    const int s = end - start, dim = 3 * s;
-    std::vector<double> a(dim * dim, 0.0);
-    for (int jl = 0; jl < s; ++jl) {
-      const int j = start + jl;
-      for (int c = 0; c < 3; ++c) a[(3 * jl + c) * dim + 3 * jl + c] = 1.0 / m.pol[j];
-      for (int il = 0; il < s; ++il) {
-        if (il == jl) continue;
-        const int i = start + il;
-        double sc = 1.0;  // scale of source i in target j's row
-        for (int k = d2d.ri[j]; k < d2d.ri[j + 1]; ++k)
-          if (d2d.src[k] == i) sc = d2d.sP[k];
-        if (sc == 0.0) continue;
-        const double *pj = pos(j), *pi = pos(i);
-        const double d[3] = {pj[0] - pi[0], pj[1] - pi[1], pj[2] - pi[2]};
-        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        const double wt = 1.0 / m.thole[m.polar_mm[j]], ws = 1.0 / m.thole[m.polar_mm[i]];
-        const double at = m.amoeba ? m.damping[j] : 0.0, as = m.amoeba ? m.damping[i] : 0.0;
-        double k3, k5;
-        damped_k35(m.amoeba, r2, wt, ws, at, as, damp_thr, k3, k5);
-        // T_ji = -s (3 k5 d d^T - k3 I)
-        for (int p = 0; p < 3; ++p)
-          for (int q = 0; q < 3; ++q)
-            a[(3 * jl + p) * dim + 3 * il + q] = -sc * (3.0 * k5 * d[p] * d[q] - (p == q ? k3 : 0.0));
-      }
-    }
-    std::vector<double> inv = a;
-    const bool ok = invert(inv, dim);
-    const int off = (int)minv.size();
-    for (int r = 0; r < dim; ++r)
-      for (int c = 0; c < dim; ++c) {
-        double v;
-        if (ok)
-          v = 0.5 * (inv[r * dim + c] + inv[c * dim + r]);  // symmetric in FP32 too
-        else
-          v = (r == c) ? 1.0 / a[r * dim + r] : 0.0;  // fall back to the diagonal
-        minv.push_back((float)v);
-      }
-    for (int jl = 0; jl < s; ++jl) {
-      int *e = &info[4 * (size_t)(start + jl)];
-      e[0] = start;
-      e[1] = s;
-      e[2] = off;
-      e[3] = jl;
-    }
+    run_start.push_back(start);
+    run_off.push_back((int)total);
+    total += 9 * (size_t)(end - start) * (end - start);
     start = end;
   }
+  const int nrun = (int)run_start.size();
+  run_start.push_back(n);
+  minv.resize(total);
+  // each run's block: built, inverted and stored independently (threads)
+  auto work = [&](int r0, int r1) {
+    std::vector<double> a, inv;
+    for (int r = r0; r < r1; ++r) {
+      const int start = run_start[r], s = run_start[r + 1] - start, dim = 3 * s, off = run_off[r];
+      a.assign((size_t)dim * dim, 0.0);
+      for (int jl = 0; jl < s; ++jl) {
+        const int j = start + jl;
+        for (int c = 0; c < 3; ++c) a[(3 * jl + c) * dim + 3 * jl + c] = 1.0 / m.pol[j];
+        for (int il = 0; il < s; ++il) {
+          if (il == jl) continue;
+          const int i = start + il;
+          double sc = 1.0;  // scale of source i in target j's row
+          for (int k = d2d.ri[j]; k < d2d.ri[j + 1]; ++k)
+            if (d2d.src[k] == i) sc = d2d.sP[k];
+          if (sc == 0.0) continue;
+          const double *pj = pos(j), *pi = pos(i);
+          const double d[3] = {pj[0] - pi[0], pj[1] - pi[1], pj[2] - pi[2]};
+          const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          const double wt = 1.0 / m.thole[m.polar_mm[j]], ws = 1.0 / m.thole[m.polar_mm[i]];
+          const double at = m.amoeba ? m.damping[j] : 0.0, as = m.amoeba ? m.damping[i] : 0.0;
+          double k3, k5;
+          damped_k35(m.amoeba, r2, wt, ws, at, as, damp_thr, k3, k5);
+          // T_ji = -s (3 k5 d d^T - k3 I)
+          for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q)
+              a[(3 * jl + p) * dim + 3 * il + q] = -sc * (3.0 * k5 * d[p] * d[q] - (p == q ? k3 : 0.0));
+        }
+      }
+      inv = a;
+      const bool ok = invert(inv, dim);
+      for (int rr = 0; rr < dim; ++rr)
+        for (int cc = 0; cc < dim; ++cc) {
+          double v;
+          if (ok)
+            v = 0.5 * (inv[rr * dim + cc] + inv[cc * dim + rr]);  // symmetric in FP32 too
+          else
+            v = (rr == cc) ? 1.0 / a[rr * dim + rr] : 0.0;  // fall back to the diagonal
+          minv[off + rr * dim + cc] = (float)v;
+        }
+      for (int jl = 0; jl < s; ++jl) {
+        int *e = &info[4 * (size_t)(start + jl)];
+        e[0] = start;
+        e[1] = s;
+        e[2] = off;
+        e[3] = jl;
+      }
+    }
+  };
+  const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), nrun / 1024));
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work, (int)((long)nrun * t / nt), (int)((long)nrun * (t + 1) / nt));
+  work(0, (int)((long)nrun / nt));
+  for (auto &x : th) x.join();
 }
 
 }  // namespace ommp

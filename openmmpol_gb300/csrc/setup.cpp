@@ -20,6 +20,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <thread>
 
 #include "ommp_internal.h"
 
@@ -27,13 +28,18 @@ namespace ommp {
 
 namespace {
 
-// Fortran list-directed input over a text file: a read of K values consumes
-// records until K values are found and drops the rest of the last record.
-// Supports blank/comma separators, 'D' exponents and r*c repeat counts.
+// Fortran list-directed input over a text file held in memory: a read of K
+// values consumes records until K values are found and drops the rest of the
+// last record.  Supports blank/comma separators, 'D' exponents and r*c
+// repeat counts.  Numbers of at most 2^53 significant units with a decimal
+// exponent within +-22 take Clinger's exact fast path (one correctly rounded
+// multiplication or division by an exact power of ten, the same double as
+// strtod); everything else goes through strtod.
 class ListReader {
+  static constexpr int kMaxLine = 128;  // values per read of the row readers
+
  public:
-  explicit ListReader(FILE *f) : f_(f) {}
-  ~ListReader() { free(line_); }
+  explicit ListReader(std::vector<char> &&buf) : b_(std::move(buf)), p_(b_.data()), e_(b_.data() + b_.size()) {}
   bool skip(long n) {
     for (long i = 0; i < n; ++i)
       if (!next_line()) return false;
@@ -43,85 +49,269 @@ class ListReader {
     int got = 0;
     while (got < want) {
       if (!next_line()) return false;
-      const char *p = line_;
-      while (*p && got < want) {
-        while (*p && (isspace((unsigned char)*p) || *p == ',')) ++p;
-        if (!*p) break;
-        char tok[128];
-        int k = 0;
-        while (*p && !isspace((unsigned char)*p) && *p != ',' && k < 127) {
-          char c = *p++;
-          tok[k++] = (c == 'D' || c == 'd') ? 'e' : c;
+      const int k = line_values(ls_, le_, out + got, want - got);
+      if (k < 0) return false;
+      got += k;
+    }
+    return true;
+  }
+  // `rows` reads of `want` values each (row r into out[r * want ...]).  When
+  // every one of the next `rows` records holds at least `want` values, each
+  // read is exactly one record and the records are parsed on several
+  // threads; otherwise the reads run one after the other.
+  bool values_rows(double *out, int want, int rows) { return rows_parallel(out, want, rows); }
+  bool ints_rows(int *out, int want, int rows) { return rows_parallel(out, want, rows); }
+  // integers: plain digit tokens are converted directly; a record holding
+  // anything else is read through values()
+  bool ints(int *out, int want) {
+    const char *save_p = p_;
+    int got = 0;
+    while (got < want) {
+      if (!next_line()) return false;
+      const char *p = ls_;
+      bool plain = true;
+      while (p < le_ && got < want) {
+        while (p < le_ && sep(*p)) ++p;
+        if (p >= le_) break;
+        bool neg = false;
+        if (*p == '-' || *p == '+') neg = *p++ == '-';
+        const char *d0 = p;
+        long v = 0;
+        while (p < le_ && *p >= '0' && *p <= '9' && p - d0 < 9) v = v * 10 + (*p++ - '0');
+        if (p == d0 || (p < le_ && !sep(*p))) {
+          plain = false;
+          break;
         }
-        tok[k] = 0;
-        long rep = 1;
-        const char *num = tok;
-        if (char *star = strchr(tok, '*')) {
-          *star = 0;
-          rep = strtol(tok, nullptr, 10);
-          num = star + 1;
-          if (rep <= 0) return false;
-        }
-        char *end = nullptr;
-        double v = strtod(num, &end);
-        if (end == num) return false;
-        for (long r = 0; r < rep && got < want; ++r) out[got++] = v;
+        out[got++] = (int)(neg ? -v : v);
+      }
+      if (!plain) {  // repeat counts, decimals, exponents: the general reader
+        p_ = save_p;
+        buf_.resize(want);
+        if (!values(buf_.data(), want)) return false;
+        for (int i = 0; i < want; ++i) out[i] = (int)buf_[i];
+        return true;
       }
     }
     return true;
   }
-  bool ints(int *out, int want) {
-    buf_.resize(want);
-    if (!values(buf_.data(), want)) return false;
-    for (int i = 0; i < want; ++i) out[i] = (int)buf_[i];
-    return true;
-  }
 
  private:
-  bool next_line() { return getline(&line_, &cap_, f_) >= 0; }
-  FILE *f_;
-  char *line_ = nullptr;
-  size_t cap_ = 0;
+  bool next_line() {
+    if (p_ >= e_) return false;
+    ls_ = p_;
+    const char *nl = static_cast<const char *>(memchr(p_, '\n', e_ - p_));
+    le_ = nl ? nl : e_;
+    p_ = nl ? nl + 1 : e_;
+    return true;
+  }
+  static bool sep(char c) { return c == ' ' || c == ',' || (c >= '\t' && c <= '\r'); }
+  // up to `want` values of the record [p, e); the count, or -1 on a bad token
+  static int line_values(const char *p, const char *e, double *out, int want) {
+    int got = 0;
+    while (p < e && got < want) {
+      while (p < e && sep(*p)) ++p;
+      if (p >= e) break;
+      const char *t = p;
+      while (p < e && !sep(*p)) ++p;
+      long rep = 1;
+      const char *num = t;
+      for (const char *q = t; q < p; ++q)
+        if (*q == '*') {
+          rep = 0;
+          for (const char *d = t; d < q; ++d) {
+            if (*d < '0' || *d > '9') return -1;
+            rep = rep * 10 + (*d - '0');
+          }
+          if (rep <= 0) return -1;
+          num = q + 1;
+          break;
+        }
+      double v;
+      if (!number(num, p, v)) return -1;
+      for (long r = 0; r < rep && got < want; ++r) out[got++] = v;
+    }
+    return got;
+  }
+  static int line_values(const char *p, const char *e, int *out, int want) {
+    int got = 0;
+    while (p < e && got < want) {
+      while (p < e && sep(*p)) ++p;
+      if (p >= e) break;
+      bool neg = false;
+      const char *t = p;
+      if (*p == '-' || *p == '+') neg = *p++ == '-';
+      const char *d0 = p;
+      long v = 0;
+      while (p < e && *p >= '0' && *p <= '9' && p - d0 < 9) v = v * 10 + (*p++ - '0');
+      if (p == d0 || (p < e && !sep(*p))) {  // not a plain integer: general parse of the rest
+        double tmp[kMaxLine];
+        const int k = line_values(t, e, tmp, std::min(want - got, kMaxLine));
+        if (k < 0) return -1;
+        for (int i = 0; i < k; ++i) out[got++] = (int)tmp[i];
+        return got;
+      }
+      out[got++] = (int)(neg ? -v : v);
+    }
+    return got;
+  }
+  template <typename T>
+  bool rows_parallel(T *out, int want, int rows) {
+    const char *start = p_;
+    std::vector<const char *> ls(rows), le(rows);
+    bool enough = true;
+    for (int r = 0; r < rows; ++r) {
+      if (!next_line()) {
+        enough = false;
+        break;
+      }
+      ls[r] = ls_;
+      le[r] = le_;
+    }
+    bool regular = enough && want <= kMaxLine;
+    if (regular) {
+      const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), rows / 2048));
+      std::vector<char> ok(nt, 1);
+      auto work = [&](int t) {
+        const int r0 = (int)((long)rows * t / nt), r1 = (int)((long)rows * (t + 1) / nt);
+        for (int r = r0; r < r1; ++r)
+          if (line_values(ls[r], le[r], out + (size_t)r * want, want) != want) {
+            ok[t] = 0;
+            return;
+          }
+      };
+      std::vector<std::thread> th;
+      for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+      work(0);
+      for (auto &x : th) x.join();
+      for (char c : ok) regular = regular && c;
+    }
+    if (regular) return true;
+    p_ = start;  // records shorter than a read: sequential list-directed reads
+    for (int r = 0; r < rows; ++r)
+      if (!read_one(out + (size_t)r * want, want)) return false;
+    return true;
+  }
+  bool read_one(double *out, int want) { return values(out, want); }
+  bool read_one(int *out, int want) { return ints(out, want); }
+  static bool number(const char *s, const char *e, double &v) {
+    static const double p10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                   1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+    const char *q = s;
+    bool neg = false;
+    if (q < e && (*q == '+' || *q == '-')) neg = *q++ == '-';
+    unsigned long long m = 0;
+    int scale = 0;
+    bool any = false, exact = true;
+    for (; q < e && *q >= '0' && *q <= '9'; ++q, any = true)
+      if (m < (1ull << 53) / 10) {
+        m = m * 10 + (*q - '0');
+      } else {
+        exact = false;
+      }
+    if (q < e && *q == '.') {
+      ++q;
+      for (; q < e && *q >= '0' && *q <= '9'; ++q, any = true)
+        if (m < (1ull << 53) / 10) {
+          m = m * 10 + (*q - '0');
+          --scale;
+        } else {
+          exact = false;
+        }
+    }
+    if (any && q < e && (*q == 'e' || *q == 'E' || *q == 'd' || *q == 'D')) {
+      ++q;
+      bool eneg = false;
+      if (q < e && (*q == '+' || *q == '-')) eneg = *q++ == '-';
+      int x = 0;
+      bool ed = false;
+      for (; q < e && *q >= '0' && *q <= '9'; ++q, ed = true)
+        if (x < 10000) x = x * 10 + (*q - '0');
+      if (!ed) exact = false;
+      scale += eneg ? -x : x;
+    }
+    if (any && exact && q == e && scale >= -22 && scale <= 22) {
+      const double d = (double)m;
+      v = scale < 0 ? d / p10[-scale] : d * p10[scale];
+      if (neg) v = -v;
+      return true;
+    }
+    // general path: strtod on a copy with Fortran 'D' exponents as 'e'
+    char tok[128];
+    const long n = std::min<long>(e - s, 127);
+    for (long k = 0; k < n; ++k) tok[k] = (s[k] == 'D' || s[k] == 'd') ? 'e' : s[k];
+    tok[n] = 0;
+    char *end = nullptr;
+    v = strtod(tok, &end);
+    return end != tok;
+  }
+  std::vector<char> b_;
+  const char *p_, *e_;
+  const char *ls_ = nullptr, *le_ = nullptr;
   std::vector<double> buf_;
 };
 
 constexpr int kMaxN12 = 8;    // mod_inputloader.F90:65
 constexpr int kMaxPgp = 120;  // mod_inputloader.F90:67
 
-// Exact bond-distance layers 1..depth from every row of `adj` (BFS).
+// Exact bond-distance layers 1..depth from every row of `adj` (BFS).  Rows
+// are independent: ranges of rows run on several threads and their pieces
+// are joined in row order.
 void distance_layers(const Csr &adj, int depth, Csr *layers) {
-  int n = adj.n;
-  std::vector<int> dist(n, -1), touched;
+  const int n = adj.n;
+  const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), n / 4096));
+  struct Piece {
+    std::vector<int> ci[4];
+    std::vector<int> len[4];
+  };
+  std::vector<Piece> pieces(nt);
+  auto work = [&](int t) {
+    const int r0 = (int)((long)n * t / nt), r1 = (int)((long)n * (t + 1) / nt);
+    Piece &pc = pieces[t];
+    std::vector<int> dist(n, -1), touched;
+    std::vector<std::vector<int>> rows(depth);
+    std::deque<int> q;
+    for (int s = r0; s < r1; ++s) {
+      for (auto &r : rows) r.clear();
+      q.assign(1, s);
+      dist[s] = 0;
+      touched.assign(1, s);
+      while (!q.empty()) {
+        int a = q.front();
+        q.pop_front();
+        if (dist[a] == depth) continue;
+        for (int k = adj.ri[a]; k < adj.ri[a + 1]; ++k) {
+          int b = adj.ci[k];
+          if (dist[b] >= 0) continue;
+          dist[b] = dist[a] + 1;
+          touched.push_back(b);
+          rows[dist[b] - 1].push_back(b);
+          q.push_back(b);
+        }
+      }
+      for (int l = 0; l < depth; ++l) {
+        std::sort(rows[l].begin(), rows[l].end());
+        pc.ci[l].insert(pc.ci[l].end(), rows[l].begin(), rows[l].end());
+        pc.len[l].push_back((int)rows[l].size());
+      }
+      for (int x : touched) dist[x] = -1;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto &x : th) x.join();
   for (int l = 0; l < depth; ++l) {
     layers[l].n = n;
     layers[l].ri.assign(n + 1, 0);
     layers[l].ci.clear();
-  }
-  std::vector<std::vector<int>> rows(depth);
-  for (int s = 0; s < n; ++s) {
-    for (auto &r : rows) r.clear();
-    std::deque<int> q{s};
-    dist[s] = 0;
-    touched.assign(1, s);
-    while (!q.empty()) {
-      int a = q.front();
-      q.pop_front();
-      if (dist[a] == depth) continue;
-      for (int k = adj.ri[a]; k < adj.ri[a + 1]; ++k) {
-        int b = adj.ci[k];
-        if (dist[b] >= 0) continue;
-        dist[b] = dist[a] + 1;
-        touched.push_back(b);
-        rows[dist[b] - 1].push_back(b);
-        q.push_back(b);
+    int row = 0;
+    for (auto &pc : pieces) {
+      layers[l].ci.insert(layers[l].ci.end(), pc.ci[l].begin(), pc.ci[l].end());
+      for (int len : pc.len[l]) {
+        layers[l].ri[row + 1] = layers[l].ri[row] + len;
+        ++row;
       }
     }
-    for (int l = 0; l < depth; ++l) {
-      std::sort(rows[l].begin(), rows[l].end());
-      layers[l].ci.insert(layers[l].ci.end(), rows[l].begin(), rows[l].end());
-      layers[l].ri[s + 1] = (int)layers[l].ci.size();
-    }
-    for (int t : touched) dist[t] = -1;
   }
 }
 
@@ -135,15 +325,28 @@ int layer_of(const Csr *layers, int nlev, int i, int j) {
 }  // namespace
 
 bool read_mmp(const std::string &path, HostModel &m, std::string &err) {
-  FILE *f = fopen(path.c_str(), "r");
+  FILE *f = fopen(path.c_str(), "rb");
   if (!f) {
     err = "Input file '" + path + "' does not exist.";
     return false;
   }
-  ListReader r(f);
+  std::vector<char> text;
+  {
+    long size = -1;
+    if (fseek(f, 0, SEEK_END) == 0) size = ftell(f);
+    if (size >= 0 && fseek(f, 0, SEEK_SET) == 0) {
+      text.resize((size_t)size);
+      text.resize(fread(text.data(), 1, text.size(), f));
+    } else {  // not seekable: read in chunks
+      char chunk[1 << 16];
+      size_t got;
+      while ((got = fread(chunk, 1, sizeof chunk, f)) > 0) text.insert(text.end(), chunk, chunk + got);
+    }
+    fclose(f);
+  }
+  ListReader r(std::move(text));
   auto fail = [&](const char *what) {
     err = std::string("error while reading MMP file '") + path + "': " + what;
-    fclose(f);
     return false;
   };
   double v[4];
@@ -151,7 +354,6 @@ bool read_mmp(const std::string &path, HostModel &m, std::string &err) {
   int rev = (int)v[0];
   if (rev != 2 && rev != 3) {
     err = "MMP file is only supported with version 2 or 3.";
-    fclose(f);
     return false;
   }
   if (!r.skip(2) || !r.values(v, 1)) return fail("ff_type");
@@ -171,13 +373,10 @@ bool read_mmp(const std::string &path, HostModel &m, std::string &err) {
   m.q.resize((size_t)m.ld_cart * mm);
   std::vector<double> pol(mm);
   if (!r.skip(mm + 1)) return fail("atomic numbers");
-  for (int i = 0; i < mm; ++i)
-    if (!r.values(&m.cmm[3 * (size_t)i], 3)) return fail("coordinates");
+  if (!r.values_rows(m.cmm.data(), 3, mm)) return fail("coordinates");
   if (!r.skip(mm)) return fail("residues");
-  for (int i = 0; i < mm; ++i)
-    if (!r.values(&m.q[(size_t)m.ld_cart * i], m.ld_cart)) return fail("multipoles");
-  for (int i = 0; i < mm; ++i)
-    if (!r.values(&pol[i], 1)) return fail("polarizabilities");
+  if (!r.values_rows(m.q.data(), m.ld_cart, mm)) return fail("multipoles");
+  if (!r.values_rows(pol.data(), 1, mm)) return fail("polarizabilities");
   for (auto &c : m.cmm) c *= kAng2Au;
   for (int i = 0; i < mm; ++i)
     if (pol[i] > 1e-8) {
@@ -209,9 +408,10 @@ bool read_mmp(const std::string &path, HostModel &m, std::string &err) {
   adj.n = mm;
   adj.ri.assign(mm + 1, 0);
   adj.ci.clear();
-  int row[kMaxPgp];
+  std::vector<int> conn12((size_t)kMaxN12 * mm);
+  if (!r.ints_rows(conn12.data(), kMaxN12, mm)) return fail("connectivity");
   for (int i = 0; i < mm; ++i) {
-    if (!r.ints(row, kMaxN12)) return fail("connectivity");
+    const int *row = &conn12[(size_t)kMaxN12 * i];
     std::vector<int> nb;
     for (int k = 0; k < kMaxN12; ++k)
       if (row[k] != 0) {
@@ -230,8 +430,7 @@ bool read_mmp(const std::string &path, HostModel &m, std::string &err) {
   if (m.amoeba) {
     // polarization groups: first listing assigns the group id (polgroup11_to_mm2pg)
     std::vector<int> lists((size_t)kMaxPgp * mm);
-    for (int i = 0; i < mm; ++i)
-      if (!r.ints(&lists[(size_t)kMaxPgp * i], kMaxPgp)) return fail("polarization groups");
+    if (!r.ints_rows(lists.data(), kMaxPgp, mm)) return fail("polarization groups");
     std::fill(m.grp.begin(), m.grp.end(), -1);
     int g = 0;
     for (int i = 0; i < mm; ++i) {
@@ -247,9 +446,10 @@ bool read_mmp(const std::string &path, HostModel &m, std::string &err) {
     for (int i = 0; i < mm; ++i)
       if (m.grp[i] < 0) return fail("atom without polarization group");
     m.ngrp = g;
+    std::vector<int> frames(4 * (size_t)mm);
+    if (!r.ints_rows(frames.data(), 4, mm)) return fail("multipole frames");
     for (int i = 0; i < mm; ++i) {
-      int t[4];
-      if (!r.ints(t, 4)) return fail("multipole frames");
+      const int *t = &frames[4 * (size_t)i];
       m.frame[i] = t[0];
       m.iz[i] = t[1] - 1;
       m.ix[i] = t[2] - 1;
@@ -261,7 +461,6 @@ bool read_mmp(const std::string &path, HostModel &m, std::string &err) {
   } else {
     m.damping.assign(m.npol, 0.0);
   }
-  fclose(f);
   return true;
 }
 

@@ -18,7 +18,7 @@ from oracle.oracle import OracleSystem
 def harness(tmp_path_factory):
     exe = str(tmp_path_factory.mktemp("host") / "dump_setup")
     cuda_inc = "/usr/local/cuda/include"
-    subprocess.run(["g++", "-O1", "-std=c++17", "-I", cuda_inc, "-o", exe,
+    subprocess.run(["g++", "-O1", "-std=c++17", "-pthread", "-I", cuda_inc, "-o", exe,
                     os.path.join(ROOT, "tests", "host", "dump_setup.cpp"),
                     os.path.join(ROOT, "openmmpol_gb300", "csrc", "setup.cpp")], check=True)
     return exe
@@ -97,3 +97,35 @@ def test_host_reader_rejects_bad_revision(harness, tmp_path):
     p.write_text("7\n")
     r = subprocess.run([harness, str(p)], capture_output=True, text=True)
     assert r.returncode == 1 and "version 2 or 3" in r.stdout
+
+
+def test_host_reader_list_directed_forms(harness, tmp_path):
+    # the same system written with list-directed variations: a record split
+    # over two lines, commas, D exponents, r*c repeat counts, extra values
+    # after a read; the reader takes its general (sequential) path for these
+    # and must give exactly what the plain file gives
+    w = synth.water_cluster(40, seed=9)
+    plain = synth.write_mmp(str(tmp_path / "plain.mmp"), w)
+    lines = open(plain).read().split("\n")
+    mm = int(lines[22])
+    base = 24 + mm  # first coordinate record
+    c, mp, pol, conn, grp = base, base + 2 * mm, base + 3 * mm, base + 4 * mm, base + 5 * mm
+    x, y, z = lines[c + 5].split()
+    lines[c + 5] = x + " " + y
+    lines.insert(c + 6, "  " + z)  # atom 5 continues on the next record
+    off = 1
+    lines[c + 7 + off - 1] = ", ".join(lines[c + 7 + off - 1].split())
+    q = [float(v) for v in lines[mp + 3 + off].split()]
+    lines[mp + 3 + off] = " ".join(("%.17E" % v).replace("E", "D") for v in q)
+    lines[pol + 2 + off] = lines[pol + 2 + off] + " 9.9 trailing"
+    t = lines[conn + 7 + off].split()
+    nz = [v for v in t if v != "0"]
+    lines[conn + 7 + off] = " ".join(nz + ["%d*0" % (len(t) - len(nz))])
+    t = lines[grp + 4 + off].split()
+    nz = [v for v in t if v != "0"]
+    lines[grp + 4 + off] = " ".join(nz + ["%d*0" % (len(t) - len(nz))])
+    varied = tmp_path / "varied.mmp"
+    varied.write_text("\n".join(lines))
+    a = subprocess.run([harness, plain], capture_output=True, text=True, check=True).stdout
+    b = subprocess.run([harness, str(varied)], capture_output=True, text=True, check=True).stdout
+    assert a == b

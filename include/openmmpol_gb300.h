@@ -237,6 +237,10 @@ int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
  * (default).  The FP64 solver and the outer convergence test always use the
  * reference's diagonal. */
 int32_t ommp_gpu_set_inner_preconditioner(OMMP_SYSTEM_PRT s, int32_t mode);
+/* runs of the block-Jacobi inner preconditioner: at most max_sites (1..32)
+ * consecutive polarizable sites, each within link_bohr of an earlier site of
+ * its run (defaults 8 and 3.0); rebuilt at once and at every geometry */
+int32_t ommp_gpu_set_inner_blocks(OMMP_SYSTEM_PRT s, int32_t max_sites, double link_bohr);
 /* forget the last dipoles as a starting guess */
 void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s);
 /* capture the inner FP32 iteration as a CUDA graph (default on) */

@@ -242,6 +242,11 @@ class OMMPSystem:
         m = {"diagonal": 0, "block": 1}.get(mode, mode)
         _check(self._L.ommp_gpu_set_inner_preconditioner(self._h, int(m)))
 
+    def set_inner_blocks(self, max_sites: int, link_bohr: float) -> None:
+        """Runs of the block-Jacobi inner preconditioner: at most max_sites
+        consecutive polarizable sites, each within link_bohr of an earlier one."""
+        _check(self._L.ommp_gpu_set_inner_blocks(self._h, int(max_sites), float(link_bohr)))
+
     def set_fp32_kernel(self, mode) -> None:
         """'auto' (autotuned) | 'pairwise' (kernel 1) | 'tiled' (kernel 2)."""
         m = {"auto": 0, "pairwise": 1, "tiled": 2}.get(mode, mode)

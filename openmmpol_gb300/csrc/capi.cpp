@@ -209,6 +209,9 @@ int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode) { return S(s)-
 int32_t ommp_gpu_set_inner_preconditioner(OMMP_SYSTEM_PRT s, int32_t mode) {
   return S(s)->set_inner_preconditioner(mode);
 }
+int32_t ommp_gpu_set_inner_blocks(OMMP_SYSTEM_PRT s, int32_t max_sites, double link_bohr) {
+  return S(s)->set_inner_blocks(max_sites, link_bohr);
+}
 void ommp_gpu_set_use_graphs(OMMP_SYSTEM_PRT s, int32_t on) { S(s)->set_use_graphs(on != 0); }
 int32_t ommp_gpu_set_external_fields_batch(OMMP_SYSTEM_PRT s, int32_t nfields, const double *fields, double *ipd_out,
                                            double *energies) {

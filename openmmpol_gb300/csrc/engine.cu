@@ -290,33 +290,48 @@ int System::upload_geometry() {
   cudaMemcpyAsync(d_.mm_q, m.q.data(), m.q.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
   // the host vectors above die at return: wait for the copies
   // block-Jacobi preconditioner of the FP32 inner solver (geometry-dependent)
-  {
-    std::vector<int> info;
-    std::vector<float> minv;
-    build_block_jacobi(m, d2d_pairs_, d_.damp_thr, info, minv);
-    cudaStreamSynchronize(st_);
-    // a captured inner iteration holds the preconditioner's device pointers:
-    // drop it before the buffers are replaced (it is captured again)
-    for (Workspace *w : {&ws_, &wsb_}) {
-      if (w->graph) cudaGraphExecDestroy(w->graph);
-      w->graph = nullptr;
-      w->graph_ncol = -1;
-    }
-    if (blk_info_) cudaFree(blk_info_);
-    if (blk_minv_) cudaFree(blk_minv_);
-    blk_info_ = nullptr;
-    blk_minv_ = nullptr;
-    if (n > 0) {
-      if (dalloc(blk_info_, (size_t)n) || dalloc(blk_minv_, minv.size())) {
-        set_last_error("out of device memory for the block preconditioner");
-        return kErrMemory;
-      }
-      cudaMemcpyAsync(blk_info_, info.data(), info.size() * sizeof(int), cudaMemcpyHostToDevice, st_);
-      cudaMemcpyAsync(blk_minv_, minv.data(), minv.size() * sizeof(float), cudaMemcpyHostToDevice, st_);
-    }
-    // the host vectors die at return: the synchronisation below covers the copies
-  }
+  int bst = build_blocks();
+  if (bst) return bst;
   return check(cudaStreamSynchronize(st_), "geometry upload");
+}
+
+int System::build_blocks() {
+  const int n = m_.npol;
+  std::vector<int> info;
+  std::vector<float> minv;
+  build_block_jacobi(m_, d2d_pairs_, d_.damp_thr, blk_max_, blk_link_, info, minv);
+  cudaStreamSynchronize(st_);
+  // a captured inner iteration holds the preconditioner's device pointers:
+  // drop it before the buffers are replaced (it is captured again)
+  for (Workspace *w : {&ws_, &wsb_}) {
+    if (w->graph) cudaGraphExecDestroy(w->graph);
+    w->graph = nullptr;
+    w->graph_ncol = -1;
+  }
+  if (blk_info_) cudaFree(blk_info_);
+  if (blk_minv_) cudaFree(blk_minv_);
+  blk_info_ = nullptr;
+  blk_minv_ = nullptr;
+  if (n > 0) {
+    if (dalloc(blk_info_, (size_t)n) || dalloc(blk_minv_, minv.size())) {
+      set_last_error("out of device memory for the block preconditioner");
+      return kErrMemory;
+    }
+    cudaMemcpyAsync(blk_info_, info.data(), info.size() * sizeof(int), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(blk_minv_, minv.data(), minv.size() * sizeof(float), cudaMemcpyHostToDevice, st_);
+  }
+  // the host vectors die at return
+  return check(cudaStreamSynchronize(st_), "block preconditioner upload");
+}
+
+int System::set_inner_blocks(int max_sites, double link_bohr) {
+  if (max_sites < 1 || max_sites > kMaxBlockLimit || !(link_bohr >= 0.0)) {
+    set_last_error("inner blocks: 1 <= max_sites <= 32 and link distance >= 0 bohr");
+    return kErrBadArg;
+  }
+  blk_max_ = max_sites;
+  blk_link_ = link_bohr;
+  return build_blocks();
 }
 
 int System::sync() {

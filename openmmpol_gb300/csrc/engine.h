@@ -104,6 +104,9 @@ class System {
   int set_fp64_kernel(int mode);
   int set_fp32_kernel(int mode);
   int set_inner_preconditioner(int mode);
+  // runs of the block-Jacobi inner preconditioner: at most max_sites
+  // consecutive polarizable sites, each within link_bohr of an earlier one
+  int set_inner_blocks(int max_sites, double link_bohr);
   int matvec_residual(int ncol, const double *x, double *y);
   int ensure_ds_scratch();
   int precision() const { return precision_; }
@@ -188,6 +191,9 @@ class System {
   int4 *blk_info_ = nullptr;   // block-Jacobi preconditioner (build_block_jacobi)
   float *blk_minv_ = nullptr;
   int inner_precond_ = 1;       // FP32 inner solver: 0 diagonal, 1 block Jacobi
+  int blk_max_ = kMaxBlock;
+  double blk_link_ = kBlockLinkBohr;
+  int build_blocks();
   double *ext_buf_ = nullptr;  // external points: coordinates, partials, output, dipoles
   size_t ext_cap_ = 0;
   double *ds_scratch_ = nullptr;  // split partials of the double-single kernels

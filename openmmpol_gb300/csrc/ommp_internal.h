@@ -82,7 +82,8 @@ void build_d2d_pairs(const HostModel &m, ScaledPairs &out);
 // inverse of each run's diagonal block of T, (3 size) x (3 size) row-major.
 constexpr int kMaxBlock = 8;
 constexpr double kBlockLinkBohr = 3.0;
-void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_thr, std::vector<int> &info,
-                        std::vector<float> &minv);
+constexpr int kMaxBlockLimit = 32;
+void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_thr, int max_sites,
+                        double link_bohr, std::vector<int> &info, std::vector<float> &minv);
 
 }  // namespace ommp

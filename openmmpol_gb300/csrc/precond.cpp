@@ -82,12 +82,12 @@ bool invert(std::vector<double> &a, int dim) {
 
 }  // namespace
 
-void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_thr, std::vector<int> &info,
-                        std::vector<float> &minv) {
+void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_thr, int max_sites,
+                        double link_bohr, std::vector<int> &info, std::vector<float> &minv) {
   const int n = m.npol;
   info.assign(4 * (size_t)n, 0);
   minv.clear();
-  const double link2 = kBlockLinkBohr * kBlockLinkBohr;
+  const double link2 = link_bohr * link_bohr;
   auto pos = [&](int j) { return &m.cmm[3 * (size_t)m.polar_mm[j]]; };
   auto dist2 = [&](int i, int j) {
     const double *a = pos(i), *b = pos(j);
@@ -99,7 +99,7 @@ void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_
   size_t total = 0;
   for (int start = 0; start < n;) {
     int end = start + 1;
-    while (end < n && end - start < kMaxBlock) {
+    while (end < n && end - start < max_sites) {
       bool linked = false;
       for (int i = start; i < end && !linked; ++i) linked = dist2(i, end) < link2;
       if (!linked) break;

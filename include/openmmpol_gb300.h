@@ -180,9 +180,15 @@ double *ommp_qm_helper_get_cqm(OMMP_QM_HELPER_PRT qm);
 int32_t ommp_qm_helper_get_npol(OMMP_QM_HELPER_PRT qm);
 int32_t ommp_qm_helper_get_nmm(OMMP_QM_HELPER_PRT qm);
 int32_t ommp_qm_helper_get_qm_atoms(OMMP_QM_HELPER_PRT qm);
-/* include/openmmpol.h:153-155 ; src/mod_c_interface.F90:1843-1879.  The fast
- * multipole method is not part of this library: enabling it logs a warning
- * and the direct sums are kept; ommp_use_fmm always returns false. */
+/* include/openmmpol.h:153-155 ; src/mod_c_interface.F90:1843-1879.  FMM
+ * switch of the FP64 dipole-field products (T.mu of the FP64 solvers and of
+ * the strict mixed mode's refinement residual): a uniform octree with
+ * Cartesian expansions of order 8 (the reference's default maximum angular
+ * momentum), near pairs (neighbouring leaves, every damped pair among them)
+ * direct.  The reference switches it on by itself above 1,000 atoms; here the
+ * direct sums stay the default and the host asks for the FMM.  The
+ * permanent-multipole field, the FP32 inner products and the double-single
+ * products stay direct. */
 void ommp_enable_fmm(OMMP_SYSTEM_PRT s);
 void ommp_disable_fmm(OMMP_SYSTEM_PRT s);
 bool ommp_use_fmm(OMMP_SYSTEM_PRT s);
@@ -202,6 +208,8 @@ int32_t ommp_gpu_set_external_field_device(OMMP_SYSTEM_PRT s, const double *ext_
 int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *energy);
 /* ommp_polelec_geomgrad returning a status instead of stopping the process */
 int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
+/* FMM on (on != 0) or off, with expansion order 2..12 */
+int32_t ommp_gpu_set_fmm(OMMP_SYSTEM_PRT s, int32_t on, int32_t order);
 /* QM helper calls returning a status instead of stopping the process */
 int32_t ommp_gpu_init_qm_helper(int32_t n, const double *cqm, const double *qqm, const int32_t *zqm,
                                 OMMP_QM_HELPER_PRT *out);

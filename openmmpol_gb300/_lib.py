@@ -72,6 +72,7 @@ SIGNATURES = {
     "ommp_field_pol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
     "ommp_polelec_geomgrad": (None, [_vp, _dp]),
     "ommp_gpu_polelec_geomgrad": (C.c_int32, [_vp, _dp]),
+    "ommp_gpu_set_fmm": (C.c_int32, [_vp, C.c_int32, C.c_int32]),
     "ommp_init_qm_helper": (_vp, [C.c_int32, _dp, _dp, _ip]),
     "ommp_gpu_init_qm_helper": (C.c_int32, [C.c_int32, _dp, _dp, _ip, C.POINTER(_vp)]),
     "ommp_terminate_qm_helper": (None, [_vp]),

@@ -189,16 +189,10 @@ int32_t ommp_qm_helper_get_npol(OMMP_QM_HELPER_PRT qm) { return Q(qm)->npol(); }
 int32_t ommp_qm_helper_get_nmm(OMMP_QM_HELPER_PRT qm) { return Q(qm)->nmm(); }
 int32_t ommp_qm_helper_get_qm_atoms(OMMP_QM_HELPER_PRT qm) { return Q(qm)->qm_atoms(); }
 
-void ommp_enable_fmm(OMMP_SYSTEM_PRT s) {
-  (void)s;
-  ommp::log_msg(ommp::kVerbLow, nullptr,
-                "The fast multipole method is not available in this library; the direct sums are used.");
-}
-void ommp_disable_fmm(OMMP_SYSTEM_PRT s) { (void)s; }
-bool ommp_use_fmm(OMMP_SYSTEM_PRT s) {
-  (void)s;
-  return false;
-}
+void ommp_enable_fmm(OMMP_SYSTEM_PRT s) { fatal_if(S(s)->set_fmm(true, S(s)->fmm_order())); }
+void ommp_disable_fmm(OMMP_SYSTEM_PRT s) { fatal_if(S(s)->set_fmm(false, S(s)->fmm_order())); }
+bool ommp_use_fmm(OMMP_SYSTEM_PRT s) { return S(s)->fmm_on(); }
+int32_t ommp_gpu_set_fmm(OMMP_SYSTEM_PRT s, int32_t on, int32_t order) { return S(s)->set_fmm(on != 0, order); }
 
 const char *ommp_gpu_last_error(void) { return ommp::last_error(); }
 void ommp_gpu_set_solver_tol(OMMP_SYSTEM_PRT s, double tol) { S(s)->set_tol(tol); }

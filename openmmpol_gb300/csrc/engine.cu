@@ -59,6 +59,7 @@ System::~System() {
   if (flush_buf_) cudaFree(flush_buf_);
   if (sym_scratch_) cudaFree(sym_scratch_);
   free_grad_state(grad_);
+  free_fmm_state(fmm_);
   kt_resolve();
   for (auto &e : kfree_) {
     cudaEventDestroy(e.a);
@@ -289,6 +290,7 @@ int System::upload_geometry() {
   cudaMemcpyAsync(d_.mm_a, ma.data(), mm * sizeof(double), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(d_.mm_q, m.q.data(), m.q.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
   // the host vectors above die at return: wait for the copies
+  fmm_invalidate();  // the tree follows the geometry
   // block-Jacobi preconditioner of the FP32 inner solver (geometry-dependent)
   int bst = build_blocks();
   if (bst) return bst;
@@ -483,7 +485,22 @@ int System::ensure_tmat() {
 int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag) {
   if (matv == kMatvIncore && tmat_ok_) {
     gpu::launch_gemv(3 * d_.n, tmat_, x, y, dodiag, d_.pol_alpha, ncol, st_);
-  } else {
+    return kOk;
+  }
+  if (fmm_on_) {
+    int st = fmm_prepare();
+    if (st) return st;
+    if (fmm_tree()) {  // else too small for a tree: the direct sums below
+      KEv e;
+      if (ktime_on_) e = kt_begin(0, ncol);
+      st = fmm_tmu(ncol, x, y, dodiag);
+      if (ktime_on_) kt_end(e);
+      if (st) return st;
+      stats_.f64_matvecs += 1;
+      return kOk;
+    }
+  }
+  {
     bool sym = fp64_kernel_ == 2 || (fp64_kernel_ == 0 && d_.n >= 2048);
     if (sym && !sym_scratch_) {
       if (dalloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 2))) {
@@ -593,7 +610,8 @@ int System::diis64(int matv, const double *rhs, double *x, int set) {
   stats_.hist[set].clear();
   stats_.iters[set] = 0;
   for (int it = 1; it <= maxiter_; ++it) {
-    matvec64(matv, 1, x, y, false);
+    int mst = matvec64(matv, 1, x, y, false);
+    if (mst) return mst;
     gpu::launch_residual(nv, rhs, y, y, st_);
     gpu::launch_scale_by_alpha(1, n, d_.pol_alpha, y, xnew, st_);
     if (nd > 0) {
@@ -928,7 +946,8 @@ int System::tmatvec(const double *xh, double *yh, int nrhs, bool dodiag, int mat
     if (st) return st;
   }
   cudaMemcpyAsync(p_, xh, nrhs * nv * sizeof(double), cudaMemcpyHostToDevice, st_);
-  matvec64(matv, nrhs, p_, h_, dodiag);
+  int mst = matvec64(matv, nrhs, p_, h_, dodiag);
+  if (mst) return mst;
   cudaMemcpyAsync(yh, h_, nrhs * nv * sizeof(double), cudaMemcpyDeviceToHost, st_);
   return check(cudaStreamSynchronize(st_), "tmatvec");
 }

@@ -46,9 +46,12 @@ struct Workspace {
   long long graph_kernels = 0;
 };
 
-// device data of the polarization gradient (grad.cu)
+// device data of the polarization gradient (grad.cu) and of the fast
+// multipole method (fmm.cu)
 struct GradState;
 void free_grad_state(GradState *g);
+struct FmmState;
+void free_fmm_state(FmmState *f);
 
 struct SolveStats {
   int iters[2] = {0, 0};
@@ -93,6 +96,10 @@ class System {
   int e_m2d(double *out_host);
   // geometric gradient of the polarization energy, out [mm][3] (overwritten)
   int polelec_geomgrad(double *grad_host);
+  // fast multipole method for the FP64 T.mu products (expansion order 2..12)
+  int set_fmm(bool on, int order);
+  bool fmm_on() const { return fmm_on_; }
+  int fmm_order() const { return fmm_order_; }
   void clear_guess() { ipd_use_guess_ = false; }
   void set_tol(double t) { tol_ = t; }
   void set_maxiter(int n) { maxiter_ = n; }
@@ -235,6 +242,13 @@ class System {
   void kt_end(KEv &e);
   void kt_resolve();
   GradState *grad_ = nullptr;
+  FmmState *fmm_ = nullptr;
+  bool fmm_on_ = false;
+  int fmm_order_ = 8;
+  int fmm_prepare();
+  void fmm_invalidate();
+  bool fmm_tree() const;  // the prepared FMM has a tree (else direct sums)
+  int fmm_tmu(int ncol, const double *x, double *y, bool dodiag);
   Workspace ws_;   // view of the default two-column buffers
   Workspace wsb_;  // batch buffers
   std::map<int, F32Shape> f32_tune_;  // columns -> tuned FP32 launch shape

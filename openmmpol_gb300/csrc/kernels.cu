@@ -1064,6 +1064,11 @@ static void tmu_finish(const DevSites &s, int nrhs, int nsplit, const T *partial
   }
 }
 
+void launch_tmu_finish64(const DevSites &s, int nrhs, const double *partial, const double *x, bool dodiag,
+                         double *y, cudaStream_t st) {
+  tmu_finish<double>(s, nrhs, 1, partial, s.pol_pos, s.pol_a, x, dodiag, y, 2, st);
+}
+
 void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
                     int nsplit, cudaStream_t st) {
   if (s.n == 0) return;

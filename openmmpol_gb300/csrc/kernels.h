@@ -72,6 +72,10 @@ size_t tmu_scratch_doubles(const DevSites &s, int nrhs, int nsplit);
 int tmu_pick_split(const DevSites &s, int nrhs, int sm_count, bool fp32);
 void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag,
                     double *scratch, int nsplit, cudaStream_t st);
+// The finishing pass alone on a field partial [nrhs][n][3] (one split): the
+// u-scaled pair corrections, the sign and the 1/alpha diagonal
+void launch_tmu_finish64(const DevSites &s, int nrhs, const double *partial, const double *x, bool dodiag,
+                         double *y, cudaStream_t st);
 // Same product with each unordered pair evaluated once (deterministic
 // half-shell schedule); scratch of tmu_sym_scratch_doubles(s, nrhs_max).
 size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs);

@@ -106,7 +106,8 @@ int System::cg64_ws(Workspace &w, int matv, int ncol, const double *rhs, double 
   if (all_zero) {
     cudaMemcpyAsync(w.r, rhs, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
   } else {
-    matvec64(matv, ncol, x, w.z, true);
+    st = matvec64(matv, ncol, x, w.z, true);
+    if (st) return st;
     gpu::launch_residual(ncol * nv, rhs, w.z, w.r, st_);
   }
   gpu::launch_scale_by_alpha(ncol, n, d_.pol_alpha, w.r, w.z, st_);
@@ -126,7 +127,8 @@ int System::cg64_ws(Workspace &w, int matv, int ncol, const double *rhs, double 
   cudaMemcpyAsync(w.cols, w.cols_h, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
   double *hist = (set0 >= 0) ? w.hist : nullptr;
   for (int it = 1; it <= maxiter_; ++it) {
-    matvec64(matv, ncol, w.p, w.h, true);
+    st = matvec64(matv, ncol, w.p, w.h, true);
+    if (st) return st;
     gpu::launch_dots(ncol, nv, w.h, w.p, w.partial, st_);
     gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
     gpu::launch_cg_alpha(ncol, w.dots, w.cols, kEpsRp, st_);

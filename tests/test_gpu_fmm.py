@@ -1,0 +1,108 @@
+"""Fast multipole method for the FP64 T.mu products (ommp_enable_fmm;
+csrc/fmm.cu) against the direct sums.
+
+The expansions are Cartesian Taylor series of order p with the one-neighbour
+separation of a uniform octree, the reference's default order being 8: on
+water the far field then carries ~1e-3 relative error (about the accuracy of
+the reference's own FMM, whose 1ubq goldens agree with direct sums only at
+the 1e-3 level), falling with the order.  Tolerances: the product against the
+direct one 3e-3 (order 8) with the error shrinking with the order; solves
+against the direct solve 1e-3 in the dipoles, 1e-5 in the energy; the
+reference's FMM-produced 1ubq goldens at their own tolerance (atol 1e-3).
+"""
+import numpy as np
+import pytest
+
+from openmmpol_gb300 import OMMPSystem, set_verbose, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def quiet():
+    set_verbose(0)
+
+
+@pytest.fixture(scope="module")
+def water(tmp_path_factory):
+    w = synth.water_cluster(4000, seed=2)
+    return synth.write_mmp(str(tmp_path_factory.mktemp("fmm") / "w4k.mmp"), w)
+
+
+def test_fmm_product_converges_with_order(water):
+    g = OMMPSystem(water)
+    x = np.random.default_rng(0).standard_normal((2, g.pol_atoms, 3)) * 0.01
+    ref = g.tmatvec(x, dodiag=False)
+    errs = {}
+    for order in (4, 8, 12):
+        g.set_fmm(True, order)
+        assert g.use_fmm()
+        errs[order] = rel(g.tmatvec(x, dodiag=False), ref)
+    assert errs[8] < 3e-3
+    assert errs[12] < 0.5 * errs[8] < 0.5 * errs[4]
+    # the diagonal term is exact
+    g.set_fmm(True, 8)
+    d = g.tmatvec(x, dodiag=True) - g.tmatvec(x, dodiag=False)
+    g.set_fmm(False)
+    d0 = g.tmatvec(x, dodiag=True) - g.tmatvec(x, dodiag=False)
+    np.testing.assert_allclose(d, d0, rtol=1e-12, atol=1e-16)
+
+
+def test_fmm_product_is_deterministic(water):
+    g = OMMPSystem(water)
+    g.set_fmm(True, 8)
+    x = np.random.default_rng(1).standard_normal((g.pol_atoms, 3))
+    assert np.array_equal(g.tmatvec(x), g.tmatvec(x))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fmm_solve_against_direct(water, precision):
+    g = OMMPSystem(water)
+    g.set_precision(precision)
+    g.set_solver_tol(1e-9)
+    ef = synth.point_charge_field(g.cpol, g.cmm.mean(0) / 1.8897261245650, seed=5, all_sites_bohr=g.cmm)[0]
+    g.set_external_field(ef)
+    ref, e_ref = g.ipd.copy(), g.get_polelec_energy()
+    g.set_fmm(True, 8)
+    g.clear_guess()
+    g.set_external_field(ef)
+    assert rel(g.ipd, ref) < 1e-3
+    assert abs(g.get_polelec_energy() - e_ref) < 1e-5 * abs(e_ref)
+
+
+def test_fmm_follows_coordinate_updates(water):
+    g = OMMPSystem(water)
+    g.set_fmm(True, 8)
+    x = np.random.default_rng(2).standard_normal((g.pol_atoms, 3)) * 0.01
+    c = g.cmm + np.random.default_rng(3).normal(scale=0.05, size=(g.mm_atoms, 3))
+    g.tmatvec(x)
+    g.update_coordinates(c)
+    y = g.tmatvec(x, dodiag=False)
+    g.set_fmm(False)
+    assert rel(y, g.tmatvec(x, dodiag=False)) < 3e-3
+
+
+@pytest.mark.parametrize("case", ["1ubq_amoeba", "1ubq_wang"])
+def test_fmm_matches_reference_fmm_goldens(case, golden, golden_mmp):
+    g = OMMPSystem(golden_mmp[case])
+    g.set_fmm(True, 8)
+    for with_field in (0, 1):
+        ef = golden[case + "_ef1"] if with_field else np.zeros((g.pol_atoms, 3))
+        g.clear_guess()
+        g.set_external_field(ef)
+        ref = golden[f"{case}_ipd{with_field}"]
+        np.testing.assert_allclose(g.ipd.reshape(-1, 3), ref, rtol=1e-6, atol=float(golden[case + "_atol"]))
+        np.testing.assert_allclose(g.get_polelec_energy(), float(golden[f"{case}_ep{with_field}"]), rtol=1e-6,
+                                   atol=1e-3)
+
+
+def test_fmm_small_system_uses_direct_sums(golden_mmp):
+    g = OMMPSystem(golden_mmp["nma_amoeba"])
+    x = np.random.default_rng(4).standard_normal((g.pol_atoms, 3))
+    ref = g.tmatvec(x)
+    g.set_fmm(True, 8)
+    np.testing.assert_array_equal(g.tmatvec(x), ref)

@@ -55,6 +55,11 @@ struct FmmState {
   int4 *pairs = nullptr;       // M2L pairs: g, index of g + h in the 2p table, h, (-1)^|g|
   int *hoff = nullptr;         // [K + 1] first pair of each target term h
   double *dunit = nullptr;     // [343][KD] derivatives of 1/r to order p at unit cell offsets
+  // translation lists (M2M, L2L), grouped by target term: source term and
+  // packed |m| (bits 0-7) with the parities of m (bits 8-10), coefficient
+  int2 *mm_e = nullptr, *ll_e = nullptr;
+  double *mm_c = nullptr, *ll_c = nullptr;
+  int *mm_off = nullptr, *ll_off = nullptr;
   double *M = nullptr, *Lc = nullptr;  // [2][ncell][K]
   double *field = nullptr;     // [2][n][3]
   size_t field_n = 0;
@@ -63,7 +68,7 @@ struct FmmState {
 void free_fmm_state(FmmState *f) {
   if (!f) return;
   void *b[] = {f->cnt, f->leaf_start, f->perm, f->spos, f->sa, f->swa, f->terms, f->pairs, f->hoff, f->dunit,
-               f->M, f->Lc, f->field};
+               f->M, f->Lc, f->field, f->mm_e, f->ll_e, f->mm_c, f->ll_c, f->mm_off, f->ll_off};
   for (void *p : b)
     if (p) cudaFree(p);
   delete f;
@@ -89,7 +94,17 @@ struct FmmArgs {
   const double *dunit;
   double *M, *Lc;
   int KD;
+  const int2 *mm_e, *ll_e;
+  const double *mm_c, *ll_c;
+  const int *mm_off, *ll_off;
 };
+
+// sign of s^m for the child offset s = (b - 1/2) h_c per axis (bit b = 0:
+// negative component) and the parities packed in e.y bits 8-10
+__device__ __forceinline__ double child_sign(int packed, int bx, int by, int bz) {
+  const int neg = (((packed >> 8) & 1) & (bx ^ 1)) ^ (((packed >> 9) & 1) & (by ^ 1)) ^ (((packed >> 10) & 1) & (bz ^ 1));
+  return neg ? -1.0 : 1.0;
+}
 
 __device__ __forceinline__ void cell_xyz(int idx, int l, int &x, int &y, int &z) {
   const int n = 1 << l;
@@ -155,31 +170,31 @@ __global__ void __launch_bounds__(FT) k_fmm_p2m(FmmArgs a, const double *__restr
   }
 }
 
-// parents at level l - 1 from their children at level l
+// parents at level l - 1 from their children at level l:
+// M_g(parent) = sum_children sum_(k <= g) M_k(child) s^(g - k) / (g - k)!
 __global__ void __launch_bounds__(FT) k_fmm_m2m(FmmArgs a, int l) {
   const int pc = blockIdx.x, col = blockIdx.y;
   if (a.cnt[level_off(l - 1) + pc] == 0) return;
   int px, py, pz;
   cell_xyz(pc, l - 1, px, py, pz);
-  const double hc = a.h0 / (1 << l);
+  double hp[fmm::kMaxOrder + 1];  // (h_c / 2)^k
+  hp[0] = 1.0;
+  for (int k = 1; k <= a.p; ++k) hp[k] = hp[k - 1] * 0.5 * a.h0 / (1 << l);
   double acc[kMaxTermsPerThread];
   for (int j = 0; j < kMaxTermsPerThread; ++j) acc[j] = 0.0;
   for (int ch = 0; ch < 8; ++ch) {
-    const int dx = ch >> 2, dy = (ch >> 1) & 1, dz = ch & 1;
-    const int cc = cell_idx(l, 2 * px + dx, 2 * py + dy, 2 * pz + dz);
+    const int bx = ch >> 2, by = (ch >> 1) & 1, bz = ch & 1;
+    const int cc = cell_idx(l, 2 * px + bx, 2 * py + by, 2 * pz + bz);
     if (a.cnt[level_off(l) + cc] == 0) continue;
-    const double s[3] = {(dx - 0.5) * hc, (dy - 0.5) * hc, (dz - 0.5) * hc};
-    double sp[3][fmm::kMaxOrder + 1];
-    for (int d = 0; d < 3; ++d) fmm::scaled_powers(s[d], a.p, sp[d]);
     const double *Mc = a.M + ((size_t)col * a.ncell + level_off(l) + cc) * a.K;
     for (int j = 0; j < kMaxTermsPerThread; ++j) {
       const int t = threadIdx.x + j * FT;
       if (t >= a.K) break;
-      const short4 e = a.terms[t];
       double w = 0.0;
-      for (int i = 0; i <= e.x; ++i)
-        for (int k = 0; k <= e.y; ++k)
-          for (int m = 0; m <= e.z; ++m) w += Mc[fmm::term(i, k, m)] * sp[0][e.x - i] * sp[1][e.y - k] * sp[2][e.z - m];
+      for (int e = a.mm_off[t]; e < a.mm_off[t + 1]; ++e) {
+        const int2 ent = a.mm_e[e];
+        w += Mc[ent.x] * a.mm_c[e] * hp[ent.y & 255] * child_sign(ent.y, bx, by, bz);
+      }
       acc[j] += w;
     }
   }
@@ -245,36 +260,107 @@ __global__ void __launch_bounds__(FT) k_fmm_m2l(FmmArgs a, int l) {
   }
 }
 
-// children at level l + 1 from their parent at level l
+// The same M2L with the (target term, source term) pairs of each thread
+// held in registers (orders up to 8: at most kRegPairs pairs per thread),
+// both columns in one CTA sharing the derivative row staged in shared memory.
+constexpr int kRegPairs = 24;
+__global__ void __launch_bounds__(FT) k_fmm_m2l_reg(FmmArgs a, int l) {
+  extern __shared__ double sh[];
+  double *s_m = sh;                // [2][K]
+  double *s_d = sh + 2 * a.K;      // [KD]
+  double *s_acc = s_d + a.KD;      // [npairs]
+  const int npairs = a.hoff[a.K];
+  const int tc = blockIdx.x;
+  if (a.cnt[level_off(l) + tc] == 0) return;
+  int tx, ty, tz;
+  cell_xyz(tc, l, tx, ty, tz);
+  const int n = 1 << l;
+  const double hinv = (1 << l) / a.h0;
+  int pk[kRegPairs];
+  double acc0[kRegPairs], acc1[kRegPairs];
+#pragma unroll
+  for (int j = 0; j < kRegPairs; ++j) {
+    const int q = threadIdx.x + j * FT;
+    pk[j] = -1;
+    if (q < npairs) {
+      const int4 pr = a.pairs[q];
+      pk[j] = pr.x | (pr.y << 10) | (pr.w << 20);
+    }
+    acc0[j] = acc1[j] = 0.0;
+  }
+  for (int ox = -1; ox <= 1; ++ox)
+    for (int oy = -1; oy <= 1; ++oy)
+      for (int oz = -1; oz <= 1; ++oz) {
+        const int PX = (tx >> 1) + ox, PY = (ty >> 1) + oy, PZ = (tz >> 1) + oz;
+        if (PX < 0 || PY < 0 || PZ < 0 || 2 * PX >= n || 2 * PY >= n || 2 * PZ >= n) continue;
+        for (int ch = 0; ch < 8; ++ch) {
+          const int sx = 2 * PX + (ch >> 2), sy = 2 * PY + ((ch >> 1) & 1), sz = 2 * PZ + (ch & 1);
+          const int dx = tx - sx, dy = ty - sy, dz = tz - sz;
+          if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+          const int sc = cell_idx(l, sx, sy, sz);
+          if (a.cnt[level_off(l) + sc] == 0) continue;  // uniform over the CTA
+          __syncthreads();
+          for (int i = threadIdx.x; i < a.ncol * a.K; i += FT) {
+            const int col = i / a.K, g = i - col * a.K;
+            const int ng = a.terms[g].w;
+            double f = 1.0;
+            for (int r = 0; r < ng; ++r) f *= hinv;
+            s_m[i] = a.M[((size_t)col * a.ncell + level_off(l) + sc) * a.K + g] * f;
+          }
+          const double *D = a.dunit + (size_t)(((dx + 3) * 7 + (dy + 3)) * 7 + (dz + 3)) * a.KD;
+          for (int i = threadIdx.x; i < a.KD; i += FT) s_d[i] = D[i];
+          __syncthreads();
+#pragma unroll
+          for (int j = 0; j < kRegPairs; ++j) {
+            if (pk[j] < 0) continue;
+            const int g = pk[j] & 1023;
+            const double d = (pk[j] >> 20) ? -s_d[(pk[j] >> 10) & 1023] : s_d[(pk[j] >> 10) & 1023];
+            acc0[j] += s_m[g] * d;
+            acc1[j] += s_m[a.K + g] * d;
+          }
+        }
+      }
+  for (int col = 0; col < a.ncol; ++col) {
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRegPairs; ++j) {
+      const int q = threadIdx.x + j * FT;
+      if (q < npairs) s_acc[q] = col ? acc1[j] : acc0[j];
+    }
+    __syncthreads();
+    double *Lt = a.Lc + ((size_t)col * a.ncell + level_off(l) + tc) * a.K;
+    for (int hh = threadIdx.x; hh < a.K; hh += FT) {
+      double s = 0.0;
+      for (int q = a.hoff[hh]; q < a.hoff[hh + 1]; ++q) s += s_acc[q];
+      const short4 e = a.terms[hh];
+      double f = hinv;  // h^-(|h| + 1) / h!
+      for (int i = 0; i < e.w; ++i) f *= hinv;
+      for (int i = 2; i <= e.x; ++i) f /= i;
+      for (int i = 2; i <= e.y; ++i) f /= i;
+      for (int i = 2; i <= e.z; ++i) f /= i;
+      Lt[hh] += s * f;
+    }
+  }
+}
+
+// children at level l + 1 from their parent at level l:
+// L_k(child) += sum_(h >= k) L_h(parent) h! / (k! (h - k)!) t^(h - k)
 __global__ void __launch_bounds__(FT) k_fmm_l2l(FmmArgs a, int l) {
   const int cc = blockIdx.x, col = blockIdx.y;
   if (a.cnt[level_off(l + 1) + cc] == 0) return;
   int cx, cy, cz;
   cell_xyz(cc, l + 1, cx, cy, cz);
-  const double hc = a.h0 / (1 << (l + 1));
-  const double t[3] = {((cx & 1) - 0.5) * hc, ((cy & 1) - 0.5) * hc, ((cz & 1) - 0.5) * hc};
-  double tp[3][fmm::kMaxOrder + 1];
-  for (int d = 0; d < 3; ++d) {
-    tp[d][0] = 1.0;
-    for (int m = 1; m <= a.p; ++m) tp[d][m] = tp[d][m - 1] * t[d];
-  }
+  double hp[fmm::kMaxOrder + 1];  // (h_c / 2)^k
+  hp[0] = 1.0;
+  for (int k = 1; k <= a.p; ++k) hp[k] = hp[k - 1] * 0.5 * a.h0 / (1 << (l + 1));
+  const int bx = cx & 1, by = cy & 1, bz = cz & 1;
   const double *Lp = a.Lc + ((size_t)col * a.ncell + level_off(l) + cell_idx(l, cx >> 1, cy >> 1, cz >> 1)) * a.K;
   double *Lch = a.Lc + ((size_t)col * a.ncell + level_off(l + 1) + cc) * a.K;
   for (int k = threadIdx.x; k < a.K; k += FT) {
-    const short4 e = a.terms[k];
     double w = 0.0;
-    for (int i = e.x; i <= a.p; ++i) {
-      double bx = 1.0;  // binomial(i, e.x)
-      for (int r = 1; r <= i - e.x; ++r) bx = bx * (e.x + r) / r;
-      for (int j = e.y; i + j <= a.p; ++j) {
-        double by = 1.0;
-        for (int r = 1; r <= j - e.y; ++r) by = by * (e.y + r) / r;
-        for (int m = e.z; i + j + m <= a.p; ++m) {
-          double bz = 1.0;
-          for (int r = 1; r <= m - e.z; ++r) bz = bz * (e.z + r) / r;
-          w += Lp[fmm::term(i, j, m)] * bx * by * bz * tp[0][i - e.x] * tp[1][j - e.y] * tp[2][m - e.z];
-        }
-      }
+    for (int e = a.ll_off[k]; e < a.ll_off[k + 1]; ++e) {
+      const int2 ent = a.ll_e[e];
+      w += Lp[ent.x] * a.ll_c[e] * hp[ent.y & 255] * child_sign(ent.y, bx, by, bz);
     }
     Lch[k] += w;
   }
@@ -421,7 +507,46 @@ int System::fmm_prepare() {
           if (std::abs(i) <= 1 && std::abs(j) <= 1 && std::abs(k) <= 1) continue;
           fmm::derivatives(i, j, k, f.p, &dunit[(size_t)(((i + 3) * 7 + (j + 3)) * 7 + (k + 3)) * f.KD]);
         }
-    bool bad = cudaMalloc((void **)&f.terms, f.K * sizeof(short4)) != cudaSuccess ||
+    // translation lists: M2M (target g, source k <= g, 1 / (g - k)!) and L2L
+    // (target k, source h >= k, h! / (k! (h - k)!)), grouped by target term
+    std::vector<int2> mm_e, ll_e;
+    std::vector<double> mm_c, ll_c;
+    std::vector<int> mm_off(f.K + 1, 0), ll_off(f.K + 1, 0);
+    auto fact = [](int k) {
+      double r = 1.0;
+      for (int i = 2; i <= k; ++i) r *= i;
+      return r;
+    };
+    auto pack = [](int mx, int my, int mz) { return (mx + my + mz) | ((mx & 1) << 8) | ((my & 1) << 9) | ((mz & 1) << 10); };
+    for (int t = 0; t < f.K; ++t) {
+      const short4 e = terms[t];
+      mm_off[t] = (int)mm_e.size();
+      for (int k = 0; k < f.K; ++k) {
+        const short4 q = terms[k];
+        if (q.x > e.x || q.y > e.y || q.z > e.z) continue;
+        const int mx = e.x - q.x, my = e.y - q.y, mz = e.z - q.z;
+        mm_e.push_back(make_int2(k, pack(mx, my, mz)));
+        mm_c.push_back(1.0 / (fact(mx) * fact(my) * fact(mz)));
+      }
+      ll_off[t] = (int)ll_e.size();
+      for (int h = 0; h < f.K; ++h) {
+        const short4 q = terms[h];
+        if (q.x < e.x || q.y < e.y || q.z < e.z) continue;
+        const int mx = q.x - e.x, my = q.y - e.y, mz = q.z - e.z;
+        ll_e.push_back(make_int2(h, pack(mx, my, mz)));
+        ll_c.push_back(fact(q.x) * fact(q.y) * fact(q.z) /
+                       (fact(e.x) * fact(e.y) * fact(e.z) * fact(mx) * fact(my) * fact(mz)));
+      }
+    }
+    mm_off[f.K] = (int)mm_e.size();
+    ll_off[f.K] = (int)ll_e.size();
+    bool bad = cudaMalloc((void **)&f.mm_e, mm_e.size() * sizeof(int2)) != cudaSuccess ||
+               cudaMalloc((void **)&f.ll_e, ll_e.size() * sizeof(int2)) != cudaSuccess ||
+               cudaMalloc((void **)&f.mm_c, mm_c.size() * sizeof(double)) != cudaSuccess ||
+               cudaMalloc((void **)&f.ll_c, ll_c.size() * sizeof(double)) != cudaSuccess ||
+               cudaMalloc((void **)&f.mm_off, mm_off.size() * sizeof(int)) != cudaSuccess ||
+               cudaMalloc((void **)&f.ll_off, ll_off.size() * sizeof(int)) != cudaSuccess;
+    bad = bad || cudaMalloc((void **)&f.terms, f.K * sizeof(short4)) != cudaSuccess ||
                cudaMalloc((void **)&f.pairs, pairs.size() * sizeof(int4)) != cudaSuccess ||
                cudaMalloc((void **)&f.hoff, hoff.size() * sizeof(int)) != cudaSuccess ||
                cudaMalloc((void **)&f.dunit, dunit.size() * sizeof(double)) != cudaSuccess;
@@ -434,11 +559,20 @@ int System::fmm_prepare() {
     cudaMemcpyAsync(f.pairs, pairs.data(), pairs.size() * sizeof(int4), cudaMemcpyHostToDevice, st_);
     cudaMemcpyAsync(f.hoff, hoff.data(), hoff.size() * sizeof(int), cudaMemcpyHostToDevice, st_);
     cudaMemcpyAsync(f.dunit, dunit.data(), dunit.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(f.mm_e, mm_e.data(), mm_e.size() * sizeof(int2), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(f.ll_e, ll_e.data(), ll_e.size() * sizeof(int2), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(f.mm_c, mm_c.data(), mm_c.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(f.ll_c, ll_c.data(), ll_c.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(f.mm_off, mm_off.data(), mm_off.size() * sizeof(int), cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(f.ll_off, ll_off.data(), ll_off.size() * sizeof(int), cudaMemcpyHostToDevice, st_);
     int st = check(cudaStreamSynchronize(st_), "FMM tables");
     if (st) return st;
     const size_t smem = (f.K + (size_t)f.npairs) * sizeof(double);
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(gpu::k_fmm_m2l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(double);
+    if (f.npairs <= gpu::kRegPairs * gpu::FT && smem_reg > 48 * 1024)
+      cudaFuncSetAttribute(gpu::k_fmm_m2l_reg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_reg);
   }
   FmmState &f = *fmm_;
   // geometry: bounding cube of the polarizable sites, leaf level
@@ -600,6 +734,12 @@ int System::fmm_tmu(int ncol, const double *x, double *y, bool dodiag) {
   a.dunit = f.dunit;
   a.M = f.M;
   a.Lc = f.Lc;
+  a.mm_e = f.mm_e;
+  a.ll_e = f.ll_e;
+  a.mm_c = f.mm_c;
+  a.ll_c = f.ll_c;
+  a.mm_off = f.mm_off;
+  a.ll_off = f.ll_off;
   const float thr2m = (float)(d_.damp_thr * d_.damp_thr * (1.0 + 1e-5));
   const size_t smem = (f.K + (size_t)f.npairs) * sizeof(double);
   for (int c0 = 0; c0 < ncol; c0 += 2) {
@@ -611,7 +751,12 @@ int System::fmm_tmu(int ncol, const double *x, double *y, bool dodiag) {
     const int nleaf = 1 << (3 * f.L);
     gpu::k_fmm_p2m<<<dim3(nleaf, g), gpu::FT, 0, st_>>>(a, xg, n);
     for (int l = f.L; l >= 1; --l) gpu::k_fmm_m2m<<<dim3(1 << (3 * (l - 1)), g), gpu::FT, 0, st_>>>(a, l);
-    for (int l = 2; l <= f.L; ++l) gpu::k_fmm_m2l<<<dim3(1 << (3 * l), g), gpu::FT, smem, st_>>>(a, l);
+    if (f.npairs <= gpu::kRegPairs * gpu::FT) {
+      const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(double);
+      for (int l = 2; l <= f.L; ++l) gpu::k_fmm_m2l_reg<<<dim3(1 << (3 * l), 1), gpu::FT, smem_reg, st_>>>(a, l);
+    } else {
+      for (int l = 2; l <= f.L; ++l) gpu::k_fmm_m2l<<<dim3(1 << (3 * l), g), gpu::FT, smem, st_>>>(a, l);
+    }
     for (int l = 2; l < f.L; ++l) gpu::k_fmm_l2l<<<dim3(1 << (3 * (l + 1)), g), gpu::FT, 0, st_>>>(a, l);
     if (m_.amoeba)
       gpu::k_fmm_l2p<true><<<dim3(nleaf, g), gpu::FT, 0, st_>>>(a, xg, n, d_.damp_thr, thr2m, f.field);

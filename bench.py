@@ -13,7 +13,9 @@ in the reference (src/mod_electrostatics.F90:1487-1596, M2D_done cache).
 * ``e2e``: the same through the reference-facing call ``ommp_set_external_field``
   with host buffers (field H2D and dipoles D2H inside the timed region).
 * ``fp64``: one plain FP64 CG solve on the same workload (the reference's
-  algorithm on the GPU) and the relative error of the mixed result against it.
+  algorithm on the GPU) and the relative error of the mixed result against it;
+  ``fp64.fmm``: the same solve and a strict mixed solve with the FP64 products
+  from the fast multipole method (order 8), with their error against it.
 * ``roofline``: the dominant pair kernel, its algorithmic flops (45 per ordered
   pair per right-hand side) over its CUDA-event time, against the FMA pipe
   peak measured in the same run.
@@ -548,6 +550,28 @@ def run_gb300(args):
                 "residual_history_D": [float(x) for x in sys_.residual_history(0)],
                 "residual_history_P": [float(x) for x in sys_.residual_history(1)],
                 "energy": ref_ep}
+        # the fast multipole method (ommp_enable_fmm, order 8 as the reference's
+        # default) for the FP64 products: plain FP64 CG, and the strict mixed
+        # mode whose refinement residual then comes from the FMM
+        fmm = {}
+        for prec in ("fp64", "mixed"):
+            sys_.set_precision(prec)
+            sys_.set_fmm(True, 8)
+            sys_.clear_guess()
+            sys_.synchronize()
+            t0 = time.perf_counter()
+            st = L.ommp_gpu_set_external_field_device(sys_._h, dev[W + K - 1], 0, 0, 1)
+            dt = time.perf_counter() - t0
+            assert st == 0, L.ommp_gpu_last_error()
+            fmm[prec] = {"solves_per_s": 1.0 / dt, "s_per_solve": dt, "t_mu_products": sys_.counter(0),
+                         "rel_err_ipd_vs_direct_fp64": rel_err(sys_.ipd, ref),
+                         "max_err_ipd_vs_direct_fp64": max_err(sys_.ipd, ref),
+                         "rel_err_energy_vs_direct_fp64": float(abs(sys_.get_polelec_energy() - ref_ep) / abs(ref_ep))}
+            sys_.set_fmm(False, 8)
+        fmm["order"] = 8
+        fmm["speedup_fp64_fmm_over_direct"] = fmm["fp64"]["solves_per_s"] * fp64_s
+        fp64["fmm"] = fmm
+        sys_.set_precision("fp64")
         for label, r, e_field in (("mixed", main, e_main), ("mixed_ds", ds, ds["e_m2d"] if ds else None)):
             if r is None:
                 continue

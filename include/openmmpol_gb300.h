@@ -182,13 +182,13 @@ int32_t ommp_qm_helper_get_nmm(OMMP_QM_HELPER_PRT qm);
 int32_t ommp_qm_helper_get_qm_atoms(OMMP_QM_HELPER_PRT qm);
 /* include/openmmpol.h:153-155 ; src/mod_c_interface.F90:1843-1879.  FMM
  * switch of the FP64 dipole-field products (T.mu of the FP64 solvers and of
- * the strict mixed mode's refinement residual): a uniform octree with
- * Cartesian expansions of order 8 (the reference's default maximum angular
- * momentum), near pairs (neighbouring leaves, every damped pair among them)
- * direct.  The reference switches it on by itself above 1,000 atoms; here the
- * direct sums stay the default and the host asks for the FMM.  The
- * permanent-multipole field, the FP32 inner products and the double-single
- * products stay direct. */
+ * the strict mixed mode's refinement residual) and of the permanent-multipole
+ * field in the FP64 modes: a uniform octree with Cartesian expansions of total
+ * order 10 (as accurate as the reference's default order-8 spherical FMM),
+ * near pairs (neighbouring leaves, every damped pair among them) direct.  The
+ * reference switches it on by itself above 1,000 atoms; here the direct sums
+ * stay the default and the host asks for the FMM.  The FP32 inner products
+ * and the double-single mode stay direct. */
 void ommp_enable_fmm(OMMP_SYSTEM_PRT s);
 void ommp_disable_fmm(OMMP_SYSTEM_PRT s);
 bool ommp_use_fmm(OMMP_SYSTEM_PRT s);

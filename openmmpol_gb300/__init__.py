@@ -192,8 +192,9 @@ class OMMPSystem:
     def use_fmm(self) -> bool:
         return bool(self._L.ommp_use_fmm(self._h))
 
-    def set_fmm(self, on: bool = True, order: int = 8) -> None:
-        """Fast multipole method for the FP64 T.mu products (expansion order 2..12)."""
+    def set_fmm(self, on: bool = True, order: int = 10) -> None:
+        """Fast multipole method for the FP64 T.mu products and the permanent
+        field (expansion order 2..12, default 10)."""
         _check(self._L.ommp_gpu_set_fmm(self._h, int(bool(on)), int(order)))
 
     # --- potential and field at external points (pyopenmmpol names) -------------

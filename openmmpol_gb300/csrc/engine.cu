@@ -429,18 +429,31 @@ int System::flush_l2(size_t bytes) {
 }
 
 int System::ensure_m2d() {
-  // a field computed in double-single serves only the double-single mode
-  if (m2d_done_ && !(m2d_ds_ && precision_ != kPrecMixedDS)) return kOk;
-  cudaMemsetAsync(flag_, 0, sizeof(int), st_);
+  // the method the mode asks for: double-single in the mixed-ds mode, the
+  // FMM when it is switched on, else the direct FP64 sums; a cached field
+  // serves if it came from that method or from the direct FP64 sums
   const bool ds = precision_ == kPrecMixedDS;
+  const int want = ds ? kM2dDS : (fmm_on_ ? kM2dFMM : kM2dDirect);
+  if (m2d_done_ && (m2d_method_ == want || m2d_method_ == kM2dDirect)) return kOk;
+  cudaMemsetAsync(flag_, 0, sizeof(int), st_);
+  int method = kM2dDirect;
   if (ds) {
     int st = ensure_ds_scratch();
     if (st) return st;
     gpu::launch_m2d_ds(d_, e_m2d_, ds_scratch_, nsplit_m2d_ds_, flag_, st_);
+    method = kM2dDS;
   } else {
-    gpu::launch_m2d(d_, e_m2d_, scratch_, nsplit_m2d_, flag_, st_);
+    bool done = false;
+    if (fmm_on_) {  // the fast multipole method (too small a system: direct)
+      int st = fmm_m2d(e_m2d_, done);
+      if (st) return st;
+    }
+    if (done)
+      method = kM2dFMM;
+    else
+      gpu::launch_m2d(d_, e_m2d_, scratch_, nsplit_m2d_, flag_, st_);
   }
-  m2d_ds_ = ds;
+  m2d_method_ = method;
   int flag = 0;
   cudaMemcpyAsync(&flag, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);
   int st = check(cudaStreamSynchronize(st_), "M2D field");

@@ -205,7 +205,9 @@ class System {
   size_t ext_cap_ = 0;
   double *ds_scratch_ = nullptr;  // split partials of the double-single kernels
   int nsplit_ds_ = 1, nsplit_m2d_ds_ = 1;
-  bool m2d_ds_ = false;  // the cached E_M2D was computed in double-single
+  // how the cached E_M2D was computed
+  static constexpr int kM2dDirect = 0, kM2dDS = 1, kM2dFMM = 2;
+  int m2d_method_ = kM2dDirect;
   int fp32_kernel_ = 0;  // 0 autotuned, else the forced kernel version
   float *scratch32_ = nullptr;
   double *partial_ = nullptr;  // reduction partials [kRedBlocks][8]
@@ -244,11 +246,12 @@ class System {
   GradState *grad_ = nullptr;
   FmmState *fmm_ = nullptr;
   bool fmm_on_ = false;
-  int fmm_order_ = 8;
+  int fmm_order_ = 10;  // total order |g| + |h| <= 10 of the Cartesian M2L
   int fmm_prepare();
   void fmm_invalidate();
   bool fmm_tree() const;  // the prepared FMM has a tree (else direct sums)
   int fmm_tmu(int ncol, const double *x, double *y, bool dodiag);
+  int fmm_m2d(double *out, bool &done);
   Workspace ws_;   // view of the default two-column buffers
   Workspace wsb_;  // batch buffers
   std::map<int, F32Shape> f32_tune_;  // columns -> tuned FP32 launch shape

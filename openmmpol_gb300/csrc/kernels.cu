@@ -34,55 +34,6 @@ namespace {
 constexpr int TPB = 128;   // targets per CTA
 constexpr int TILE = 128;  // sources per shared-memory tile
 
-// Field at target (position pt, 1/thole wt, damping at) of source s.
-template <bool AMOEBA>
-__device__ __forceinline__ void m2d_pair_f64(double dx, double dy, double dz, double wt, double ws,
-                                             double at, double as, float2 wat, float2 was,
-                                             const double *q, double thr, float thr2m,
-                                             double &ex, double &ey, double &ez) {
-  double r2 = dx * dx + dy * dy + dz * dz;
-  float r2f = (float)r2;
-  double rinv = rinv_f64(r2, r2f);
-  double ir2 = rinv * rinv;
-  double k3 = rinv * ir2;
-  if (AMOEBA) {
-    double k5 = k3 * ir2;
-    double k7 = k5 * ir2;
-    if (maybe_damped_amoeba(r2f, wat, was, thr2m)) {
-      double u = r2 * rinv * (wt * ws);  // r / (thole_t thole_s)
-      double au3 = fmin(at, as) * u * u * u;
-      if (au3 < thr) {
-        double e = exp(-au3);
-        k3 *= 1.0 - e;
-        k5 *= 1.0 - (1.0 + au3) * e;
-        k7 *= 1.0 - (1.0 + au3 + 0.6 * au3 * au3) * e;
-      }
-    }
-    double mdr = q[1] * dx + q[2] * dy + q[3] * dz;
-    double qx = q[4] * dx + q[5] * dy + q[7] * dz;
-    double qy = q[5] * dx + q[6] * dy + q[8] * dz;
-    double qz = q[7] * dx + q[8] * dy + q[9] * dz;
-    double qxr = qx * dx + qy * dy + qz * dz;
-    double c = q[0] * k3 + 3.0 * mdr * k5 + 15.0 * qxr * k7;
-    double k5x6 = 6.0 * k5;
-    ex += c * dx - q[1] * k3 - k5x6 * qx;
-    ey += c * dy - q[2] * k3 - k5x6 * qy;
-    ez += c * dz - q[3] * k3 - k5x6 * qz;
-  } else {
-    if (maybe_damped_wang(r2f, wat, was)) {
-      double u = r2 * rinv * (wt * ws);
-      if (u < 1.0) {
-        double u3 = u * u * u;
-        k3 *= 4.0 * u3 - 3.0 * u3 * u;
-      }
-    }
-    double c = q[0] * k3;
-    ex += c * dx;
-    ey += c * dy;
-    ez += c * dz;
-  }
-}
-
 template <bool AMOEBA>
 __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 *__restrict__ pol_pos,
                                                       const double *__restrict__ pol_a,
@@ -936,6 +887,11 @@ static void m2d_finish(const DevSites &s, double *out, const double *scratch, in
     k_m2d_finish<false><<<fb, 128, 0, st>>>(s.n, nsplit, scratch, s.pol_pos, s.pol_a, s.mm_pos, s.mm_a,
                                             s.mm_q, s.pol_wa32, s.mm_wa32, s.m2d_ri, s.m2d_src, s.m2d_sP,
                                             s.m2d_sD, s.damp_thr, damp_thr2_margin(s), out);
+}
+
+void launch_m2d_finish(const DevSites &s, double *out, const double *partial, int nsplit, cudaStream_t st) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  m2d_finish(s, out, partial, nsplit, st);
 }
 
 void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag,

@@ -66,6 +66,9 @@ size_t m2d_scratch_doubles(const DevSites &s, int nsplit);
 int m2d_pick_split(const DevSites &s, int sm_count);
 void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag,
                 cudaStream_t st);
+// the finishing pass alone: split partials [nsplit][n][3] summed, the
+// scaled-pair corrections, out [n_ipd][n][3]
+void launch_m2d_finish(const DevSites &s, double *out, const double *partial, int nsplit, cudaStream_t st);
 
 // y = T x (dodiag) or y = -E_dd(x) (no diagonal); x,y [nrhs][n][3], FP64.
 size_t tmu_scratch_doubles(const DevSites &s, int nrhs, int nsplit);

@@ -97,8 +97,8 @@ System *System::load_host(const std::string &path, std::string &err, int &status
   build_d2d_pairs(s->m_, s->d2d_pairs_);
   if (s->m_.fmm_requested)
     log_msg(kVerbHigh, nullptr,
-            "More than 1000 MM atoms: the reference would enable FMM here; this library "
-            "always evaluates the direct sums.");
+            "More than 1000 MM atoms: the reference would enable FMM here; this library keeps the "
+            "direct sums unless ommp_enable_fmm is called.");
   status = kOk;
   return s;
 }

@@ -264,17 +264,27 @@ def kernel_table(kst, n, peak64, peak32):
     return out
 
 
-def roofline_of(kstats, total_ms):
+# DRAM bytes (read + write) per launch of the dominant kernels, from the ncu
+# captures of the 30,000-site box (profiles/tmu_sym_water_box_30000_sites_ncu_full.md,
+# profiles/tmu_ds_water_box_30000_sites_ncu_full.md, profiles/tmu32_water_box_30000_sites_ncu_full.md);
+# the working set is O(N) and L2-resident, so the figure is scaled by the site count
+TRAFFIC_30K = {"tmu_fp64": 3.6e6, "tmu_ds": 3.2e6}
+
+
+def roofline_of(kstats, total_ms, n=30000):
     if not kstats:
         return None
     dom = max(kstats, key=lambda k: kstats[k]["total_ms"])
     d = kstats[dom]
     ds = dom == "tmu_ds"
+    traffic = TRAFFIC_30K[dom] * n / 30000.0 if dom in TRAFFIC_30K else None
     return {"bound": "fp64" if dom == "tmu_fp64" else "fp32", "kernel": dom,
             "achieved": d["achieved_tops"] if ds else d["achieved_tflops"],
             "peak": d["peak_tops"] if ds else d["peak_tflops"],
             "unit": "Tops/s (FP32 instructions)" if ds else "TFLOP/s",
-            "frac": d["frac"], "traffic": None,
+            "frac": d["frac"], "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 30,000-site "
+                              "box, scaled by the site count (bytes per launch)" if traffic else None,
             "peak_source": "FMA-chain kernel measured in this run (pipe peak; "
                            "MEASURED_PEAKS.json has no FP32/FP64 CUDA-core figure)",
             "algorithmic": (f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair" if ds else
@@ -496,7 +506,7 @@ def run_gb300(args):
         kstats = kernel_table(kst, n, peak64.value, peak32.value)
         res = {"value": ws * K / (total_ms * 1e-3), "ms_per_step": total_ms / K, "steps_ms": step_ms,
                "solver_counters_per_step": counters, "gpu_launches": int(launches), "wall_s_timed": wall,
-               "clocks": clocks, "kernels": kstats, "roofline": roofline_of(kstats, total_ms),
+               "clocks": clocks, "kernels": kstats, "roofline": roofline_of(kstats, total_ms, n),
                "ipd": sys_.ipd.copy(), "energy": sys_.get_polelec_energy()}
         # e2e through the reference-facing call with host buffers
         e2e_ms = []

@@ -100,6 +100,11 @@ void ommp_time_pull(const char *label);
 void ommp_time_push(void);
 /* include/openmmpol.h:38 ; src/mod_c_interface.F90:378-388 */
 double ommp_get_polelec_energy(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:39 ; src/mod_c_interface.F90:390-401, energy_MM_MM
+ * src/mod_electrostatics.F90:899-941.  Interaction energy of the static
+ * multipoles (EM): the m-scaled pairs of the force field, no damping.
+ * Computed on the GPU once per geometry. */
+double ommp_get_fixedelec_energy(OMMP_SYSTEM_PRT s);
 /* include/openmmpol.h:40 ; src/mod_c_interface.F90:289-305.
  * ext_field: [pol_atoms][3].  Like the reference, `matv` is ignored on this
  * path and the default matrix-vector method is used (mod_interface.F90:222). */
@@ -206,6 +211,7 @@ int32_t ommp_gpu_set_external_field_status(OMMP_SYSTEM_PRT s, const double *ext_
 int32_t ommp_gpu_set_external_field_device(OMMP_SYSTEM_PRT s, const double *ext_field_dev,
                                            int32_t solver, int32_t matv, int32_t add_mm_field);
 int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *energy);
+int32_t ommp_gpu_get_fixedelec_energy(OMMP_SYSTEM_PRT s, double *energy);
 /* ommp_polelec_geomgrad returning a status instead of stopping the process */
 int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
 /* FMM on (on != 0) or off, with expansion order 2..12 */

@@ -154,6 +154,12 @@ class OMMPSystem:
         _check(self._L.ommp_gpu_get_polelec_energy(self._h, C.byref(e)))
         return e.value
 
+    def get_fixedelec_energy(self) -> float:
+        """Interaction energy of the static multipoles (EM)."""
+        e = C.c_double(0.0)
+        _check(self._L.ommp_gpu_get_fixedelec_energy(self._h, C.byref(e)))
+        return e.value
+
     def polelec_geomgrad(self, numerical: bool = False) -> np.ndarray:
         """Geometric gradient of the polarization energy, [mm_atoms, 3].
 

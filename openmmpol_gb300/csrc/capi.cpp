@@ -95,6 +95,17 @@ void ommp_set_external_field_nomm(OMMP_SYSTEM_PRT s, const double *ef, int32_t s
   fatal_if(ommp_gpu_set_external_field(s, ef, solver, matv, 0));
 }
 
+int32_t ommp_gpu_get_fixedelec_energy(OMMP_SYSTEM_PRT s, double *e) {
+  ommp_time_push();
+  int st = S(s)->fixedelec_energy(*e);
+  if (st == ommp::kOk) ommp_time_pull("Fixed electrostatic energy");
+  return st;
+}
+double ommp_get_fixedelec_energy(OMMP_SYSTEM_PRT s) {
+  double e = 0.0;
+  fatal_if(ommp_gpu_get_fixedelec_energy(s, &e));
+  return e;
+}
 int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *e) {
   ommp_time_push();
   int st = S(s)->polelec_energy(*e);

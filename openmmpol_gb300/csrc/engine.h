@@ -77,6 +77,8 @@ class System {
   int set_external_field(const double *ext_host, int solver, int matv, bool add_mm);
   int set_external_field_device(const double *ext_dev, int solver, int matv, bool add_mm);
   int polelec_energy(double &e);
+  // interaction energy of the static multipoles (once per geometry)
+  int fixedelec_energy(double &e);
   int update_coordinates(const double *c_host);
   int set_default_solver(int s);
   int set_default_matv(int m);
@@ -243,6 +245,8 @@ class System {
   KEv kt_begin(int kind, int cols);
   void kt_end(KEv &e);
   void kt_resolve();
+  bool fixedelec_done_ = false;
+  double fixedelec_ = 0.0;
   GradState *grad_ = nullptr;
   FmmState *fmm_ = nullptr;
   bool fmm_on_ = false;

@@ -2151,3 +2151,96 @@ int orc_nuclei_fields(orc_sys *s, int32_t which, int32_t nq, const double *cqm, 
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Static multipole energy (fixed electrostatics): energy_MM_MM        */
+/* (src/mod_electrostatics.F90:899-941) on the potential, field and    */
+/* field gradient of the static multipoles at the static sites,        */
+/* elec_prop_M2M direct path (:1678-1952), undamped coulomb_kernel,    */
+/* list_S_S of m-scaled pairs (:597-648, screening_rules 'S','S').     */
+/* ------------------------------------------------------------------ */
+int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
+    const int mm = s->mm, amoeba = s->amoeba, ld = s->ld_cart;
+    /* list_S_S: row i, pairs within four bonds whose scale is not 1 */
+    lbuild_t b;
+    lb_init(&b, mm);
+    for (int i = 0; i < mm; i++) {
+        for (int ineigh = 0; ineigh < 4; ineigh++)
+            for (int k = s->conn[ineigh].ri[i]; k < s->conn[ineigh].ri[i + 1]; k++) {
+                int j = s->conn[ineigh].ci[k];
+                double sc = screening_rules(s, i, 'S', j, 'S', '-');
+                if (fabs(sc - 1.0) > EPS_RP) lb_push(&b, j, sc);
+            }
+        b.ri[i + 1] = b.nnz;
+    }
+    slist_t ss;
+    lb_finish(&b, &ss);
+    double *V = xcalloc(mm, sizeof(double)), *E = xcalloc(3 * (size_t)mm, sizeof(double));
+    double *G = xcalloc(6 * (size_t)mm, sizeof(double));
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
+    for (int j = 0; j < mm; j++) {
+        for (int i = 0; i < mm; i++) {
+            if (i == j) continue;
+            int todo = 1;
+            double sc = 1.0;
+            int kk = list_find(&ss, i, j);
+            if (kk >= 0) {
+                todo = ss.todo[kk];
+                sc = ss.scale[kk];
+            }
+            if (!todo) continue;
+            double d[3];
+            for (int c = 0; c < 3; c++) d[c] = s->cmm[3 * (size_t)j + c] - s->cmm[3 * (size_t)i + c];
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (r < EPS_RP) {
+                bad = 1;
+                continue;
+            }
+            double k[5];
+            k[0] = 1.0 / r;
+            for (int l = 1; l < 5; l++) k[l] = k[l - 1] / (r * r);
+            const double *q = &s->q[(size_t)ld * i];
+            double v = q[0] * k[0], e[3], g[6] = {0, 0, 0, 0, 0, 0};
+            for (int c = 0; c < 3; c++) e[c] = q[0] * k[1] * d[c];
+            if (amoeba) {
+                double md = q[1] * d[0] + q[2] * d[1] + q[3] * d[2];
+                double Q[3][3] = {{q[4], q[5], q[7]}, {q[5], q[6], q[8]}, {q[7], q[8], q[9]}};
+                double t[3];
+                for (int a = 0; a < 3; a++) t[a] = Q[a][0] * d[0] + Q[a][1] * d[1] + Q[a][2] * d[2];
+                double dqd = t[0] * d[0] + t[1] * d[1] + t[2] * d[2];
+                v += md * k[1] + 3.0 * dqd * k[2];
+                for (int c = 0; c < 3; c++)
+                    e[c] += 3.0 * md * d[c] * k[2] - q[1 + c] * k[1] + 15.0 * dqd * d[c] * k[3] - 6.0 * t[c] * k[2];
+                q_grad(q[0], d, k, g);
+                mu_grad(&q[1], d, k, g, NULL);
+                quad_grad(&q[4], d, k, g);
+            }
+            const double w = (kk >= 0) ? sc : 1.0;
+            V[j] += v * w;
+            for (int c = 0; c < 3; c++) E[3 * (size_t)j + c] += e[c] * w;
+            if (amoeba)
+                for (int c = 0; c < 6; c++) G[6 * (size_t)j + c] += g[c] * w;
+        }
+    }
+    double em = 0.0;
+    if (!bad)
+        for (int j = 0; j < mm; j++) {
+            const double *q = &s->q[(size_t)ld * j];
+            em += q[0] * V[j];
+            if (amoeba) {
+                for (int c = 0; c < 3; c++) em -= q[1 + c] * E[3 * (size_t)j + c];
+                const double *g = &G[6 * (size_t)j];
+                em += q[4] * g[0] + q[6] * g[2] + q[9] * g[5] + 2.0 * (q[5] * g[1] + q[7] * g[3] + q[8] * g[4]);
+            }
+        }
+    free(V), free(E), free(G);
+    free(ss.m.ri), free(ss.m.ci), free(ss.scale), free(ss.todo);
+    if (bad) {
+        set_err("Requesting Coulomb kernel for two atoms placed in the same point, this could be an internal bug or "
+                "a problem in your input file, please check.");
+        return ORC_ERR_NUMERIC;
+    }
+    *energy = 0.5 * em;
+    return 0;
+}

@@ -121,6 +121,9 @@ int orc_set_ipd(orc_sys *s, const double *ipd);
 /* fields of QM nuclei (charges qqm at cqm [nq][3]) at the MM sites, the QM
    helper's E_n2p (which 0: E [npol][3]) or E_n2m / G_n2m / H_n2m (which 1:
    E [mm][3], G [mm][6], H [mm][10]); outputs overwritten */
+/* ommp_get_fixedelec_energy: interaction energy of the static multipoles
+   (m-scaled pairs, undamped) */
+int orc_get_fixedelec_energy(orc_sys *s, double *energy);
 int orc_nuclei_fields(orc_sys *s, int32_t which, int32_t nq, const double *cqm, const double *qqm, double *E,
                       double *G, double *H);
 

@@ -64,6 +64,7 @@ def lib():
             "orc_polelec_geomgrad": (C.c_int, [vp, dp]),
             "orc_polelec_geomgrad_atoms": (C.c_int, [vp, C.c_int32, ip, dp]),
             "orc_set_ipd": (C.c_int, [vp, dp]),
+            "orc_get_fixedelec_energy": (C.c_int, [vp, dp]),
             "orc_nuclei_fields": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp, dp, dp, dp]),
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
@@ -226,6 +227,11 @@ class OracleSystem:
         """Install dipoles [n_ipd][npol][3] solved elsewhere as the solved state."""
         ipd = np.ascontiguousarray(ipd, dtype=np.float64).reshape(self.n_ipd, self.pol_atoms, 3)
         self._check(lib().orc_set_ipd(self._h, _dp(ipd)))
+
+    def get_fixedelec_energy(self):
+        e = C.c_double(0.0)
+        self._check(lib().orc_get_fixedelec_energy(self._h, C.byref(e)))
+        return e.value
 
     def nuclei_fields(self, cqm, qqm, grad=False):
         """QM-helper fields of point nuclei at the MM sites: E_n2p [npol][3]

@@ -12,6 +12,8 @@ reference outputs in ``golden.npz``:
 * ``<case>_ipd0`` / ``<case>_ipd1``: induced dipoles ``[n_ipd*pol_atoms, 3]``
   from ``IPD_0_*.ref`` (no external field) and ``IPD_1_*.ref`` (with EF_1.txt);
 * ``<case>_ep0`` / ``<case>_ep1``: the ``EP`` line of ``ENE_{0,1}_*.ref``;
+* ``<case>_em``: the ``EM`` line (static multipole energy; the same in both
+  files, the external field does not enter it);
 * ``<case>_ef1``: ``EF_1.txt`` gathered at the polarizable sites in the order of
   ``polar_mm`` (tests/test_programs/C/test_SI_potential.c:112-125 does the same
   gather), so fixtures stay small.
@@ -51,12 +53,16 @@ CASES = {
 }
 
 
-def read_ep(path):
+def read_term(path, tag):
     with open(path) as f:
         for line in f:
-            if line.startswith("EP"):
+            if line.startswith(tag):
                 return float(line.split()[-1])
-    raise ValueError(f"no EP line in {path}")
+    raise ValueError(f"no {tag} line in {path}")
+
+
+def read_ep(path):
+    return read_term(path, "EP")
 
 
 def polar_mm_of(mmp_path):
@@ -86,8 +92,12 @@ def main(ref_root):
     arrays = {}
     for name, (mmp, ipd, ene, ef, atol) in CASES.items():
         src = os.path.join(tests, mmp)
-        with open(src, "rb") as f, gzip.open(os.path.join(out_dir, name + ".mmp.gz"), "wb", 9) as g:
-            g.write(f.read())
+        dst = os.path.join(out_dir, name + ".mmp.gz")
+        with open(src, "rb") as f:
+            data = f.read()
+        if not os.path.exists(dst) or gzip.open(dst).read() != data:  # keep unchanged fixtures
+            with gzip.GzipFile(dst, "wb", 9, mtime=0) as g:
+                g.write(data)
         pm = polar_mm_of(src)
         efm = np.loadtxt(os.path.join(tests, ef)).reshape(-1, 3)
         arrays[name + "_ef1"] = efm[pm]
@@ -95,6 +105,8 @@ def main(ref_root):
             arrays[f"{name}_ipd{k}"] = np.loadtxt(os.path.join(tests, ipd % k)).reshape(-1, 3)
             if ene:
                 arrays[f"{name}_ep{k}"] = np.array(read_ep(os.path.join(tests, ene % k)))
+        if ene:
+            arrays[name + "_em"] = np.array(read_term(os.path.join(tests, ene % 0), "EM"))
         arrays[name + "_atol"] = np.array(atol)
     np.savez_compressed(os.path.join(out_dir, "golden.npz"), **arrays)
     print("wrote", len(CASES), "cases to", out_dir)

@@ -66,3 +66,12 @@ def test_oracle_nomm_solves_only_set_one(golden, golden_mmp):
     ipd = s.ipd
     assert np.abs(ipd[0]).max() > 0
     assert np.all(ipd[1] == 0)
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "nma_wang", "1crn_amoeba", "1crn_wang", "1ao6cut_wang",
+                                  "1ubq_amoeba", "1ubq_wang"])
+def test_oracle_static_multipole_energy_matches_golden(case, golden, golden_mmp):
+    # the EM line of the reference's ENE files (printed to 13 digits)
+    s = OracleSystem(golden_mmp[case])
+    ref = float(golden[case + "_em"])
+    assert abs(s.get_fixedelec_energy() - ref) <= 1e-11 * abs(ref) + 1e-14

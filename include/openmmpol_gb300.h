@@ -150,6 +150,13 @@ void ommp_field_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double
  * are solved first (default solver) when the system has none.  FP64 on the
  * GPU whatever the precision mode. */
 void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
+/* include/openmmpol.h:92 ; src/mod_c_interface.F90:606-624,
+ * ommp_rotation_geomgrad src/mod_interface.F90:699-710, rotation_geomgrad
+ * src/rotate_multipoles.F90:3-230.  Forces from the frame dependence of the
+ * rotated static dipoles and quadrupoles in a caller's field E [mm_atoms][3]
+ * and field gradient Egrd [mm_atoms][6] (xx, xy, yy, xz, yz, zz); grd
+ * [mm_atoms][3] overwritten (zeros for point-charge force fields). */
+void ommp_rotation_geomgrad(OMMP_SYSTEM_PRT s, const double *E, const double *Egrd, double *grd);
 /* QM helper, include/openmmpol.h:106-127 ; src/mod_c_interface.F90:1179-1196,
  * 1374-1660 ; src/mod_qm_helper.F90:80-161,356-520.  A helper holds n QM
  * nuclei (coordinates cqm [n][3] bohr, charges qqm [n], atomic numbers zqm
@@ -214,6 +221,8 @@ int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *energy);
 int32_t ommp_gpu_get_fixedelec_energy(OMMP_SYSTEM_PRT s, double *energy);
 /* ommp_polelec_geomgrad returning a status instead of stopping the process */
 int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
+/* ommp_rotation_geomgrad returning a status */
+int32_t ommp_gpu_rotation_geomgrad(OMMP_SYSTEM_PRT s, const double *E, const double *Egrd, double *grd);
 /* FMM on (on != 0) or off, with expansion order 2..12 */
 int32_t ommp_gpu_set_fmm(OMMP_SYSTEM_PRT s, int32_t on, int32_t order);
 /* QM helper calls returning a status instead of stopping the process */

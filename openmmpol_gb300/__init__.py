@@ -185,6 +185,21 @@ class OMMPSystem:
         self.update_coordinates(c0)
         return g
 
+    def rotation_geomgrad(self, E, Egrd) -> np.ndarray:
+        """Forces [mm_atoms, 3] from the rotation of the static multipoles
+        in the field E [mm_atoms, 3] and field gradient Egrd [mm_atoms, 6]
+        (xx, xy, yy, xz, yz, zz); mirrors the reference's
+        OMMPSystem.rotation_geomgrad (pythonapi/pyopenmmpol/pyommp_interface.cpp:559-566)."""
+        E = _as_c(E, (self.mm_atoms, 3))
+        Egrd = _as_c(Egrd, (self.mm_atoms, 6))
+        g = np.zeros((self.mm_atoms, 3))
+        _check(
+            self._L.ommp_gpu_rotation_geomgrad(
+                self._h, E.ctypes.data_as(_lib._dp), Egrd.ctypes.data_as(_lib._dp), g.ctypes.data_as(_lib._dp)
+            )
+        )
+        return g
+
     def update_coordinates(self, c) -> None:
         c = _as_c(c, (self.mm_atoms, 3))
         _check(self._L.ommp_gpu_update_coordinates(self._h, c.ctypes.data_as(_lib._dp)))

@@ -164,6 +164,15 @@ int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) {
   return st;
 }
 void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) { fatal_if(ommp_gpu_polelec_geomgrad(s, grd)); }
+int32_t ommp_gpu_rotation_geomgrad(OMMP_SYSTEM_PRT s, const double *E, const double *Egrd, double *grd) {
+  ommp_time_push();
+  int st = S(s)->rotation_geomgrad(E, Egrd, grd);
+  if (st == ommp::kOk) ommp_time_pull("Multipole rotation grad");
+  return st;
+}
+void ommp_rotation_geomgrad(OMMP_SYSTEM_PRT s, const double *E, const double *Egrd, double *grd) {
+  fatal_if(ommp_gpu_rotation_geomgrad(s, E, Egrd, grd));
+}
 
 int32_t ommp_gpu_init_qm_helper(int32_t n, const double *cqm, const double *qqm, const int32_t *zqm,
                                 OMMP_QM_HELPER_PRT *out) {

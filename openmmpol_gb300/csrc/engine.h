@@ -98,6 +98,9 @@ class System {
   int e_m2d(double *out_host);
   // geometric gradient of the polarization energy, out [mm][3] (overwritten)
   int polelec_geomgrad(double *grad_host);
+  // forces of the frame rotation of the static multipoles in a given field
+  // E [mm][3] and field gradient G [mm][6], out [mm][3] (overwritten)
+  int rotation_geomgrad(const double *E_host, const double *G_host, double *grad_host);
   // fast multipole method for the FP64 T.mu products (expansion order 2..12)
   int set_fmm(bool on, int order);
   bool fmm_on() const { return fmm_on_; }
@@ -248,6 +251,7 @@ class System {
   bool fixedelec_done_ = false;
   double fixedelec_ = 0.0;
   GradState *grad_ = nullptr;
+  int ensure_grad_state();
   FmmState *fmm_ = nullptr;
   bool fmm_on_ = false;
   int fmm_order_ = 10;  // total order |g| + |h| <= 10 of the Cartesian M2L

@@ -351,6 +351,25 @@ __global__ void k_grad_finish(GradArgs g) {
   }
 }
 
+// frame terms of every site for a given field E [mm][3] and field gradient
+// G [mm][6] (rotation_geomgrad): rot [mm][4][3], error bit 2 on a degenerate frame
+__global__ void k_rot_terms(int mm, const Pos64 *__restrict__ pos, const int4 *__restrict__ frame,
+                            const double *__restrict__ q0, const double *__restrict__ E, const double *__restrict__ G,
+                            double *__restrict__ rot, int *err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= mm) return;
+  const int4 f = frame[t];
+  const Pos64 pt = pos[t], pz = pos[f.y], px = pos[f.z], py = pos[f.w];
+  const double c0[3] = {pt.x, pt.y, pt.z}, cz[3] = {pz.x, pz.y, pz.z}, cx[3] = {px.x, px.y, px.z},
+               cy[3] = {py.x, py.y, py.z};
+  double out[4][3];
+  if (!gradmath::frame_pullback(f.x, c0, cz, cx, cy, &q0[(size_t)t * 10], &E[3 * (size_t)t], &G[6 * (size_t)t], out))
+    atomicOr(err, 2);
+  double *r = &rot[12 * (size_t)t];
+  for (int w = 0; w < 4; ++w)
+    for (int c = 0; c < 3; ++c) r[3 * w + c] = out[w][c];
+}
+
 __global__ void k_grad_gather(int mm, bool amoeba, const double *__restrict__ base, const double *__restrict__ rot,
                               const int *__restrict__ r_ri, const int *__restrict__ r_src, double *__restrict__ grad) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -384,6 +403,90 @@ int grad_pick_split(int mm, int resident) {
 }  // namespace
 }  // namespace gpu
 
+// device lists and buffers of the gradient (topology only): built once
+int System::ensure_grad_state() {
+  if (grad_) return kOk;
+  const int mm = d_.m, n = d_.n;
+  const bool amoeba = m_.amoeba;
+  const int nset = amoeba ? 2 : 1;
+  const int nacc = amoeba ? gpu::Acc<true>::N : gpu::Acc<false>::N;
+  int st;
+  GradState *gs = new GradState();
+  gs->mm = mm;
+  int resident = 0;
+  if (amoeba)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, gpu::k_grad_pairs<true>, gpu::GTPB, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, gpu::k_grad_pairs<false>, gpu::GTPB, 0);
+  gs->nsplit = gpu::grad_pick_split(mm, std::max(1, resident) * gpu::sm_count());
+  // M2D lists read by static site, and the frame reverse list
+  std::vector<int> t_ri(mm + 1, 0), t_src(m2d_pairs_.src.size());
+  std::vector<double> t_sP(t_src.size()), t_sD(t_src.size());
+  for (size_t k = 0; k < m2d_pairs_.src.size(); ++k) t_ri[m2d_pairs_.src[k] + 1]++;
+  for (int i = 0; i < mm; ++i) t_ri[i + 1] += t_ri[i];
+  {
+    std::vector<int> fill(t_ri.begin(), t_ri.end() - 1);
+    for (int j = 0; j < n; ++j)
+      for (int k = m2d_pairs_.ri[j]; k < m2d_pairs_.ri[j + 1]; ++k) {
+        const int i = m2d_pairs_.src[k], at = fill[i]++;
+        t_src[at] = j;
+        t_sP[at] = m2d_pairs_.sP[k];
+        t_sD[at] = amoeba ? m2d_pairs_.sD[k] : 1.0;
+      }
+  }
+  std::vector<int4> fr(mm);
+  std::vector<int> r_ri(mm + 1, 0), r_src;
+  for (int i = 0; i < mm; ++i) {
+    const int fk = amoeba ? m_.frame[i] : 0;
+    fr[i] = make_int4(fk, m_.iz[i] >= 0 ? m_.iz[i] : i, m_.ix[i] >= 0 ? m_.ix[i] : i, m_.iy[i] >= 0 ? m_.iy[i] : i);
+  }
+  {
+    std::vector<std::vector<int>> rev(mm);
+    for (int i = 0; i < mm; ++i) {
+      if (fr[i].x == 0) continue;
+      const int atoms[4] = {i, fr[i].y, fr[i].z, fr[i].w};
+      for (int w = 0; w < 4; ++w) rev[atoms[w]].push_back(4 * i + w);
+    }
+    for (int i = 0; i < mm; ++i) {
+      r_ri[i + 1] = r_ri[i] + (int)rev[i].size();
+      r_src.insert(r_src.end(), rev[i].begin(), rev[i].end());
+    }
+  }
+  auto alloc = [&](auto *&p, size_t cnt) {
+    return cudaMalloc((void **)&p, std::max<size_t>(cnt, 1) * sizeof(*p)) == cudaSuccess ? 0 : 1;
+  };
+  int bad = alloc(gs->q0, amoeba ? 10 * (size_t)mm : 1) | alloc(gs->frame, mm) | alloc(gs->mm_polar, mm) |
+            alloc(gs->t_ri, mm + 1) | alloc(gs->t_src, t_src.size()) | alloc(gs->t_sP, t_src.size()) |
+            alloc(gs->t_sD, t_src.size()) | alloc(gs->r_ri, mm + 1) | alloc(gs->r_src, r_src.size()) |
+            alloc(gs->mu, 3 * (size_t)nset * mm) | alloc(gs->partial, (size_t)gs->nsplit * nacc * mm) |
+            alloc(gs->base, 3 * (size_t)mm) | alloc(gs->rot, 12 * (size_t)mm) | alloc(gs->grad, 3 * (size_t)mm);
+  if (bad) {
+    cudaGetLastError();
+    free_grad_state(gs);
+    set_last_error("out of device memory for the polarization gradient");
+    return kErrMemory;
+  }
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
+  };
+  if (amoeba) up(gs->q0, m_.q0.data(), 10 * (size_t)mm * sizeof(double));
+  up(gs->frame, fr.data(), mm * sizeof(int4));
+  up(gs->mm_polar, m_.mm_polar.data(), mm * sizeof(int));
+  up(gs->t_ri, t_ri.data(), t_ri.size() * sizeof(int));
+  up(gs->t_src, t_src.data(), t_src.size() * sizeof(int));
+  up(gs->t_sP, t_sP.data(), t_sP.size() * sizeof(double));
+  up(gs->t_sD, t_sD.data(), t_sD.size() * sizeof(double));
+  up(gs->r_ri, r_ri.data(), r_ri.size() * sizeof(int));
+  up(gs->r_src, r_src.data(), r_src.size() * sizeof(int));
+  st = check(cudaStreamSynchronize(st_), "gradient setup");  // host vectors die here
+  if (st) {
+    free_grad_state(gs);
+    return st;
+  }
+  grad_ = gs;
+  return kOk;
+}
+
 int System::polelec_geomgrad(double *grad_h) {
   const int mm = d_.m, n = d_.n;
   std::fill(grad_h, grad_h + 3 * (size_t)mm, 0.0);
@@ -398,81 +501,8 @@ int System::polelec_geomgrad(double *grad_h) {
   const bool amoeba = m_.amoeba;
   const int nset = amoeba ? 2 : 1;
   const int nacc = amoeba ? gpu::Acc<true>::N : gpu::Acc<false>::N;
-  if (!grad_) {
-    GradState *gs = new GradState();
-    gs->mm = mm;
-    int resident = 0;
-    if (amoeba)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, gpu::k_grad_pairs<true>, gpu::GTPB, 0);
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, gpu::k_grad_pairs<false>, gpu::GTPB, 0);
-    gs->nsplit = gpu::grad_pick_split(mm, std::max(1, resident) * gpu::sm_count());
-    // M2D lists read by static site, and the frame reverse list
-    std::vector<int> t_ri(mm + 1, 0), t_src(m2d_pairs_.src.size());
-    std::vector<double> t_sP(t_src.size()), t_sD(t_src.size());
-    for (size_t k = 0; k < m2d_pairs_.src.size(); ++k) t_ri[m2d_pairs_.src[k] + 1]++;
-    for (int i = 0; i < mm; ++i) t_ri[i + 1] += t_ri[i];
-    {
-      std::vector<int> fill(t_ri.begin(), t_ri.end() - 1);
-      for (int j = 0; j < n; ++j)
-        for (int k = m2d_pairs_.ri[j]; k < m2d_pairs_.ri[j + 1]; ++k) {
-          const int i = m2d_pairs_.src[k], at = fill[i]++;
-          t_src[at] = j;
-          t_sP[at] = m2d_pairs_.sP[k];
-          t_sD[at] = amoeba ? m2d_pairs_.sD[k] : 1.0;
-        }
-    }
-    std::vector<int4> fr(mm);
-    std::vector<int> r_ri(mm + 1, 0), r_src;
-    for (int i = 0; i < mm; ++i) {
-      const int fk = amoeba ? m_.frame[i] : 0;
-      fr[i] = make_int4(fk, m_.iz[i] >= 0 ? m_.iz[i] : i, m_.ix[i] >= 0 ? m_.ix[i] : i, m_.iy[i] >= 0 ? m_.iy[i] : i);
-    }
-    {
-      std::vector<std::vector<int>> rev(mm);
-      for (int i = 0; i < mm; ++i) {
-        if (fr[i].x == 0) continue;
-        const int atoms[4] = {i, fr[i].y, fr[i].z, fr[i].w};
-        for (int w = 0; w < 4; ++w) rev[atoms[w]].push_back(4 * i + w);
-      }
-      for (int i = 0; i < mm; ++i) {
-        r_ri[i + 1] = r_ri[i] + (int)rev[i].size();
-        r_src.insert(r_src.end(), rev[i].begin(), rev[i].end());
-      }
-    }
-    auto alloc = [&](auto *&p, size_t cnt) {
-      return cudaMalloc((void **)&p, std::max<size_t>(cnt, 1) * sizeof(*p)) == cudaSuccess ? 0 : 1;
-    };
-    int bad = alloc(gs->q0, amoeba ? 10 * (size_t)mm : 1) | alloc(gs->frame, mm) | alloc(gs->mm_polar, mm) |
-              alloc(gs->t_ri, mm + 1) | alloc(gs->t_src, t_src.size()) | alloc(gs->t_sP, t_src.size()) |
-              alloc(gs->t_sD, t_src.size()) | alloc(gs->r_ri, mm + 1) | alloc(gs->r_src, r_src.size()) |
-              alloc(gs->mu, 3 * (size_t)nset * mm) | alloc(gs->partial, (size_t)gs->nsplit * nacc * mm) |
-              alloc(gs->base, 3 * (size_t)mm) | alloc(gs->rot, 12 * (size_t)mm) | alloc(gs->grad, 3 * (size_t)mm);
-    if (bad) {
-      cudaGetLastError();
-      free_grad_state(gs);
-      set_last_error("out of device memory for the polarization gradient");
-      return kErrMemory;
-    }
-    auto up = [&](void *dst, const void *src, size_t bytes) {
-      if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
-    };
-    if (amoeba) up(gs->q0, m_.q0.data(), 10 * (size_t)mm * sizeof(double));
-    up(gs->frame, fr.data(), mm * sizeof(int4));
-    up(gs->mm_polar, m_.mm_polar.data(), mm * sizeof(int));
-    up(gs->t_ri, t_ri.data(), t_ri.size() * sizeof(int));
-    up(gs->t_src, t_src.data(), t_src.size() * sizeof(int));
-    up(gs->t_sP, t_sP.data(), t_sP.size() * sizeof(double));
-    up(gs->t_sD, t_sD.data(), t_sD.size() * sizeof(double));
-    up(gs->r_ri, r_ri.data(), r_ri.size() * sizeof(int));
-    up(gs->r_src, r_src.data(), r_src.size() * sizeof(int));
-    st = check(cudaStreamSynchronize(st_), "gradient setup");  // host vectors die here
-    if (st) {
-      free_grad_state(gs);
-      return st;
-    }
-    grad_ = gs;
-  }
+  st = ensure_grad_state();
+  if (st) return st;
   GradState &gs = *grad_;
   gpu::GradArgs a{};
   a.mm = mm;
@@ -572,6 +602,35 @@ int System::polelec_geomgrad(double *grad_h) {
         "a problem in your input file, please check.");
     return kErrNumeric;
   }
+  if (flag & 2) {
+    std::fill(grad_h, grad_h + 3 * (size_t)mm, 0.0);
+    set_last_error("Ill defined rotation axis (either u or v vectors have 0 norm.");
+    return kErrInput;
+  }
+  return kOk;
+}
+
+int System::rotation_geomgrad(const double *E_h, const double *G_h, double *grad_h) {
+  const int mm = d_.m;
+  std::fill(grad_h, grad_h + 3 * (size_t)mm, 0.0);
+  if (mm == 0 || !m_.amoeba) return kOk;  // point charges have no frame
+  int st = ensure_grad_state();
+  if (st) return st;
+  GradState &gs = *grad_;
+  // E, G staged in the partial buffer (at least 24 mm doubles), zero base
+  double *E = gs.partial, *G = gs.partial + 3 * (size_t)mm;
+  cudaMemcpyAsync(E, E_h, 3 * (size_t)mm * sizeof(double), cudaMemcpyHostToDevice, st_);
+  cudaMemcpyAsync(G, G_h, 6 * (size_t)mm * sizeof(double), cudaMemcpyHostToDevice, st_);
+  cudaMemsetAsync(gs.base, 0, 3 * (size_t)mm * sizeof(double), st_);
+  cudaMemsetAsync(flag_, 0, sizeof(int), st_);
+  gpu::k_rot_terms<<<(mm + 127) / 128, 128, 0, st_>>>(mm, d_.mm_pos, gs.frame, gs.q0, E, G, gs.rot, flag_);
+  gpu::k_grad_gather<<<(mm + 255) / 256, 256, 0, st_>>>(mm, true, gs.base, gs.rot, gs.r_ri, gs.r_src, gs.grad);
+  gpu::add_launch_count(2);
+  int flag = 0;
+  cudaMemcpyAsync(grad_h, gs.grad, 3 * (size_t)mm * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  cudaMemcpyAsync(&flag, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  st = check(cudaStreamSynchronize(st_), "rotation gradient");
+  if (st) return st;
   if (flag & 2) {
     std::fill(grad_h, grad_h + 3 * (size_t)mm, 0.0);
     set_last_error("Ill defined rotation axis (either u or v vectors have 0 norm.");

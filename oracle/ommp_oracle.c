@@ -2244,3 +2244,15 @@ int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
     *energy = 0.5 * em;
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* ommp_rotation_geomgrad (src/mod_interface.F90:699-710): the output  */
+/* zeroed, then the frame forces of the rotated static dipoles and     */
+/* quadrupoles in a given E [mm][3] and field gradient G [mm][6]       */
+/* (src/rotate_multipoles.F90:3-230).  Point charges have no frame.    */
+/* ------------------------------------------------------------------ */
+int orc_rotation_geomgrad(orc_sys *s, const double *E, const double *G, double *grad) {
+    memset(grad, 0, 3 * (size_t)s->mm * sizeof(double));
+    if (!s->amoeba) return 0;
+    return rotation_geomgrad(s, E, G, grad, NULL);
+}

@@ -23,7 +23,10 @@ MATV_NONE, MATV_INCORE, MATV_DIRECT = 0, 1, 2
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc + OpenMP)."""
-    if force or not os.path.exists(_LIB_PATH):
+    srcs = [os.path.join(_HERE, f) for f in ("ommp_oracle.c", "ommp_oracle.h", "Makefile")]
+    stale = not os.path.exists(_LIB_PATH) or any(
+        os.path.getmtime(f) > os.path.getmtime(_LIB_PATH) for f in srcs if os.path.exists(f))
+    if force or stale:
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -65,6 +68,7 @@ def lib():
             "orc_polelec_geomgrad_atoms": (C.c_int, [vp, C.c_int32, ip, dp]),
             "orc_set_ipd": (C.c_int, [vp, dp]),
             "orc_get_fixedelec_energy": (C.c_int, [vp, dp]),
+            "orc_rotation_geomgrad": (C.c_int, [vp, dp, dp, dp]),
             "orc_nuclei_fields": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp, dp, dp, dp]),
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
@@ -232,6 +236,15 @@ class OracleSystem:
         e = C.c_double(0.0)
         self._check(lib().orc_get_fixedelec_energy(self._h, C.byref(e)))
         return e.value
+
+    def rotation_geomgrad(self, E, G):
+        """Frame forces [mm][3] of the static multipoles in the field E
+        [mm][3] and field gradient G [mm][6] (xx, xy, yy, xz, yz, zz)."""
+        E = np.ascontiguousarray(E, dtype=np.float64).reshape(self.mm_atoms, 3)
+        G = np.ascontiguousarray(G, dtype=np.float64).reshape(self.mm_atoms, 6)
+        g = np.zeros((self.mm_atoms, 3))
+        self._check(lib().orc_rotation_geomgrad(self._h, _dp(E), _dp(G), _dp(g)))
+        return g
 
     def nuclei_fields(self, cqm, qqm, grad=False):
         """QM-helper fields of point nuclei at the MM sites: E_n2p [npol][3]

@@ -140,3 +140,45 @@ def test_water_box_gradient_sampled(precision, tmp_path):
     atoms = np.sort(np.random.default_rng(7).choice(g.mm_atoms, 48, replace=False)).astype(np.int32)
     ref = o.polelec_geomgrad_atoms(atoms)
     assert np.abs(gg[atoms] - ref).max() / np.abs(ref).max() < 1e-11
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "1crn_amoeba", "1ubq_amoeba", "nma_wang", "1ubq_wang"])
+def test_rotation_gradient_matches_oracle(case, golden_mmp):
+    # ommp_rotation_geomgrad (src/rotate_multipoles.F90:3-230) in a random
+    # field and field gradient: FP64 frame pullback on the GPU against the
+    # oracle's rotation-matrix derivatives; zeros for point charges
+    g = OMMPSystem(golden_mmp[case])
+    o = OracleSystem(golden_mmp[case])
+    rng = np.random.default_rng(11)
+    E = rng.standard_normal((g.mm_atoms, 3)) * 1e-2
+    G = rng.standard_normal((g.mm_atoms, 6)) * 1e-2
+    gg = g.rotation_geomgrad(E, G)
+    go = o.rotation_geomgrad(E, G)
+    if case.endswith("wang"):
+        assert not gg.any() and not go.any()
+        return
+    assert maxrel(gg, go) < 1e-12
+    # again after a coordinate update (frames follow the new geometry)
+    c = g.cmm + rng.standard_normal((g.mm_atoms, 3)) * 1e-2
+    g.update_coordinates(c)
+    o.update_coordinates(c)
+    assert maxrel(g.rotation_geomgrad(E, G), o.rotation_geomgrad(E, G)) < 1e-12
+
+
+def test_rotation_gradient_rejects_bad_shapes(golden_mmp):
+    g = OMMPSystem(golden_mmp["nma_amoeba"])
+    with pytest.raises(ValueError):
+        g.rotation_geomgrad(np.zeros((g.mm_atoms, 6)), np.zeros((g.mm_atoms, 6)))
+
+
+def test_rotation_gradient_on_water_box(tmp_path):
+    # the water box's bisector frames (6,000 sites)
+    p = synth.write_mmp(str(tmp_path / "w.mmp"), synth.water_cluster(2000, seed=4))
+    g = OMMPSystem(p)
+    o = OracleSystem(p)
+    rng = np.random.default_rng(2)
+    E = rng.standard_normal((g.mm_atoms, 3))
+    G = rng.standard_normal((g.mm_atoms, 6))
+    gg = g.rotation_geomgrad(E, G)
+    assert maxrel(gg, o.rotation_geomgrad(E, G)) < 1e-12
+    assert np.abs(gg.sum(axis=0)).max() < 1e-10 * np.abs(gg).max()

@@ -90,3 +90,44 @@ def test_gradient_rows_and_installed_dipoles(case, golden_mmp):
     o2 = OracleSystem(golden_mmp[case])
     o2.set_ipd(o.ipd)
     assert np.array_equal(o2.polelec_geomgrad(), g)
+
+
+def rotation_energy(o, c, E, G):
+    """-mu.E + Q:G of the rotated static multipoles at geometry c (E, G held
+    fixed; off-diagonal quadrupole components counted twice)."""
+    o.update_coordinates(c)
+    q = o.q
+    w = np.array([1.0, 2.0, 1.0, 2.0, 2.0, 1.0])
+    return -np.sum(q[:, 1:4] * E) + np.sum(q[:, 4:10] * G * w)
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "1crn_amoeba"])
+def test_rotation_gradient_matches_finite_differences(case, golden_mmp):
+    # ommp_rotation_geomgrad (src/rotate_multipoles.F90:3-230) is the
+    # derivative of -mu.E + Q:G through the frame rotation alone
+    o = OracleSystem(golden_mmp[case])
+    rng = np.random.default_rng(5)
+    E = rng.standard_normal((o.mm_atoms, 3)) * 1e-2
+    G = rng.standard_normal((o.mm_atoms, 6)) * 1e-2
+    c0 = o.cmm.copy()
+    g = o.rotation_geomgrad(E, G)
+    atoms = range(o.mm_atoms) if o.mm_atoms < 40 else [0, 1, 2, 57, 101, 250, 377, 640]
+    h = 1e-5
+    fd = np.zeros((len(atoms), 3))
+    for r, a in enumerate(atoms):
+        for k in range(3):
+            cp, cm = c0.copy(), c0.copy()
+            cp[a, k] += h
+            cm[a, k] -= h
+            fd[r, k] = (rotation_energy(o, cp, E, G) - rotation_energy(o, cm, E, G)) / (2 * h)
+    o.update_coordinates(c0)
+    assert np.abs(g).max() > 0
+    assert np.abs(fd - g[list(atoms)]).max() / np.abs(g).max() < 1e-8
+    # the rotation forces of a rigid frame sum to zero (no net force)
+    assert np.abs(g.sum(axis=0)).max() < 1e-12 * np.abs(g).max() * o.mm_atoms
+
+
+def test_rotation_gradient_of_point_charges_is_zero(golden_mmp):
+    o = OracleSystem(golden_mmp["nma_wang"])
+    g = o.rotation_geomgrad(np.ones((o.mm_atoms, 3)), np.ones((o.mm_atoms, 6)))
+    assert g.shape == (o.mm_atoms, 3) and not g.any()

@@ -150,6 +150,13 @@ void ommp_field_pol2ext(OMMP_SYSTEM_PRT s, int32_t n, const double *cext, double
  * are solved first (default solver) when the system has none.  FP64 on the
  * GPU whatever the precision mode. */
 void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
+/* include/openmmpol.h:90 ; src/mod_c_interface.F90:818-831,
+ * ommp_fixedelec_geomgrad src/mod_interface.F90:657-668, fixedelec_geomgrad
+ * src/mod_geomgrad.F90:17-111.  Geometric gradient of the static multipole
+ * energy (the m-scaled, undamped interaction of the static multipoles),
+ * grd [mm_atoms][3] overwritten; FP64 on the GPU, computed once per
+ * geometry. */
+void ommp_fixedelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
 /* include/openmmpol.h:92 ; src/mod_c_interface.F90:606-624,
  * ommp_rotation_geomgrad src/mod_interface.F90:699-710, rotation_geomgrad
  * src/rotate_multipoles.F90:3-230.  Forces from the frame dependence of the
@@ -221,6 +228,8 @@ int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *energy);
 int32_t ommp_gpu_get_fixedelec_energy(OMMP_SYSTEM_PRT s, double *energy);
 /* ommp_polelec_geomgrad returning a status instead of stopping the process */
 int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
+/* ommp_fixedelec_geomgrad returning a status */
+int32_t ommp_gpu_fixedelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
 /* ommp_rotation_geomgrad returning a status */
 int32_t ommp_gpu_rotation_geomgrad(OMMP_SYSTEM_PRT s, const double *E, const double *Egrd, double *grd);
 /* FMM on (on != 0) or off, with expansion order 2..12 */

@@ -160,29 +160,46 @@ class OMMPSystem:
         _check(self._L.ommp_gpu_get_fixedelec_energy(self._h, C.byref(e)))
         return e.value
 
-    def polelec_geomgrad(self, numerical: bool = False) -> np.ndarray:
-        """Geometric gradient of the polarization energy, [mm_atoms, 3].
-
-        Mirrors the reference's OMMPSystem.polelec_geomgrad
-        (pythonapi/pyopenmmpol/pyommp_interface.cpp:592-606): analytic on the
-        GPU, or with numerical=True central differences of
-        get_polelec_energy with a 1e-5 bohr step (:518-543)."""
+    def _numerical_grad(self, energy) -> np.ndarray:
+        """Central differences of energy() with a 1e-5 bohr step, as the
+        reference's numerical_grad (pythonapi/pyopenmmpol/pyommp_interface.cpp:518-543)."""
         g = np.zeros((self.mm_atoms, 3))
-        if not numerical:
-            _check(self._L.ommp_gpu_polelec_geomgrad(self._h, g.ctypes.data_as(_lib._dp)))
-            return g
         c0 = np.array(self.cmm, copy=True)
         c = c0.copy()
         dd = 1e-5
         for k in range(c.size):
             c.flat[k] = c0.flat[k] + dd
             self.update_coordinates(c)
-            ep = self.get_polelec_energy()
+            ep = energy()
             c.flat[k] = c0.flat[k] - dd
             self.update_coordinates(c)
-            g.flat[k] = (ep - self.get_polelec_energy()) / (2 * dd)
+            g.flat[k] = (ep - energy()) / (2 * dd)
             c.flat[k] = c0.flat[k]
         self.update_coordinates(c0)
+        return g
+
+    def polelec_geomgrad(self, numerical: bool = False) -> np.ndarray:
+        """Geometric gradient of the polarization energy, [mm_atoms, 3].
+
+        Mirrors the reference's OMMPSystem.polelec_geomgrad
+        (pythonapi/pyopenmmpol/pyommp_interface.cpp:592-606): analytic on the
+        GPU, or with numerical=True central differences of
+        get_polelec_energy."""
+        if numerical:
+            return self._numerical_grad(self.get_polelec_energy)
+        g = np.zeros((self.mm_atoms, 3))
+        _check(self._L.ommp_gpu_polelec_geomgrad(self._h, g.ctypes.data_as(_lib._dp)))
+        return g
+
+    def fixedelec_geomgrad(self, numerical: bool = False) -> np.ndarray:
+        """Geometric gradient of the static multipole energy, [mm_atoms, 3]
+        (pythonapi/pyopenmmpol/pyommp_interface.cpp:574-590): analytic on the
+        GPU, or with numerical=True central differences of
+        get_fixedelec_energy."""
+        if numerical:
+            return self._numerical_grad(self.get_fixedelec_energy)
+        g = np.zeros((self.mm_atoms, 3))
+        _check(self._L.ommp_gpu_fixedelec_geomgrad(self._h, g.ctypes.data_as(_lib._dp)))
         return g
 
     def rotation_geomgrad(self, E, Egrd) -> np.ndarray:

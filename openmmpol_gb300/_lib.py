@@ -74,6 +74,8 @@ SIGNATURES = {
     "ommp_field_pol2ext": (None, [_vp, C.c_int32, _dp, _dp]),
     "ommp_polelec_geomgrad": (None, [_vp, _dp]),
     "ommp_gpu_polelec_geomgrad": (C.c_int32, [_vp, _dp]),
+    "ommp_fixedelec_geomgrad": (None, [_vp, _dp]),
+    "ommp_gpu_fixedelec_geomgrad": (C.c_int32, [_vp, _dp]),
     "ommp_rotation_geomgrad": (None, [_vp, _dp, _dp, _dp]),
     "ommp_gpu_rotation_geomgrad": (C.c_int32, [_vp, _dp, _dp, _dp]),
     "ommp_gpu_set_fmm": (C.c_int32, [_vp, C.c_int32, C.c_int32]),

@@ -164,6 +164,13 @@ int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) {
   return st;
 }
 void ommp_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) { fatal_if(ommp_gpu_polelec_geomgrad(s, grd)); }
+int32_t ommp_gpu_fixedelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) {
+  ommp_time_push();
+  int st = S(s)->fixedelec_geomgrad(grd);
+  if (st == ommp::kOk) ommp_time_pull("Fixed Elctrostatic grad");
+  return st;
+}
+void ommp_fixedelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd) { fatal_if(ommp_gpu_fixedelec_geomgrad(s, grd)); }
 int32_t ommp_gpu_rotation_geomgrad(OMMP_SYSTEM_PRT s, const double *E, const double *Egrd, double *grd) {
   ommp_time_push();
   int st = S(s)->rotation_geomgrad(E, Egrd, grd);

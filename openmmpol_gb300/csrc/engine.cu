@@ -898,6 +898,7 @@ int System::update_coordinates(const double *c) {
   }
   m2d_done_ = ipd_done_ = ipd_use_guess_ = false;
   fixedelec_done_ = false;
+  fixedelec_grad_done_ = false;
   tmat_ok_ = lu_ok_ = false;
   return upload_geometry();
 }

@@ -101,6 +101,8 @@ class System {
   // forces of the frame rotation of the static multipoles in a given field
   // E [mm][3] and field gradient G [mm][6], out [mm][3] (overwritten)
   int rotation_geomgrad(const double *E_host, const double *G_host, double *grad_host);
+  // gradient of the static multipole energy, out [mm][3] (overwritten)
+  int fixedelec_geomgrad(double *grad_host);
   // fast multipole method for the FP64 T.mu products (expansion order 2..12)
   int set_fmm(bool on, int order);
   bool fmm_on() const { return fmm_on_; }
@@ -250,8 +252,12 @@ class System {
   void kt_resolve();
   bool fixedelec_done_ = false;
   double fixedelec_ = 0.0;
+  bool fixedelec_grad_done_ = false;
+  std::vector<double> fixedelec_grad_;
+  int m2m_launch(bool grad, double **buf, double **site, double **E, double **G, double **base);
   GradState *grad_ = nullptr;
   int ensure_grad_state();
+  int frame_forces(const double *E_dev, const double *G_dev, const double *base_dev, double *grad_host);
   FmmState *fmm_ = nullptr;
   bool fmm_on_ = false;
   int fmm_order_ = 10;  // total order |g| + |h| <= 10 of the Cartesian M2L

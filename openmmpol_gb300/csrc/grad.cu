@@ -610,6 +610,31 @@ int System::polelec_geomgrad(double *grad_h) {
   return kOk;
 }
 
+// gradient = base [mm][3] + the frame forces of the static multipoles in E
+// [mm][3] and field gradient G [mm][6] (device arrays), copied to grad_h
+int System::frame_forces(const double *E, const double *G, const double *base, double *grad_h) {
+  const int mm = d_.m;
+  int st = ensure_grad_state();
+  if (st) return st;
+  GradState &gs = *grad_;
+  const bool amoeba = m_.amoeba;
+  cudaMemsetAsync(flag_, 0, sizeof(int), st_);
+  if (amoeba) gpu::k_rot_terms<<<(mm + 127) / 128, 128, 0, st_>>>(mm, d_.mm_pos, gs.frame, gs.q0, E, G, gs.rot, flag_);
+  gpu::k_grad_gather<<<(mm + 255) / 256, 256, 0, st_>>>(mm, amoeba, base, gs.rot, gs.r_ri, gs.r_src, gs.grad);
+  gpu::add_launch_count(amoeba ? 2 : 1);
+  int flag = 0;
+  cudaMemcpyAsync(grad_h, gs.grad, 3 * (size_t)mm * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  cudaMemcpyAsync(&flag, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+  st = check(cudaStreamSynchronize(st_), "frame forces");
+  if (st) return st;
+  if (flag & 2) {
+    std::fill(grad_h, grad_h + 3 * (size_t)mm, 0.0);
+    set_last_error("Ill defined rotation axis (either u or v vectors have 0 norm.");
+    return kErrInput;
+  }
+  return kOk;
+}
+
 int System::rotation_geomgrad(const double *E_h, const double *G_h, double *grad_h) {
   const int mm = d_.m;
   std::fill(grad_h, grad_h + 3 * (size_t)mm, 0.0);
@@ -622,21 +647,7 @@ int System::rotation_geomgrad(const double *E_h, const double *G_h, double *grad
   cudaMemcpyAsync(E, E_h, 3 * (size_t)mm * sizeof(double), cudaMemcpyHostToDevice, st_);
   cudaMemcpyAsync(G, G_h, 6 * (size_t)mm * sizeof(double), cudaMemcpyHostToDevice, st_);
   cudaMemsetAsync(gs.base, 0, 3 * (size_t)mm * sizeof(double), st_);
-  cudaMemsetAsync(flag_, 0, sizeof(int), st_);
-  gpu::k_rot_terms<<<(mm + 127) / 128, 128, 0, st_>>>(mm, d_.mm_pos, gs.frame, gs.q0, E, G, gs.rot, flag_);
-  gpu::k_grad_gather<<<(mm + 255) / 256, 256, 0, st_>>>(mm, true, gs.base, gs.rot, gs.r_ri, gs.r_src, gs.grad);
-  gpu::add_launch_count(2);
-  int flag = 0;
-  cudaMemcpyAsync(grad_h, gs.grad, 3 * (size_t)mm * sizeof(double), cudaMemcpyDeviceToHost, st_);
-  cudaMemcpyAsync(&flag, flag_, sizeof(int), cudaMemcpyDeviceToHost, st_);
-  st = check(cudaStreamSynchronize(st_), "rotation gradient");
-  if (st) return st;
-  if (flag & 2) {
-    std::fill(grad_h, grad_h + 3 * (size_t)mm, 0.0);
-    set_last_error("Ill defined rotation axis (either u or v vectors have 0 norm.");
-    return kErrInput;
-  }
-  return kOk;
+  return frame_forces(E, G, gs.base, grad_h);
 }
 
 }  // namespace ommp

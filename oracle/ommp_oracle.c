@@ -2153,13 +2153,38 @@ int orc_nuclei_fields(orc_sys *s, int32_t which, int32_t nq, const double *cqm, 
 }
 
 /* ------------------------------------------------------------------ */
-/* Static multipole energy (fixed electrostatics): energy_MM_MM        */
-/* (src/mod_electrostatics.F90:899-941) on the potential, field and    */
-/* field gradient of the static multipoles at the static sites,        */
-/* elec_prop_M2M direct path (:1678-1952), undamped coulomb_kernel,    */
-/* list_S_S of m-scaled pairs (:597-648, screening_rules 'S','S').     */
+/* Electrostatic properties of the static multipoles at the static     */
+/* sites, elec_prop_M2M direct path (src/mod_electrostatics.F90:       */
+/* 1678-1952): undamped coulomb_kernel, list_S_S of m-scaled pairs     */
+/* (:597-648, screening_rules 'S','S'); potential V [mm], field E      */
+/* [mm][3], and for AMOEBA field gradient G [mm][6] and (H not NULL)   */
+/* field Hessian H [mm][10], from q_elec_prop / mu_elec_prop /         */
+/* quad_elec_prop (:1097-1405).                                        */
 /* ------------------------------------------------------------------ */
-int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
+/* field Hessian of a point charge (q_elec_prop, do_HE) */
+static void q_hess(double q, const double *d, const double *k, double *h) {
+    for (int c = 0; c < 10; c++) {
+        int a = H10A[c], b = H10B[c], e = H10C[c];
+        h[c] += q * (15.0 * k[3] * d[a] * d[b] * d[e] - 3.0 * k[2] * (kd(a, b) * d[e] + kd(a, e) * d[b] + kd(b, e) * d[a]));
+    }
+}
+/* field Hessian of a point quadrupole stored xx,xy,yy,xz,yz,zz (quad_elec_prop, do_HE) */
+static void quad_hess(const double *q6, const double *d, const double *k, double *h) {
+    double Q[3][3] = {{q6[0], q6[1], q6[3]}, {q6[1], q6[2], q6[4]}, {q6[3], q6[4], q6[5]}};
+    double t[3];
+    for (int a = 0; a < 3; a++) t[a] = Q[a][0] * d[0] + Q[a][1] * d[1] + Q[a][2] * d[2];
+    double sdr = t[0] * d[0] + t[1] * d[1] + t[2] * d[2];
+    for (int c = 0; c < 10; c++) {
+        int a = H10A[c], b = H10B[c], e = H10C[c];
+        h[c] += 945.0 * k[5] * sdr * d[a] * d[b] * d[e] -
+                105.0 * k[4] * (sdr * (kd(a, b) * d[e] + kd(a, e) * d[b] + kd(b, e) * d[a]) +
+                                2.0 * (t[a] * d[b] * d[e] + t[b] * d[a] * d[e] + t[e] * d[a] * d[b])) +
+                30.0 * k[3] * (Q[a][b] * d[e] + Q[a][e] * d[b] + Q[b][e] * d[a] + kd(a, b) * t[e] + kd(a, e) * t[b] +
+                               kd(b, e) * t[a]);
+    }
+}
+
+static int m2m_props(orc_sys *s, double *V, double *E, double *G, double *H) {
     const int mm = s->mm, amoeba = s->amoeba, ld = s->ld_cart;
     /* list_S_S: row i, pairs within four bonds whose scale is not 1 */
     lbuild_t b;
@@ -2175,8 +2200,10 @@ int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
     }
     slist_t ss;
     lb_finish(&b, &ss);
-    double *V = xcalloc(mm, sizeof(double)), *E = xcalloc(3 * (size_t)mm, sizeof(double));
-    double *G = xcalloc(6 * (size_t)mm, sizeof(double));
+    memset(V, 0, mm * sizeof(double));
+    memset(E, 0, 3 * (size_t)mm * sizeof(double));
+    if (amoeba) memset(G, 0, 6 * (size_t)mm * sizeof(double));
+    if (amoeba && H) memset(H, 0, 10 * (size_t)mm * sizeof(double));
     int bad = 0;
 #pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
     for (int j = 0; j < mm; j++) {
@@ -2197,11 +2224,11 @@ int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
                 bad = 1;
                 continue;
             }
-            double k[5];
+            double k[6];
             k[0] = 1.0 / r;
-            for (int l = 1; l < 5; l++) k[l] = k[l - 1] / (r * r);
+            for (int l = 1; l < 6; l++) k[l] = k[l - 1] / (r * r);
             const double *q = &s->q[(size_t)ld * i];
-            double v = q[0] * k[0], e[3], g[6] = {0, 0, 0, 0, 0, 0};
+            double v = q[0] * k[0], e[3], g[6] = {0, 0, 0, 0, 0, 0}, h[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
             for (int c = 0; c < 3; c++) e[c] = q[0] * k[1] * d[c];
             if (amoeba) {
                 double md = q[1] * d[0] + q[2] * d[1] + q[3] * d[2];
@@ -2213,18 +2240,42 @@ int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
                 for (int c = 0; c < 3; c++)
                     e[c] += 3.0 * md * d[c] * k[2] - q[1 + c] * k[1] + 15.0 * dqd * d[c] * k[3] - 6.0 * t[c] * k[2];
                 q_grad(q[0], d, k, g);
-                mu_grad(&q[1], d, k, g, NULL);
+                mu_grad(&q[1], d, k, g, H ? h : NULL);
                 quad_grad(&q[4], d, k, g);
+                if (H) {
+                    q_hess(q[0], d, k, h);
+                    quad_hess(&q[4], d, k, h);
+                }
             }
             const double w = (kk >= 0) ? sc : 1.0;
             V[j] += v * w;
             for (int c = 0; c < 3; c++) E[3 * (size_t)j + c] += e[c] * w;
             if (amoeba)
                 for (int c = 0; c < 6; c++) G[6 * (size_t)j + c] += g[c] * w;
+            if (amoeba && H)
+                for (int c = 0; c < 10; c++) H[10 * (size_t)j + c] += h[c] * w;
         }
     }
+    free(ss.m.ri), free(ss.m.ci), free(ss.scale), free(ss.todo);
+    if (bad) {
+        set_err("Requesting Coulomb kernel for two atoms placed in the same point, this could be an internal bug or "
+                "a problem in your input file, please check.");
+        return ORC_ERR_NUMERIC;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Static multipole energy (fixed electrostatics): energy_MM_MM        */
+/* (src/mod_electrostatics.F90:899-941) on m2m_props.                  */
+/* ------------------------------------------------------------------ */
+int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
+    const int mm = s->mm, amoeba = s->amoeba, ld = s->ld_cart;
+    double *V = xcalloc(mm, sizeof(double)), *E = xcalloc(3 * (size_t)mm, sizeof(double));
+    double *G = xcalloc(6 * (size_t)mm, sizeof(double));
+    int st = m2m_props(s, V, E, G, NULL);
     double em = 0.0;
-    if (!bad)
+    if (!st)
         for (int j = 0; j < mm; j++) {
             const double *q = &s->q[(size_t)ld * j];
             em += q[0] * V[j];
@@ -2235,14 +2286,41 @@ int orc_get_fixedelec_energy(orc_sys *s, double *energy) {
             }
         }
     free(V), free(E), free(G);
-    free(ss.m.ri), free(ss.m.ci), free(ss.scale), free(ss.todo);
-    if (bad) {
-        set_err("Requesting Coulomb kernel for two atoms placed in the same point, this could be an internal bug or "
-                "a problem in your input file, please check.");
-        return ORC_ERR_NUMERIC;
-    }
+    if (st) return st;
     *energy = 0.5 * em;
     return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* ommp_fixedelec_geomgrad (src/mod_interface.F90:657-668): the output */
+/* zeroed, then fixedelec_geomgrad (src/mod_geomgrad.F90:17-111):      */
+/* per static site -q E + mu.Egrd - Q:EHes (off-diagonal quadrupole    */
+/* components twice) and, for AMOEBA, rotation_geomgrad with E, Egrd.  */
+/* ------------------------------------------------------------------ */
+int orc_fixedelec_geomgrad(orc_sys *s, double *grad) {
+    const int mm = s->mm, amoeba = s->amoeba, ld = s->ld_cart;
+    memset(grad, 0, 3 * (size_t)mm * sizeof(double));
+    double *V = xcalloc(mm, sizeof(double)), *E = xcalloc(3 * (size_t)mm, sizeof(double));
+    double *G = xcalloc(6 * (size_t)mm, sizeof(double)), *H = xcalloc(10 * (size_t)mm, sizeof(double));
+    int st = m2m_props(s, V, E, G, H);
+    if (!st) {
+        for (int i = 0; i < mm; i++) {
+            const double *q = &s->q[(size_t)ld * i], *e = &E[3 * (size_t)i];
+            double *g = &grad[3 * (size_t)i];
+            for (int a = 0; a < 3; a++) g[a] -= q[0] * e[a];
+            if (!amoeba) continue;
+            const double *eg = &G[6 * (size_t)i], *h = &H[10 * (size_t)i];
+            double Q[3][3] = {{q[4], q[5], q[7]}, {q[5], q[6], q[8]}, {q[7], q[8], q[9]}};
+            for (int a = 0; a < 3; a++) {
+                for (int b = 0; b < 3; b++) g[a] += q[1 + b] * eg[G6[a][b]];
+                for (int b = 0; b < 3; b++)
+                    for (int c = 0; c < 3; c++) g[a] -= Q[b][c] * h[H10[b][c][a]];
+            }
+        }
+        if (amoeba) st = rotation_geomgrad(s, E, G, grad, NULL);
+    }
+    free(V), free(E), free(G), free(H);
+    return st;
 }
 
 /* ------------------------------------------------------------------ */

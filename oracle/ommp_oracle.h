@@ -127,6 +127,9 @@ int orc_get_fixedelec_energy(orc_sys *s, double *energy);
 /* ommp_rotation_geomgrad: frame forces of the static multipoles in E [mm][3]
    and field gradient G [mm][6]; grad [mm][3] overwritten */
 int orc_rotation_geomgrad(orc_sys *s, const double *E, const double *G, double *grad);
+/* ommp_fixedelec_geomgrad: gradient of the static multipole energy,
+   grad [mm][3] overwritten */
+int orc_fixedelec_geomgrad(orc_sys *s, double *grad);
 int orc_nuclei_fields(orc_sys *s, int32_t which, int32_t nq, const double *cqm, const double *qqm, double *E,
                       double *G, double *H);
 

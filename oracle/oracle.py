@@ -69,6 +69,7 @@ def lib():
             "orc_set_ipd": (C.c_int, [vp, dp]),
             "orc_get_fixedelec_energy": (C.c_int, [vp, dp]),
             "orc_rotation_geomgrad": (C.c_int, [vp, dp, dp, dp]),
+            "orc_fixedelec_geomgrad": (C.c_int, [vp, dp]),
             "orc_nuclei_fields": (C.c_int, [vp, C.c_int32, C.c_int32, dp, dp, dp, dp, dp]),
             "orc_set_external_field": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32]),
             "orc_get_polelec_energy": (C.c_double, [vp, ip]),
@@ -236,6 +237,12 @@ class OracleSystem:
         e = C.c_double(0.0)
         self._check(lib().orc_get_fixedelec_energy(self._h, C.byref(e)))
         return e.value
+
+    def fixedelec_geomgrad(self):
+        """Gradient [mm][3] of the static multipole energy."""
+        g = np.zeros((self.mm_atoms, 3))
+        self._check(lib().orc_fixedelec_geomgrad(self._h, _dp(g)))
+        return g
 
     def rotation_geomgrad(self, E, G):
         """Frame forces [mm][3] of the static multipoles in the field E

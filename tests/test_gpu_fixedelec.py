@@ -3,7 +3,12 @@
 against the reference's EM goldens (printed to 13 digits: 1e-11 relative) and
 against the oracle on a synthetic water box and after a coordinate update
 (1e-9: the water total is ~1,000 times smaller than its largest site terms,
-whose FP64 sums differ in order between the two)."""
+whose FP64 sums differ in order between the two).
+
+Its gradient (ommp_fixedelec_geomgrad, src/mod_geomgrad.F90:17-111) against
+the oracle's restatement (itself pinned by finite differences of the energy):
+1e-11 of the largest component; the GPU's own finite differences (the
+reference's numerical=True) on a small system; zero net force."""
 import numpy as np
 import pytest
 
@@ -38,3 +43,44 @@ def test_static_energy_water_and_update(tmp_path):
     e2 = g.get_fixedelec_energy()
     assert e2 != e
     assert abs(e2 - o.get_fixedelec_energy()) <= 1e-9 * abs(e2)
+
+
+def maxrel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "nma_wang", "nma_amoeba_cut", "1crn_amoeba", "1crn_wang",
+                                  "1ubq_amoeba", "1ubq_wang", "1ao6cut_wang"])
+def test_static_gradient_matches_oracle(case, golden_mmp):
+    g, o = OMMPSystem(golden_mmp[case]), OracleSystem(golden_mmp[case])
+    gg = g.fixedelec_geomgrad()
+    go = o.fixedelec_geomgrad()
+    assert maxrel(gg, go) < 1e-11
+    # no net force, up to the quadrupole trace of the 1crn / 1ubq inputs
+    # (3.3e-6), which the reference's fields drop and its Hessian keeps
+    net = 1e-6 if case.startswith(("1crn_amoeba", "1ubq_amoeba")) else 1e-10
+    assert np.abs(gg.sum(axis=0)).max() < net * np.abs(gg).max()
+    assert np.array_equal(g.fixedelec_geomgrad(), gg)  # cached per geometry
+
+
+@pytest.mark.parametrize("case", ["nma_amoeba", "nma_wang"])
+def test_static_gradient_matches_finite_differences(case, golden_mmp):
+    g = OMMPSystem(golden_mmp[case])
+    ga = g.fixedelec_geomgrad()
+    gn = g.fixedelec_geomgrad(numerical=True)
+    # the quotient divides energy differences of ~1e-15 (the rounding of
+    # the GPU's pair sums) by 2e-5 bohr: 1e-7 of the largest component
+    assert maxrel(gn, ga) < 2e-7
+
+
+def test_static_gradient_water_and_update(tmp_path):
+    p = synth.write_mmp(str(tmp_path / "w.mmp"), synth.water_cluster(1500, seed=4))
+    g, o = OMMPSystem(p), OracleSystem(p)
+    gg = g.fixedelec_geomgrad()
+    assert maxrel(gg, o.fixedelec_geomgrad()) < 1e-11
+    c = g.cmm + np.random.default_rng(3).normal(scale=0.05, size=(g.mm_atoms, 3))
+    g.update_coordinates(c)
+    o.update_coordinates(c)
+    g2 = g.fixedelec_geomgrad()
+    assert not np.array_equal(g2, gg)
+    assert maxrel(g2, o.fixedelec_geomgrad()) < 1e-11

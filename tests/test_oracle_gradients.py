@@ -131,3 +131,33 @@ def test_rotation_gradient_of_point_charges_is_zero(golden_mmp):
     o = OracleSystem(golden_mmp["nma_wang"])
     g = o.rotation_geomgrad(np.ones((o.mm_atoms, 3)), np.ones((o.mm_atoms, 6)))
     assert g.shape == (o.mm_atoms, 3) and not g.any()
+
+
+@pytest.mark.parametrize("case,tol", [("nma_amoeba", 1e-8), ("nma_wang", 1e-8), ("1crn_amoeba", 5e-8)])
+def test_static_gradient_matches_finite_differences(case, tol, golden_mmp):
+    # fixedelec_geomgrad (src/mod_geomgrad.F90:17-111) against central
+    # differences of the static multipole energy, which holds the
+    # reference's EM goldens (tests/test_oracle_golden.py); 1crn's larger
+    # total energy leaves ~5e-10 of rounding in each difference quotient
+    o = OracleSystem(golden_mmp[case])
+    g = o.fixedelec_geomgrad()
+    c0 = o.cmm.copy()
+    atoms = range(o.mm_atoms) if o.mm_atoms < 40 else [0, 1, 57, 250, 377, 640]
+    h = 1e-5
+    fd = np.zeros((len(atoms), 3))
+    for r, a in enumerate(atoms):
+        for k in range(3):
+            cp, cm = c0.copy(), c0.copy()
+            cp[a, k] += h
+            cm[a, k] -= h
+            o.update_coordinates(cp)
+            ep = o.get_fixedelec_energy()
+            o.update_coordinates(cm)
+            fd[r, k] = (ep - o.get_fixedelec_energy()) / (2 * h)
+    o.update_coordinates(c0)
+    assert np.abs(fd - g[list(atoms)]).max() / np.abs(g).max() < tol
+    # no net force, up to the 1crn input's quadrupole trace (3.3e-6 on two
+    # oxygens): the reference's fields drop the trace, its Hessian
+    # contraction keeps it, so the pair terms are not exactly antisymmetric
+    net = 1e-6 if case.startswith("1crn") else 1e-12 * o.mm_atoms
+    assert np.abs(g.sum(axis=0)).max() < net * np.abs(g).max()

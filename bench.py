@@ -17,9 +17,11 @@ in the reference (src/mod_electrostatics.F90:1487-1596, M2D_done cache).
   ``fp64.fmm``: the same solve and a strict mixed solve with the FP64 products
   and the permanent field from the fast multipole method (default order 10),
   with their error against it.
-* ``roofline``: the dominant pair kernel, its algorithmic flops (45 per ordered
-  pair per right-hand side) over its CUDA-event time, against the FMA pipe
-  peak measured in the same run.
+* ``roofline``: the dominant pair kernel, its algorithmic operations over its
+  CUDA-event time against its pipe's peak measured in the same run: FP64
+  instructions of the symmetric FP64 product (32 per unordered pair and
+  right-hand side, both directions), FP32 instructions of the double-single
+  product; the conventional 45 flop per ordered pair is reported beside.
 * ``geomgrad``: the polarization-energy gradient (ommp_polelec_geomgrad) on
   the solved system: calls/s with the double-single pair passes of the mixed
   modes and with the FP64 pass, each against its pipe, their difference, and
@@ -48,7 +50,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "induced-dipole solves/s (mixed FP32/FP64 at <=1e-7 rel. error vs FP64)"
-FLOP_PER_PAIR = 45.0  # per ordered T.mu pair and right-hand side
+FLOP_PER_PAIR = 45.0  # per ordered T.mu pair and right-hand side (conventional count)
+# FP64 operations (an FMA counts once) per unordered pair and right-hand side
+# of the symmetric FP64 product (k_tmu_sym, openmmpol_gb300/csrc/kernels.cu,
+# both directions): 3 coordinate differences, r^2 (3), the Newton step of the
+# reciprocal square root (3), r^-2 / r^-3 / r^-5 (3) and per direction mu.d
+# (3), the field factor (1) and six accumulations (6); the FP32 seed, the
+# conversions and the damping pre-test run on other pipes
+FP64_SYM_OPS_PER_PAIR = 32.0
+SYM_MIN_SITES = 2048  # the engine's automatic choice of the symmetric product
 # FP32 operations (an FMA counts once) per undamped ordered pair of the
 # double-single kernel, counted in openmmpol_gb300/csrc/ds_kernels.cu: 3 coordinate differences
 # (33), r^2 (31), reciprocal square root (17 + 1 MUFU), r^-2 / r^-3 / 3 r^-5
@@ -251,10 +261,16 @@ def kernel_table(kst, n, peak64, peak32):
                                       ("tmu_ds", kst[2], peak32)):
         if not cnt:
             continue
-        # algorithmic flop of all timed launches: 45 per ordered pair per column
+        # conventional flop of all timed launches: 45 per ordered pair per column
         ach = FLOP_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
         out[name] = {"launches": cnt, "columns": cols, "total_ms": ms, "avg_ms": ms / cnt,
                      "achieved_tflops": ach, "peak_tflops": pk, "frac": ach / pk if pk else None}
+        if name == "tmu_fp64" and n >= SYM_MIN_SITES:
+            # FP64 pipe: operations of the symmetric product issued per second
+            # against the FP64 instruction rate (peak flop / 2)
+            ops = FP64_SYM_OPS_PER_PAIR * pairs / 2 * cols / (ms * 1e-3) / 1e12
+            out[name].update({"fp64_flop_equivalent_tflops": ach, "achieved_tops": ops, "peak_tops": pk / 2,
+                              "frac": ops / (pk / 2) if pk else None})
         if name == "tmu_ds":
             # FP32 pipe: double-single operations issued per second against
             # the FMA-pipe instruction rate (peak flop / 2)
@@ -277,20 +293,23 @@ def roofline_of(kstats, total_ms, n=30000):
     dom = max(kstats, key=lambda k: kstats[k]["total_ms"])
     d = kstats[dom]
     ds = dom == "tmu_ds"
+    sym = dom == "tmu_fp64" and "achieved_tops" in d
     traffic = TRAFFIC_30K[dom] * n / 30000.0 if dom in TRAFFIC_30K else None
     return {"bound": "fp64" if dom == "tmu_fp64" else "fp32", "kernel": dom,
-            "achieved": d["achieved_tops"] if ds else d["achieved_tflops"],
-            "peak": d["peak_tops"] if ds else d["peak_tflops"],
-            "unit": "Tops/s (FP32 instructions)" if ds else "TFLOP/s",
+            "achieved": d["achieved_tops"] if (ds or sym) else d["achieved_tflops"],
+            "peak": d["peak_tops"] if (ds or sym) else d["peak_tflops"],
+            "unit": ("Tops/s (FP32 instructions)" if ds else "Tops/s (FP64 instructions)" if sym else "TFLOP/s"),
             "frac": d["frac"], "traffic": traffic,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 30,000-site "
                               "box, scaled by the site count (bytes per launch)" if traffic else None,
             "peak_source": "FMA-chain kernel measured in this run (pipe peak; "
                            "MEASURED_PEAKS.json has no FP32/FP64 CUDA-core figure)",
-            "algorithmic": (f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair" if ds else
-                            f"{FLOP_PER_PAIR:.0f} flop per ordered pair") +
-                           f" x N(N-1) pairs x right-hand sides ({d['columns']} columns over "
-                           f"{d['launches']} launches)",
+            "algorithmic": (f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair x N(N-1) pairs" if ds else
+                            f"{FP64_SYM_OPS_PER_PAIR:.0f} FP64 operations per unordered pair x N(N-1)/2 pairs "
+                            f"(symmetric product; {d.get('fp64_flop_equivalent_tflops', 0):.3f} TFLOP/s at the "
+                            f"conventional {FLOP_PER_PAIR:.0f} flop per ordered pair)" if sym else
+                            f"{FLOP_PER_PAIR:.0f} flop per ordered pair x N(N-1) pairs") +
+                           f" x right-hand sides ({d['columns']} columns over {d['launches']} launches)",
             "share_of_timed": d["total_ms"] / total_ms}
 
 

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(EXT_TPB) k_ext(int n, const double *__restrict
         bad = 1;
         continue;
       }
-      const double k1 = rinv_f64(r2, (float)r2);
+      const double k1 = rinv_f64(r2, r2_f32(r2));
       const double ir2 = k1 * k1;
       const double k2 = k1 * ir2;  // r^-3
       const double *q = &s_d[k * LD];

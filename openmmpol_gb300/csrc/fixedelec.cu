@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(MTPB) k_m2m_pairs(M2mArgs a, int per_split) {
         bad = 1;
         continue;
       }
-      m2m_any<AMOEBA, GRAD>(&s_q[k * LD], dx, dy, dz, rinv_f64(r2, (float)r2), 1.0, Qt, trq, acc);
+      m2m_any<AMOEBA, GRAD>(&s_q[k * LD], dx, dy, dz, rinv_f64(r2, r2_f32(r2)), 1.0, Qt, trq, acc);
     }
   }
   if (bad) atomicOr(a.err, 1);

@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(GTPB) k_grad_pairs(GradArgs g, int per_split) 
         if (tpol || spol) bad = 1;
         continue;
       }
-      const float r2f = (float)r2;
+      const float r2f = r2_f32(r2);
       const double rinv = rinv_f64(r2, r2f);
       const bool test = AMOEBA ? maybe_damped_amoeba(r2f, wat, s_wa[k], g.thr2m) : maybe_damped_wang(r2f, wat, s_wa[k]);
       double k3, k5, k7, k9;

@@ -280,10 +280,14 @@ __global__ void k_tmu_finish(int n, int nrhs, int nsplit, const T *__restrict__ 
 // Symmetric FP64 dipole field: every unordered pair is evaluated once and
 // both directions are accumulated (T_ij = T_ji), halving the FP64 work of
 // the geometry.  Sites are grouped in super-tiles of 128 (4 warps x 32
-// lanes).  CTA (I, part) owns super-tile I and the slots k of its half shell
+// lanes).  Super-tile I meets the slots k of its half shell
 // J = (I + k) mod ntile, k = 0..K (K = ntile / 2); slot 0 is the diagonal
 // block (target side only, all ordered pairs); for even ntile the slot
-// k = ntile/2 is handled by the lower of the two tiles only.  Inside a slot a
+// k = ntile/2 is handled by the lower of the two tiles only.  The work items
+// (I, a chunk of consecutive slots) are handed out by an atomic counter to a
+// persistent grid of as many CTAs as fit on the GPU at once, so that every
+// SM stays busy to the end (a static grid leaves 4 CTAs on some SMs and 5 on
+// others).  Inside a slot a
 // warp pairs its 32 targets with each 32-site sub-tile of J in 32 rotation
 // steps: at step t lane l meets source (l + t) mod 32, read from shared
 // memory, and the source-side accumulators travel one lane per step by
@@ -323,7 +327,8 @@ __device__ __forceinline__ double fixed_value(unsigned long long lo, unsigned lo
 }
 
 template <int NRHS, bool AMOEBA>
-__global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, int nparts, int per_part,
+__global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, int chunk, int nchunk, int nitems,
+                                                       unsigned *__restrict__ next,
                                                        const Pos64 *__restrict__ pos,
                                                        const double *__restrict__ damp,
                                                        const float2 *__restrict__ wa,
@@ -337,98 +342,118 @@ __global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, i
   __shared__ float2 s_wa[SYM_TILE];
   __shared__ double s_mu[C][SYM_TILE];
   __shared__ double s_accj[4][C][SYM_TILE];
-  const int I = blockIdx.x, part = blockIdx.y;
+  __shared__ int s_item;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int ti = I * SYM_TILE + tid;
-  const bool vi = ti < n;
-  const Pos64 pi = vi ? pos[ti] : Pos64{0, 0, 0, 0};
-  const double ai = (AMOEBA && vi) ? damp[ti] : 0.0;
-  const float2 wai = vi ? wa[ti] : make_float2(0.f, 0.f);
-  double mui[C], acci[C];
-#pragma unroll
-  for (int c = 0; c < C; ++c) {
-    mui[c] = vi ? x[((size_t)(c / 3) * n + ti) * 3 + (c % 3)] : 0.0;
-    acci[c] = 0.0;
-  }
-  const int k0 = part * per_part;
-  const int k1 = min(K + 1, k0 + per_part);
-  for (int k = k0; k < k1; ++k) {
-    int J = I + k;
-    if (J >= ntile) J -= ntile;
-    if (k > 0 && 2 * k == ntile && I >= ntile / 2) continue;  // the other tile of the pair owns it
-    const bool diag = (k == 0);
+  for (;;) {
+    __syncthreads();  // every thread has read the previous item
+    if (tid == 0) s_item = (int)atomicAdd(next, 1u);
     __syncthreads();
-    {
-      int sj = J * SYM_TILE + tid;
-      bool v = sj < n;
-      Pos64 p = v ? pos[sj] : Pos64{0, 0, 0, 0};
-      s_x[tid] = p.x;
-      s_y[tid] = p.y;
-      s_z[tid] = p.z;
-      s_w[tid] = p.w;
-      s_a[tid] = (AMOEBA && v) ? damp[sj] : 0.0;
-      s_wa[tid] = v ? wa[sj] : make_float2(0.f, 0.f);
+    const int item = s_item;
+    if (item >= nitems) break;
+    const int I = item / nchunk;
+    const int ti = I * SYM_TILE + tid;
+    const bool vi = ti < n;
+    const Pos64 pi = vi ? pos[ti] : Pos64{0, 0, 0, 0};
+    const double ai = (AMOEBA && vi) ? damp[ti] : 0.0;
+    const float2 wai = vi ? wa[ti] : make_float2(0.f, 0.f);
+    // each side's field 3 sum f d - sum k3 mu (f = k5 mu.d) is accumulated
+    // as its two sums, one FMA per component each
+    double mui[C], afi[C], aki[C];
 #pragma unroll
-      for (int c = 0; c < C; ++c) s_mu[c][tid] = v ? x[((size_t)(c / 3) * n + sj) * 3 + (c % 3)] : 0.0;
+    for (int c = 0; c < C; ++c) {
+      mui[c] = vi ? x[((size_t)(c / 3) * n + ti) * 3 + (c % 3)] : 0.0;
+      afi[c] = 0.0;
+      aki[c] = 0.0;
     }
-    __syncthreads();
-    for (int js = 0; js < 4; ++js) {
-      double accj[C];
+    const int k0 = (item - I * nchunk) * chunk;
+    const int k1 = min(K + 1, k0 + chunk);
+    for (int k = k0; k < k1; ++k) {
+      int J = I + k;
+      if (J >= ntile) J -= ntile;
+      if (k > 0 && 2 * k == ntile && I >= ntile / 2) continue;  // the other tile of the pair owns it
+      const bool diag = (k == 0);
+      __syncthreads();
+      {
+        int sj = J * SYM_TILE + tid;
+        bool v = sj < n;
+        Pos64 p = v ? pos[sj] : Pos64{0, 0, 0, 0};
+        s_x[tid] = p.x;
+        s_y[tid] = p.y;
+        s_z[tid] = p.z;
+        s_w[tid] = p.w;
+        s_a[tid] = (AMOEBA && v) ? damp[sj] : 0.0;
+        s_wa[tid] = v ? wa[sj] : make_float2(0.f, 0.f);
 #pragma unroll
-      for (int c = 0; c < C; ++c) accj[c] = 0.0;
-      for (int t = 0; t < 32; ++t) {
-        const int jl = js * 32 + ((lane + t) & 31);
-        const int gj = J * SYM_TILE + jl;
-        if (vi && gj < n && gj != ti) {
-          double dx = pi.x - s_x[jl], dy = pi.y - s_y[jl], dz = pi.z - s_z[jl];
-          double r2 = dx * dx + dy * dy + dz * dz;
-          double k3, k5x3;
-          dd_pair<double, AMOEBA>(r2, pi.w, s_w[jl], ai, s_a[jl], wai, s_wa[jl], thr, thr2m, k3, k5x3);
+        for (int c = 0; c < C; ++c) s_mu[c][tid] = v ? x[((size_t)(c / 3) * n + sj) * 3 + (c % 3)] : 0.0;
+      }
+      __syncthreads();
+      for (int js = 0; js < 4; ++js) {
+        double afj[C], akj[C];
 #pragma unroll
-          for (int r = 0; r < NRHS; ++r) {
-            double mx = s_mu[3 * r][jl], my = s_mu[3 * r + 1][jl], mz = s_mu[3 * r + 2][jl];
-            double f = k5x3 * (mx * dx + my * dy + mz * dz);
-            acci[3 * r] += f * dx - k3 * mx;
-            acci[3 * r + 1] += f * dy - k3 * my;
-            acci[3 * r + 2] += f * dz - k3 * mz;
-            if (!diag) {
-              double g = k5x3 * (mui[3 * r] * dx + mui[3 * r + 1] * dy + mui[3 * r + 2] * dz);
-              accj[3 * r] += g * dx - k3 * mui[3 * r];
-              accj[3 * r + 1] += g * dy - k3 * mui[3 * r + 1];
-              accj[3 * r + 2] += g * dz - k3 * mui[3 * r + 2];
+        for (int c = 0; c < C; ++c) afj[c] = akj[c] = 0.0;
+        for (int t = 0; t < 32; ++t) {
+          const int jl = js * 32 + ((lane + t) & 31);
+          const int gj = J * SYM_TILE + jl;
+          if (vi && gj < n && gj != ti) {
+            double dx = pi.x - s_x[jl], dy = pi.y - s_y[jl], dz = pi.z - s_z[jl];
+            double r2 = dx * dx + dy * dy + dz * dz;
+            double k3, k5;
+            dd_pair_f64<AMOEBA>(r2, pi.w, s_w[jl], ai, s_a[jl], wai, s_wa[jl], thr, thr2m, k3, k5);
+#pragma unroll
+            for (int r = 0; r < NRHS; ++r) {
+              double mx = s_mu[3 * r][jl], my = s_mu[3 * r + 1][jl], mz = s_mu[3 * r + 2][jl];
+              double f = k5 * (mx * dx + my * dy + mz * dz);
+              afi[3 * r] = fma(f, dx, afi[3 * r]);
+              afi[3 * r + 1] = fma(f, dy, afi[3 * r + 1]);
+              afi[3 * r + 2] = fma(f, dz, afi[3 * r + 2]);
+              aki[3 * r] = fma(k3, mx, aki[3 * r]);
+              aki[3 * r + 1] = fma(k3, my, aki[3 * r + 1]);
+              aki[3 * r + 2] = fma(k3, mz, aki[3 * r + 2]);
+              if (!diag) {
+                double g = k5 * (mui[3 * r] * dx + mui[3 * r + 1] * dy + mui[3 * r + 2] * dz);
+                afj[3 * r] = fma(g, dx, afj[3 * r]);
+                afj[3 * r + 1] = fma(g, dy, afj[3 * r + 1]);
+                afj[3 * r + 2] = fma(g, dz, afj[3 * r + 2]);
+                akj[3 * r] = fma(k3, mui[3 * r], akj[3 * r]);
+                akj[3 * r + 1] = fma(k3, mui[3 * r + 1], akj[3 * r + 1]);
+                akj[3 * r + 2] = fma(k3, mui[3 * r + 2], akj[3 * r + 2]);
+              }
+            }
+          }
+          if (!diag) {
+            // the accumulators of source s move to the lane that meets s next
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+              afj[c] = __shfl_sync(0xffffffffu, afj[c], (lane + 1) & 31);
+              akj[c] = __shfl_sync(0xffffffffu, akj[c], (lane + 1) & 31);
             }
           }
         }
         if (!diag) {
-          // the accumulator of source s moves to the lane that meets s next
+          // after 32 steps lane l holds the accumulators of source js*32 + l
 #pragma unroll
-          for (int c = 0; c < C; ++c) accj[c] = __shfl_sync(0xffffffffu, accj[c], (lane + 1) & 31);
+          for (int c = 0; c < C; ++c) s_accj[warp][c][js * 32 + lane] = fma(3.0, afj[c], -akj[c]);
         }
       }
       if (!diag) {
-        // after 32 steps lane l holds the accumulator of source js*32 + l
+        __syncthreads();
+        const int sj = J * SYM_TILE + tid;
+        if (sj < n) {
 #pragma unroll
-        for (int c = 0; c < C; ++c) s_accj[warp][c][js * 32 + lane] = accj[c];
-      }
-    }
-    if (!diag) {
-      __syncthreads();
-      const int sj = J * SYM_TILE + tid;
-      if (sj < n) {
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-          const double v = ((s_accj[0][c][tid] + s_accj[1][c][tid]) + s_accj[2][c][tid]) + s_accj[3][c][tid];
-          const size_t o = ((size_t)(c / 3) * n + sj) * 3 + (c % 3);
-          fixed_add(acc_lo + o, acc_hi + o, v, bad);
+          for (int c = 0; c < C; ++c) {
+            const double v = ((s_accj[0][c][tid] + s_accj[1][c][tid]) + s_accj[2][c][tid]) + s_accj[3][c][tid];
+            const size_t o = ((size_t)(c / 3) * n + sj) * 3 + (c % 3);
+            fixed_add(acc_lo + o, acc_hi + o, v, bad);
+          }
         }
       }
     }
-  }
-  if (vi) {
+    if (vi) {
 #pragma unroll
-    for (int c = 0; c < C; ++c) {
-      const size_t o = ((size_t)(c / 3) * n + ti) * 3 + (c % 3);
-      fixed_add(acc_lo + o, acc_hi + o, acci[c], bad);
+      for (int c = 0; c < C; ++c) {
+        const size_t o = ((size_t)(c / 3) * n + ti) * 3 + (c % 3);
+        fixed_add(acc_lo + o, acc_hi + o, fma(3.0, afi[c], -aki[c]), bad);
+      }
     }
   }
 }
@@ -1047,17 +1072,31 @@ void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool
 
 namespace {
 struct SymPlan {
-  int ntile, K, nparts, per_part;
+  int ntile, K, chunk, nchunk, nitems, ctas;
 };
-SymPlan sym_plan(int n) {
+template <int NRHS, bool AMOEBA>
+int sym_resident() {
+  static int r = 0;
+  if (!r) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tmu_sym<NRHS, AMOEBA>, SYM_TILE, 0);
+    if (r < 1) r = 1;
+  }
+  return r;
+}
+
+// work items: about 16 per resident CTA, each a tile and a chunk of its slots
+SymPlan sym_plan(int n, int ctas) {
   SymPlan p;
   p.ntile = (n + SYM_TILE - 1) / SYM_TILE;
   p.K = p.ntile / 2;
-  int want = (4 * sm_count() + p.ntile - 1) / p.ntile;  // >= 4 CTAs per SM in total
-  if (want < 1) want = 1;
-  if (want > p.K + 1) want = p.K + 1;
-  p.per_part = (p.K + 1 + want - 1) / want;
-  p.nparts = (p.K + 1 + p.per_part - 1) / p.per_part;
+  const long long units = (long long)p.ntile * (p.K + 1);
+  long long chunk = units / (16LL * ctas);
+  if (chunk < 1) chunk = 1;
+  if (chunk > p.K + 1) chunk = p.K + 1;
+  p.chunk = (int)chunk;
+  p.nchunk = (p.K + 1 + p.chunk - 1) / p.chunk;
+  p.nitems = p.ntile * p.nchunk;
+  p.ctas = ctas < p.nitems ? ctas : p.nitems;
   return p;
 }
 }  // namespace
@@ -1066,14 +1105,14 @@ size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs) {
   if (s.n == 0) return 0;
   // two 64-bit accumulator words and one double per value of a column group
   // (at most two columns)
+  // (at most two columns), the error flag and the work counter
   size_t C = 3 * (size_t)(nrhs < 2 ? nrhs : 2);
-  return 3 * C * (size_t)s.n + 1;
+  return 3 * C * (size_t)s.n + 2;
 }
 
 void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
                         cudaStream_t st) {
   if (s.n == 0) return;
-  SymPlan p = sym_plan(s.n);
   float thr2m = damp_thr2_margin(s);
   // columns in groups of 2 (and a last single one) share the pair geometry
   int done = 0;
@@ -1084,26 +1123,29 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
     unsigned long long *hi = lo + C * s.n;
     double *e = scratch + 2 * C * s.n;
     unsigned long long *bad = reinterpret_cast<unsigned long long *>(scratch + 3 * C * s.n);
+    unsigned *next = reinterpret_cast<unsigned *>(bad + 1);
     const double *xg = x + (size_t)done * s.n * 3;
-    dim3 grid(p.ntile, p.nparts);
+    const int res = g == 2 ? (s.amoeba ? sym_resident<2, true>() : sym_resident<2, false>())
+                           : (s.amoeba ? sym_resident<1, true>() : sym_resident<1, false>());
+    const SymPlan p = sym_plan(s.n, res * sm_count());
     g_launches.fetch_add(3, std::memory_order_relaxed);
     cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
-    cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), st);  // flag and counter
+#define OMMP_SYM_ARGS                                                                                         \
+  s.n, p.ntile, p.K, p.chunk, p.nchunk, p.nitems, next, s.pol_pos, s.pol_a, s.pol_wa32, xg, lo, hi, bad, \
+      s.damp_thr, thr2m
     if (g == 2) {
       if (s.amoeba)
-        k_tmu_sym<2, true><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos, s.pol_a,
-                                                      s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
+        k_tmu_sym<2, true><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
       else
-        k_tmu_sym<2, false><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos,
-                                                       s.pol_a, s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
+        k_tmu_sym<2, false><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
     } else {
       if (s.amoeba)
-        k_tmu_sym<1, true><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos, s.pol_a,
-                                                      s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
+        k_tmu_sym<1, true><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
       else
-        k_tmu_sym<1, false><<<grid, SYM_TILE, 0, st>>>(s.n, p.ntile, p.K, p.nparts, p.per_part, s.pol_pos,
-                                                       s.pol_a, s.pol_wa32, xg, lo, hi, bad, s.damp_thr, thr2m);
+        k_tmu_sym<1, false><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
     }
+#undef OMMP_SYM_ARGS
     k_fixed_to_double<<<blocks_for(C * s.n, 256), 256, 0, st>>>(C * s.n, lo, hi, bad, e);
     const float2 *wa = s.pol_wa32;
     dim3 fgrid((s.n + 127) / 128, g);

@@ -14,15 +14,35 @@ namespace ommp {
 namespace gpu {
 namespace {
 
+// FP32 value of a non-negative FP64 r2 by integer operations (exponent
+// rebias, mantissa rounded to nearest), so that the conversion does not
+// take a slot of GB300's narrow FP64 pipe.  Values below the FP32 normal
+// range (only coincident sites) become 0.
+__device__ __forceinline__ float r2_f32(double r2) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(r2) + (1ull << 28);
+  const unsigned hi = (unsigned)(b >> 32);
+  // (b >> 29) holds sign | exponent | 23 mantissa bits; subtracting
+  // (1023 - 127) << 23 modulo 2^32 (0xC0000000) rebiases the exponent
+  const unsigned f = (unsigned)(b >> 29) - 0xC0000000u;
+  return __uint_as_float(hi < 0x38100000u ? 0u : f);
+}
+
 // 1/sqrt(r2) in FP64 from the FP32 hardware estimate and one Newton-Raphson
-// step y <- y + y (1 - r2 y^2) / 2 (quadratic convergence: the ~2^-23
+// step y <- y + (y / 2) (1 - r2 y^2) (quadratic convergence: the ~2^-23
 // relative error of the seed becomes ~2e-14).  GB300 runs FP64 at 1/64 of
-// the FP32 rate, so the seed and the conversions cost less than a full-
-// precision FP64 reciprocal square root.
+// the FP32 rate, so the seed costs less than a full-precision FP64
+// reciprocal square root.  The seed y and y / 2 are widened to FP64 by
+// integer operations (exponent rebias; infinities and NaNs kept), so the
+// step takes three FP64 operations.
 __device__ __forceinline__ double rinv_f64(double r2, float r2f) {
-  double y = (double)rsqrtf(r2f);
-  double e = fma(-r2, y * y, 1.0);
-  return fma(0.5 * y, e, y);
+  const unsigned u = __float_as_uint(rsqrtf(r2f));
+  const bool special = (u & 0x7F800000u) == 0x7F800000u;
+  const unsigned hi = special ? (0x7FF00000u | (u >> 3)) : (u >> 3) + 0x38000000u;
+  const unsigned lo = u << 29;
+  const double y = __hiloint2double((int)hi, (int)lo);
+  const double hy = __hiloint2double((int)(special ? hi : hi - 0x00100000u), (int)lo);
+  const double e = fma(-r2, y * y, 1.0);
+  return fma(hy, e, y);
 }
 
 // Damping pre-test in FP32 for the FP64 kernels.  AMOEBA damps when
@@ -84,46 +104,53 @@ __device__ __forceinline__ void dd_kernel(T r2, T wt, T ws, T at, T as, T thr, T
   k5x3 = T(3) * k5;
 }
 
-// The pair factors in the precision of the kernel.  FP64: reciprocal square
-// root from the FP32 seed plus one Newton step and the FP32 damping
-// pre-test, so that only the arithmetic that needs FP64 runs on GB300's
-// FP64 pipe.  FP32: the plain formulas.
+// Damped r^-3 and r^-5 factors of one pair in FP64: reciprocal square root
+// from the FP32 seed plus one Newton step and the FP32 damping pre-test, so
+// that only the arithmetic that needs FP64 runs on GB300's FP64 pipe.
+template <bool AMOEBA>
+__device__ __forceinline__ void dd_pair_f64(double r2, double wt, double ws, double at, double as, float2 wat,
+                                            float2 was, double thr, float thr2m, double &k3, double &k5) {
+  const float r2f = r2_f32(r2);
+  const double rinv = rinv_f64(r2, r2f);
+  const double ir2 = rinv * rinv;
+  k3 = rinv * ir2;
+  k5 = k3 * ir2;
+  if (AMOEBA) {
+    if (maybe_damped_amoeba(r2f, wat, was, thr2m)) {
+      double u = r2 * rinv * (wt * ws);
+      double au3 = fmin(at, as) * u * u * u;
+      if (au3 < thr) {
+        double e = exp(-au3);
+        k3 *= 1.0 - e;
+        k5 *= 1.0 - (1.0 + au3) * e;
+      }
+    }
+  } else {
+    if (maybe_damped_wang(r2f, wat, was)) {
+      double u = r2 * rinv * (wt * ws);
+      if (u < 1.0) {
+        double u3 = u * u * u;
+        double u4 = u3 * u;
+        k3 *= 4.0 * u3 - 3.0 * u4;
+        k5 *= u4;
+      }
+    }
+  }
+}
+
+// The pair factors k3 and 3 k5 in the precision of the kernel (FP64:
+// dd_pair_f64; FP32: the plain formulas).
 template <typename T, bool AMOEBA>
 __device__ __forceinline__ void dd_pair(T r2, T wt, T ws, T at, T as, float2 wat, float2 was, T thr,
                                         float thr2m, T &k3, T &k5x3) {
   if constexpr (std::is_same<T, double>::value) {
-    float r2f = (float)r2;
-    double rinv = rinv_f64(r2, r2f);
-    double ir2 = rinv * rinv;
-    k3 = rinv * ir2;
-    double k5 = k3 * ir2;
-    if (AMOEBA) {
-      if (maybe_damped_amoeba(r2f, wat, was, thr2m)) {
-        double u = r2 * rinv * (wt * ws);
-        double au3 = fmin(at, as) * u * u * u;
-        if (au3 < thr) {
-          double e = exp(-au3);
-          k3 *= 1.0 - e;
-          k5 *= 1.0 - (1.0 + au3) * e;
-        }
-      }
-    } else {
-      if (maybe_damped_wang(r2f, wat, was)) {
-        double u = r2 * rinv * (wt * ws);
-        if (u < 1.0) {
-          double u3 = u * u * u;
-          double u4 = u3 * u;
-          k3 *= 4.0 * u3 - 3.0 * u4;
-          k5 *= u4;
-        }
-      }
-    }
+    double k5;
+    dd_pair_f64<AMOEBA>(r2, wt, ws, at, as, wat, was, thr, thr2m, k3, k5);
     k5x3 = 3.0 * k5;
   } else {
     dd_kernel<T, AMOEBA>(r2, wt, ws, at, as, thr, k3, k5x3);
   }
 }
-
 
 // Field of a static multipole (charge; + dipole and quadrupole for AMOEBA,
 // q[0..9]) at a polarizable target, d = target - source, Thole-damped
@@ -134,7 +161,7 @@ __device__ __forceinline__ void m2d_pair_f64(double dx, double dy, double dz, do
                                              const double *q, double thr, float thr2m,
                                              double &ex, double &ey, double &ez) {
   double r2 = dx * dx + dy * dy + dz * dz;
-  float r2f = (float)r2;
+  float r2f = r2_f32(r2);
   double rinv = rinv_f64(r2, r2f);
   double ir2 = rinv * rinv;
   double k3 = rinv * ir2;

@@ -45,11 +45,13 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
                                                       const float2 *__restrict__ mm_wa,
                                                       double *__restrict__ partial, int per_split,
                                                       double thr, float thr2m, int *err_flag) {
-  constexpr int LD = AMOEBA ? 10 : 1;
+  constexpr int LD = AMOEBA ? 10 : 1;         // multipole record in memory
+  constexpr int SLD = AMOEBA ? M2D_SLD : 1;    // staged record (m2d_stage)
+  constexpr int NA = AMOEBA ? 9 : 3;          // field sums (m2d_pair_acc)
   __shared__ Pos64 s_pos[TILE];
   __shared__ double s_a[TILE];
   __shared__ float2 s_wa[TILE];
-  __shared__ double s_q[TILE * LD];
+  __shared__ double s_q[TILE * SLD];
   const int j = blockIdx.x * TPB + threadIdx.x;
   const bool valid = j < n;
   Pos64 pt = valid ? pol_pos[j] : Pos64{0, 0, 0, 0};
@@ -57,7 +59,9 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
   const int tm = valid ? polar_mm[j] : -1;
   const double at = valid && AMOEBA ? pol_a[j] : 0.0;
   const float2 wat = valid ? pol_wa[j] : make_float2(0.f, 0.f);
-  double ex = 0, ey = 0, ez = 0;
+  double acc[NA];
+#pragma unroll
+  for (int c = 0; c < NA; ++c) acc[c] = 0.0;
   int bad = 0;
   const int s0 = blockIdx.y * per_split;
   const int s1 = min(m, s0 + per_split);
@@ -69,11 +73,8 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
         s_pos[k] = mm_pos[i];
         s_a[k] = AMOEBA ? mm_a[i] : 0.0;
         s_wa[k] = mm_wa[i];
+        m2d_stage<AMOEBA>(&mm_q[(size_t)i * LD], &s_q[k * SLD]);
       }
-    }
-    for (int k = threadIdx.x; k < TILE * LD; k += TPB) {
-      size_t g = (size_t)t0 * LD + k;
-      if (g < (size_t)s1 * LD) s_q[k] = mm_q[g];
     }
     __syncthreads();
     const int cnt = min(TILE, s1 - t0);
@@ -83,21 +84,17 @@ __global__ void __launch_bounds__(TPB) k_m2d_allpairs(int n, int m, const Pos64 
       if (i == tm) continue;
       const Pos64 ps = s_pos[k];
       double dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
-      double r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 < 4.9e-28) {  // |r| < 100 eps: coincident sites
+      if (coincident(dx * dx + dy * dy + dz * dz)) {
         bad = 1;
         continue;
       }
-      m2d_pair_f64<AMOEBA>(dx, dy, dz, pt.w, ps.w, at, s_a[k], wat, s_wa[k], &s_q[k * LD], thr, thr2m, ex,
-                           ey, ez);
+      m2d_pair_acc<AMOEBA>(dx, dy, dz, pt.w, ps.w, at, s_a[k], wat, s_wa[k], &s_q[k * SLD], thr, thr2m, acc);
     }
   }
   if (bad) atomicOr(err_flag, 1);
   if (valid) {
     double *o = partial + ((size_t)blockIdx.y * n + j) * 3;
-    o[0] = ex;
-    o[1] = ey;
-    o[2] = ez;
+    m2d_field<AMOEBA>(acc, o[0], o[1], o[2]);
   }
 }
 

@@ -203,6 +203,93 @@ __device__ __forceinline__ void m2d_pair_f64(double dx, double dy, double dz, do
   }
 }
 
+// The all-pairs form of m2d_pair_f64: the source record is staged once per
+// tile as m2d_stage writes it (q, mu, 3 mu, 15 Q: 13 values for AMOEBA, the
+// charge alone otherwise) and the field is kept as three sums, a = sum c d,
+// b = sum k3 mu, t = sum k5 (15 Q) d, so that E = a - b - 0.4 t (m2d_field)
+// and every accumulation is one FMA: 40 FP64 operations per AMOEBA pair.
+constexpr int M2D_SLD = 13;
+
+template <bool AMOEBA>
+__device__ __forceinline__ void m2d_stage(const double *q, double *o) {
+  o[0] = q[0];
+  if (!AMOEBA) return;
+  for (int c = 0; c < 3; ++c) {
+    o[1 + c] = q[1 + c];
+    o[4 + c] = 3.0 * q[1 + c];
+  }
+  for (int c = 0; c < 6; ++c) o[7 + c] = 15.0 * q[4 + c];
+}
+
+template <bool AMOEBA>
+__device__ __forceinline__ void m2d_pair_acc(double dx, double dy, double dz, double wt, double ws, double at,
+                                             double as, float2 wat, float2 was, const double *q, double thr,
+                                             float thr2m, double *acc) {
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  const float r2f = r2_f32(r2);
+  const double rinv = rinv_f64(r2, r2f);
+  const double ir2 = rinv * rinv;
+  double k3 = rinv * ir2;
+  if (AMOEBA) {
+    double k5 = k3 * ir2;
+    double k7 = k5 * ir2;
+    if (maybe_damped_amoeba(r2f, wat, was, thr2m)) {
+      double u = r2 * rinv * (wt * ws);  // r / (thole_t thole_s)
+      double au3 = fmin(at, as) * u * u * u;
+      if (au3 < thr) {
+        double e = exp(-au3);
+        k3 *= 1.0 - e;
+        k5 *= 1.0 - (1.0 + au3) * e;
+        k7 *= 1.0 - (1.0 + au3 + 0.6 * au3 * au3) * e;
+      }
+    }
+    const double mdr3 = q[4] * dx + q[5] * dy + q[6] * dz;
+    const double tx = q[7] * dx + q[8] * dy + q[10] * dz;
+    const double ty = q[8] * dx + q[9] * dy + q[11] * dz;
+    const double tz = q[10] * dx + q[11] * dy + q[12] * dz;
+    const double qxr = tx * dx + ty * dy + tz * dz;
+    const double c = fma(qxr, k7, fma(mdr3, k5, q[0] * k3));
+    acc[0] = fma(c, dx, acc[0]);
+    acc[1] = fma(c, dy, acc[1]);
+    acc[2] = fma(c, dz, acc[2]);
+    acc[3] = fma(k3, q[1], acc[3]);
+    acc[4] = fma(k3, q[2], acc[4]);
+    acc[5] = fma(k3, q[3], acc[5]);
+    acc[6] = fma(k5, tx, acc[6]);
+    acc[7] = fma(k5, ty, acc[7]);
+    acc[8] = fma(k5, tz, acc[8]);
+  } else {
+    if (maybe_damped_wang(r2f, wat, was)) {
+      double u = r2 * rinv * (wt * ws);
+      if (u < 1.0) {
+        double u3 = u * u * u;
+        k3 *= 4.0 * u3 - 3.0 * u3 * u;
+      }
+    }
+    const double c = q[0] * k3;
+    acc[0] = fma(c, dx, acc[0]);
+    acc[1] = fma(c, dy, acc[1]);
+    acc[2] = fma(c, dz, acc[2]);
+  }
+}
+
+template <bool AMOEBA>
+__device__ __forceinline__ void m2d_field(const double *acc, double &ex, double &ey, double &ez) {
+  if (AMOEBA) {
+    ex = acc[0] - acc[3] - 0.4 * acc[6];
+    ey = acc[1] - acc[4] - 0.4 * acc[7];
+    ez = acc[2] - acc[5] - 0.4 * acc[8];
+  } else {
+    ex = acc[0];
+    ey = acc[1];
+    ez = acc[2];
+  }
+}
+
+// |r| below 100 machine epsilons, r2 < 4.9e-28 (coincident sites), tested on
+// the high word of the non-negative r2 (integer compare, no FP64 instruction)
+__device__ __forceinline__ bool coincident(double r2) { return __double2hiint(r2) < 0x3a436930; }
+
 }  // namespace
 }  // namespace gpu
 }  // namespace ommp

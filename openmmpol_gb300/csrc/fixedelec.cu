@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(MTPB) k_m2m_pairs(M2mArgs a, int per_split) {
       const Pos64 ps = s_pos[k];
       const double dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
       const double r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 < 4.9e-28) {  // |r| < 100 eps: coincident sites
+      if (coincident(r2)) {
         bad = 1;
         continue;
       }

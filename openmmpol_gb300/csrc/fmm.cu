@@ -420,6 +420,8 @@ __global__ void __launch_bounds__(FT) k_fmm_l2p(FmmArgs a, const double *__restr
     const double at = valid && AMOEBA ? a.sa[si] : 0.0;
     const float2 wat = valid ? a.swa[si] : make_float2(0.f, 0.f);
     double e[3] = {0.0, 0.0, 0.0};
+    // near field 3 sum f d - sum k3 mu (f = k5 mu.d) as its two sums
+    double nf[3] = {0.0, 0.0, 0.0}, nk[3] = {0.0, 0.0, 0.0};
     __syncthreads();
     if (valid) {
       const double u[3] = {pt.x - ctr[0], pt.y - ctr[1], pt.z - ctr[2]};
@@ -461,18 +463,22 @@ __global__ void __launch_bounds__(FT) k_fmm_l2p(FmmArgs a, const double *__restr
               const Pos64 ps = s_pos[q];
               const double dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
               const double r2 = dx * dx + dy * dy + dz * dz;
-              if (r2 < 4.9e-28) continue;
-              double k3, k5x3;
-              dd_pair<double, AMOEBA>(r2, pt.w, ps.w, at, s_a[q], wat, s_wa[q], thr, thr2m, k3, k5x3);
+              if (coincident(r2)) continue;
+              double k3, k5;
+              dd_pair_f64<AMOEBA>(r2, pt.w, ps.w, at, s_a[q], wat, s_wa[q], thr, thr2m, k3, k5);
               const double *mu = &s_mu[q * 3];
-              const double f = k5x3 * (mu[0] * dx + mu[1] * dy + mu[2] * dz);
-              e[0] += f * dx - k3 * mu[0];
-              e[1] += f * dy - k3 * mu[1];
-              e[2] += f * dz - k3 * mu[2];
+              const double f = k5 * (mu[0] * dx + mu[1] * dy + mu[2] * dz);
+              nf[0] = fma(f, dx, nf[0]);
+              nf[1] = fma(f, dy, nf[1]);
+              nf[2] = fma(f, dz, nf[2]);
+              nk[0] = fma(k3, mu[0], nk[0]);
+              nk[1] = fma(k3, mu[1], nk[1]);
+              nk[2] = fma(k3, mu[2], nk[2]);
             }
           }
         }
     if (valid) {
+      for (int d = 0; d < 3; ++d) e[d] += fma(3.0, nf[d], -nk[d]);
       const int pi = a.perm[si];
       for (int d = 0; d < 3; ++d) field[((size_t)col * n + pi) * 3 + d] = e[d];
     }
@@ -626,7 +632,7 @@ __global__ void __launch_bounds__(FT) k_fmm_l2p_m2d(FmmArgs a, const int *__rest
               if (s_mm[q] == self) continue;
               const Pos64 ps = s_pos[q];
               const double dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
-              if (dx * dx + dy * dy + dz * dz < 4.9e-28) {
+              if (coincident(dx * dx + dy * dy + dz * dz)) {
                 bad = 1;
                 continue;
               }

@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(GTPB) k_grad_pairs(GradArgs g, int per_split) 
       const double dx = pt.x - ps.x, dy = pt.y - ps.y, dz = pt.z - ps.z;
       const double r2 = dx * dx + dy * dy + dz * dz;
       const int spol = s_pol[k];
-      if (r2 < 4.9e-28) {  // |r| < 100 eps: coincident sites
+      if (coincident(r2)) {
         if (tpol || spol) bad = 1;
         continue;
       }

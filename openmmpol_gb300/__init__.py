@@ -45,6 +45,12 @@ def set_verbose(level) -> None:
     _lib.load().ommp_set_verbose(lvl)
 
 
+def kernel_launch_count() -> int:
+    """Kernels the library has launched in this process (CUDA graph launches
+    count their kernels)."""
+    return int(_lib.load().ommp_gpu_kernel_launch_count())
+
+
 def _as_c(a, shape, dtype=np.float64):
     a = np.ascontiguousarray(a, dtype=dtype)
     if a.shape != shape:

@@ -858,13 +858,21 @@ inline int blocks_for(size_t n, int tpb, int cap = 4 * 152 * 4) {
 
 }  // namespace
 
+// kernels launched by the library: process total, and per host thread (the
+// server drives several systems from several threads; a graph capture
+// subtracts the kernels its own thread recorded, not those of the others)
 static std::atomic<long long> g_launches{0};
+static thread_local long long t_launches = 0;
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
-void add_launch_count(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+long long thread_launch_count() { return t_launches; }
+void add_launch_count(long long k) {
+  g_launches.fetch_add(k, std::memory_order_relaxed);
+  t_launches += k;
+}
 
 double launch_fma_peak(bool fp64, int iters, void *out, cudaStream_t st) {
   int blocks = sm_count() * 8, threads = 256;
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   if (fp64)
     k_fma_peak<double><<<blocks, threads, 0, st>>>((double *)out, iters, 0.999999, 1e-7);
   else
@@ -912,14 +920,14 @@ static void m2d_finish(const DevSites &s, double *out, const double *scratch, in
 }
 
 void launch_m2d_finish(const DevSites &s, double *out, const double *partial, int nsplit, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   m2d_finish(s, out, partial, nsplit, st);
 }
 
 void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag,
                 cudaStream_t st) {
   if (s.n == 0) return;
-  g_launches.fetch_add(2, std::memory_order_relaxed);
+  add_launch_count(2);
   int tiles = (s.m + TILE - 1) / TILE;
   int per = ((tiles + nsplit - 1) / nsplit) * TILE;
   dim3 grid((s.n + TPB - 1) / TPB, nsplit);
@@ -936,7 +944,7 @@ void launch_m2d(const DevSites &s, double *out, double *scratch, int nsplit, int
 
 void launch_m2d_ds(const DevSites &s, double *out, double *scratch, int nsplit, int *err_flag, cudaStream_t st) {
   if (s.n == 0) return;
-  g_launches.fetch_add(2, std::memory_order_relaxed);
+  add_launch_count(2);
   launch_m2d_ds_pairs(s, scratch, nsplit, err_flag, st);
   m2d_finish(s, out, scratch, nsplit, st);
 }
@@ -969,7 +977,7 @@ size_t tmu_scratch_doubles(const DevSites &s, int nrhs, int nsplit) {
 template <typename T, int NRHS, bool KAHAN>
 static void tmu_allpairs(const DevSites &s, const typename Vec4<T>::type *pos, const T *damp, const T *x,
                          T *partial, int nsplit, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   int tiles = (s.n + TILE - 1) / TILE;
   int per = ((tiles + nsplit - 1) / nsplit) * TILE;
   dim3 grid((s.n + TPB - 1) / TPB, nsplit);
@@ -1000,7 +1008,7 @@ static void tmu_dispatch(const DevSites &s, int nrhs, const typename Vec4<T>::ty
     T *pg = partial + (size_t)nsplit * done * s.n * 3;
     if constexpr (std::is_same<T, float>::value) {
       if (kver == 2) {
-        g_launches.fetch_add(1, std::memory_order_relaxed);
+        add_launch_count(1);
         launch_tmu32_pairs(s, g, x + xo, pg, nsplit, st);
         done += g;
         continue;
@@ -1025,7 +1033,7 @@ static void tmu_finish(const DevSites &s, int nrhs, int nsplit, const T *partial
   while (done < nrhs) {
     int g = column_group(nrhs - done, gmax);
     const T *pg = partial + (size_t)nsplit * done * s.n * 3;
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    add_launch_count(1);
     dim3 grid((s.n + 127) / 128, g);
     size_t xo = (size_t)done * s.n * 3;
     const float2 *wa = std::is_same<T, double>::value ? s.pol_wa32 : nullptr;
@@ -1060,7 +1068,7 @@ void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool
   const size_t nv = 3 * (size_t)s.n;
   for (int c = 0; c < nrhs;) {
     const int g = nrhs - c >= 2 ? 2 : 1;
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    add_launch_count(1);
     launch_tmu_ds_pairs(s, g, x + c * nv, scratch, nsplit, st);
     tmu_finish<double>(s, g, nsplit, scratch, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 2, st);
     c += g;
@@ -1125,7 +1133,7 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
     const int res = g == 2 ? (s.amoeba ? sym_resident<2, true>() : sym_resident<2, false>())
                            : (s.amoeba ? sym_resident<1, true>() : sym_resident<1, false>());
     const SymPlan p = sym_plan(s.n, res * sm_count());
-    g_launches.fetch_add(3, std::memory_order_relaxed);
+    add_launch_count(3);
     cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
     cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), st);  // flag and counter
 #define OMMP_SYM_ARGS                                                                                         \
@@ -1193,7 +1201,7 @@ __global__ void k_block_apply(int n, const int4 *__restrict__ info, const float 
 void launch_block_apply(int ncol, int n, const int4 *info, const float *minv, const float *r, float *z,
                         cudaStream_t st) {
   if (n == 0) return;
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   dim3 grid((n + 127) / 128, ncol);
   k_block_apply<<<grid, 128, 0, st>>>(n, info, minv, r, z);
 }
@@ -1226,18 +1234,18 @@ __global__ void k_batch_scatter(int n, int nf, int nipd, int nsolved, const doub
 
 void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
                       cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_batch_rhs<<<blocks_for((size_t)3 * n * nf * nset, 256), 256, 0, st>>>(n, nf, nset, e_m2d, fields, rhs);
 }
 
 void launch_batch_scatter(int n, int nf, int nipd, int nsolved, const double *x, double *out, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_batch_scatter<<<blocks_for((size_t)3 * n * nf * nipd, 256), 256, 0, st>>>(n, nf, nipd, nsolved, x, out);
 }
 
 // ---- dense T ------------------------------------------------------------------
 void launch_build_tmat(const DevSites &s, double *tmat, cudaStream_t st) {
-  g_launches.fetch_add(s.d2d_nnz ? 2 : 1, std::memory_order_relaxed);
+  add_launch_count(s.d2d_nnz ? 2 : 1);
   dim3 grid((s.n + 127) / 128, s.n);
   if (s.amoeba)
     k_build_tmat<true><<<grid, 128, 0, st>>>(s.n, s.pol_pos, s.pol_a, s.pol_alpha, s.damp_thr, tmat);
@@ -1248,7 +1256,7 @@ void launch_build_tmat(const DevSites &s, double *tmat, cudaStream_t st) {
 
 void launch_gemv(int nn, const double *A, const double *x, double *y, bool dodiag, const double *alpha,
                  int nrhs, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   dim3 grid((nn + 127) / 128, nrhs);
   k_gemv<<<grid, 128, 0, st>>>(nn, A, x, y, dodiag, alpha);
 }
@@ -1257,7 +1265,7 @@ void launch_lu_factor(int nn, double *A, int *piv, int *info, double *work, cuda
   (void)work;
   cudaMemsetAsync(info, 0, sizeof(int), st);
   for (int k = 0; k < nn; ++k) {
-    g_launches.fetch_add(nn - k - 1 > 0 ? 4 : 2, std::memory_order_relaxed);
+    add_launch_count(nn - k - 1 > 0 ? 4 : 2);
     k_lu_pivot<<<1, 1024, 0, st>>>(nn, k, A, piv, info);
     k_lu_swap<<<(nn + 255) / 256, 256, 0, st>>>(nn, k, A, piv);
     int rows = nn - k - 1;
@@ -1270,98 +1278,98 @@ void launch_lu_factor(int nn, double *A, int *piv, int *info, double *work, cuda
 }
 
 void launch_lu_solve(int nn, const double *A, const int *piv, double *b, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_lu_solve<<<1, 1024, 0, st>>>(nn, A, piv, b);
 }
 
 // ---- BLAS-1 ---------------------------------------------------------------------
 void launch_dots(int ncol, size_t n, const double *a, const double *b, double *partial, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_dots<double><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, a, b, n, partial);
 }
 void launch_dots_bcast(int ncol, size_t n, const double *a, const double *b, double *partial,
                        cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_dots<double><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, a, b, 0, partial);
 }
 void launch_dots_f32(int ncol, size_t n, const float *a, const float *b, double *partial, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_dots<float><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, a, b, n, partial);
 }
 void launch_reduce_partials(int ncol, const double *partial, double *result, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_reduce_partials<<<ncol, 32, 0, st>>>(ncol, kRedBlocks, partial, result);
 }
 void launch_axpby(size_t n, double a, const double *x, double b, double *y, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_axpby<<<blocks_for(n, 256), 256, 0, st>>>(n, a, x, b, y);
 }
 void launch_add(size_t n, const double *a, const double *b, double *out, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_add<<<blocks_for(n, 256), 256, 0, st>>>(n, a, b, out);
 }
 void launch_scale_by_alpha(int nrhs, int n, const double *alpha, const double *x, double *y, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_scale_alpha<<<blocks_for((size_t)nrhs * n * 3, 256), 256, 0, st>>>(nrhs, n, alpha, x, y);
 }
 void launch_to_f32(size_t n, const double *x, const double *scale, float *y, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_to_f32<<<blocks_for(n, 256), 256, 0, st>>>(n, x, scale, y);
 }
 void launch_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_cg_alpha<<<(ncol + 127) / 128, 128, 0, st>>>(ncol, dots, cols, eps);
 }
 void launch_cg_update(int ncol, int n, double *x, double *r, const double *p, const double *h, double *z,
                       const double *alpha_pol, const CgCol *cols, double *partial, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_cg_update<double><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, x, r, p, h, z, alpha_pol, cols, partial);
 }
 void launch_cg_update_f32(int ncol, int n, float *x, float *r, const float *p, const float *h, float *z,
                           const float *alpha_pol, const CgCol *cols, double *partial, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_cg_update<float><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, x, r, p, h, z, alpha_pol, cols, partial);
 }
 void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double *hist, int hist_stride,
                     cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_cg_gnew<<<(ncol + 127) / 128, 128, 0, st>>>(ncol, n, dots, cols, hist, hist_stride);
 }
 void launch_cg_pupdate(int ncol, int n, double *p, const double *z, const CgCol *cols, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_cg_pupdate<double><<<blocks_for(3 * (size_t)n, 256), 256, 0, st>>>(ncol, n, p, z, cols);
 }
 void launch_cg_pupdate_f32(int ncol, int n, float *p, const float *z, const CgCol *cols, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_cg_pupdate<float><<<blocks_for(3 * (size_t)n, 256), 256, 0, st>>>(ncol, n, p, z, cols);
 }
 void launch_ir_accumulate(int ncol, int n, double *mu, const float *d32, const double *scale, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_ir_accumulate<<<blocks_for((size_t)ncol * n * 3, 256), 256, 0, st>>>(ncol, n, mu, d32, scale);
 }
 void launch_residual(size_t total, const double *rhs, const double *tmu, double *r, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_residual<<<blocks_for(total, 256), 256, 0, st>>>(total, rhs, tmu, r);
 }
 void launch_lincomb(int nvec, size_t n, const double *X, size_t ldx, const double *c, double *out,
                     cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_lincomb<<<blocks_for(n, 256), 256, 0, st>>>(nvec, n, X, ldx, c, out);
 }
 void launch_diff_norms(size_t n, const double *a, const double *b, double *partial, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_diff_norms<<<kRedBlocks, kRedThreads, 0, st>>>(n, a, b, partial);
 }
 void launch_reduce_norms(const double *partial, double *out, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_reduce_norms<<<1, 32, 0, st>>>(kRedBlocks, partial, out);
 }
 void launch_any_diff(size_t n, const double *a, const double *b, int *flag, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_any_diff<<<blocks_for(n, 256), 256, 0, st>>>(n, a, b, flag);
 }
 void launch_check_finite(size_t n, const double *x, int *flag, cudaStream_t st) {
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  add_launch_count(1);
   k_check_finite<<<blocks_for(n, 256), 256, 0, st>>>(n, x, flag);
 }
 

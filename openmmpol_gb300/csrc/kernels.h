@@ -210,6 +210,7 @@ int sm_count();
 // Kernels launched by this library since load (all streams); graph replays
 // add the kernels of the replayed graph.
 long long launch_count();
+long long thread_launch_count();
 void add_launch_count(long long k);
 // FMA-chain kernel for the FP32 / FP64 pipe peak; returns its flop count.
 double launch_fma_peak(bool fp64, int iters, void *out, cudaStream_t st);

@@ -297,11 +297,11 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
     w.graph = nullptr;
     w.graph_ncol = -1;
     cudaGraph_t g = nullptr;
-    long long before = gpu::launch_count();
+    long long before = gpu::thread_launch_count();
     if (cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       iteration();
       cudaError_t e = cudaStreamEndCapture(st_, &g);
-      long long kernels = gpu::launch_count() - before;
+      long long kernels = gpu::thread_launch_count() - before;
       gpu::add_launch_count(-kernels);  // captured, not launched
       if (e == cudaSuccess && g && cudaGraphInstantiate(&w.graph, g, 0) == cudaSuccess) {
         w.graph_ncol = ncol;

@@ -9,7 +9,7 @@ mixed ones to 1e-7; the admission bookkeeping never exceeds the budget.
 import numpy as np
 import pytest
 
-from openmmpol_gb300 import OMMPError, OMMPSystem, Server, set_verbose, synth
+from openmmpol_gb300 import OMMPError, OMMPSystem, Server, kernel_launch_count, set_verbose, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -76,10 +76,15 @@ def check(systems, first, second, precision):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_results_same_alone_and_in_the_mix(systems, precision):
     srv = Server(8 << 30, slots=4, precision=precision, tol=1e-10)
+    l0 = kernel_launch_count()
     first, second = served(srv, systems)
+    launched = kernel_launch_count() - l0
     st = srv.stats()
     srv.close()
     check(systems, first, second, precision)
+    # the launch count stays exact while solves on several threads capture
+    # and replay CUDA graphs (10 solves of at most a few hundred kernels)
+    assert 0 < launched < 20000
     for a, b in zip(first, second):
         assert a["instance"] == b["instance"]  # follow-ups reuse the resident system
     assert st["evictions"] == 0 and st["resident"] == len(systems)

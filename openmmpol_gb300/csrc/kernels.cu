@@ -894,14 +894,25 @@ int sm_count() {
 }
 
 // ---- M2D -----------------------------------------------------------------
+// Source splits of the FP64 permanent field: about 16 waves of CTAs, so
+// that the last, partly filled wave idles few SMs (one wave of ~4.6 CTAs
+// per SM left the SMs with 4 idle while those with 5 finished), with the
+// split partials kept below 64 MiB.
 int m2d_pick_split(const DevSites &s, int sms) {
-  int tblocks = (s.n + TPB - 1) / TPB;
-  int want = 4 * sms;  // a few CTAs per SM
-  int split = (want + tblocks - 1) / tblocks;
-  int maxsplit = (s.m + TILE - 1) / TILE;
+  static int resident = 0;
+  if (!resident) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_m2d_allpairs<true>, TPB, 0);
+    if (resident < 1) resident = 1;
+  }
+  const long long tblocks = (s.n + TPB - 1) / TPB;
+  const long long want = 16LL * resident * sms;
+  long long split = (want + tblocks - 1) / tblocks;
+  const long long maxsplit = (s.m + TILE - 1) / TILE;
+  const long long maxmem = (64LL << 20) / (24LL * (s.n > 0 ? s.n : 1));
+  if (split > maxmem) split = maxmem;
   if (split > maxsplit) split = maxsplit;
   if (split < 1) split = 1;
-  return split;
+  return (int)split;
 }
 
 size_t m2d_scratch_doubles(const DevSites &s, int nsplit) { return (size_t)nsplit * s.n * 3; }

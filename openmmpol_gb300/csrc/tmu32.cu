@@ -12,8 +12,8 @@
 //  * a per-tile classification: each 128-site source tile is compared with
 //    the bounding box of the CTA's targets, and when the boxes are farther
 //    apart than the largest distance at which Thole damping can act, the
-//    whole tile runs an undamped inner loop with no self-pair test (about 21
-//    FP32 instructions and one MUFU per pair and column); only the few tiles
+//    whole tile runs an undamped inner loop with no self-pair test (20 FP32
+//    instructions and one MUFU per pair and column); only the few tiles
 //    near the targets run the damped loop;
 //  * compensated (Kahan) accumulation across tiles, as before, and the same
 //    [split][column][n][3] partial layout, so the scaled-pair correction and
@@ -35,11 +35,11 @@ constexpr int T32_TILE = 128;  // sources per shared-memory tile (= tile-box gra
 
 template <bool AMOEBA>
 __device__ __forceinline__ void damped_factors(float r2, float wt, float ws, float at, float as, float thr,
-                                               float &k3, float &k5x3) {
+                                               float &k3, float &k5) {
   float rinv = rsqrtf(r2);
   float ir2 = rinv * rinv;
   k3 = rinv * ir2;
-  float k5 = k3 * ir2;
+  k5 = k3 * ir2;
   float u = r2 * rinv * (wt * ws);
   if (AMOEBA) {
     float au3 = fminf(at, as) * u * u * u;
@@ -56,7 +56,6 @@ __device__ __forceinline__ void damped_factors(float r2, float wt, float ws, flo
       k5 *= u4;
     }
   }
-  k5x3 = 3.f * k5;
 }
 
 // partial[split][g][j][3] over the split's sources.  TPT targets per thread:
@@ -91,7 +90,10 @@ __global__ void __launch_bounds__(T32_TPB) k_tmu32(int n, const float4 *__restri
     bhi.x = fmaxf(bhi.x, hi.x), bhi.y = fmaxf(bhi.y, hi.y), bhi.z = fmaxf(bhi.z, hi.z);
   }
 
-  float acc[TPT][G * 3], sum[TPT][G * 3], comp[TPT][G * 3];
+  // per tile the field 3 sum f d - sum k3 mu (f = k5 mu.d) is kept as its
+  // two sums (one FMA per component each), combined into the compensated
+  // cross-tile sum
+  float acc[TPT][G * 3], acb[TPT][G * 3], sum[TPT][G * 3], comp[TPT][G * 3];
 #pragma unroll
   for (int t = 0; t < TPT; ++t)
 #pragma unroll
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(T32_TPB) k_tmu32(int n, const float4 *__restri
 #pragma unroll
     for (int t = 0; t < TPT; ++t)
 #pragma unroll
-      for (int c = 0; c < G * 3; ++c) acc[t][c] = 0.f;
+      for (int c = 0; c < G * 3; ++c) acc[t][c] = acb[t][c] = 0.f;
     if (far_tile) {
 #pragma unroll 4
       for (int k = 0; k < cnt; ++k) {
@@ -137,14 +139,17 @@ __global__ void __launch_bounds__(T32_TPB) k_tmu32(int n, const float4 *__restri
           const float rinv = rsqrtf(r2);
           const float ir2 = rinv * rinv;
           const float k3 = rinv * ir2;
-          const float k5x3 = k3 * (3.f * ir2);
+          const float k5 = k3 * ir2;
 #pragma unroll
           for (int c = 0; c < G; ++c) {
             const float4 m = s_mu[c][k];
-            const float f = k5x3 * fmaf(m.x, dx, fmaf(m.y, dy, m.z * dz));
-            acc[t][c * 3 + 0] = fmaf(f, dx, fmaf(-k3, m.x, acc[t][c * 3 + 0]));
-            acc[t][c * 3 + 1] = fmaf(f, dy, fmaf(-k3, m.y, acc[t][c * 3 + 1]));
-            acc[t][c * 3 + 2] = fmaf(f, dz, fmaf(-k3, m.z, acc[t][c * 3 + 2]));
+            const float f = k5 * fmaf(m.x, dx, fmaf(m.y, dy, m.z * dz));
+            acc[t][c * 3 + 0] = fmaf(f, dx, acc[t][c * 3 + 0]);
+            acc[t][c * 3 + 1] = fmaf(f, dy, acc[t][c * 3 + 1]);
+            acc[t][c * 3 + 2] = fmaf(f, dz, acc[t][c * 3 + 2]);
+            acb[t][c * 3 + 0] = fmaf(k3, m.x, acb[t][c * 3 + 0]);
+            acb[t][c * 3 + 1] = fmaf(k3, m.y, acb[t][c * 3 + 1]);
+            acb[t][c * 3 + 2] = fmaf(k3, m.z, acb[t][c * 3 + 2]);
           }
         }
       }
@@ -158,15 +163,18 @@ __global__ void __launch_bounds__(T32_TPB) k_tmu32(int n, const float4 *__restri
           if (!valid[t] || t0 + k == jb + t * T32_TPB + (int)threadIdx.x) continue;
           const float dx = pt[t].x - ps.x, dy = pt[t].y - ps.y, dz = pt[t].z - ps.z;
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          float k3, k5x3;
-          damped_factors<AMOEBA>(r2, pt[t].w, ps.w, at[t], as, thr, k3, k5x3);
+          float k3, k5;
+          damped_factors<AMOEBA>(r2, pt[t].w, ps.w, at[t], as, thr, k3, k5);
 #pragma unroll
           for (int c = 0; c < G; ++c) {
             const float4 m = s_mu[c][k];
-            const float f = k5x3 * fmaf(m.x, dx, fmaf(m.y, dy, m.z * dz));
-            acc[t][c * 3 + 0] = fmaf(f, dx, fmaf(-k3, m.x, acc[t][c * 3 + 0]));
-            acc[t][c * 3 + 1] = fmaf(f, dy, fmaf(-k3, m.y, acc[t][c * 3 + 1]));
-            acc[t][c * 3 + 2] = fmaf(f, dz, fmaf(-k3, m.z, acc[t][c * 3 + 2]));
+            const float f = k5 * fmaf(m.x, dx, fmaf(m.y, dy, m.z * dz));
+            acc[t][c * 3 + 0] = fmaf(f, dx, acc[t][c * 3 + 0]);
+            acc[t][c * 3 + 1] = fmaf(f, dy, acc[t][c * 3 + 1]);
+            acc[t][c * 3 + 2] = fmaf(f, dz, acc[t][c * 3 + 2]);
+            acb[t][c * 3 + 0] = fmaf(k3, m.x, acb[t][c * 3 + 0]);
+            acb[t][c * 3 + 1] = fmaf(k3, m.y, acb[t][c * 3 + 1]);
+            acb[t][c * 3 + 2] = fmaf(k3, m.z, acb[t][c * 3 + 2]);
           }
         }
       }
@@ -176,7 +184,7 @@ __global__ void __launch_bounds__(T32_TPB) k_tmu32(int n, const float4 *__restri
     for (int t = 0; t < TPT; ++t)
 #pragma unroll
       for (int c = 0; c < G * 3; ++c) {
-        const float y = acc[t][c] - comp[t][c];
+        const float y = fmaf(3.f, acc[t][c], -acb[t][c]) - comp[t][c];
         const float s = sum[t][c] + y;
         comp[t][c] = (s - sum[t][c]) - y;
         sum[t][c] = s;

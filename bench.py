@@ -65,6 +65,11 @@ SYM_MIN_SITES = 2048  # the engine's automatic choice of the symmetric product
 # (27), mu.d (31), the field factor (7), six accumulations (72) and three
 # renormalisations (9)
 DS_OPS_PER_PAIR = 227.0
+# the symmetric double-single product (k_tmu_ds_sym, from 2048 sites) forms
+# the geometry (coordinate differences, r^2, reciprocal square root, r^-2 /
+# r^-3 / 3 r^-5: 108 with the MUFU) once per unordered pair and the rest
+# (mu.d, field factor, accumulations, renormalisations: 119) per direction
+DS_SYM_OPS_PER_PAIR = 108.0 + 2 * 119.0
 # FP64 instructions per ordered (target, source) pair of the AMOEBA gradient
 # pair kernel (k_grad_pairs, openmmpol_gb300/csrc/grad.cu): 95 DFMA + 78 DMUL
 # + 34 DADD, from the ncu instruction counters of one launch on the
@@ -274,7 +279,8 @@ def kernel_table(kst, n, peak64, peak32):
         if name == "tmu_ds":
             # FP32 pipe: double-single operations issued per second against
             # the FMA-pipe instruction rate (peak flop / 2)
-            ops = DS_OPS_PER_PAIR * pairs * cols / (ms * 1e-3) / 1e12
+            ops = (DS_SYM_OPS_PER_PAIR * pairs / 2 if n >= SYM_MIN_SITES else DS_OPS_PER_PAIR * pairs) * cols / (
+                ms * 1e-3) / 1e12
             out[name].update({"fp64_equivalent_tflops": ach, "achieved_tops": ops, "peak_tops": pk / 2,
                               "frac": ops / (pk / 2) if pk else None})
     return out
@@ -284,7 +290,7 @@ def kernel_table(kst, n, peak64, peak32):
 # captures of the 30,000-site box (profiles/tmu_sym_water_box_30000_sites_ncu_full.md,
 # profiles/tmu_ds_water_box_30000_sites_ncu_full.md, profiles/tmu32_water_box_30000_sites_ncu_full.md);
 # the working set is O(N) and L2-resident, so the figure is scaled by the site count
-TRAFFIC_30K = {"tmu_fp64": 3.6e6, "tmu_ds": 3.2e6}
+TRAFFIC_30K = {"tmu_fp64": 3.6e6, "tmu_ds": 4.6e6}
 
 
 def roofline_of(kstats, total_ms, n=30000):
@@ -304,7 +310,9 @@ def roofline_of(kstats, total_ms, n=30000):
                               "box, scaled by the site count (bytes per launch)" if traffic else None,
             "peak_source": "FMA-chain kernel measured in this run (pipe peak; "
                            "MEASURED_PEAKS.json has no FP32/FP64 CUDA-core figure)",
-            "algorithmic": (f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair x N(N-1) pairs" if ds else
+            "algorithmic": ((f"{DS_SYM_OPS_PER_PAIR:.0f} FP32 operations per unordered pair x N(N-1)/2 pairs "
+                             "(symmetric double-single product)" if n >= SYM_MIN_SITES else
+                             f"{DS_OPS_PER_PAIR:.0f} FP32 operations per ordered pair x N(N-1) pairs") if ds else
                             f"{FP64_SYM_OPS_PER_PAIR:.0f} FP64 operations per unordered pair x N(N-1)/2 pairs "
                             f"(symmetric product; {d.get('fp64_flop_equivalent_tflops', 0):.3f} TFLOP/s at the "
                             f"conventional {FLOP_PER_PAIR:.0f} flop per ordered pair)" if sym else

@@ -256,6 +256,196 @@ __global__ void __launch_bounds__(DS_TPB, 5) k_tmu_ds(int n, const float4 *__res
 }
 
 // ---------------------------------------------------------------------------
+// Symmetric double-single T.mu: each unordered pair's geometry (coordinate
+// differences, r^2, the reciprocal square root and the r^-3 / 3 r^-5
+// factors, about 106 of the 227 FP32 operations of an ordered pair) is
+// formed once and serves both directions, as in the FP64 kernel k_tmu_sym
+// (kernels.cu): 128-site super-tile I meets the slots k of its half shell
+// J = (I + k) mod ntile, work items (I, a chunk of slots) are taken from an
+// atomic counter by a persistent grid, a warp pairs its 32 targets with 32
+// sources in 32 rotation steps with the source-side double-single
+// accumulators moving one lane per step by shuffle, and both sides end in
+// the per-site 128-bit fixed-point accumulators (deterministic).  A slot
+// whose tile boxes are farther apart than the damping range runs the
+// undamped pair form; the others test each pair in FP32 first.
+// ---------------------------------------------------------------------------
+template <bool NEAR, bool AMOEBA, int G>
+__device__ __forceinline__ void ds_sym_slot(bool diag, bool vi, int ti, int gbase, int n, const float4 &th,
+                                            const float4 &tl, double wt, double at, float2 wat,
+                                            const float4 (&mih)[G], const float4 (&mil)[G], const float4 *s_ph,
+                                            const float4 *s_pl, const double *s_w, const double *s_a,
+                                            const float2 *s_wa, const float4 (*s_mh)[DS_TILE],
+                                            const float4 (*s_ml)[DS_TILE], double (*s_accj)[3 * G][DS_TILE],
+                                            int warp, int lane, double thr, float thr2m, float (&aih)[G][3],
+                                            float (&ail)[G][3]) {
+  for (int js = 0; js < 4; ++js) {
+    float ajh[G][3], ajl[G][3];
+#pragma unroll
+    for (int col = 0; col < G; ++col)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) ajh[col][c] = ajl[col][c] = 0.f;
+#pragma unroll 1
+    for (int t = 0; t < 32; ++t) {
+      const int jl = js * 32 + ((lane + t) & 31);
+      const int gj = gbase + jl;
+      if (vi && gj < n && gj != ti) {
+        const DsGeom g = ds_geometry<NEAR, AMOEBA>(th, tl, s_ph[jl], s_pl[jl], wt, s_w[jl], at, s_a[jl], wat,
+                                                   s_wa[jl], thr, thr2m);
+#pragma unroll
+        for (int col = 0; col < G; ++col) {
+          ds_column(g, s_mh[col][jl], s_ml[col][jl], aih[col], ail[col]);
+          if (!diag) ds_column(g, mih[col], mil[col], ajh[col], ajl[col]);
+        }
+      }
+      if (!diag) {
+        // the accumulators of source s move to the lane that meets s next
+#pragma unroll
+        for (int col = 0; col < G; ++col)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            ajh[col][c] = __shfl_sync(0xffffffffu, ajh[col][c], (lane + 1) & 31);
+            ajl[col][c] = __shfl_sync(0xffffffffu, ajl[col][c], (lane + 1) & 31);
+          }
+      }
+    }
+    if (!diag) {
+      // after 32 steps lane l holds the accumulators of source js*32 + l
+#pragma unroll
+      for (int col = 0; col < G; ++col)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          s_accj[warp][3 * col + c][js * 32 + lane] = (double)ajh[col][c] + (double)ajl[col][c];
+    }
+  }
+}
+
+template <bool AMOEBA, int G>
+__global__ void __launch_bounds__(DS_TPB) k_tmu_ds_sym(int n, int ntile, int K, int chunk, int nchunk, int nitems,
+                                                       unsigned *__restrict__ next, const float4 *__restrict__ ph,
+                                                       const float4 *__restrict__ pl, const Pos64 *__restrict__ p64,
+                                                       const double *__restrict__ damp,
+                                                       const float2 *__restrict__ wa,
+                                                       const float4 *__restrict__ boxes,
+                                                       const double *__restrict__ x,
+                                                       unsigned long long *__restrict__ acc_lo,
+                                                       unsigned long long *__restrict__ acc_hi,
+                                                       unsigned long long *__restrict__ bad, double thr, float thr2m,
+                                                       float r2max) {
+  constexpr int C = 3 * G;
+  __shared__ float4 s_ph[DS_TILE], s_pl[DS_TILE], s_mh[G][DS_TILE], s_ml[G][DS_TILE];
+  __shared__ double s_w[DS_TILE], s_a[DS_TILE];
+  __shared__ float2 s_wa[DS_TILE];
+  __shared__ double s_accj[4][C][DS_TILE];
+  __shared__ int s_item;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (;;) {
+    __syncthreads();  // every thread has read the previous item
+    if (tid == 0) s_item = (int)atomicAdd(next, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= nitems) break;
+    const int I = item / nchunk;
+    const int ti = I * DS_TILE + tid;
+    const bool vi = ti < n;
+    const float4 th = vi ? ph[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 tl = vi ? pl[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const double wt = vi ? p64[ti].w : 0.0;
+    const double at = (AMOEBA && vi) ? damp[ti] : 0.0;
+    const float2 wat = vi ? wa[ti] : make_float2(0.f, 0.f);
+    float4 mih[G], mil[G];
+#pragma unroll
+    for (int col = 0; col < G; ++col) {
+      float mh[3] = {0.f, 0.f, 0.f}, ml[3] = {0.f, 0.f, 0.f};
+      if (vi)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double m = x[((size_t)col * n + ti) * 3 + c];
+          mh[c] = (float)m;
+          ml[c] = (float)(m - (double)mh[c]);
+        }
+      mih[col] = make_float4(mh[0], mh[1], mh[2], 0.f);
+      mil[col] = make_float4(ml[0], ml[1], ml[2], 0.f);
+    }
+    const float4 ilo = boxes[2 * I], ihi = boxes[2 * I + 1];
+    double sumi[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) sumi[c] = 0.0;
+    const int k0 = (item - I * nchunk) * chunk;
+    const int k1 = min(K + 1, k0 + chunk);
+    for (int k = k0; k < k1; ++k) {
+      int J = I + k;
+      if (J >= ntile) J -= ntile;
+      if (k > 0 && 2 * k == ntile && I >= ntile / 2) continue;  // the other tile of the pair owns it
+      const bool diag = (k == 0);
+      __syncthreads();
+      {
+        const int sj = J * DS_TILE + tid;
+        const bool v = sj < n;
+        s_ph[tid] = v ? ph[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
+        s_pl[tid] = v ? pl[sj] : make_float4(0.f, 0.f, 0.f, 0.f);
+        s_w[tid] = v ? p64[sj].w : 0.0;
+        s_a[tid] = (AMOEBA && v) ? damp[sj] : 0.0;
+        s_wa[tid] = v ? wa[sj] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int col = 0; col < G; ++col) {
+          float mh[3] = {0.f, 0.f, 0.f}, ml[3] = {0.f, 0.f, 0.f};
+          if (v)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const double m = x[((size_t)col * n + sj) * 3 + c];
+              mh[c] = (float)m;
+              ml[c] = (float)(m - (double)mh[c]);
+            }
+          s_mh[col][tid] = make_float4(mh[0], mh[1], mh[2], 0.f);
+          s_ml[col][tid] = make_float4(ml[0], ml[1], ml[2], 0.f);
+        }
+      }
+      __syncthreads();
+      // uniform over the CTA: are the two tiles' boxes within damping range?
+      const float4 jlo = boxes[2 * J], jhi = boxes[2 * J + 1];
+      const float gx = fmaxf(0.f, fmaxf(jlo.x - ihi.x, ilo.x - jhi.x));
+      const float gy = fmaxf(0.f, fmaxf(jlo.y - ihi.y, ilo.y - jhi.y));
+      const float gz = fmaxf(0.f, fmaxf(jlo.z - ihi.z, ilo.z - jhi.z));
+      const bool far_slot = !diag && gx * gx + gy * gy + gz * gz > r2max;
+      float aih[G][3], ail[G][3];
+#pragma unroll
+      for (int col = 0; col < G; ++col)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) aih[col][c] = ail[col][c] = 0.f;
+      if (far_slot)
+        ds_sym_slot<false, AMOEBA, G>(diag, vi, ti, J * DS_TILE, n, th, tl, wt, at, wat, mih, mil, s_ph, s_pl, s_w,
+                                      s_a, s_wa, s_mh, s_ml, s_accj, warp, lane, thr, thr2m, aih, ail);
+      else
+        ds_sym_slot<true, AMOEBA, G>(diag, vi, ti, J * DS_TILE, n, th, tl, wt, at, wat, mih, mil, s_ph, s_pl, s_w,
+                                     s_a, s_wa, s_mh, s_ml, s_accj, warp, lane, thr, thr2m, aih, ail);
+#pragma unroll
+      for (int col = 0; col < G; ++col)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sumi[3 * col + c] += (double)aih[col][c] + (double)ail[col][c];
+      if (!diag) {
+        __syncthreads();
+        const int sj = J * DS_TILE + tid;
+        if (sj < n) {
+#pragma unroll
+          for (int c = 0; c < C; ++c) {
+            const double v = ((s_accj[0][c][tid] + s_accj[1][c][tid]) + s_accj[2][c][tid]) + s_accj[3][c][tid];
+            const size_t o = ((size_t)(c / 3) * n + sj) * 3 + (c % 3);
+            fixed_add(acc_lo + o, acc_hi + o, v, bad);
+          }
+        }
+      }
+    }
+    if (vi) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        const size_t o = ((size_t)(c / 3) * n + ti) * 3 + (c % 3);
+        fixed_add(acc_lo + o, acc_hi + o, sumi[c], bad);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // E_M2D in double-single: field of the static multipoles (charge, dipole,
 // quadrupole for AMOEBA; charge for Wang-AL) at the polarizable sites, the
 // all-pairs part of elec_prop_M2D (src/mod_electrostatics.F90:2579-2731) at
@@ -504,6 +694,54 @@ void launch_tmu_ds_pairs(const DevSites &s, int g, const double *x, double *part
       launch_ds_shape<true, 1, DS_TPT>(s, x, partial, nsplit, st);
     else
       launch_ds_shape<false, 1, DS_TPT>(s, x, partial, nsplit, st);
+  }
+}
+
+namespace {
+template <bool AMOEBA, int G>
+int ds_sym_resident() {
+  static int r = 0;
+  if (!r) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tmu_ds_sym<AMOEBA, G>, DS_TPB, 0);
+    if (r < 1) r = 1;
+  }
+  return r;
+}
+
+template <bool AMOEBA, int G>
+void launch_ds_sym_shape(const DevSites &s, const double *x, unsigned long long *lo, unsigned long long *hi,
+                         unsigned long long *bad, unsigned *next, cudaStream_t st) {
+  const int ntile = (s.n + DS_TILE - 1) / DS_TILE;
+  const int K = ntile / 2;
+  const int ctas_max = ds_sym_resident<AMOEBA, G>() * sm_count();
+  // about 16 work items per resident CTA
+  long long chunk = (long long)ntile * (K + 1) / (16LL * ctas_max);
+  if (chunk < 1) chunk = 1;
+  if (chunk > K + 1) chunk = K + 1;
+  const int nchunk = (int)((K + 1 + chunk - 1) / chunk);
+  const int nitems = ntile * nchunk;
+  const int ctas = ctas_max < nitems ? ctas_max : nitems;
+  const float thr2m = (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));
+  k_tmu_ds_sym<AMOEBA, G><<<ctas, DS_TPB, 0, st>>>(s.n, ntile, K, (int)chunk, nchunk, nitems, next, s.pol_pos32,
+                                                   s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32, s.tile_box32, x,
+                                                   lo, hi, bad, s.damp_thr, thr2m, s.damp_r2max32);
+}
+}  // namespace
+
+// symmetric double-single pair sums of g (1 or 2) columns into the
+// fixed-point accumulators lo / hi [g][n][3] (zeroed by the caller)
+void launch_tmu_ds_sym_pairs(const DevSites &s, int g, const double *x, unsigned long long *lo,
+                             unsigned long long *hi, unsigned long long *bad, unsigned *next, cudaStream_t st) {
+  if (g == 2) {
+    if (s.amoeba)
+      launch_ds_sym_shape<true, 2>(s, x, lo, hi, bad, next, st);
+    else
+      launch_ds_sym_shape<false, 2>(s, x, lo, hi, bad, next, st);
+  } else {
+    if (s.amoeba)
+      launch_ds_sym_shape<true, 1>(s, x, lo, hi, bad, next, st);
+    else
+      launch_ds_sym_shape<false, 1>(s, x, lo, hi, bad, next, st);
   }
 }
 

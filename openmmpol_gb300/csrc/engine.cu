@@ -557,9 +557,15 @@ int System::matvec_residual(int ncol, const double *x, double *y) {
   if (precision_ != kPrecMixedDS) return matvec64(kMatvDirect, ncol, x, y, true);
   int st = ensure_ds_scratch();
   if (st) return st;
+  // the symmetric double-single kernel shares the FP64 one's fixed-point
+  // scratch (without it: the target-outer double-single kernel)
+  if (d_.n >= 2048 && !sym_scratch_ && dalloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 2))) {
+    sym_scratch_ = nullptr;
+    log_msg(kVerbHigh, nullptr, "symmetric T.mu scratch does not fit: using the target-outer kernel");
+  }
   KEv e;
   if (ktime_on_) e = kt_begin(2, ncol);
-  gpu::launch_tmu_ds(d_, ncol, x, y, true, ds_scratch_, nsplit_ds_, st_);
+  gpu::launch_tmu_ds(d_, ncol, x, y, true, ds_scratch_, nsplit_ds_, sym_scratch_, st_);
   if (ktime_on_) kt_end(e);
   stats_.ds_matvecs += 1;
   return kOk;

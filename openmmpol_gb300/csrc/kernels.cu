@@ -297,32 +297,6 @@ __global__ void k_tmu_finish(int n, int nrhs, int nsplit, const T *__restrict__ 
 // ---------------------------------------------------------------------------
 constexpr int SYM_TILE = 128;
 
-// v added exactly into the two-word fixed-point value hi * 2^-16 + lo * 2^-80
-// (hi two's complement, lo unsigned).  A value that is not finite or not
-// below 2^36 in magnitude sets *bad instead (the whole product is then NaN).
-__device__ __forceinline__ void fixed_add(unsigned long long *lo, unsigned long long *hi, double v,
-                                          unsigned long long *bad) {
-  if (!(fabs(v) < 68719476736.0)) {
-    atomicOr(bad, 1ull);
-    return;
-  }
-  const double s = v * 65536.0;  // exact
-  double fl = floor(s);
-  double fr = s - fl;  // exact, in [0, 1]
-  if (fr >= 1.0) {     // s - floor(s) rounded up to 1 for tiny negative s
-    fr = 0.0;
-    fl += 1.0;
-  }
-  const unsigned long long h = (unsigned long long)(long long)fl;
-  const unsigned long long l = (unsigned long long)(fr * 18446744073709551616.0);
-  const unsigned long long old = atomicAdd(lo, l);
-  atomicAdd(hi, h + (old + l < old ? 1ull : 0ull));
-}
-
-__device__ __forceinline__ double fixed_value(unsigned long long lo, unsigned long long hi) {
-  return ((double)(long long)hi + (double)lo * 5.421010862427522e-20) * 1.52587890625e-05;
-}
-
 template <int NRHS, bool AMOEBA>
 __global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, int chunk, int nchunk, int nitems,
                                                        unsigned *__restrict__ next,
@@ -1074,14 +1048,31 @@ void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, boo
 }
 
 void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
-                   int nsplit, cudaStream_t st) {
+                   int nsplit, double *sym_scratch, cudaStream_t st) {
   if (s.n == 0) return;
   const size_t nv = 3 * (size_t)s.n;
+  const bool sym = sym_scratch && s.n >= 2048;
   for (int c = 0; c < nrhs;) {
     const int g = nrhs - c >= 2 ? 2 : 1;
-    add_launch_count(1);
-    launch_tmu_ds_pairs(s, g, x + c * nv, scratch, nsplit, st);
-    tmu_finish<double>(s, g, nsplit, scratch, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 2, st);
+    if (sym) {
+      // fixed-point sums (layout of launch_tmu_f64_sym), read out to doubles
+      const size_t C = 3 * (size_t)g;
+      unsigned long long *lo = reinterpret_cast<unsigned long long *>(sym_scratch);
+      unsigned long long *hi = lo + C * s.n;
+      double *e = sym_scratch + 2 * C * s.n;
+      unsigned long long *bad = reinterpret_cast<unsigned long long *>(sym_scratch + 3 * C * s.n);
+      unsigned *next = reinterpret_cast<unsigned *>(bad + 1);
+      add_launch_count(2);
+      cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
+      cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), st);  // flag and counter
+      launch_tmu_ds_sym_pairs(s, g, x + c * nv, lo, hi, bad, next, st);
+      k_fixed_to_double<<<blocks_for(C * s.n, 256), 256, 0, st>>>(C * s.n, lo, hi, bad, e);
+      tmu_finish<double>(s, g, 1, e, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 2, st);
+    } else {
+      add_launch_count(1);
+      launch_tmu_ds_pairs(s, g, x + c * nv, scratch, nsplit, st);
+      tmu_finish<double>(s, g, nsplit, scratch, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 2, st);
+    }
     c += g;
   }
 }

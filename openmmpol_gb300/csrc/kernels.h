@@ -105,8 +105,12 @@ float damp_r2max32(bool amoeba, double damp_thr, const double *inv_thole, const 
 // scratch of nsplit * 2 * n * 3.
 int tmu_ds_pick_split(const DevSites &s, int sm_count);
 void launch_tmu_ds_pairs(const DevSites &s, int g, const double *x, double *partial, int nsplit, cudaStream_t st);
+// sym_scratch (tmu_sym_scratch_doubles(s, 2), or null): from 2048 sites
+// each unordered pair is evaluated once (launch_tmu_ds_sym_pairs)
 void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
-                   int nsplit, cudaStream_t st);
+                   int nsplit, double *sym_scratch, cudaStream_t st);
+void launch_tmu_ds_sym_pairs(const DevSites &s, int g, const double *x, unsigned long long *lo,
+                             unsigned long long *hi, unsigned long long *bad, unsigned *next, cudaStream_t st);
 // E_M2D with the all-pairs part in double-single (scratch nsplit * n * 3)
 int m2d_ds_pick_split(const DevSites &s, int sm_count);
 void launch_m2d_ds_pairs(const DevSites &s, double *partial, int nsplit, int *err_flag, cudaStream_t st);

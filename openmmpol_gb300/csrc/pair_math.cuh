@@ -290,6 +290,35 @@ __device__ __forceinline__ void m2d_field(const double *acc, double &ex, double 
 // the high word of the non-negative r2 (integer compare, no FP64 instruction)
 __device__ __forceinline__ bool coincident(double r2) { return __double2hiint(r2) < 0x3a436930; }
 
+// Per-site 128-bit fixed-point accumulators of the symmetric products
+// (kernels.cu, ds_kernels.cu): integer addition is exact and associative,
+// so the sums do not depend on the order of the CTAs.
+// v added exactly into the two-word fixed-point value hi * 2^-16 + lo * 2^-80
+// (hi two's complement, lo unsigned).  A value that is not finite or not
+// below 2^36 in magnitude sets *bad instead (the whole product is then NaN).
+__device__ __forceinline__ void fixed_add(unsigned long long *lo, unsigned long long *hi, double v,
+                                          unsigned long long *bad) {
+  if (!(fabs(v) < 68719476736.0)) {
+    atomicOr(bad, 1ull);
+    return;
+  }
+  const double s = v * 65536.0;  // exact
+  double fl = floor(s);
+  double fr = s - fl;  // exact, in [0, 1]
+  if (fr >= 1.0) {     // s - floor(s) rounded up to 1 for tiny negative s
+    fr = 0.0;
+    fl += 1.0;
+  }
+  const unsigned long long h = (unsigned long long)(long long)fl;
+  const unsigned long long l = (unsigned long long)(fr * 18446744073709551616.0);
+  const unsigned long long old = atomicAdd(lo, l);
+  atomicAdd(hi, h + (old + l < old ? 1ull : 0ull));
+}
+
+__device__ __forceinline__ double fixed_value(unsigned long long lo, unsigned long long hi) {
+  return ((double)(long long)hi + (double)lo * 5.421010862427522e-20) * 1.52587890625e-05;
+}
+
 }  // namespace
 }  // namespace gpu
 }  // namespace ommp

@@ -288,6 +288,25 @@ def test_double_single_operator_accuracy(case, w1k, chains, golden_mmp):
     assert site.max() < 1e-9
 
 
+def test_double_single_symmetric_kernel(tmp_path):
+    """From 2048 sites the double-single product evaluates each unordered pair
+    once (2,100 sites: 17 tiles of 128, odd, the last one partial): the same
+    bar against FP64, one and two columns, and bit-identical repeats (the
+    fixed-point sums do not depend on the order of the work items)."""
+    p = synth.write_mmp(str(tmp_path / "w700.mmp"), synth.water_cluster(700, seed=6))
+    g = OMMPSystem(p)
+    assert g.pol_atoms == 2100
+    x = np.random.default_rng(6).standard_normal((2, g.pol_atoms, 3)) * 0.05
+    y64 = g.tmatvec(x)
+    yds = g.tmatvec_ds(x)
+    assert rel(yds, y64) < 1e-11
+    site = np.linalg.norm(yds - y64, axis=2) / np.maximum(np.linalg.norm(y64, axis=2), 1e-3 * np.abs(y64).max())
+    assert site.max() < 1e-9
+    y1 = g.tmatvec_ds(x[0])
+    assert rel(y1, y64[0]) < 1e-11
+    assert np.array_equal(y1, g.tmatvec_ds(x[0]))
+
+
 @pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba", "nma_wang_cut",
                                   "1ubq_amoeba"])
 def test_double_single_m2d_accuracy(case, w1k, chains, golden_mmp):

@@ -8,8 +8,9 @@
 // time step must not stall: cudaMalloc and cudaFree synchronise the device
 // and can fail at an arbitrary point of a long run.  The regular entry point
 // ommp_gpu_tmatvec stages through the system's own buffers; this variant
-// takes device pointers and keeps its only scratch (the per-source-split
-// partial fields of the pair kernel) in a fixed, file-scope device array.
+// takes device pointers and keeps its only scratch (the fixed-point sums of
+// the symmetric product from 2048 sites, else the per-source-split partial
+// fields of the target-outer kernel) in a fixed, file-scope device array.
 //
 // The scratch array (kNoAllocScratchBytes = 16 MiB) lives in every GPU that
 // loads this library until the process exits.  Its device address is looked
@@ -94,9 +95,14 @@ extern "C" int32_t ommp_gpu_tmatvec_noalloc(OMMP_SYSTEM_PRT sp, const double *x_
   double *scratch = nullptr;
   int st = scratch_address(&scratch);
   if (st) return st;
-  int nsplit = ommp::gpu::tmu_pick_split(d, nrhs, ommp::gpu::sm_count(), false);
-  if ((size_t)nsplit > fit) nsplit = (int)fit;
-  ommp::gpu::launch_tmu_f64(d, nrhs, x_dev, y_dev, dodiag != 0, scratch, nsplit, s->stream());
+  if (d.n >= 2048 && ommp::gpu::tmu_sym_scratch_doubles(d, nrhs) <= kNoAllocScratchDoubles) {
+    // each unordered pair once, fixed-point sums in the static scratch
+    ommp::gpu::launch_tmu_f64_sym(d, nrhs, x_dev, y_dev, dodiag != 0, scratch, s->stream());
+  } else {
+    int nsplit = ommp::gpu::tmu_pick_split(d, nrhs, ommp::gpu::sm_count(), false);
+    if ((size_t)nsplit > fit) nsplit = (int)fit;
+    ommp::gpu::launch_tmu_f64(d, nrhs, x_dev, y_dev, dodiag != 0, scratch, nsplit, s->stream());
+  }
   cudaError_t e = cudaStreamSynchronize(s->stream());
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {

@@ -15,7 +15,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from openmmpol_gb300 import OMMPSystem, _lib, set_verbose
+from openmmpol_gb300 import OMMPSystem, _lib, set_verbose, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -26,11 +26,17 @@ def _dev_buffer(L, nbytes):
     return p
 
 
-@pytest.mark.parametrize("case,nrhs,dodiag", [("1crn_wang", 1, 1), ("1ubq_amoeba", 2, 1), ("1crn_amoeba", 1, 0)])
-def test_noalloc_tmatvec_matches_regular_entry_point(case, nrhs, dodiag, golden_mmp):
+@pytest.mark.parametrize("case,nrhs,dodiag", [("1crn_wang", 1, 1), ("1ubq_amoeba", 2, 1), ("1crn_amoeba", 1, 0),
+                                              ("w900", 1, 1), ("w900", 2, 0)])
+def test_noalloc_tmatvec_matches_regular_entry_point(case, nrhs, dodiag, golden_mmp, tmp_path):
+    # w900: 2,700 sites, the symmetric product with its fixed-point sums in
+    # the static scratch
     set_verbose(0)
     L = _lib.load()
-    s = OMMPSystem(golden_mmp[case])
+    if case == "w900":
+        s = OMMPSystem(synth.write_mmp(str(tmp_path / "w900.mmp"), synth.water_cluster(900, seed=8)))
+    else:
+        s = OMMPSystem(golden_mmp[case])
     n = s.pol_atoms
     nbytes = nrhs * n * 3 * 8
     xd, yd = _dev_buffer(L, nbytes), _dev_buffer(L, nbytes)

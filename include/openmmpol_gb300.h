@@ -105,6 +105,9 @@ double ommp_get_polelec_energy(OMMP_SYSTEM_PRT s);
  * multipoles (EM): the m-scaled pairs of the force field, no damping.
  * Computed on the GPU once per geometry. */
 double ommp_get_fixedelec_energy(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:63 ; ommp_get_full_ele_energy src/mod_interface.F90:388-398.
+ * The electrostatic energy: ommp_get_fixedelec_energy + ommp_get_polelec_energy. */
+double ommp_get_full_ele_energy(OMMP_SYSTEM_PRT s);
 /* include/openmmpol.h:40 ; src/mod_c_interface.F90:289-305.
  * ext_field: [pol_atoms][3].  Like the reference, `matv` is ignored on this
  * path and the default matrix-vector method is used (mod_interface.F90:222). */

@@ -166,6 +166,11 @@ class OMMPSystem:
         _check(self._L.ommp_gpu_get_fixedelec_energy(self._h, C.byref(e)))
         return e.value
 
+    def get_full_ele_energy(self) -> float:
+        """Static multipole plus polarization energy (the reference's
+        ommp_get_full_ele_energy, src/mod_interface.F90:388-398)."""
+        return self.get_fixedelec_energy() + self.get_polelec_energy()
+
     def _numerical_grad(self, energy) -> np.ndarray:
         """Central differences of energy() with a 1e-5 bohr step, as the
         reference's numerical_grad (pythonapi/pyopenmmpol/pyommp_interface.cpp:518-543)."""

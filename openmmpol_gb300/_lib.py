@@ -31,6 +31,7 @@ SIGNATURES = {
     "ommp_time_push": (None, []),
     "ommp_get_polelec_energy": (C.c_double, [_vp]),
     "ommp_get_fixedelec_energy": (C.c_double, [_vp]),
+    "ommp_get_full_ele_energy": (C.c_double, [_vp]),
     "ommp_gpu_get_fixedelec_energy": (C.c_int32, [_vp, _dp]),
     "ommp_set_external_field": (None, [_vp, _dp, C.c_int32, C.c_int32]),
     "ommp_set_external_field_nomm": (None, [_vp, _dp, C.c_int32, C.c_int32]),

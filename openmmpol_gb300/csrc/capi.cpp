@@ -106,6 +106,12 @@ double ommp_get_fixedelec_energy(OMMP_SYSTEM_PRT s) {
   fatal_if(ommp_gpu_get_fixedelec_energy(s, &e));
   return e;
 }
+double ommp_get_full_ele_energy(OMMP_SYSTEM_PRT s) {
+  double em = 0.0, ep = 0.0;
+  fatal_if(ommp_gpu_get_fixedelec_energy(s, &em));
+  fatal_if(ommp_gpu_get_polelec_energy(s, &ep));
+  return em + ep;
+}
 int32_t ommp_gpu_get_polelec_energy(OMMP_SYSTEM_PRT s, double *e) {
   ommp_time_push();
   int st = S(s)->polelec_energy(*e);

@@ -84,3 +84,13 @@ def test_static_gradient_water_and_update(tmp_path):
     g2 = g.fixedelec_geomgrad()
     assert not np.array_equal(g2, gg)
     assert maxrel(g2, o.fixedelec_geomgrad()) < 1e-11
+
+
+def test_full_ele_energy_is_static_plus_polarization(golden, golden_mmp):
+    # ommp_get_full_ele_energy (src/mod_interface.F90:388-398) through the C ABI
+    from openmmpol_gb300 import _lib
+    g = OMMPSystem(golden_mmp["1crn_amoeba"])
+    g.set_external_field(golden["1crn_amoeba_ef1"])
+    full = _lib.load().ommp_get_full_ele_energy(g._h)
+    assert full == g.get_fixedelec_energy() + g.get_polelec_energy()
+    assert g.get_full_ele_energy() == full

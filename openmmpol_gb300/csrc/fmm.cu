@@ -54,6 +54,7 @@ struct FmmTree {
   double *sq = nullptr;                                // sorted multipoles [n][ld] (M2D sources)
   int *tmm = nullptr;                                  // targets' static index (M2D self pair)
   double *M = nullptr, *Lc = nullptr;                  // [2][ncell][K]
+  float *M32 = nullptr;  // M scaled to the cell size, FP32 (the M2L input), after M in its block
   bool shared = false;                                 // targets are the sources
 };
 
@@ -63,6 +64,7 @@ struct FmmState {
   int4 *pairs = nullptr;       // M2L pairs: g, index of g + h in the derivative table, h, (-1)^|g|
   int *hoff = nullptr;         // [K + 1] first pair of each target term h
   double *dunit = nullptr;     // [343][KD] derivatives of 1/r to order p at unit cell offsets
+  float *dunit32 = nullptr;    // the same in FP32 (the FP32 M2L)
   // translation lists (M2M, L2L), grouped by target term: source term and
   // packed |m| (bits 0-7) with the parities of m (bits 8-10), coefficient
   int2 *mm_e = nullptr, *ll_e = nullptr;
@@ -90,7 +92,7 @@ void free_tree(FmmTree &t) {
 
 void free_fmm_state(FmmState *f) {
   if (!f) return;
-  void *b[] = {f->terms, f->pairs, f->hoff, f->dunit, f->field, f->mm_e, f->ll_e, f->mm_c, f->ll_c, f->mm_off,
+  void *b[] = {f->terms, f->pairs, f->hoff, f->dunit, f->dunit32, f->field, f->mm_e, f->ll_e, f->mm_c, f->ll_c, f->mm_off,
                f->ll_off};
   for (void *p : b)
     if (p) cudaFree(p);
@@ -118,7 +120,9 @@ struct FmmArgs {
   const int4 *pairs;
   const int *hoff;
   const double *dunit;
+  const float *dunit32;
   double *M, *Lc;
+  float *M32;
   int KD;
   const int2 *mm_e, *ll_e;
   const double *mm_c, *ll_c;
@@ -286,16 +290,55 @@ __global__ void __launch_bounds__(FT) k_fmm_m2l(FmmArgs a, int l) {
   }
 }
 
+// The FP32 M2L input: the multipoles of the cells of levels 2..L scaled to
+// the cell size, M_g h^-|g| (h the level's cell side), in FP32; one thread
+// per (column, cell, term)
+__global__ void k_fmm_m32(FmmArgs a, int first_cell, int ncells) {
+  const size_t total = (size_t)a.ncol * ncells * a.K;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(i % a.K);
+    const size_t cc = i / a.K;
+    const int col = (int)(cc / ncells);
+    const int c = first_cell + (int)(cc % ncells);
+    int l = 0;
+    while (l < a.L && level_off(l + 1) <= c) ++l;
+    const double hinv = (1 << l) / a.h0;
+    double f = 1.0;
+    for (int r = 0; r < a.terms[g].w; ++r) f *= hinv;
+    const size_t o = ((size_t)col * a.ncell + c) * a.K + g;
+    a.M32[o] = (float)(a.M[o] * f);
+  }
+}
+
+// the unit-offset derivative table of the arithmetic type
+template <typename T>
+__device__ __forceinline__ const T *tables(const FmmArgs &a);
+template <>
+__device__ __forceinline__ const double *tables<double>(const FmmArgs &a) {
+  return a.dunit;
+}
+template <>
+__device__ __forceinline__ const float *tables<float>(const FmmArgs &a) {
+  return a.dunit32;
+}
+
 // The same M2L with the (target term, source term) pairs of each thread
 // held in registers (PJ pairs per thread of NT), both columns in one CTA
 // sharing the derivative row staged in shared memory.
-// instantiations: 128 threads x 24 pairs (orders <= 8), 256 x 32 (<= 10)
-template <int NT, int PJ>
+// instantiations: 128 threads x 24 pairs (orders <= 8), 256 x 32 (<= 10).
+// T = float: the multipoles (scaled to the cell size), the unit-offset
+// derivatives and the pair sums in FP32, the sum over source terms of each
+// local term and the local expansion in FP64.  The FP32 rounding (~1e-6
+// of a local coefficient) is far below the expansion's own truncation
+// error (~1e-4 at order 10), and GB300 issues FP32 at 64x its FP64 rate.
+template <typename T, int NT, int PJ>
 __global__ void __launch_bounds__(NT) k_fmm_m2l_reg(FmmArgs a, int l) {
-  extern __shared__ double sh[];
-  double *s_m = sh;                // [2][K]
-  double *s_d = sh + 2 * a.K;      // [KD]
-  double *s_acc = s_d + a.KD;      // [npairs]
+  extern __shared__ __align__(16) unsigned char sh_raw[];
+  T *sh = reinterpret_cast<T *>(sh_raw);
+  T *s_m = sh;                // [2][K]
+  T *s_d = sh + 2 * a.K;      // [KD]
+  T *s_acc = s_d + a.KD;      // [npairs]
+  const T *dunit = tables<T>(a);
   const int npairs = a.hoff[a.K];
   const int tc = blockIdx.x;
   if (a.cnt_t[level_off(l) + tc] == 0) return;
@@ -304,7 +347,7 @@ __global__ void __launch_bounds__(NT) k_fmm_m2l_reg(FmmArgs a, int l) {
   const int n = 1 << l;
   const double hinv = (1 << l) / a.h0;
   int pk[PJ];
-  double acc0[PJ], acc1[PJ];
+  T acc0[PJ], acc1[PJ];
 #pragma unroll
   for (int j = 0; j < PJ; ++j) {
     const int q = threadIdx.x + j * NT;
@@ -313,7 +356,7 @@ __global__ void __launch_bounds__(NT) k_fmm_m2l_reg(FmmArgs a, int l) {
       const int4 pr = a.pairs[q];
       pk[j] = pr.x | (pr.y << 10) | (pr.w << 20);
     }
-    acc0[j] = acc1[j] = 0.0;
+    acc0[j] = acc1[j] = T(0);
   }
   for (int ox = -1; ox <= 1; ++ox)
     for (int oy = -1; oy <= 1; ++oy)
@@ -329,19 +372,23 @@ __global__ void __launch_bounds__(NT) k_fmm_m2l_reg(FmmArgs a, int l) {
           __syncthreads();
           for (int i = threadIdx.x; i < a.ncol * a.K; i += NT) {
             const int col = i / a.K, g = i - col * a.K;
-            const int ng = a.terms[g].w;
-            double f = 1.0;
-            for (int r = 0; r < ng; ++r) f *= hinv;
-            s_m[i] = a.M[((size_t)col * a.ncell + level_off(l) + sc) * a.K + g] * f;
+            if constexpr (std::is_same<T, float>::value) {
+              s_m[i] = a.M32[((size_t)col * a.ncell + level_off(l) + sc) * a.K + g];  // k_fmm_m32
+            } else {
+              const int ng = a.terms[g].w;
+              double f = 1.0;
+              for (int r = 0; r < ng; ++r) f *= hinv;
+              s_m[i] = a.M[((size_t)col * a.ncell + level_off(l) + sc) * a.K + g] * f;
+            }
           }
-          const double *D = a.dunit + (size_t)(((dx + 3) * 7 + (dy + 3)) * 7 + (dz + 3)) * a.KD;
+          const T *D = dunit + (size_t)(((dx + 3) * 7 + (dy + 3)) * 7 + (dz + 3)) * a.KD;
           for (int i = threadIdx.x; i < a.KD; i += NT) s_d[i] = D[i];
           __syncthreads();
 #pragma unroll
           for (int j = 0; j < PJ; ++j) {
             if (pk[j] < 0) continue;
             const int g = pk[j] & 1023;
-            const double d = (pk[j] >> 20) ? -s_d[(pk[j] >> 10) & 1023] : s_d[(pk[j] >> 10) & 1023];
+            const T d = (pk[j] >> 20) ? -s_d[(pk[j] >> 10) & 1023] : s_d[(pk[j] >> 10) & 1023];
             acc0[j] += s_m[g] * d;
             acc1[j] += s_m[a.K + g] * d;
           }
@@ -358,7 +405,7 @@ __global__ void __launch_bounds__(NT) k_fmm_m2l_reg(FmmArgs a, int l) {
     double *Lt = a.Lc + ((size_t)col * a.ncell + level_off(l) + tc) * a.K;
     for (int hh = threadIdx.x; hh < a.K; hh += NT) {
       double s = 0.0;
-      for (int q = a.hoff[hh]; q < a.hoff[hh + 1]; ++q) s += s_acc[q];
+      for (int q = a.hoff[hh]; q < a.hoff[hh + 1]; ++q) s += (double)s_acc[q];
       const short4 e = a.terms[hh];
       double f = hinv;  // h^-(|h| + 1) / h!
       for (int i = 0; i < e.w; ++i) f *= hinv;
@@ -741,7 +788,9 @@ int build_tables(FmmState &f, int p, cudaStream_t st) {
     cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, st);
     return 0;
   };
-  int bad = up(f.terms, terms) | up(f.pairs, pairs) | up(f.hoff, hoff) | up(f.dunit, dunit) | up(f.mm_e, mm_e) |
+  std::vector<float> dunit32(dunit.begin(), dunit.end());
+  int bad = up(f.terms, terms) | up(f.pairs, pairs) | up(f.hoff, hoff) | up(f.dunit, dunit) |
+            up(f.dunit32, dunit32) | up(f.mm_e, mm_e) |
             up(f.ll_e, ll_e) | up(f.mm_c, mm_c) | up(f.ll_c, ll_c) | up(f.mm_off, mm_off) | up(f.ll_off, ll_off);
   if (bad) {
     cudaGetLastError();
@@ -750,10 +799,12 @@ int build_tables(FmmState &f, int p, cudaStream_t st) {
   }
   const size_t smem = (f.K + (size_t)f.npairs) * sizeof(double);
   if (smem > 48 * 1024) cudaFuncSetAttribute(gpu::k_fmm_m2l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(double);
+  const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(float);
   if (smem_reg > 48 * 1024) {
-    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<128, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_reg);
-    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<256, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_reg);
+    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<float, 128, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_reg);
+    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<float, 256, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_reg);
   }
   return cudaStreamSynchronize(st) == cudaSuccess ? kOk : kErrCuda;  // host vectors die here
 }
@@ -882,7 +933,9 @@ void tree_args(const FmmState &f, const FmmTree &t, int ncol, gpu::FmmArgs &a) {
   a.pairs = f.pairs;
   a.hoff = f.hoff;
   a.dunit = f.dunit;
+  a.dunit32 = f.dunit32;
   a.M = t.M;
+  a.M32 = t.M32;
   a.Lc = t.Lc;
   a.mm_e = f.mm_e;
   a.ll_e = f.ll_e;
@@ -896,11 +949,19 @@ void tree_args(const FmmState &f, const FmmTree &t, int ncol, gpu::FmmArgs &a) {
 void run_tree(const FmmState &f, const FmmTree &t, const gpu::FmmArgs &a, int ncol, cudaStream_t st) {
   const size_t smem = (f.K + (size_t)f.npairs) * sizeof(double);
   for (int l = t.L; l >= 1; --l) gpu::k_fmm_m2m<<<dim3(1 << (3 * (l - 1)), ncol), gpu::FT, 0, st>>>(a, l);
-  const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(double);
+  const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(float);
+  const bool reg = f.npairs <= 32 * 256;
+  if (reg && t.L >= 2) {
+    const int c0 = ((1 << 6) - 1) / 7, nc = t.ncell - c0;  // the cells of levels 2..L
+    gpu::k_fmm_m32<<<gpu::sm_count() * 8, 256, 0, st>>>(a, c0, nc);
+    gpu::add_launch_count(1);
+  }
   if (f.npairs <= 24 * 128) {
-    for (int l = 2; l <= t.L; ++l) gpu::k_fmm_m2l_reg<128, 24><<<dim3(1 << (3 * l), 1), 128, smem_reg, st>>>(a, l);
+    for (int l = 2; l <= t.L; ++l)
+      gpu::k_fmm_m2l_reg<float, 128, 24><<<dim3(1 << (3 * l), 1), 128, smem_reg, st>>>(a, l);
   } else if (f.npairs <= 32 * 256) {
-    for (int l = 2; l <= t.L; ++l) gpu::k_fmm_m2l_reg<256, 32><<<dim3(1 << (3 * l), 1), 256, smem_reg, st>>>(a, l);
+    for (int l = 2; l <= t.L; ++l)
+      gpu::k_fmm_m2l_reg<float, 256, 32><<<dim3(1 << (3 * l), 1), 256, smem_reg, st>>>(a, l);
   } else {
     for (int l = 2; l <= t.L; ++l) gpu::k_fmm_m2l<<<dim3(1 << (3 * l), ncol), gpu::FT, smem, st>>>(a, l);
   }
@@ -959,8 +1020,9 @@ int System::fmm_prepare() {
     if (t.M) cudaFree(t.M);
     if (t.Lc) cudaFree(t.Lc);
     t.M = t.Lc = nullptr;
-    bad |= cudaMalloc((void **)&t.M, 2 * (size_t)t.ncell * f.K * sizeof(double)) != cudaSuccess;
+    bad |= cudaMalloc((void **)&t.M, 2 * (size_t)t.ncell * f.K * (sizeof(double) + sizeof(float))) != cudaSuccess;
     bad |= cudaMalloc((void **)&t.Lc, 2 * (size_t)t.ncell * f.K * sizeof(double)) != cudaSuccess;
+    t.M32 = t.M ? reinterpret_cast<float *>(t.M + 2 * (size_t)t.ncell * f.K) : nullptr;
     t.nalloc_cell = t.ncell;
   }
   if (f.field_n < 6 * (size_t)n) {
@@ -1074,8 +1136,9 @@ int System::fmm_m2d(double *out, bool &done) {
       if (t.M) cudaFree(t.M);
       if (t.Lc) cudaFree(t.Lc);
       t.M = t.Lc = nullptr;
-      bad |= cudaMalloc((void **)&t.M, (size_t)t.ncell * f.K * sizeof(double)) != cudaSuccess;
+      bad |= cudaMalloc((void **)&t.M, (size_t)t.ncell * f.K * (sizeof(double) + sizeof(float))) != cudaSuccess;
       bad |= cudaMalloc((void **)&t.Lc, (size_t)t.ncell * f.K * sizeof(double)) != cudaSuccess;
+      t.M32 = t.M ? reinterpret_cast<float *>(t.M + (size_t)t.ncell * f.K) : nullptr;
       t.nalloc_cell = t.ncell;
     }
     if (bad) {

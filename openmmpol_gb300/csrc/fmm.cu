@@ -325,7 +325,7 @@ __device__ __forceinline__ const float *tables<float>(const FmmArgs &a) {
 // The same M2L with the (target term, source term) pairs of each thread
 // held in registers (PJ pairs per thread of NT), both columns in one CTA
 // sharing the derivative row staged in shared memory.
-// instantiations: 128 threads x 24 pairs (orders <= 8), 256 x 32 (<= 10).
+// instantiations: 256 threads x 12 pairs (orders <= 8), 512 x 16 (<= 10).
 // T = float: the multipoles (scaled to the cell size), the unit-offset
 // derivatives and the pair sums in FP32, the sum over source terms of each
 // local term and the local expansion in FP64.  The FP32 rounding (~1e-6
@@ -801,9 +801,9 @@ int build_tables(FmmState &f, int p, cudaStream_t st) {
   if (smem > 48 * 1024) cudaFuncSetAttribute(gpu::k_fmm_m2l, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(float);
   if (smem_reg > 48 * 1024) {
-    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<float, 128, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<float, 256, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem_reg);
-    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<float, 256, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(gpu::k_fmm_m2l_reg<float, 512, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem_reg);
   }
   return cudaStreamSynchronize(st) == cudaSuccess ? kOk : kErrCuda;  // host vectors die here
@@ -950,18 +950,18 @@ void run_tree(const FmmState &f, const FmmTree &t, const gpu::FmmArgs &a, int nc
   const size_t smem = (f.K + (size_t)f.npairs) * sizeof(double);
   for (int l = t.L; l >= 1; --l) gpu::k_fmm_m2m<<<dim3(1 << (3 * (l - 1)), ncol), gpu::FT, 0, st>>>(a, l);
   const size_t smem_reg = (2 * (size_t)f.K + f.KD + f.npairs) * sizeof(float);
-  const bool reg = f.npairs <= 32 * 256;
+  const bool reg = f.npairs <= 16 * 512;
   if (reg && t.L >= 2) {
     const int c0 = ((1 << 6) - 1) / 7, nc = t.ncell - c0;  // the cells of levels 2..L
     gpu::k_fmm_m32<<<gpu::sm_count() * 8, 256, 0, st>>>(a, c0, nc);
     gpu::add_launch_count(1);
   }
-  if (f.npairs <= 24 * 128) {
+  if (f.npairs <= 12 * 256) {
     for (int l = 2; l <= t.L; ++l)
-      gpu::k_fmm_m2l_reg<float, 128, 24><<<dim3(1 << (3 * l), 1), 128, smem_reg, st>>>(a, l);
-  } else if (f.npairs <= 32 * 256) {
+      gpu::k_fmm_m2l_reg<float, 256, 12><<<dim3(1 << (3 * l), 1), 256, smem_reg, st>>>(a, l);
+  } else if (f.npairs <= 16 * 512) {
     for (int l = 2; l <= t.L; ++l)
-      gpu::k_fmm_m2l_reg<float, 256, 32><<<dim3(1 << (3 * l), 1), 256, smem_reg, st>>>(a, l);
+      gpu::k_fmm_m2l_reg<float, 512, 16><<<dim3(1 << (3 * l), 1), 512, smem_reg, st>>>(a, l);
   } else {
     for (int l = 2; l <= t.L; ++l) gpu::k_fmm_m2l<<<dim3(1 << (3 * l), ncol), gpu::FT, smem, st>>>(a, l);
   }

@@ -27,10 +27,14 @@ in the reference (src/mod_electrostatics.F90:1487-1596, M2D_done cache).
   modes and with the FP64 pass, each against its pipe, their difference, and
   the oracle's gradient on the host cores (3,000-molecule sample scaled).
 * ``cpu_baseline``: the C/OpenMP oracle (restatement of the reference's
-  OpenMP path) timed on a bounded sample of target rows of one matrix-vector
-  product, scaled to a full solve with the FP64 solve's product count.
+  OpenMP path) timed on two whole T.mu products of the box on all host cores,
+  scaled to a solve by the oracle's own product count (20).
 
-``--impl reference`` times that CPU implementation alone and prints its line.
+``--impl reference`` times that CPU implementation alone and prints its line:
+each step is one whole oracle T.mu product (1/20 of a solve, so
+``ms_per_step`` is the real step time and ``value`` the solves/s it implies),
+and one whole oracle solve of the box outside the timed steps gives the
+measured solve time and product count beside the per-step figure.
 Multi-GPU (``--gpus N`` under torchrun): independent replicas, one per GPU.
 """
 from __future__ import annotations
@@ -90,6 +94,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="w30k", choices=["w30k", "w10k", "w1k", "b64", "c60k", "s1024"])
     ap.add_argument("--skip-cpu", action="store_true", help="leave out the CPU baseline (profiling runs)")
+    ap.add_argument("--no-full-solve", action="store_true",
+                    help="--impl reference: leave out the whole oracle solve that checks the per-step figure")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
     ap.add_argument("--no-fp64", action="store_true")
@@ -206,22 +212,42 @@ def cpu_sample(path, rows_n, threads=None):
     return dt * n / len(rows), len(rows), n
 
 
+def cpu_full_products(o, count):
+    """Wall seconds of `count` whole oracle T.mu products (the function its CG
+    calls, all target rows, OpenMP over the host cores)."""
+    n = o.pol_atoms
+    x = np.random.default_rng(0).standard_normal((n, 3)) * 0.01
+    out = []
+    for _ in range(count):
+        t0 = time.perf_counter()
+        o.tmatvec(x)
+        out.append(time.perf_counter() - t0)
+    return out
+
+
+# T.mu products of the oracle's plain CG solve of the 90,000-site box (D: 16
+# iterations with the initial and final residual products; P, seeded with D,
+# converges at once), counted by its whole solve of that box; the reference
+# arm counts them again in its own whole solve
+ORACLE_MV_PER_SOLVE = 20
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from oracle import oracle as orc
     orc.build()
-    path, _ = workload(args.config, args.cache)
+    path, w = workload(args.config, args.cache)
     cores = os.cpu_count() or 1
-    if args.config in ("w1k", "w10k") and not args.cpu_rows:
+    orc.set_num_threads(cores)
+    o = orc.OracleSystem(path)
+    o.set_tol(1e-10)
+    n = o.pol_atoms
+    cmm = o.cmm
+    extra = {}
+    if args.config in ("w1k", "w10k"):
         # small boxes: whole solves (D + P, CG to 1e-10) on all host cores
-        orc.set_num_threads(cores)
-        o = orc.OracleSystem(path)
-        o.set_tol(1e-10)
-        n = o.pol_atoms
-        w = workload(args.config, args.cache)[1]
-        cmm = o.cmm
         fl = fields_for(cmm[o.polar_mm], cmm, w.box_center(), [100 + k for k in range(args.warmup + args.steps)])
         o.e_m2d()  # cached per geometry, as on the GPU side
         times = []
@@ -231,30 +257,56 @@ def run_reference(args):
             o.set_external_field(f)
             if k >= args.warmup:
                 times.append(time.perf_counter() - t0)
-        nrows, mv_per_solve = n, o.matvec_count()
+        mv_per_solve = o.matvec_count()
+        step_s = statistics.mean(times)
+        v = 1.0 / step_s
         sample = f"whole solves, one per step ({mv_per_solve} T.mu products each)"
     else:
-        # T.mu products of the plain CG solve of the 90,000-site box (D: 16
-        # iterations plus residual products; P equals D and converges at once),
-        # counted by the oracle's full solve of that box
-        mv_per_solve = {"w30k": 20, "b64": 20}.get(args.config, 20)
-        rows = args.cpu_rows or 1500
-        times = []
-        for k in range(args.warmup + args.steps):
-            sec_per_mv, nrows, n = cpu_sample(path, rows, cores)
-            if k >= args.warmup:
-                times.append(sec_per_mv * mv_per_solve)
-        sample = (f"{nrows} of {n} target rows of one T.mu product per step, scaled by {n}/{nrows} rows "
-                  f"and {mv_per_solve} products per solve")
-    v = 1.0 / statistics.mean(times)
+        # Each step is one whole oracle T.mu product of the box (all target
+        # rows on all host cores), the unit of work of the plain CG solve: a
+        # solve of this box is ORACLE_MV_PER_SOLVE products, so a step is that
+        # fraction of a solve and solves/s = 1 / (products x seconds/product).
+        times = cpu_full_products(o, args.warmup + args.steps)[args.warmup:]
+        step_s = statistics.mean(times)
+        mv_per_solve = ORACLE_MV_PER_SOLVE
+        full = None
+        if not args.no_full_solve:
+            # one whole solve of the 90,000-site box outside the timed steps
+            # (permanent field computed first and cached, as on the GPU, D + P
+            # to 1e-10 with a fresh 30-charge field): the measured solve time
+            # and product count against the per-step figure
+            f = fields_for(cmm[o.polar_mm], cmm, w.box_center(), [100])[0]
+            t0 = time.perf_counter()
+            o.e_m2d()
+            m2d_s = time.perf_counter() - t0
+            mv0 = o.matvec_count()
+            o.clear_guess()
+            t0 = time.perf_counter()
+            o.set_external_field(f)
+            full_s = time.perf_counter() - t0
+            mv_full = o.matvec_count() - mv0
+            mv_per_solve = mv_full
+            full = {"measured_full_solve_s": full_s, "t_mu_products": mv_full,
+                    "cg_iterations": [o.last_iterations(0), o.last_iterations(1)],
+                    "m2d_s": m2d_s,
+                    "per_step_estimate_s": step_s * mv_full,
+                    "estimate_vs_measured_pct": 100.0 * (step_s * mv_full - full_s) / full_s}
+        v = 1.0 / (step_s * mv_per_solve)
+        sample = (f"one whole T.mu product of the {n}-site box per step (all target rows), "
+                  f"{mv_per_solve} products per solve")
+        extra = {"step_unit": f"one T.mu product = 1/{mv_per_solve} of a solve",
+                 "s_per_tmu_product": step_s, "steps_s": times, "extrapolated": True}
+        if full:
+            extra["full_solve"] = full
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"water box {args.config}: {n} AMOEBA sites, 30-charge field, "
                                    "CG tol 1e-10, direct matvec", "sites": n},
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line.update(extra)
     print(json.dumps(line), flush=True)
 
 
@@ -286,10 +338,10 @@ def kernel_table(kst, n, peak64, peak32):
     return out
 
 
-# DRAM bytes (read + write) per launch of the dominant kernels, from the ncu
-# captures of the 30,000-site box (profiles/tmu_sym_water_box_30000_sites_ncu_full.md,
-# profiles/tmu_ds_water_box_30000_sites_ncu_full.md, profiles/tmu32_water_box_30000_sites_ncu_full.md);
-# the working set is O(N) and L2-resident, so the figure is scaled by the site count
+# DRAM bytes (read + write) per launch of the dominant kernels, from ncu
+# captures (dram__bytes_read.sum + dram__bytes_write.sum) of one launch on the
+# 30,000-site box; the working set is O(N) and L2-resident, so the figure is
+# scaled by the site count
 TRAFFIC_30K = {"tmu_fp64": 3.6e6, "tmu_ds": 4.6e6}
 
 
@@ -653,15 +705,22 @@ def run_gb300(args):
     elif rank == 0:
         # CPU baseline on the host cores (oracle port, bounded sample)
         try:
+            from oracle import oracle as orc
             cores = os.cpu_count() or 1
-            rows = args.cpu_rows or (1500 if n > 30000 else 3000)
-            sec_mv, nrows, _ = cpu_sample(path, rows, cores)
-            mv = fp64["t_mu_products"] if fp64 else 36
+            orc.set_num_threads(cores)
+            o = orc.OracleSystem(path)
+            o.tmatvec_rows(np.zeros((n, 3)), np.arange(min(n, 512), dtype=np.int32))  # thread warm-up
+            sec_mv = statistics.mean(cpu_full_products(o, 2))
+            mv = ORACLE_MV_PER_SOLVE
             cpu_v = 1.0 / (sec_mv * mv)
             line["cpu_baseline"] = {"value": cpu_v, "unit": "solves/s", "cores": cores, "kind": "port",
-                                    "sample": f"{nrows} of {n} target rows of one T.mu product, scaled to "
-                                              f"{mv} products (the plain FP64 CG solve on this workload)",
+                                    "sample": f"two whole T.mu products of the {n}-site box (all target rows), "
+                                              f"scaled to the {mv} products of the oracle's plain CG solve",
                                     "s_per_tmu_product": sec_mv}
+            if fp64:
+                # precision-matched: the plain FP64 GPU solve against the FP64 CPU solve
+                line["fp64"]["gpu_fp64_vs_cpu_fp64"] = fp64["solves_per_s"] / cpu_v
+                line["fp64"]["e2e_mixed_vs_cpu_fp64"] = main["e2e"]["value"] / cpu_v
         except Exception as ex:  # report, do not hide
             line["cpu_baseline"] = {"value": None, "error": repr(ex)}
         print(json.dumps(line), flush=True)

@@ -336,6 +336,8 @@ int32_t ommp_gpu_device_alloc(int64_t bytes, void **ptr);
 int32_t ommp_gpu_device_free(void *ptr);
 int32_t ommp_gpu_copy_to_device(void *dst, const void *src, int64_t bytes);
 int32_t ommp_gpu_copy_to_host(void *dst, const void *src, int64_t bytes);
+/* free and total device memory of the current device, bytes */
+int32_t ommp_gpu_device_mem_info(int64_t *free_bytes, int64_t *total_bytes);
 /* measured FMA throughput of the FP64 (fp64 = 1) or FP32 pipe, TFLOP/s */
 int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops);
 /* SM count of the current device, 0 without a GPU */
@@ -375,11 +377,17 @@ void ommp_gpu_server_stats(void *server, double *out7);
  * (dodiag = 0) for nrhs (1|2) columns [nrhs][pol_atoms][3], with x and y in
  * caller-owned DEVICE memory, and no memory allocation inside the call: for
  * hosts that manage all GPU memory themselves (a QM code's SCF loop with its
- * own memory pool, an MD step that must not stall on cudaMalloc).  Scratch is
- * a 16 MiB static device array, so pol_atoms * nrhs <= 699050; larger sizes
- * are rejected with OMMP_GPU_ERR_BAD_ARG.  The first call on each device
- * looks the array up (cudaGetSymbolAddress): make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race.  The
+ * own memory pool, an MD step that must not stall on cudaMalloc).  The
+ * product is always the direct FP64 sum over all pairs, whatever the
+ * system's FMM, matrix-vector or FP64-kernel settings.  Scratch is a 16 MiB
+ * static device array, so pol_atoms * nrhs <= 699050; larger sizes are
+ * rejected with OMMP_GPU_ERR_BAD_ARG, and so are overlapping x and y (no
+ * in-place product).  The array is placed on a device when a system is
+ * created there; a call on a device without a system created first places
+ * it itself (make such a first call before any stream capture).  The kernels
+ * run on the system's own stream, which is not ordered against the caller's
+ * streams: whatever wrote x (a copy or a kernel) must have completed before
+ * the call.  Calls share the array: calls that overlap on the GPU race.  The
  * call returns after its kernels have finished. */
 int32_t ommp_gpu_tmatvec_noalloc(OMMP_SYSTEM_PRT s, const double *x_dev, double *y_dev, int32_t nrhs,
                                  int32_t dodiag);

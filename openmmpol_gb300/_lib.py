@@ -124,6 +124,7 @@ SIGNATURES = {
     "ommp_gpu_device_alloc": (C.c_int32, [C.c_int64, C.POINTER(_vp)]),
     "ommp_gpu_device_free": (C.c_int32, [_vp]),
     "ommp_gpu_copy_to_device": (C.c_int32, [_vp, _vp, C.c_int64]),
+    "ommp_gpu_device_mem_info": (C.c_int32, [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "ommp_gpu_copy_to_host": (C.c_int32, [_vp, _vp, C.c_int64]),
     "ommp_gpu_measure_pipe_peak": (C.c_int32, [C.c_int32, _dp]),
     "ommp_gpu_device_sm_count": (C.c_int32, []),

@@ -327,6 +327,17 @@ int32_t ommp_gpu_copy_to_host(void *dst, const void *src, int64_t bytes) {
   }
   return ommp::kOk;
 }
+int32_t ommp_gpu_device_mem_info(int64_t *free_bytes, int64_t *total_bytes) {
+  size_t f = 0, t = 0;
+  cudaError_t e = cudaMemGetInfo(&f, &t);
+  *free_bytes = (int64_t)f;
+  *total_bytes = (int64_t)t;
+  if (e != cudaSuccess) {
+    ommp::set_last_error(std::string("cudaMemGetInfo: ") + cudaGetErrorString(e));
+    return ommp::kErrCuda;
+  }
+  return ommp::kOk;
+}
 int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops) {
   *tflops = 0.0;
   void *out = nullptr;

@@ -233,6 +233,9 @@ int System::upload_static() {
   polar_mm_h_ = m.polar_mm;
   st = upload_geometry();
   if (st) return st;
+  // place the no-allocation entry point's static scratch on this device now,
+  // while the system allocates anyway (a failure here is retried by that call)
+  noalloc_prepare_device();
   return check(cudaStreamSynchronize(st_), "upload");
 }
 

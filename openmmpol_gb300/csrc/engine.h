@@ -276,6 +276,10 @@ class System {
   unsigned flush_tag_ = 0;
 };
 
+// resolves the static scratch of ommp_gpu_tmatvec_noalloc on the current
+// device (noalloc.cu); called once per system set-up
+int noalloc_prepare_device();
+
 // process-wide error text of the last failing call
 void set_last_error(const std::string &s);
 const char *last_error();

@@ -12,18 +12,29 @@
 // the symmetric product from 2048 sites, else the per-source-split partial
 // fields of the target-outer kernel) in a fixed, file-scope device array.
 //
+// The product is always the direct FP64 sum over all pairs: the system's FMM
+// switch, its matrix-vector selector (in-core T) and its FP64 kernel choice
+// do not apply here.
+//
 // The scratch array (kNoAllocScratchBytes = 16 MiB) lives in every GPU that
 // loads this library until the process exits.  Its device address is looked
-// up once per device, with that device current, on the first call made on
-// that device; make that first call before any stream capture.  All calls
-// share the array: two calls whose kernels overlap on a GPU (from different
-// host threads, or different systems on different streams) race on it.  The
-// call itself waits for its kernels, so calls issued one after another from
-// one thread never overlap.  Every partial entry the finishing kernel reads
-// is written by the pair kernel of the same call first, so nothing needs
-// clearing between calls.
+// up with that device current when a system is created on it
+// (noalloc_prepare_device, called from the system's device set-up, where
+// allocation already happens); that lookup is what makes the CUDA runtime
+// load this file's module and place the array.  A call on a device where no
+// system was created first does the lookup itself: that first call is then
+// set-up and should come before any stream capture.  All calls share the
+// array: two calls whose kernels overlap on a GPU (from different host
+// threads, or different systems on different streams) race on it.  The call
+// itself waits for its kernels, so calls issued one after another from one
+// thread never overlap.  What must start at zero is cleared on every call:
+// the symmetric branch clears its fixed-point accumulators with
+// cudaMemsetAsync before its pair kernel; in the target-outer branch every
+// partial the finishing kernel reads is first written by the pair kernel of
+// the same call.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -68,7 +79,24 @@ int scratch_address(double **out) {
   return ommp::kOk;
 }
 
+bool ranges_overlap(const void *a, const void *b, size_t bytes) {
+  const uintptr_t pa = reinterpret_cast<uintptr_t>(a), pb = reinterpret_cast<uintptr_t>(b);
+  return pa < pb + bytes && pb < pa + bytes;
+}
+
 }  // namespace
+
+namespace ommp {
+
+// Resolves the scratch address on the current device.  Called when a system
+// is set up on a device, so that a later ommp_gpu_tmatvec_noalloc call on it
+// neither loads a module nor places the array.
+int noalloc_prepare_device() {
+  double *p = nullptr;
+  return scratch_address(&p);
+}
+
+}  // namespace ommp
 
 extern "C" int32_t ommp_gpu_tmatvec_noalloc(OMMP_SYSTEM_PRT sp, const double *x_dev, double *y_dev, int32_t nrhs,
                                             int32_t dodiag) {
@@ -83,6 +111,12 @@ extern "C" int32_t ommp_gpu_tmatvec_noalloc(OMMP_SYSTEM_PRT sp, const double *x_
   }
   const ommp::gpu::DevSites &d = s->dev();
   if (d.n == 0) return ommp::kOk;
+  // the finishing kernel reads x at the scaled-pair neighbours of a site
+  // while other threads already write y: x and y must be disjoint
+  if (ranges_overlap(x_dev, y_dev, (size_t)nrhs * (size_t)d.n * 3 * sizeof(double))) {
+    ommp::set_last_error("ommp_gpu_tmatvec_noalloc: x and y overlap (an in-place product is not supported)");
+    return ommp::kErrBadArg;
+  }
   // the pair kernel needs nsplit * nrhs * n * 3 doubles of partials
   size_t per_split = (size_t)nrhs * (size_t)d.n * 3;
   size_t fit = kNoAllocScratchDoubles / per_split;

@@ -28,10 +28,10 @@ in the reference (src/mod_electrostatics.F90:1487-1596, M2D_done cache).
   the oracle's gradient on the host cores (3,000-molecule sample scaled).
 * ``cpu_baseline``: the C/OpenMP oracle (restatement of the reference's
   OpenMP path) timed on two whole T.mu products of the box on all host cores,
-  scaled to a solve by the oracle's own product count (20).
+  scaled to a solve by the oracle's own product count (19).
 
 ``--impl reference`` times that CPU implementation alone and prints its line:
-each step is one whole oracle T.mu product (1/20 of a solve, so
+each step is one whole oracle T.mu product (1/19 of a solve, so
 ``ms_per_step`` is the real step time and ``value`` the solves/s it implies),
 and one whole oracle solve of the box outside the timed steps gives the
 measured solve time and product count beside the per-step figure.
@@ -103,7 +103,7 @@ def parse():
     ap.add_argument("--no-grad", action="store_true", help="leave out the polarization-gradient pass")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-ds"],
                     help="mixed: FP64 refinement residual products; mixed-ds: double-single ones")
-    ap.add_argument("--fp32-kernel", default="auto", choices=["auto", "pairwise", "tiled"],
+    ap.add_argument("--fp32-kernel", default="auto", choices=["auto", "pairwise", "tiled", "symmetric"],
                     help="FP32 inner T.mu kernel (auto = autotuned)")
     ap.add_argument("--requests", type=int, default=1024, help="s1024: requests in the mixed stream")
     ap.add_argument("--fp64-requests", type=int, default=64, help="s1024: requests in the FP64 stream")
@@ -225,11 +225,11 @@ def cpu_full_products(o, count):
     return out
 
 
-# T.mu products of the oracle's plain CG solve of the 90,000-site box (D: 16
-# iterations with the initial and final residual products; P, seeded with D,
-# converges at once), counted by its whole solve of that box; the reference
-# arm counts them again in its own whole solve
-ORACLE_MV_PER_SOLVE = 20
+# T.mu products of the oracle's plain CG solve of the 90,000-site box with the
+# field of seed 100 (D: 16 iterations and its residual products; P, seeded
+# with D, converges at once), counted by its whole solve of that box; the
+# reference arm counts them again in its own whole solve
+ORACLE_MV_PER_SOLVE = 19
 
 
 def run_reference(args):

@@ -214,6 +214,22 @@ int32_t ommp_qm_helper_get_qm_atoms(OMMP_QM_HELPER_PRT qm);
 void ommp_enable_fmm(OMMP_SYSTEM_PRT s);
 void ommp_disable_fmm(OMMP_SYSTEM_PRT s);
 bool ommp_use_fmm(OMMP_SYSTEM_PRT s);
+/* include/openmmpol.h:156-160 ; src/mod_c_interface.F90:1781-1841.  The
+ * reference's FMM settings.  lmax_pol: expansion order of the induced-dipole
+ * (T.mu) products; lmax: order of the permanent-multipole field; both map to
+ * the total order of this FMM's Cartesian expansions (2..12, default 10 each;
+ * the reference's default 8 is a spherical-harmonic order, about as accurate
+ * as 10 here).  distance (bohr): the reference treats leaf cells closer than
+ * this as near; min_cell_size (bohr): it stops subdividing below this half
+ * diagonal.  This FMM's near field is the 27 neighbouring leaves of a uniform
+ * octree, so both become lower bounds of the leaf side (distance, and
+ * 2 min_cell_size / sqrt 3), beside the Thole damping range; default 0 (the
+ * damping range alone).  Out-of-range values stop the process like the
+ * reference's errors. */
+void ommp_set_fmm_lmax_pol(OMMP_SYSTEM_PRT s, int32_t l);
+void ommp_set_fmm_lmax(OMMP_SYSTEM_PRT s, int32_t l);
+void ommp_set_fmm_distance(OMMP_SYSTEM_PRT s, double d);
+void ommp_set_fmm_min_cell_size(OMMP_SYSTEM_PRT s, double d);
 
 /* ---- extensions (no counterpart in the reference) ---------------------- */
 
@@ -235,8 +251,21 @@ int32_t ommp_gpu_polelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
 int32_t ommp_gpu_fixedelec_geomgrad(OMMP_SYSTEM_PRT s, double *grd);
 /* ommp_rotation_geomgrad returning a status */
 int32_t ommp_gpu_rotation_geomgrad(OMMP_SYSTEM_PRT s, const double *E, const double *Egrd, double *grd);
-/* FMM on (on != 0) or off, with expansion order 2..12 */
+/* FMM on (on != 0) or off, with expansion order 2..12 (both orders) */
 int32_t ommp_gpu_set_fmm(OMMP_SYSTEM_PRT s, int32_t on, int32_t order);
+/* the four FMM settings above returning a status instead of stopping */
+int32_t ommp_gpu_set_fmm_lmax_pol(OMMP_SYSTEM_PRT s, int32_t l);
+int32_t ommp_gpu_set_fmm_lmax(OMMP_SYSTEM_PRT s, int32_t l);
+int32_t ommp_gpu_set_fmm_distance(OMMP_SYSTEM_PRT s, double d);
+int32_t ommp_gpu_set_fmm_min_cell_size(OMMP_SYSTEM_PRT s, double d);
+/* current orders and the leaf-side lower bound (bohr) from the settings */
+void ommp_gpu_get_fmm_settings(OMMP_SYSTEM_PRT s, int32_t *lmax_pol, int32_t *lmax, double *min_leaf);
+/* Process-wide, default off: systems created while on get the FMM switched
+ * on when they have more than 1,000 MM atoms, as the reference does by
+ * default (src/mod_electrostatics.F90:294-306).  Off, the direct sums stay
+ * the default (the plain FP64 path then reproduces the reference's direct
+ * results to 1e-9, which an FMM truncated at ~1e-4 cannot). */
+void ommp_gpu_set_fmm_auto(int32_t on);
 /* QM helper calls returning a status instead of stopping the process */
 int32_t ommp_gpu_init_qm_helper(int32_t n, const double *cqm, const double *qqm, const int32_t *zqm,
                                 OMMP_QM_HELPER_PRT *out);
@@ -265,7 +294,9 @@ int32_t ommp_gpu_potential_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, cons
 int32_t ommp_gpu_field_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, const double *cext, double *E);
 /* FP32 inner T.mu kernel: 0 autotuned (default), 1 one target per thread
  * with a per-pair damping test, 2 tile-classified (undamped inner loop for
- * tiles beyond the damping range, two targets per thread) */
+ * tiles beyond the damping range, two targets per thread), 3 symmetric (each
+ * unordered pair once for both directions, tile-classified, deterministic
+ * fixed-point sums) */
 int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
 /* preconditioner of the FP32 inner solver of the mixed modes: 0 the
  * reference's diagonal (alpha), 1 block Jacobi over runs of bonded sites

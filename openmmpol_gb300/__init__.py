@@ -45,6 +45,13 @@ def set_verbose(level) -> None:
     _lib.load().ommp_set_verbose(lvl)
 
 
+def set_fmm_auto(on: bool) -> None:
+    """Process-wide: systems created while on get the FMM when they have more
+    than 1,000 MM atoms (the reference's default); off (the default), the
+    direct sums stay until set_fmm / ommp_enable_fmm."""
+    _lib.load().ommp_gpu_set_fmm_auto(int(bool(on)))
+
+
 def kernel_launch_count() -> int:
     """Kernels the library has launched in this process (CUDA graph launches
     count their kernels)."""
@@ -246,6 +253,27 @@ class OMMPSystem:
         field (expansion order 2..12, default 10)."""
         _check(self._L.ommp_gpu_set_fmm(self._h, int(bool(on)), int(order)))
 
+    # the reference's FMM settings (pyopenmmpol names)
+    def set_fmm_lmax_pol(self, lmax: int) -> None:
+        _check(self._L.ommp_gpu_set_fmm_lmax_pol(self._h, int(lmax)))
+
+    def set_fmm_lmax(self, lmax: int) -> None:
+        _check(self._L.ommp_gpu_set_fmm_lmax(self._h, int(lmax)))
+
+    def set_fmm_distance(self, d: float) -> None:
+        """near-field distance, bohr"""
+        _check(self._L.ommp_gpu_set_fmm_distance(self._h, float(d)))
+
+    def set_fmm_min_cell_size(self, d: float) -> None:
+        """minimum cell size (half diagonal), bohr"""
+        _check(self._L.ommp_gpu_set_fmm_min_cell_size(self._h, float(d)))
+
+    def fmm_settings(self):
+        """(lmax_pol, lmax, leaf-side lower bound in bohr)"""
+        a, b, c = C.c_int32(), C.c_int32(), C.c_double()
+        self._L.ommp_gpu_get_fmm_settings(self._h, C.byref(a), C.byref(b), C.byref(c))
+        return a.value, b.value, c.value
+
     # --- potential and field at external points (pyopenmmpol names) -------------
     def _ext(self, field: bool, which: int, cext) -> np.ndarray:
         c = np.ascontiguousarray(cext, dtype=np.float64)
@@ -302,8 +330,9 @@ class OMMPSystem:
         _check(self._L.ommp_gpu_set_inner_blocks(self._h, int(max_sites), float(link_bohr)))
 
     def set_fp32_kernel(self, mode) -> None:
-        """'auto' (autotuned) | 'pairwise' (kernel 1) | 'tiled' (kernel 2)."""
-        m = {"auto": 0, "pairwise": 1, "tiled": 2}.get(mode, mode)
+        """'auto' (autotuned) | 'pairwise' (kernel 1) | 'tiled' (kernel 2) |
+        'symmetric' (kernel 3: each unordered pair once)."""
+        m = {"auto": 0, "pairwise": 1, "tiled": 2, "symmetric": 3}.get(mode, mode)
         _check(self._L.ommp_gpu_set_fp32_kernel(self._h, int(m)))
 
     def clear_guess(self) -> None:

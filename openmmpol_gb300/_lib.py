@@ -80,6 +80,16 @@ SIGNATURES = {
     "ommp_rotation_geomgrad": (None, [_vp, _dp, _dp, _dp]),
     "ommp_gpu_rotation_geomgrad": (C.c_int32, [_vp, _dp, _dp, _dp]),
     "ommp_gpu_set_fmm": (C.c_int32, [_vp, C.c_int32, C.c_int32]),
+    "ommp_set_fmm_lmax_pol": (None, [_vp, C.c_int32]),
+    "ommp_set_fmm_lmax": (None, [_vp, C.c_int32]),
+    "ommp_set_fmm_distance": (None, [_vp, C.c_double]),
+    "ommp_set_fmm_min_cell_size": (None, [_vp, C.c_double]),
+    "ommp_gpu_set_fmm_lmax_pol": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_set_fmm_lmax": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_set_fmm_distance": (C.c_int32, [_vp, C.c_double]),
+    "ommp_gpu_set_fmm_min_cell_size": (C.c_int32, [_vp, C.c_double]),
+    "ommp_gpu_get_fmm_settings": (None, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp]),
+    "ommp_gpu_set_fmm_auto": (None, [C.c_int32]),
     "ommp_init_qm_helper": (_vp, [C.c_int32, _dp, _dp, _ip]),
     "ommp_gpu_init_qm_helper": (C.c_int32, [C.c_int32, _dp, _dp, _ip, C.POINTER(_vp)]),
     "ommp_terminate_qm_helper": (None, [_vp]),

@@ -226,6 +226,20 @@ void ommp_enable_fmm(OMMP_SYSTEM_PRT s) { fatal_if(S(s)->set_fmm(true, S(s)->fmm
 void ommp_disable_fmm(OMMP_SYSTEM_PRT s) { fatal_if(S(s)->set_fmm(false, S(s)->fmm_order())); }
 bool ommp_use_fmm(OMMP_SYSTEM_PRT s) { return S(s)->fmm_on(); }
 int32_t ommp_gpu_set_fmm(OMMP_SYSTEM_PRT s, int32_t on, int32_t order) { return S(s)->set_fmm(on != 0, order); }
+void ommp_set_fmm_lmax_pol(OMMP_SYSTEM_PRT s, int32_t l) { fatal_if(S(s)->set_fmm_order_pol(l)); }
+void ommp_set_fmm_lmax(OMMP_SYSTEM_PRT s, int32_t l) { fatal_if(S(s)->set_fmm_order_static(l)); }
+void ommp_set_fmm_distance(OMMP_SYSTEM_PRT s, double d) { fatal_if(S(s)->set_fmm_distance(d)); }
+void ommp_set_fmm_min_cell_size(OMMP_SYSTEM_PRT s, double d) { fatal_if(S(s)->set_fmm_min_cell_size(d)); }
+int32_t ommp_gpu_set_fmm_lmax_pol(OMMP_SYSTEM_PRT s, int32_t l) { return S(s)->set_fmm_order_pol(l); }
+int32_t ommp_gpu_set_fmm_lmax(OMMP_SYSTEM_PRT s, int32_t l) { return S(s)->set_fmm_order_static(l); }
+int32_t ommp_gpu_set_fmm_distance(OMMP_SYSTEM_PRT s, double d) { return S(s)->set_fmm_distance(d); }
+int32_t ommp_gpu_set_fmm_min_cell_size(OMMP_SYSTEM_PRT s, double d) { return S(s)->set_fmm_min_cell_size(d); }
+void ommp_gpu_get_fmm_settings(OMMP_SYSTEM_PRT s, int32_t *lmax_pol, int32_t *lmax, double *min_leaf) {
+  if (lmax_pol) *lmax_pol = S(s)->fmm_order();
+  if (lmax) *lmax = S(s)->fmm_order_static();
+  if (min_leaf) *min_leaf = S(s)->fmm_min_leaf();
+}
+void ommp_gpu_set_fmm_auto(int32_t on) { ommp::set_fmm_auto(on != 0); }
 
 const char *ommp_gpu_last_error(void) { return ommp::last_error(); }
 void ommp_gpu_set_solver_tol(OMMP_SYSTEM_PRT s, double tol) { S(s)->set_tol(tol); }

@@ -60,6 +60,7 @@ System::~System() {
   if (sym_scratch_) cudaFree(sym_scratch_);
   free_grad_state(grad_);
   free_fmm_state(fmm_);
+  free_fmm_state(fmms_);
   kt_resolve();
   for (auto &e : kfree_) {
     cudaEventDestroy(e.a);
@@ -95,10 +96,14 @@ System *System::load_host(const std::string &path, std::string &err, int &status
   }
   build_m2d_pairs(s->m_, s->m2d_pairs_);
   build_d2d_pairs(s->m_, s->d2d_pairs_);
-  if (s->m_.fmm_requested)
+  if (s->m_.fmm_requested && fmm_auto()) {
+    s->fmm_on_ = true;
+    log_msg(kVerbHigh, nullptr, "More than 1000 MM atoms: FMM enabled (ommp_gpu_set_fmm_auto is on).");
+  } else if (s->m_.fmm_requested) {
     log_msg(kVerbHigh, nullptr,
             "More than 1000 MM atoms: the reference would enable FMM here; this library keeps the "
-            "direct sums unless ommp_enable_fmm is called.");
+            "direct sums unless ommp_enable_fmm or ommp_gpu_set_fmm_auto is called.");
+  }
   status = kOk;
   return s;
 }
@@ -518,12 +523,9 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
   }
   {
     bool sym = fp64_kernel_ == 2 || (fp64_kernel_ == 0 && d_.n >= 2048);
-    if (sym && !sym_scratch_) {
-      if (dalloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 2))) {
-        sym_scratch_ = nullptr;
-        sym = false;  // not enough memory for the partials: all-ordered-pairs kernel
-        log_msg(kVerbHigh, nullptr, "symmetric T.mu scratch does not fit: using the target-outer kernel");
-      }
+    if (sym && ensure_sym_scratch() != kOk) {
+      sym = false;  // not enough memory for the partials: all-ordered-pairs kernel
+      log_msg(kVerbHigh, nullptr, "symmetric T.mu scratch does not fit: using the target-outer kernel");
     }
     KEv e;
     if (ktime_on_) e = kt_begin(0, ncol);
@@ -538,6 +540,19 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
     }
     if (ktime_on_) kt_end(e);
     stats_.f64_matvecs += 1;
+  }
+  return kOk;
+}
+
+// fixed-point accumulators of the symmetric products (FP64, double-single
+// and FP32 share them: they run one after another on the system's stream)
+int System::ensure_sym_scratch() {
+  if (sym_scratch_) return kOk;
+  if (dalloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 2))) {
+    sym_scratch_ = nullptr;
+    cudaGetLastError();
+    set_last_error("out of device memory for the symmetric-product accumulators");
+    return kErrMemory;
   }
   return kOk;
 }
@@ -931,8 +946,8 @@ int System::set_inner_preconditioner(int mode) {
 }
 
 int System::set_fp32_kernel(int mode) {
-  if (mode < 0 || mode > 2) {
-    set_last_error("FP32 kernel mode must be 0 (autotuned), 1 or 2");
+  if (mode < 0 || mode > 3) {
+    set_last_error("FP32 kernel mode must be 0 (autotuned), 1, 2 or 3");
     return kErrBadArg;
   }
   if (mode != fp32_kernel_) f32_tune_.clear();
@@ -1000,9 +1015,10 @@ int System::tmatvec_f32(const double *xh, double *yh, int nrhs) {
   }
   cudaMemcpyAsync(p_, xh, nrhs * nv * sizeof(double), cudaMemcpyHostToDevice, st_);
   gpu::launch_to_f32(nrhs * nv, p_, nullptr, p32_, st_);
-  const int kver = fp32_kernel_ ? fp32_kernel_ : 2;
+  int kver = fp32_kernel_ ? fp32_kernel_ : 2;
+  if (kver == 3 && ensure_sym_scratch() != kOk) kver = 2;
   const int split = kver == 2 ? nsplit_tmu32_ : gpu::tmu_pick_split(d_, nrhs, gpu::sm_count(), true);
-  gpu::launch_tmu_f32(d_, nrhs, p32_, h32_, scratch32_, split, st_, 4, kver);
+  gpu::launch_tmu_f32(d_, nrhs, p32_, h32_, scratch32_, split, st_, kver == 3 ? 2 : 4, kver, sym_scratch_);
   std::vector<float> tmp(nrhs * nv);
   cudaMemcpyAsync(tmp.data(), h32_, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, st_);
   int st = check(cudaStreamSynchronize(st_), "tmatvec_f32");

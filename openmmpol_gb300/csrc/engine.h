@@ -107,6 +107,16 @@ class System {
   int set_fmm(bool on, int order);
   bool fmm_on() const { return fmm_on_; }
   int fmm_order() const { return fmm_order_; }
+  // the reference's FMM settings (mod_c_interface.F90:1781-1841): expansion
+  // order of the induced-dipole products (lmax_pol) and of the permanent
+  // field (lmax), near-field distance and minimum cell size (bohr), mapped
+  // onto this FMM's orders and the leaf side of its uniform octree
+  int set_fmm_order_pol(int order);
+  int set_fmm_order_static(int order);
+  int set_fmm_distance(double d);
+  int set_fmm_min_cell_size(double d);
+  int fmm_order_static() const { return fmm_order_static_; }
+  double fmm_min_leaf() const;
   void clear_guess() { ipd_use_guess_ = false; }
   void set_tol(double t) { tol_ = t; }
   void set_maxiter(int n) { maxiter_ = n; }
@@ -123,6 +133,7 @@ class System {
   int set_inner_blocks(int max_sites, double link_bohr);
   int matvec_residual(int ncol, const double *x, double *y);
   int ensure_ds_scratch();
+  int ensure_sym_scratch();
   int precision() const { return precision_; }
   double tol() const { return tol_; }
   const SolveStats &stats() const { return stats_; }
@@ -258,9 +269,13 @@ class System {
   GradState *grad_ = nullptr;
   int ensure_grad_state();
   int frame_forces(const double *E_dev, const double *G_dev, const double *base_dev, double *grad_host);
-  FmmState *fmm_ = nullptr;
+  FmmState *fmm_ = nullptr;   // induced-dipole products: tables of fmm_order_, the T.mu tree
+  FmmState *fmms_ = nullptr;  // permanent field: tables of fmm_order_static_, the M2D tree
   bool fmm_on_ = false;
   int fmm_order_ = 10;  // total order |g| + |h| <= 10 of the Cartesian M2L
+  int fmm_order_static_ = 10;
+  double fmm_dfar_ = 0.0, fmm_mincell_ = 0.0;  // 0: leaf side from the damping range alone
+  void fmm_drop_static();
   int fmm_prepare();
   void fmm_invalidate();
   bool fmm_tree() const;  // the prepared FMM has a tree (else direct sums)
@@ -275,6 +290,12 @@ class System {
   size_t flush_bytes_ = 0;
   unsigned flush_tag_ = 0;
 };
+
+// process-wide: systems created while this is on get the FMM switched on when
+// they have more than 1,000 MM atoms, as the reference does by default
+// (src/mod_electrostatics.F90:294-306, OMMP_FMM_ENABLE_THR)
+void set_fmm_auto(bool on);
+bool fmm_auto();
 
 // resolves the static scratch of ommp_gpu_tmatvec_noalloc on the current
 // device (noalloc.cu); called once per system set-up

@@ -26,6 +26,7 @@
 // with exact pair terms, sign, 1/alpha diagonal).  Sites are kept in leaf
 // order on the device (a counting sort per geometry).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -699,7 +700,23 @@ __global__ void __launch_bounds__(FT) k_fmm_l2p_m2d(FmmArgs a, const int *__rest
 }  // namespace
 }  // namespace gpu
 
+namespace {
+std::atomic<bool> g_fmm_auto{false};
+}  // namespace
+
+void set_fmm_auto(bool on) { g_fmm_auto = on; }
+bool fmm_auto() { return g_fmm_auto; }
+
 int System::set_fmm(bool on, int order) {
+  int st = set_fmm_order_pol(order);
+  if (st) return st;
+  st = set_fmm_order_static(order);
+  if (st) return st;
+  fmm_on_ = on;
+  return kOk;
+}
+
+int System::set_fmm_order_pol(int order) {
   if (order < 2 || order > fmm::kMaxOrder) {
     set_last_error("FMM expansion order must be between 2 and 12");
     return kErrBadArg;
@@ -708,17 +725,67 @@ int System::set_fmm(bool on, int order) {
     free_fmm_state(fmm_);
     fmm_ = nullptr;
   }
-  if (order != fmm_order_ && m2d_method_ == kM2dFMM) m2d_done_ = false;  // a field of the old order
-  fmm_on_ = on;
   fmm_order_ = order;
   return kOk;
 }
 
+void System::fmm_drop_static() {
+  if (fmms_) fmms_->m2d.built = false;
+  if (m2d_method_ == kM2dFMM) m2d_done_ = false;  // a field of the old settings
+}
+
+int System::set_fmm_order_static(int order) {
+  if (order < 2 || order > fmm::kMaxOrder) {
+    set_last_error("FMM expansion order must be between 2 and 12");
+    return kErrBadArg;
+  }
+  if (order == fmm_order_static_) return kOk;
+  if (fmms_) {
+    free_fmm_state(fmms_);
+    fmms_ = nullptr;
+  }
+  fmm_order_static_ = order;
+  fmm_drop_static();
+  return kOk;
+}
+
+// The reference treats two leaf cells as near when the gap between them is
+// below fmm_distance and stops subdividing a cell whose half diagonal is below
+// fmm_min_cell_size (src/fast_multipoles/mod_tree.F90:177,
+// mod_octatree.F90:98).  Here the near field is the 27 neighbouring leaves of
+// a uniform octree, so cells farther apart are separated by at least one leaf
+// side: both settings become lower bounds of that side (the min cell size as
+// a half diagonal, side = 2 d / sqrt 3), beside the damping range.
+double System::fmm_min_leaf() const { return std::max(fmm_dfar_, 2.0 * fmm_mincell_ / std::sqrt(3.0)); }
+
+int System::set_fmm_distance(double d) {
+  if (!(d >= 0.0) || !std::isfinite(d)) {
+    set_last_error("FMM distance must be a finite non-negative length (bohr)");
+    return kErrBadArg;
+  }
+  fmm_dfar_ = d;
+  fmm_invalidate();
+  fmm_drop_static();
+  return kOk;
+}
+
+int System::set_fmm_min_cell_size(double d) {
+  if (!(d >= 0.0) || !std::isfinite(d)) {
+    set_last_error("FMM minimum cell size must be a finite non-negative length (bohr)");
+    return kErrBadArg;
+  }
+  fmm_mincell_ = d;
+  fmm_invalidate();
+  fmm_drop_static();
+  return kOk;
+}
+
 void System::fmm_invalidate() {
-  if (!fmm_) return;
-  fmm_->built = false;
-  fmm_->d2d.built = false;
-  fmm_->m2d.built = false;
+  if (fmm_) {
+    fmm_->built = false;
+    fmm_->d2d.built = false;
+  }
+  if (fmms_) fmms_->m2d.built = false;
 }
 
 namespace {
@@ -991,7 +1058,8 @@ int System::fmm_prepare() {
   for (int j = 0; j < n; ++j)
     for (int d = 0; d < 3; ++d) xp[3 * (size_t)j + d] = m_.cmm[3 * (size_t)m_.polar_mm[j] + d];
   TreeLayout o;
-  if (!plan_tree(n, xp.data(), 0, nullptr, std::sqrt((double)d_.damp_r2max32), f.npairs, o)) {
+  if (!plan_tree(n, xp.data(), 0, nullptr, std::max((double)std::sqrt(d_.damp_r2max32), fmm_min_leaf()), f.npairs,
+                 o)) {
     t.L = -1;  // fewer than four damping ranges across: the direct sums serve
     f.built = true;
     log_msg(kVerbHigh, nullptr, "FMM: system too small for a tree with near field >= damping range; direct sums");
@@ -1082,17 +1150,37 @@ int System::fmm_tmu(int ncol, const double *x, double *y, bool dodiag) {
 // sites as targets; done = false when the system is too small for a tree
 int System::fmm_m2d(double *out, bool &done) {
   done = false;
-  int st = fmm_prepare();  // tables
-  if (st) return st;
-  FmmState &f = *fmm_;
+  if (!fmms_) {  // tables of the static order
+    fmms_ = new FmmState();
+    int st = build_tables(*fmms_, fmm_order_static_, st_);
+    if (st) {
+      free_fmm_state(fmms_);
+      fmms_ = nullptr;
+      return st == kErrCuda ? check(cudaGetLastError(), "FMM tables") : st;
+    }
+  }
+  int st = kOk;
+  FmmState &f = *fmms_;
   FmmTree &t = f.m2d;
   const int n = d_.n, mm = d_.m, ld = m_.ld_cart;
+  if (f.field_n < 3 * (size_t)n) {
+    if (f.field) cudaFree(f.field);
+    f.field = nullptr;
+    if (cudaMalloc((void **)&f.field, 3 * (size_t)n * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      f.field_n = 0;
+      set_last_error("out of device memory for the FMM field");
+      return kErrMemory;
+    }
+    f.field_n = 3 * (size_t)n;
+  }
   if (!t.built) {
     std::vector<double> xp(3 * (size_t)n);
     for (int j = 0; j < n; ++j)
       for (int d = 0; d < 3; ++d) xp[3 * (size_t)j + d] = m_.cmm[3 * (size_t)m_.polar_mm[j] + d];
     TreeLayout o;
-    if (!plan_tree(mm, m_.cmm.data(), n, xp.data(), std::sqrt((double)d_.m2d_r2max32), f.npairs, o)) {
+    if (!plan_tree(mm, m_.cmm.data(), n, xp.data(), std::max((double)std::sqrt(d_.m2d_r2max32), fmm_min_leaf()),
+                   f.npairs, o)) {
       t.L = -1;
       t.built = true;
       return kOk;

@@ -1169,8 +1169,27 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
 }
 
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch, int nsplit,
-                    cudaStream_t st, int gmax, int kver) {
+                    cudaStream_t st, int gmax, int kver, double *sym_scratch) {
   if (s.n == 0) return;
+  if (kver == 3 && sym_scratch) {
+    // symmetric kernel: fixed-point sums read out as floats into the third
+    // block of the symmetric scratch, then the shared finishing pass
+    const size_t nv = 3 * (size_t)s.n;
+    for (int c = 0; c < nrhs;) {
+      const int g = (nrhs - c >= 2 && gmax >= 2) ? 2 : 1;
+      const size_t C = 3 * (size_t)g;
+      unsigned long long *lo = reinterpret_cast<unsigned long long *>(sym_scratch);
+      unsigned long long *hi = lo + C * s.n;
+      float *e = reinterpret_cast<float *>(sym_scratch + 2 * C * s.n);
+      unsigned long long *bad = reinterpret_cast<unsigned long long *>(sym_scratch + 3 * C * s.n);
+      unsigned *next = reinterpret_cast<unsigned *>(bad + 1);
+      add_launch_count(2);
+      launch_tmu32_sym_pairs(s, g, x + c * nv, lo, hi, bad, next, e, st);
+      tmu_finish<float>(s, g, 1, e, s.pol_pos32, s.pol_a32, x + c * nv, true, y + c * nv, 2, st);
+      c += g;
+    }
+    return;
+  }
   tmu_dispatch<float, true>(s, nrhs, s.pol_pos32, s.pol_a32, x, scratch, nsplit, gmax, st, kver);
   tmu_finish<float>(s, nrhs, nsplit, scratch, s.pol_pos32, s.pol_a32, x, true, y, gmax, st);
 }

@@ -89,8 +89,17 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
 // the pair geometry; scratch holds nsplit * nrhs * n * 3 floats.
 // kver 1: one target per thread, per-pair damping test (kernels.cu);
 // kver 2: the tile-classified kernel of tmu32.cu.
+// kver 3: the symmetric kernel of tmu32.cu (each unordered pair once),
+// columns in groups of gmax (1 or 2), sums in sym_scratch (laid out as for
+// launch_tmu_f64_sym, tmu_sym_scratch_doubles(s, 2)); scratch unused.
 void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float *scratch,
-                    int nsplit, cudaStream_t st, int gmax = 4, int kver = 2);
+                    int nsplit, cudaStream_t st, int gmax = 4, int kver = 2, double *sym_scratch = nullptr);
+// symmetric FP32 pair sums of g (1 or 2) columns into the fixed-point
+// accumulators lo / hi [g][n][3] (zeroed here), read out into out [g][n][3]
+void launch_tmu32_sym_pairs(const DevSites &s, int g, const float *x, unsigned long long *lo,
+                            unsigned long long *hi, unsigned long long *bad, unsigned *next, float *out,
+                            cudaStream_t st);
+int tmu32_sym_resident(int g, bool amoeba);
 void launch_tmu32_pairs(const DevSites &s, int g, const float *x, float *partial, int nsplit, cudaStream_t st);
 // source splits an FP32 scratch must hold (per column) for every shape the
 // autotuner may pick

@@ -176,7 +176,7 @@ int System::cg64_ws(Workspace &w, int matv, int ncol, const double *rhs, double 
 // FP32 product with the tuned launch shape
 // ---------------------------------------------------------------------------
 void System::f32_product(Workspace &w, int ncol, const F32Shape &sh) {
-  gpu::launch_tmu_f32(d_, ncol, w.p32, w.h32, w.scratch32, sh.nsplit, st_, sh.g, sh.kver);
+  gpu::launch_tmu_f32(d_, ncol, w.p32, w.h32, w.scratch32, sh.nsplit, st_, sh.g, sh.kver, sym_scratch_);
 }
 
 int System::tune_f32(Workspace &w, int ncol, F32Shape &shape) {
@@ -196,14 +196,20 @@ int System::tune_f32(Workspace &w, int ncol, F32Shape &shape) {
   // targets per thread for one or two columns
   const int s1 = gpu::tmu_pick_split(d_, ncol, sms, true), s2 = gpu::tmu32_pick_split(d_, sms);
   for (int g : widths) {
-    if (fp32_kernel_ != 2)
+    if (fp32_kernel_ == 0 || fp32_kernel_ == 1)
       for (int s : {s1, 2 * s1})
         if (s <= cap) cands.push_back({g, s, 1});
-    if (fp32_kernel_ != 1)
+    if (fp32_kernel_ == 0 || fp32_kernel_ == 2)
       for (int s : {std::max(1, s2 / 2), s2, 2 * s2})
         if (s <= cap) cands.push_back({g, s, 2});
   }
-  if (cands.empty()) cands.push_back({1, 1, fp32_kernel_ ? fp32_kernel_ : 2});
+  // kernel 3: each unordered pair once (tmu32.cu), column groups of 1 or 2,
+  // from 2048 sites (or when forced); its accumulators are allocated here,
+  // before any capture of the inner iteration
+  if ((fp32_kernel_ == 3 || (fp32_kernel_ == 0 && d_.n >= 2048)) && ensure_sym_scratch() == kOk)
+    for (int g : {1, 2})
+      if (g <= ncol) cands.push_back({g, 1, 3});
+  if (cands.empty()) cands.push_back({1, 1, fp32_kernel_ == 1 ? 1 : 2});
   const size_t nv = 3 * (size_t)d_.n;
   cudaMemsetAsync(w.p32, 0, ncol * nv * sizeof(float), st_);
   cudaEvent_t a, b;

@@ -21,9 +21,13 @@
 //
 // Compiled with -ftz=true: the reciprocal square root is the plain MUFU
 // approximation (r^2 is never subnormal for distinct sites).
+//
+// The symmetric form (k_tmu32_sym, further down) evaluates each unordered
+// pair once and accumulates both directions, as the FP64 product does.
 #include <cmath>
 
 #include "kernels.h"
+#include "pair_math.cuh"
 
 namespace ommp {
 namespace gpu {
@@ -214,7 +218,380 @@ void launch_g(const DevSites &s, const float *x, float *partial, int nsplit, cud
                                                      (float)s.damp_thr, s.damp_r2max32);
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric FP32 operator.  The ordered kernel above spends ~20 FP32
+// instructions per ordered pair, half of them on the geometry (differences,
+// r^2, powers), which T_ij = T_ji lets two directions share.  Here every
+// unordered pair is evaluated once: 9 geometry instructions and 10 per
+// direction (mu.d, the field factor, six accumulations), 29 in all instead of
+// 40, on the half-shell schedule of the symmetric FP64 product (super-tile I
+// meets the slots k = 0..ntile/2 of J = I + k, handed out by an atomic
+// counter to a persistent grid).
+//
+// Per CTA 128 threads own a super-tile of 256 targets, two per thread (lanes
+// l and l + 32 of a 64-target warp slice), so that each source read from
+// shared memory feeds two pairs.  A warp pairs its targets with each 32-site
+// sub-tile of J in 32 rotation steps: at step t lane l meets source
+// (l + t) mod 32 and the source-side sums travel one lane per step by
+// shuffle (three per column and step, 1.5 per pair).  Every sub-tile is
+// staged twice in a row, so the lane's read address is its base plus t with
+// no wrap-around, an immediate offset.  The target side keeps the field's two
+// sums (f d and k3 mu, f = k5 mu.d) and applies the factor 3 once per slot;
+// the source side uses its own dipoles divided by 3 (held in registers), so
+// g d - k3 mu/3 needs no extra instruction and the factor 3 is applied when
+// the four warps' sums are combined in shared memory.
+//
+// Slots whose tile boxes are farther apart than the damping range run an
+// undamped loop; near slots and the diagonal slot (target side only, all
+// ordered pairs of the tile, self pairs skipped) run the damped one.  Absent
+// sites of the last tile sit at +-1e15 with zero dipoles.  Slot sums
+// (FP32, at most 256 terms) go into per-site 128-bit fixed-point
+// accumulators with integer atomics (converted from FP32 by integer
+// operations), so the product is deterministic in any CTA order.
+// ---------------------------------------------------------------------------
+constexpr int S32_TPB = 128;
+constexpr int S32_TILE = 256;
+constexpr int S32_SUB = 32;
+constexpr int S32_NSUB = S32_TILE / S32_SUB;
+constexpr float S32_FAR = 1.0e15f;
+
+template <int G>
+struct S32Smem {
+  float4 pos[S32_NSUB][2 * S32_SUB];    // each sub-tile twice in a row
+  float4 mu[G][S32_NSUB][2 * S32_SUB];  // x, y, z; w = damping a of the source
+  float accj[4][3 * G][S32_TILE];       // source-side sums of the four warps
+};
+
+// fixed_add (pair_math.cuh) for an FP32 value, with integer operations only:
+// the same 128-bit accumulator (units of 2^-80, hi holding the bits from
+// 2^-16 up), fed with |v| = m 2^(e - 150) shifted to m 2^(e - 70) units and
+// negated in two's complement for negative v.  The FP64 conversion of
+// fixed_add takes ~6 FP64 instructions per value at 1/64 of the FP32 rate.
+// |v| >= 2^36 (or not finite) raises the flag; |v| < 2^-80 adds nothing.
+__device__ __forceinline__ void fixed_add_f32(unsigned long long *lo, unsigned long long *hi, float v,
+                                              unsigned long long *bad) {
+  const unsigned b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  if (e >= 127 + 36) {
+    atomicOr(bad, 1ull);
+    return;
+  }
+  const int sh = e - 70;
+  if (e == 0 || sh <= -24) return;
+  const unsigned long long m = (unsigned long long)((b & 0x7fffffu) | 0x800000u);
+  unsigned long long l, h;
+  if (sh < 0) {
+    l = m >> (-sh);
+    h = 0ull;
+  } else if (sh < 64) {
+    l = m << sh;
+    h = sh == 0 ? 0ull : m >> (64 - sh);
+  } else {
+    l = 0ull;
+    h = m << (sh - 64);
+  }
+  if (b >> 31) {
+    l = ~l + 1ull;
+    h = ~h + (l == 0ull ? 1ull : 0ull);
+  }
+  const unsigned long long old = atomicAdd(lo, l);
+  atomicAdd(hi, h + (old + l < old ? 1ull : 0ull));
+}
+
+__device__ __forceinline__ void box_of_supertile(const float4 *__restrict__ boxes, int nbox, int T, float4 &lo,
+                                                 float4 &hi) {
+  lo = boxes[4 * T];
+  hi = boxes[4 * T + 1];
+  if (2 * T + 1 < nbox) {
+    const float4 l2 = boxes[4 * T + 2], h2 = boxes[4 * T + 3];
+    lo.x = fminf(lo.x, l2.x), lo.y = fminf(lo.y, l2.y), lo.z = fminf(lo.z, l2.z);
+    hi.x = fmaxf(hi.x, h2.x), hi.y = fmaxf(hi.y, h2.y), hi.z = fmaxf(hi.z, h2.z);
+  }
+}
+
+// one slot: the warp's 64 targets against the 256 staged sources.  The far
+// loop is unrolled by 8 and the near one not at all: fully unrolled, the two
+// loops overflowed the instruction cache (ncu: issue stalled on instruction
+// fetch, 44 % issue activity).
+template <bool NEAR, bool AMOEBA, int G>
+__device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, int lane, const float4 (&pt)[2],
+                                         const float (&at)[2], const float (&mt)[2][3 * G],
+                                         const float (&mt3)[2][3 * G], const int (&pl)[2], float thr,
+                                         float (&af)[2][3 * G], float (&ak)[2][3 * G]) {
+  constexpr int C = 3 * G;
+  const int src = (lane + 1) & 31;
+  const bool source_side = !NEAR || !diag;
+#pragma unroll 1
+  for (int js = 0; js < S32_NSUB; ++js) {
+    float aj[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) aj[c] = 0.f;
+    const float4 *pb = &sm.pos[js][lane];
+    const float4 *mb[G];
+#pragma unroll
+    for (int col = 0; col < G; ++col) mb[col] = &sm.mu[col][js][lane];
+    auto step = [&](int t) {
+      const float4 ps = pb[t];
+      float4 m[G];
+#pragma unroll
+      for (int col = 0; col < G; ++col) m[col] = mb[col][t];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const float dx = pt[u].x - ps.x, dy = pt[u].y - ps.y, dz = pt[u].z - ps.z;
+        float k3, k5;
+        if (NEAR) {
+          // the self pair of the diagonal slot contributes nothing
+          const bool self = diag && (js * S32_SUB + ((lane + t) & 31)) == pl[u];
+          const float r2 = self ? 1.f : fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          damped_factors<AMOEBA>(r2, pt[u].w, ps.w, at[u], m[0].w, thr, k3, k5);
+          if (self) k3 = k5 = 0.f;
+        } else {
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          const float rinv = rsqrtf(r2);
+          const float ir2 = rinv * rinv;
+          k3 = rinv * ir2;
+          k5 = k3 * ir2;
+        }
+#pragma unroll
+        for (int col = 0; col < G; ++col) {
+          const float f = k5 * fmaf(m[col].x, dx, fmaf(m[col].y, dy, m[col].z * dz));
+          af[u][3 * col + 0] = fmaf(f, dx, af[u][3 * col + 0]);
+          af[u][3 * col + 1] = fmaf(f, dy, af[u][3 * col + 1]);
+          af[u][3 * col + 2] = fmaf(f, dz, af[u][3 * col + 2]);
+          ak[u][3 * col + 0] = fmaf(k3, m[col].x, ak[u][3 * col + 0]);
+          ak[u][3 * col + 1] = fmaf(k3, m[col].y, ak[u][3 * col + 1]);
+          ak[u][3 * col + 2] = fmaf(k3, m[col].z, ak[u][3 * col + 2]);
+          if (source_side) {
+            const float g = k5 * fmaf(mt[u][3 * col], dx, fmaf(mt[u][3 * col + 1], dy, mt[u][3 * col + 2] * dz));
+            aj[3 * col + 0] = fmaf(g, dx, fmaf(-k3, mt3[u][3 * col + 0], aj[3 * col + 0]));
+            aj[3 * col + 1] = fmaf(g, dy, fmaf(-k3, mt3[u][3 * col + 1], aj[3 * col + 1]));
+            aj[3 * col + 2] = fmaf(g, dz, fmaf(-k3, mt3[u][3 * col + 2], aj[3 * col + 2]));
+          }
+        }
+      }
+      if (source_side) {
+        // the sums of source s move to the lane that meets s next
+#pragma unroll
+        for (int c = 0; c < C; ++c) aj[c] = __shfl_sync(0xffffffffu, aj[c], src);
+      }
+    };
+    if (NEAR) {
+#pragma unroll 1
+      for (int t = 0; t < S32_SUB; ++t) step(t);
+    } else {
+#pragma unroll 8  // far steps
+      for (int t = 0; t < S32_SUB; ++t) step(t);
+    }
+    if (source_side) {
+      // after 32 steps lane l holds the sums of source js*32 + l
+#pragma unroll
+      for (int c = 0; c < C; ++c) sm.accj[warp][c][js * S32_SUB + lane] = aj[c];
+    }
+  }
+}
+
+template <int G, bool AMOEBA>
+__global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, int ntile, int nbox, int K, int chunk, int nchunk,
+                                                        int nitems, unsigned *__restrict__ next,
+                                                        const float4 *__restrict__ pos,
+                                                        const float *__restrict__ damp,
+                                                        const float4 *__restrict__ boxes,
+                                                        const float *__restrict__ x,
+                                                        unsigned long long *__restrict__ acc_lo,
+                                                        unsigned long long *__restrict__ acc_hi,
+                                                        unsigned long long *__restrict__ bad, float thr,
+                                                        float r2max) {
+  constexpr int C = 3 * G;
+  extern __shared__ float4 s32_dyn[];
+  S32Smem<G> &sm = *reinterpret_cast<S32Smem<G> *>(s32_dyn);
+  __shared__ int s_item;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (;;) {
+    __syncthreads();  // every thread has read the previous item and its sums
+    if (tid == 0) s_item = (int)atomicAdd(next, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= nitems) break;
+    const int I = item / nchunk;
+    float4 pt[2];
+    float at[2], mt[2][C], mt3[2][C];
+    int pl[2];
+    bool vt[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      pl[u] = warp * 64 + u * 32 + lane;
+      const int ti = I * S32_TILE + pl[u];
+      vt[u] = ti < n;
+      pt[u] = vt[u] ? pos[ti] : make_float4(S32_FAR, S32_FAR, S32_FAR, 0.f);
+      at[u] = (AMOEBA && vt[u]) ? damp[ti] : 0.f;
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        mt[u][c] = vt[u] ? x[((size_t)(c / 3) * n + ti) * 3 + (c % 3)] : 0.f;
+        mt3[u][c] = mt[u][c] * (1.f / 3.f);
+      }
+    }
+    float4 ilo, ihi;
+    box_of_supertile(boxes, nbox, I, ilo, ihi);
+    float sum[2][C], cmp[2][C];
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int c = 0; c < C; ++c) sum[u][c] = cmp[u][c] = 0.f;
+    const int k0 = (item - I * nchunk) * chunk;
+    const int k1 = min(K + 1, k0 + chunk);
+    for (int k = k0; k < k1; ++k) {
+      int J = I + k;
+      if (J >= ntile) J -= ntile;
+      if (k > 0 && 2 * k == ntile && I >= ntile / 2) continue;  // the other tile of the pair owns it
+      const bool diag = (k == 0);
+      __syncthreads();  // the previous slot's staging and sums are read
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = h * S32_TPB + tid;
+        const int sj = J * S32_TILE + q;
+        const bool v = sj < n;
+        const float4 p = v ? pos[sj] : make_float4(-S32_FAR, -S32_FAR, -S32_FAR, 0.f);
+        const int sb = q >> 5, e = q & 31;
+        sm.pos[sb][e] = p;
+        sm.pos[sb][e + S32_SUB] = p;
+        const float a = (AMOEBA && v) ? damp[sj] : 0.f;
+#pragma unroll
+        for (int col = 0; col < G; ++col) {
+          float4 m = make_float4(0.f, 0.f, 0.f, a);
+          if (v) {
+            const float *xs = x + ((size_t)col * n + sj) * 3;
+            m.x = xs[0], m.y = xs[1], m.z = xs[2];
+          }
+          sm.mu[col][sb][e] = m;
+          sm.mu[col][sb][e + S32_SUB] = m;
+        }
+      }
+      __syncthreads();
+      bool far = false;
+      if (!diag) {
+        float4 jlo, jhi;
+        box_of_supertile(boxes, nbox, J, jlo, jhi);
+        const float gx = fmaxf(0.f, fmaxf(jlo.x - ihi.x, ilo.x - jhi.x));
+        const float gy = fmaxf(0.f, fmaxf(jlo.y - ihi.y, ilo.y - jhi.y));
+        const float gz = fmaxf(0.f, fmaxf(jlo.z - ihi.z, ilo.z - jhi.z));
+        far = gx * gx + gy * gy + gz * gz > r2max;
+      }
+      float af[2][C], ak[2][C];
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int c = 0; c < C; ++c) af[u][c] = ak[u][c] = 0.f;
+      if (far)
+        s32_slot<false, AMOEBA, G>(false, sm, warp, lane, pt, at, mt, mt3, pl, thr, af, ak);
+      else
+        s32_slot<true, AMOEBA, G>(diag, sm, warp, lane, pt, at, mt, mt3, pl, thr, af, ak);
+      // the slot's target sums, compensated across slots
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          const float y = fmaf(3.f, af[u][c], -ak[u][c]) - cmp[u][c];
+          const float s = sum[u][c] + y;
+          cmp[u][c] = (s - sum[u][c]) - y;
+          sum[u][c] = s;
+        }
+      if (!diag) {
+        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int q = h * S32_TPB + tid;
+          const int sj = J * S32_TILE + q;
+          if (sj < n) {
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+              const float v = ((sm.accj[0][c][q] + sm.accj[1][c][q]) + sm.accj[2][c][q]) + sm.accj[3][c][q];
+              const size_t o = ((size_t)(c / 3) * n + sj) * 3 + (c % 3);
+              fixed_add_f32(acc_lo + o, acc_hi + o, 3.f * v, bad);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (!vt[u]) continue;
+      const int ti = I * S32_TILE + pl[u];
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        const size_t o = ((size_t)(c / 3) * n + ti) * 3 + (c % 3);
+        fixed_add_f32(acc_lo + o, acc_hi + o, sum[u][c] - cmp[u][c], bad);
+      }
+    }
+  }
+}
+
+// fixed-point sums -> float (NaN when an accumulator overflowed)
+__global__ void k_fixed_to_float(size_t total, const unsigned long long *__restrict__ lo,
+                                 const unsigned long long *__restrict__ hi, const unsigned long long *bad,
+                                 float *__restrict__ out) {
+  const bool nan = *bad != 0ull;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = nan ? __int_as_float(0x7fc00000) : (float)fixed_value(lo[k], hi[k]);
+}
+
+template <int G, bool AMOEBA>
+struct S32Launch {
+  int resident = 0;
+  S32Launch() {
+    const int smem = (int)sizeof(S32Smem<G>);
+    cudaFuncSetAttribute(k_tmu32_sym<G, AMOEBA>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_tmu32_sym<G, AMOEBA>, S32_TPB, smem);
+    if (resident < 1) resident = 1;
+  }
+};
+
+template <int G, bool AMOEBA>
+void launch_s32(const DevSites &s, const float *x, unsigned long long *lo, unsigned long long *hi,
+                unsigned long long *bad, unsigned *next, cudaStream_t st) {
+  static const S32Launch<G, AMOEBA> cfg;  // thread-safe one-time set-up
+  const int ntile = (s.n + S32_TILE - 1) / S32_TILE;
+  const int K = ntile / 2;
+  const int ctas_max = cfg.resident * sm_count();
+  // about 16 work items per resident CTA
+  long long chunk = (long long)ntile * (K + 1) / (16LL * ctas_max);
+  if (chunk < 1) chunk = 1;
+  if (chunk > K + 1) chunk = K + 1;
+  const int nchunk = (int)((K + 1 + chunk - 1) / chunk);
+  const int nitems = ntile * nchunk;
+  const int ctas = ctas_max < nitems ? ctas_max : nitems;
+  k_tmu32_sym<G, AMOEBA><<<ctas, S32_TPB, sizeof(S32Smem<G>), st>>>(
+      s.n, ntile, s.ntile, K, (int)chunk, nchunk, nitems, next, s.pol_pos32, s.pol_a32, s.tile_box32, x, lo, hi,
+      bad, (float)s.damp_thr, s.damp_r2max32);
+}
+
 }  // namespace
+
+int tmu32_sym_resident(int g, bool amoeba) {
+  if (g == 2) return amoeba ? S32Launch<2, true>().resident : S32Launch<2, false>().resident;
+  return amoeba ? S32Launch<1, true>().resident : S32Launch<1, false>().resident;
+}
+
+void launch_tmu32_sym_pairs(const DevSites &s, int g, const float *x, unsigned long long *lo, unsigned long long *hi,
+                            unsigned long long *bad, unsigned *next, float *out, cudaStream_t st) {
+  const size_t C = 3 * (size_t)g;
+  cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
+  cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), st);  // flag and counter
+  if (g == 2) {
+    if (s.amoeba)
+      launch_s32<2, true>(s, x, lo, hi, bad, next, st);
+    else
+      launch_s32<2, false>(s, x, lo, hi, bad, next, st);
+  } else {
+    if (s.amoeba)
+      launch_s32<1, true>(s, x, lo, hi, bad, next, st);
+    else
+      launch_s32<1, false>(s, x, lo, hi, bad, next, st);
+  }
+  const size_t total = C * s.n;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 4 * 152 * 4) blocks = 4 * 152 * 4;
+  k_fixed_to_float<<<blocks, 256, 0, st>>>(total, lo, hi, bad, out);
+}
 
 // one column group through the v2 pair kernel (g = 1, 2, 4 or 8)
 void launch_tmu32_pairs(const DevSites &s, int g, const float *x, float *partial, int nsplit, cudaStream_t st) {

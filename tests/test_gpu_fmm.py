@@ -137,3 +137,58 @@ def test_fmm_permanent_field_water(water):
     f_new = g.e_m2d()
     g.set_fmm(False)
     assert rel(f_new, g.e_m2d()) < 3e-3
+
+
+def test_fmm_reference_settings(water, golden_mmp):
+    """ommp_set_fmm_lmax_pol / _lmax / _distance / _min_cell_size: the two
+    orders set the induced-dipole and permanent-field expansions separately;
+    the distance and the minimum cell size bound the leaf side from below."""
+    from openmmpol_gb300 import OMMPError
+    g = OMMPSystem(water)
+    x = np.random.default_rng(3).standard_normal((g.pol_atoms, 3)) * 0.01
+    g.set_fmm(True, 10)
+    g.set_fmm_lmax_pol(8)
+    assert g.fmm_settings()[:2] == (8, 10)
+    ref8 = OMMPSystem(water)
+    ref8.set_fmm(True, 8)
+    assert np.array_equal(g.tmatvec(x, dodiag=False), ref8.tmatvec(x, dodiag=False))
+    ref10 = OMMPSystem(water)
+    ref10.set_fmm(True, 10)
+    e10 = ref10.e_m2d()
+    assert np.array_equal(g.e_m2d(), e10)  # the static order is still 10
+    g.set_fmm_lmax(8)
+    assert g.fmm_settings()[:2] == (8, 8)
+    assert np.array_equal(g.e_m2d(), ref8.e_m2d())
+    # leaf lower bound: distance, and the minimum cell size as a half diagonal
+    g.set_fmm_min_cell_size(15.0)
+    assert abs(g.fmm_settings()[2] - 30.0 / np.sqrt(3.0)) < 1e-12
+    g.set_fmm_distance(20.0)
+    assert g.fmm_settings()[2] == 20.0
+    # larger leaves: more of the sum in the exact near field
+    direct = OMMPSystem(water)
+    yd = direct.tmatvec(x, dodiag=False)
+    err_big = rel(g.tmatvec(x, dodiag=False), yd)
+    err_def = rel(ref8.tmatvec(x, dodiag=False), yd)
+    assert err_big < err_def
+    # leaves wider than a quarter of the box: no tree, the direct sums serve
+    g.set_fmm_distance(1e4)  # far beyond the ~93 bohr box
+    np.testing.assert_allclose(g.tmatvec(x, dodiag=False), yd, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(g.e_m2d(), direct.e_m2d(), rtol=1e-13, atol=0)
+    for bad in (lambda: g.set_fmm_distance(-1.0), lambda: g.set_fmm_lmax(1), lambda: g.set_fmm_lmax_pol(13)):
+        with pytest.raises(OMMPError):
+            bad()
+
+
+def test_fmm_default_off_and_reference_auto_switch(water, golden_mmp):
+    """The direct sums are the default for every size; the process-wide
+    switch mirrors the reference's FMM above 1,000 MM atoms."""
+    from openmmpol_gb300 import set_fmm_auto
+    assert not OMMPSystem(water).use_fmm()  # 12,000 MM atoms
+    set_fmm_auto(True)
+    try:
+        big = OMMPSystem(water)
+        small = OMMPSystem(golden_mmp["1crn_amoeba"])  # 648 MM atoms
+        assert big.use_fmm() and not small.use_fmm()
+    finally:
+        set_fmm_auto(False)
+    assert not OMMPSystem(water).use_fmm()

@@ -257,10 +257,10 @@ def test_w1k_mixed_precision_within_1e7(w1k):
     assert hist[-1] < 1e-10
 
 
-@pytest.mark.parametrize("kernel", ["pairwise", "tiled"])
+@pytest.mark.parametrize("kernel", ["pairwise", "tiled", "symmetric"])
 @pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba"])
 def test_fp32_operator_accuracy(case, kernel, w1k, chains, golden_mmp):
-    """Both FP32 kernels against the FP64 operator: relative 1e-5 overall and
+    """The FP32 kernels against the FP64 operator: relative 1e-5 overall and
     at every site (damped near pairs and scaled pairs included)."""
     p = {"w1k": w1k[0], "chains": chains[0]}.get(case) or golden_mmp[case]
     g = OMMPSystem(p)
@@ -371,7 +371,24 @@ def test_block_preconditioner_saves_inner_iterations(w1k):
     assert counts["block"] < counts["diagonal"]
 
 
-@pytest.mark.parametrize("kernel", ["pairwise", "tiled"])
+@pytest.mark.parametrize("case", ["w1k", "1crn_amoeba", "chains"])
+def test_symmetric_fp32_operator_two_columns_and_determinism(case, w1k, chains, golden_mmp):
+    """The symmetric FP32 kernel (each unordered pair once, fixed-point sums):
+    two columns in one launch equal to the columns one at a time within FP32
+    rounding, both within 1e-5 of FP64, and bitwise repeatable."""
+    p = {"w1k": w1k[0], "chains": chains[0]}.get(case) or golden_mmp[case]
+    g = OMMPSystem(p)
+    g.set_fp32_kernel("symmetric")
+    x = np.random.default_rng(5).standard_normal((2, g.pol_atoms, 3)) * 0.05
+    y2 = g.tmatvec_fp32(x)
+    assert np.array_equal(y2, g.tmatvec_fp32(x))
+    y64 = g.tmatvec(x)
+    assert rel(y2, y64) < 1e-5
+    for c in range(2):
+        assert rel(g.tmatvec_fp32(x[c]), y64[c]) < 1e-5
+
+
+@pytest.mark.parametrize("kernel", ["pairwise", "tiled", "symmetric"])
 def test_mixed_solve_with_each_fp32_kernel(kernel, chains):
     p, ef = chains
     ref = converged_reference(p, ef).ipd

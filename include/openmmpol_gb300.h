@@ -311,6 +311,10 @@ int32_t ommp_gpu_set_inner_blocks(OMMP_SYSTEM_PRT s, int32_t max_sites, double l
 void ommp_gpu_clear_guess(OMMP_SYSTEM_PRT s);
 /* capture the inner FP32 iteration as a CUDA graph (default on) */
 void ommp_gpu_set_use_graphs(OMMP_SYSTEM_PRT s, int32_t on);
+/* FP32 inner solve of batches (mixed modes, at least 4 columns): 1 (default)
+ * block CG, the columns sharing one Krylov space; 0 the scalar PCG per
+ * column */
+void ommp_gpu_set_block_cg(OMMP_SYSTEM_PRT s, int32_t on);
 
 /* Batched right-hand sides: nfields external fields (e.g. from several QM
  * densities) solved together, each as ommp_set_external_field would solve it
@@ -374,10 +378,27 @@ int32_t ommp_gpu_measure_pipe_peak(int32_t fp64, double *tflops);
 /* SM count of the current device, 0 without a GPU */
 int32_t ommp_gpu_device_sm_count(void);
 
+/* No counterpart in the reference.  The solves of nsys systems (mixed or
+ * mixed-ds precision, direct products), each with its own external field
+ * fields[k] [pol_atoms][3] (host memory), advanced together on one stream:
+ * every round, the pair products of all systems that need one share one
+ * persistent launch per product kind and column width (work items: system,
+ * super-tile, chunk of slots), each product getting a bounded share per round
+ * (a fair share first, then the shortest), so that small systems keep
+ * iterating while a large product is spread over several rounds.  Results and
+ * state as after ommp_gpu_set_external_field on each system; energies [nsys]
+ * the polarization energies.  stats5 (may be NULL): rounds, product
+ * launches, launches that served two or more systems, most systems in one
+ * launch, products spread over several launches. */
+int32_t ommp_gpu_solve_multi(int32_t nsys, OMMP_SYSTEM_PRT *systems, const double *const *fields, double *energies,
+                             int64_t *stats5);
+
 /* ---- request server (no counterpart in the reference) -------------------
- * Continuous admission of solves on one GPU: `slots` worker threads each run
- * one request at a time on its system's own CUDA stream (solves of different
- * systems overlap on the device); a request starts as soon as a slot is free
+ * Continuous admission of solves on one GPU: `slots` worker threads each carry
+ * one request at a time (host setup, upload and E_M2D on its system's own
+ * CUDA stream; in the mixed modes the solve then joins the multi-system
+ * engine of ommp_gpu_solve_multi, in FP64 it runs on the system's stream);
+ * a request starts as soon as a slot is free
  * and its device memory fits `hbm_budget_bytes`, idle systems being evicted
  * least-recently-used first.  ommp_gpu_server_submit reads a new system from
  * a .mmp file (host setup, upload, E_M2D, solve); _submit_followup solves a
@@ -403,6 +424,10 @@ int32_t ommp_gpu_server_wait(void *server, int64_t request_id, double *ipd_out, 
 void ommp_gpu_server_release(void *server, int64_t instance);
 int32_t ommp_gpu_server_cancel(void *server, int64_t request_id);
 void ommp_gpu_server_stats(void *server, double *out7);
+/* the multi-system engine of the mixed modes: rounds, product launches,
+ * launches that served two or more systems, most systems in one launch,
+ * products spread over several rounds (zeros in FP64) */
+void ommp_gpu_server_engine_stats(void *server, int64_t *out5);
 
 /* No counterpart in the reference.  y = T x (dodiag = 1) or y = -E_dd(x)
  * (dodiag = 0) for nrhs (1|2) columns [nrhs][pol_atoms][3], with x and y in

@@ -52,6 +52,25 @@ def set_fmm_auto(on: bool) -> None:
     _lib.load().ommp_gpu_set_fmm_auto(int(bool(on)))
 
 
+def solve_multi(systems, fields):
+    """Solve several systems (mixed or mixed-ds precision), each for its own
+    external field [pol_atoms][3], together: their pair products share
+    multi-system launches (ommp_gpu_solve_multi).  Returns the energies and a
+    dict of engine statistics; the dipoles are on each system as after
+    set_external_field."""
+    L = _lib.load()
+    n = len(systems)
+    fs = [np.ascontiguousarray(f, dtype=np.float64).reshape(s.pol_atoms, 3) for s, f in zip(systems, fields)]
+    hs = (C.c_void_p * n)(*[s._h for s in systems])
+    fp = (_lib._dp * n)(*[f.ctypes.data_as(_lib._dp) for f in fs])
+    en = np.zeros(n)
+    st = np.zeros(5, dtype=np.int64)
+    _check(L.ommp_gpu_solve_multi(n, hs, fp, en.ctypes.data_as(_lib._dp),
+                                  st.ctypes.data_as(C.POINTER(C.c_int64))))
+    keys = ("rounds", "launches", "shared_launches", "max_systems_per_launch", "spread_products")
+    return en, dict(zip(keys, (int(v) for v in st)))
+
+
 def kernel_launch_count() -> int:
     """Kernels the library has launched in this process (CUDA graph launches
     count their kernels)."""
@@ -161,6 +180,11 @@ class OMMPSystem:
 
     def set_use_graphs(self, on: bool = True) -> None:
         self._L.ommp_gpu_set_use_graphs(self._h, int(on))
+
+    def set_block_cg(self, on: bool = True) -> None:
+        """Batches of at least 4 columns in the mixed modes: block CG for the
+        FP32 inner solve (default) or the scalar PCG per column."""
+        self._L.ommp_gpu_set_block_cg(self._h, int(on))
 
     def get_polelec_energy(self) -> float:
         e = C.c_double(0.0)
@@ -526,6 +550,13 @@ class Server:
     def cancel(self, rid: int) -> bool:
         """True when the request was still queued and is now cancelled."""
         return self._L.ommp_gpu_server_cancel(self._h, int(rid)) == 0
+
+    def engine_stats(self) -> dict:
+        """The multi-system engine of the mixed modes (zeros in FP64)."""
+        o = np.zeros(5, dtype=np.int64)
+        self._L.ommp_gpu_server_engine_stats(self._h, o.ctypes.data_as(C.POINTER(C.c_int64)))
+        keys = ("rounds", "launches", "shared_launches", "max_systems_per_launch", "spread_products")
+        return dict(zip(keys, (int(v) for v in o)))
 
     def stats(self) -> dict:
         o = np.zeros(7)

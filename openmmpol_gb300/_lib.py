@@ -112,6 +112,7 @@ SIGNATURES = {
     "ommp_qm_helper_get_nmm": (C.c_int32, [_vp]),
     "ommp_qm_helper_get_qm_atoms": (C.c_int32, [_vp]),
     "ommp_gpu_set_use_graphs": (None, [_vp, C.c_int32]),
+    "ommp_gpu_set_block_cg": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_external_fields_batch": (C.c_int32, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ommp_gpu_set_external_fields_batch_device": (C.c_int32, [_vp, C.c_int32, _vp, _vp, _dp]),
     "ommp_gpu_clear_guess": (None, [_vp]),
@@ -139,6 +140,7 @@ SIGNATURES = {
     "ommp_gpu_measure_pipe_peak": (C.c_int32, [C.c_int32, _dp]),
     "ommp_gpu_device_sm_count": (C.c_int32, []),
     "ommp_gpu_tmatvec_noalloc": (C.c_int32, [_vp, _vp, _vp, C.c_int32, C.c_int32]),
+    "ommp_gpu_solve_multi": (C.c_int32, [C.c_int32, C.POINTER(_vp), C.POINTER(_dp), _dp, _i64p]),
     "ommp_gpu_server_create": (C.c_int32, [C.c_int64, C.c_int32, C.c_int32, C.c_double, C.POINTER(_vp)]),
     "ommp_gpu_server_destroy": (None, [_vp]),
     "ommp_gpu_server_submit": (C.c_int32, [_vp, C.c_char_p, _dp, C.c_int32, _i64p]),
@@ -147,6 +149,7 @@ SIGNATURES = {
     "ommp_gpu_server_release": (None, [_vp, C.c_int64]),
     "ommp_gpu_server_cancel": (C.c_int32, [_vp, C.c_int64]),
     "ommp_gpu_server_stats": (None, [_vp, _dp]),
+    "ommp_gpu_server_engine_stats": (None, [_vp, _i64p]),
 }
 
 _lib = None

@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "libommp_gb300.so")
 
 CU_SOURCES = ["kernels.cu", "engine.cu", "solvers.cu", "noalloc.cu", "tmu32.cu", "ds_kernels.cu", "external.cu", "grad.cu",
               "grad_ds.cu", "qm_helper.cu", "fmm.cu",
-              "fixedelec.cu"]
+              "fixedelec.cu", "block_cg.cu", "multisolve.cu"]
 # per-file nvcc flags: the FP32 operators flush subnormals (plain MUFU rsqrt);
 # the double-single kernel fuses nothing implicitly (its FMAs are explicit)
 CU_EXTRA = {"tmu32.cu": ["-ftz=true"], "ds_kernels.cu": ["-ftz=true", "--fmad=false"],

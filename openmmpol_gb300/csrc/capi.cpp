@@ -254,6 +254,7 @@ int32_t ommp_gpu_set_inner_blocks(OMMP_SYSTEM_PRT s, int32_t max_sites, double l
   return S(s)->set_inner_blocks(max_sites, link_bohr);
 }
 void ommp_gpu_set_use_graphs(OMMP_SYSTEM_PRT s, int32_t on) { S(s)->set_use_graphs(on != 0); }
+void ommp_gpu_set_block_cg(OMMP_SYSTEM_PRT s, int32_t on) { S(s)->set_block_cg(on != 0); }
 int32_t ommp_gpu_set_external_fields_batch(OMMP_SYSTEM_PRT s, int32_t nfields, const double *fields, double *ipd_out,
                                            double *energies) {
   return S(s)->solve_batch_host(nfields, fields, ipd_out, energies);

@@ -319,18 +319,32 @@ __device__ __forceinline__ void ds_sym_slot(bool diag, bool vi, int ti, int gbas
   }
 }
 
+// A launch serves the products of several systems (same column count and
+// damping kind): job j covers the items [item0, item0 + base[j+1] - base[j])
+// of its system's product (item space fixed per system), so a product may
+// also be spread over several launches.  A one-job table is the
+// single-system product.
+struct DsSymJob {
+  const float4 *ph, *pl;
+  const Pos64 *p64;
+  const double *damp;
+  const float2 *wa;
+  const float4 *boxes;
+  const double *x;
+  unsigned long long *lo, *hi, *bad;
+  int n, ntile, K, chunk, nchunk, item0;
+  double thr;
+  float thr2m, r2max;
+};
+struct DsSymTable {
+  int njobs;
+  int base[kMaxSymSlices + 1];
+  DsSymJob job[kMaxSymSlices];
+};
+
 template <bool AMOEBA, int G>
-__global__ void __launch_bounds__(DS_TPB) k_tmu_ds_sym(int n, int ntile, int K, int chunk, int nchunk, int nitems,
-                                                       unsigned *__restrict__ next, const float4 *__restrict__ ph,
-                                                       const float4 *__restrict__ pl, const Pos64 *__restrict__ p64,
-                                                       const double *__restrict__ damp,
-                                                       const float2 *__restrict__ wa,
-                                                       const float4 *__restrict__ boxes,
-                                                       const double *__restrict__ x,
-                                                       unsigned long long *__restrict__ acc_lo,
-                                                       unsigned long long *__restrict__ acc_hi,
-                                                       unsigned long long *__restrict__ bad, double thr, float thr2m,
-                                                       float r2max) {
+__global__ void __launch_bounds__(DS_TPB) k_tmu_ds_sym(const __grid_constant__ DsSymTable tab,
+                                                       unsigned *__restrict__ next) {
   constexpr int C = 3 * G;
   __shared__ float4 s_ph[DS_TILE], s_pl[DS_TILE], s_mh[G][DS_TILE], s_ml[G][DS_TILE];
   __shared__ double s_w[DS_TILE], s_a[DS_TILE];
@@ -338,13 +352,29 @@ __global__ void __launch_bounds__(DS_TPB) k_tmu_ds_sym(int n, int ntile, int K, 
   __shared__ double s_accj[4][C][DS_TILE];
   __shared__ int s_item;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int total = tab.base[tab.njobs];
   for (;;) {
     __syncthreads();  // every thread has read the previous item
     if (tid == 0) s_item = (int)atomicAdd(next, 1u);
     __syncthreads();
     const int item = s_item;
-    if (item >= nitems) break;
-    const int I = item / nchunk;
+    if (item >= total) break;
+    int jx = 0;
+    while (jx + 1 < tab.njobs && tab.base[jx + 1] <= item) ++jx;
+    const DsSymJob &jb = tab.job[jx];
+    const int n = jb.n, ntile = jb.ntile, K = jb.K, chunk = jb.chunk, nchunk = jb.nchunk;
+    const float4 *__restrict__ ph = jb.ph;
+    const float4 *__restrict__ pl = jb.pl;
+    const Pos64 *__restrict__ p64 = jb.p64;
+    const double *__restrict__ damp = jb.damp;
+    const float2 *__restrict__ wa = jb.wa;
+    const float4 *__restrict__ boxes = jb.boxes;
+    const double *__restrict__ x = jb.x;
+    unsigned long long *acc_lo = jb.lo, *acc_hi = jb.hi, *bad = jb.bad;
+    const double thr = jb.thr;
+    const float thr2m = jb.thr2m, r2max = jb.r2max;
+    const int local = jb.item0 + (item - tab.base[jx]);
+    const int I = local / nchunk;
     const int ti = I * DS_TILE + tid;
     const bool vi = ti < n;
     const float4 th = vi ? ph[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -370,7 +400,7 @@ __global__ void __launch_bounds__(DS_TPB) k_tmu_ds_sym(int n, int ntile, int K, 
     double sumi[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) sumi[c] = 0.0;
-    const int k0 = (item - I * nchunk) * chunk;
+    const int k0 = (local - I * nchunk) * chunk;
     const int k1 = min(K + 1, k0 + chunk);
     for (int k = k0; k < k1; ++k) {
       int J = I + k;
@@ -700,49 +730,84 @@ void launch_tmu_ds_pairs(const DevSites &s, int g, const double *x, double *part
 namespace {
 template <bool AMOEBA, int G>
 int ds_sym_resident() {
-  static int r = 0;
-  if (!r) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tmu_ds_sym<AMOEBA, G>, DS_TPB, 0);
-    if (r < 1) r = 1;
-  }
+  static const int r = [] {
+    int v = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_tmu_ds_sym<AMOEBA, G>, DS_TPB, 0);
+    return v < 1 ? 1 : v;
+  }();
   return r;
 }
 
+int ds_sym_res(int g, bool amoeba) {
+  if (g == 2) return amoeba ? ds_sym_resident<true, 2>() : ds_sym_resident<false, 2>();
+  return amoeba ? ds_sym_resident<true, 1>() : ds_sym_resident<false, 1>();
+}
+
+// the item space of one system's product: about 16 items per resident CTA
+void ds_sym_schedule(int n, int g, bool amoeba, int &ntile, int &K, int &chunk, int &nchunk) {
+  ntile = (n + DS_TILE - 1) / DS_TILE;
+  K = ntile / 2;
+  const int ctas_max = ds_sym_res(g, amoeba) * sm_count();
+  long long c = (long long)ntile * (K + 1) / (16LL * ctas_max);
+  if (c < 1) c = 1;
+  if (c > K + 1) c = K + 1;
+  chunk = (int)c;
+  nchunk = (K + 1 + chunk - 1) / chunk;
+}
+
 template <bool AMOEBA, int G>
-void launch_ds_sym_shape(const DevSites &s, const double *x, unsigned long long *lo, unsigned long long *hi,
-                         unsigned long long *bad, unsigned *next, cudaStream_t st) {
-  const int ntile = (s.n + DS_TILE - 1) / DS_TILE;
-  const int K = ntile / 2;
+void launch_ds_sym_table(const DsSymTable &tab, unsigned *next, cudaStream_t st) {
+  const int total = tab.base[tab.njobs];
+  if (total <= 0) return;
   const int ctas_max = ds_sym_resident<AMOEBA, G>() * sm_count();
-  // about 16 work items per resident CTA
-  long long chunk = (long long)ntile * (K + 1) / (16LL * ctas_max);
-  if (chunk < 1) chunk = 1;
-  if (chunk > K + 1) chunk = K + 1;
-  const int nchunk = (int)((K + 1 + chunk - 1) / chunk);
-  const int nitems = ntile * nchunk;
-  const int ctas = ctas_max < nitems ? ctas_max : nitems;
-  const float thr2m = (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));
-  k_tmu_ds_sym<AMOEBA, G><<<ctas, DS_TPB, 0, st>>>(s.n, ntile, K, (int)chunk, nchunk, nitems, next, s.pol_pos32,
-                                                   s.pol_pos32lo, s.pol_pos, s.pol_a, s.pol_wa32, s.tile_box32, x,
-                                                   lo, hi, bad, s.damp_thr, thr2m, s.damp_r2max32);
+  const int ctas = ctas_max < total ? ctas_max : total;
+  cudaMemsetAsync(next, 0, sizeof(unsigned), st);
+  k_tmu_ds_sym<AMOEBA, G><<<ctas, DS_TPB, 0, st>>>(tab, next);
 }
 }  // namespace
+
+int tmu_ds_sym_items(const DevSites &s, int g) {
+  if (s.n == 0) return 0;
+  int ntile, K, chunk, nchunk;
+  ds_sym_schedule(s.n, g, s.amoeba, ntile, K, chunk, nchunk);
+  return ntile * nchunk;
+}
+
+void launch_tmu_ds_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st) {
+  DsSymTable tab{};
+  int total = 0;
+  for (int k = 0; k < nsl && tab.njobs < kMaxSymSlices; ++k) {
+    const DevSites &s = *sl[k].s;
+    if (sl[k].count <= 0 || s.n == 0) continue;
+    DsSymJob &j = tab.job[tab.njobs];
+    j.ph = s.pol_pos32, j.pl = s.pol_pos32lo, j.p64 = s.pol_pos, j.damp = s.pol_a, j.wa = s.pol_wa32;
+    j.boxes = s.tile_box32, j.x = static_cast<const double *>(sl[k].x);
+    j.lo = sl[k].lo, j.hi = sl[k].hi, j.bad = sl[k].bad;
+    j.n = s.n;
+    ds_sym_schedule(s.n, g, amoeba, j.ntile, j.K, j.chunk, j.nchunk);
+    j.item0 = sl[k].item0;
+    j.thr = s.damp_thr;
+    j.thr2m = (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));
+    j.r2max = s.damp_r2max32;
+    tab.base[tab.njobs] = total;
+    total += sl[k].count;
+    ++tab.njobs;
+  }
+  tab.base[tab.njobs] = total;
+  if (!total) return;
+  add_launch_count(1);
+  if (g == 2)
+    amoeba ? launch_ds_sym_table<true, 2>(tab, next, st) : launch_ds_sym_table<false, 2>(tab, next, st);
+  else
+    amoeba ? launch_ds_sym_table<true, 1>(tab, next, st) : launch_ds_sym_table<false, 1>(tab, next, st);
+}
 
 // symmetric double-single pair sums of g (1 or 2) columns into the
 // fixed-point accumulators lo / hi [g][n][3] (zeroed by the caller)
 void launch_tmu_ds_sym_pairs(const DevSites &s, int g, const double *x, unsigned long long *lo,
                              unsigned long long *hi, unsigned long long *bad, unsigned *next, cudaStream_t st) {
-  if (g == 2) {
-    if (s.amoeba)
-      launch_ds_sym_shape<true, 2>(s, x, lo, hi, bad, next, st);
-    else
-      launch_ds_sym_shape<false, 2>(s, x, lo, hi, bad, next, st);
-  } else {
-    if (s.amoeba)
-      launch_ds_sym_shape<true, 1>(s, x, lo, hi, bad, next, st);
-    else
-      launch_ds_sym_shape<false, 1>(s, x, lo, hi, bad, next, st);
-  }
+  SymSlice one{&s, x, lo, hi, bad, 0, tmu_ds_sym_items(s, g)};
+  launch_tmu_ds_sym_multi(g, s.amoeba, &one, 1, next, st);
 }
 
 }  // namespace gpu

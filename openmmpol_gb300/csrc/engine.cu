@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 
 #include "engine.h"
 #include "log.h"
@@ -43,6 +44,45 @@ int System::check(cudaError_t e, const char *what) {
   return kErrCuda;
 }
 
+template <typename T>
+int System::alloc(T *&p, size_t count) {
+  p = nullptr;
+  if (count == 0) count = 1;
+  if (async_alloc_ && st_) {
+    static std::once_flag pool_once;
+    std::call_once(pool_once, [] {
+      // keep freed memory in the pool: returning it to the driver would
+      // synchronise
+      int dev = 0;
+      cudaMemPool_t pool;
+      if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long thr = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      }
+      cudaGetLastError();
+    });
+    if (cudaMallocAsync((void **)&p, count * sizeof(T), st_) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return 1;
+    }
+    async_bufs_.push_back((void *)p);
+    return 0;
+  }
+  return cudaMalloc((void **)&p, count * sizeof(T)) == cudaSuccess ? 0 : 1;
+}
+
+void System::release(void *p) {
+  if (!p) return;
+  auto it = std::find(async_bufs_.begin(), async_bufs_.end(), p);
+  if (it != async_bufs_.end()) {
+    cudaFreeAsync(p, st_);
+    async_bufs_.erase(it);
+  } else {
+    cudaFree(p);
+  }
+}
+
 System::~System() {
   if (st_) cudaStreamSynchronize(st_);
   free_ws(ws_);
@@ -54,10 +94,9 @@ System::~System() {
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
                   alpha32_, scratch_, scratch32_, partial_, dots_, hist_, cols_, flag_, tmat_, piv_,
                   info_, diis_x_, diis_e_, d_.tile_box32, ext_buf_, blk_info_, blk_minv_};
-  for (void *b : bufs)
-    if (b) cudaFree(b);
+  for (void *b : bufs) release(b);
   if (flush_buf_) cudaFree(flush_buf_);
-  if (sym_scratch_) cudaFree(sym_scratch_);
+  release(sym_scratch_);
   free_grad_state(grad_);
   free_fmm_state(fmm_);
   free_fmm_state(fmms_);
@@ -72,6 +111,7 @@ System::~System() {
   if (scal_h_) cudaFreeHost(scal_h_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
+  if (st_) cudaStreamSynchronize(st_);  // stream-ordered frees
   if (st_) cudaStreamDestroy(st_);
 }
 
@@ -120,7 +160,7 @@ size_t System::device_bytes_estimate() const {
   size_t s32 = gpu::tmu_scratch_doubles(d, 2, gpu::tmu32_max_split(d, sms)) + 8 * ((n + 127) / 128);
   size_t s64 = std::max(gpu::m2d_scratch_doubles(d, gpu::m2d_pick_split(d, sms)),
                         gpu::tmu_scratch_doubles(d, 2, gpu::tmu_pick_split(d, 2, sms, false)));
-  size_t sym = n >= 2048 ? gpu::tmu_sym_scratch_doubles(d, 2) : 0;
+  size_t sym = n >= 2048 ? gpu::tmu_sym_scratch_doubles(d, 4) : 0;
   size_t bytes = 8 * (6 * n + 5 * m + m * m_.ld_cart + 2 * nm2d + nd2d + nv * (2 * nipd + 3 + 10)) +
                  4 * (9 * n + 2 * m + 10 * nv + 2 * (n + 1) + nm2d + nd2d) + 4 * s32 + 8 * s64 + 8 * sym +
                  8 * (gpu::kRedBlocks * 32 + 64 + 2 * (size_t)maxhist_);
@@ -151,25 +191,25 @@ int System::upload_static() {
   size_t nv = 3 * (size_t)n;
   int nipd = m.n_ipd;
   int bad = 0;
-  bad |= dalloc(d_.pol_pos, n) | dalloc(d_.pol_a, n) | dalloc(d_.pol_alpha, n) | dalloc(d_.polar_mm, n);
-  bad |= dalloc(d_.pol_pos32, n) | dalloc(d_.pol_pos32lo, n) | dalloc(d_.pol_a32, n) | dalloc(alpha32_, n);
-  bad |= dalloc(d_.pol_wa32, n) | dalloc(d_.mm_wa32, mm);
-  bad |= dalloc(d_.mm_pos, mm) | dalloc(d_.mm_a, mm) | dalloc(d_.mm_q, (size_t)mm * m.ld_cart);
-  bad |= dalloc(d_.m2d_ri, n + 1) | dalloc(d_.m2d_src, m2d_pairs_.src.size()) |
-         dalloc(d_.m2d_sP, m2d_pairs_.src.size()) | dalloc(d_.m2d_sD, m2d_pairs_.src.size());
-  bad |= dalloc(d_.d2d_ri, n + 1) | dalloc(d_.d2d_src, d2d_pairs_.src.size()) |
-         dalloc(d_.d2d_s, d2d_pairs_.src.size());
-  bad |= dalloc(e_m2d_, nv * nipd) | dalloc(ipd_, nv * nipd) | dalloc(rhs_, nv * 2) | dalloc(ext_, nv);
-  bad |= dalloc(x_, nv * 2) | dalloc(r_, nv * 2) | dalloc(p_, nv * 2) | dalloc(h_, nv * 2) | dalloc(z_, nv * 2);
-  bad |= dalloc(x32_, nv * 2) | dalloc(r32_, nv * 2) | dalloc(p32_, nv * 2) | dalloc(h32_, nv * 2) |
-         dalloc(z32_, nv * 2);
+  bad |= alloc(d_.pol_pos, n) | alloc(d_.pol_a, n) | alloc(d_.pol_alpha, n) | alloc(d_.polar_mm, n);
+  bad |= alloc(d_.pol_pos32, n) | alloc(d_.pol_pos32lo, n) | alloc(d_.pol_a32, n) | alloc(alpha32_, n);
+  bad |= alloc(d_.pol_wa32, n) | alloc(d_.mm_wa32, mm);
+  bad |= alloc(d_.mm_pos, mm) | alloc(d_.mm_a, mm) | alloc(d_.mm_q, (size_t)mm * m.ld_cart);
+  bad |= alloc(d_.m2d_ri, n + 1) | alloc(d_.m2d_src, m2d_pairs_.src.size()) |
+         alloc(d_.m2d_sP, m2d_pairs_.src.size()) | alloc(d_.m2d_sD, m2d_pairs_.src.size());
+  bad |= alloc(d_.d2d_ri, n + 1) | alloc(d_.d2d_src, d2d_pairs_.src.size()) |
+         alloc(d_.d2d_s, d2d_pairs_.src.size());
+  bad |= alloc(e_m2d_, nv * nipd) | alloc(ipd_, nv * nipd) | alloc(rhs_, nv * 2) | alloc(ext_, nv);
+  bad |= alloc(x_, nv * 2) | alloc(r_, nv * 2) | alloc(p_, nv * 2) | alloc(h_, nv * 2) | alloc(z_, nv * 2);
+  bad |= alloc(x32_, nv * 2) | alloc(r32_, nv * 2) | alloc(p32_, nv * 2) | alloc(h32_, nv * 2) |
+         alloc(z32_, nv * 2);
   scratch_n_ = std::max(gpu::m2d_scratch_doubles(d_, nsplit_m2d_), gpu::tmu_scratch_doubles(d_, 2, nsplit_tmu_));
   // FP32 scratch for twice the default source split (the autotuner tries both)
-  bad |= dalloc(scratch_, scratch_n_) | dalloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, f32_splits));
-  bad |= dalloc(d_.tile_box32, 2 * (size_t)d_.ntile);
-  bad |= dalloc(d_.mm_pos32, mm) | dalloc(d_.mm_pos32lo, mm) | dalloc(d_.mm_tile_box32, 2 * (size_t)((mm + 127) / 128));
-  bad |= dalloc(partial_, (size_t)gpu::kRedBlocks * 32) | dalloc(dots_, 64) | dalloc(hist_, 2 * (size_t)maxhist_);
-  bad |= dalloc(cols_, 2) | dalloc(flag_, 1) | dalloc(info_, 1);
+  bad |= alloc(scratch_, scratch_n_) | alloc(scratch32_, gpu::tmu_scratch_doubles(d_, 2, f32_splits));
+  bad |= alloc(d_.tile_box32, 2 * (size_t)d_.ntile);
+  bad |= alloc(d_.mm_pos32, mm) | alloc(d_.mm_pos32lo, mm) | alloc(d_.mm_tile_box32, 2 * (size_t)((mm + 127) / 128));
+  bad |= alloc(partial_, (size_t)gpu::kRedBlocks * 32) | alloc(dots_, 64) | alloc(hist_, 2 * (size_t)maxhist_);
+  bad |= alloc(cols_, 2) | alloc(flag_, 1) | alloc(info_, 1);
   if (bad || cudaMallocHost((void **)&cols_h_, 2 * sizeof(gpu::CgCol)) != cudaSuccess ||
       cudaMallocHost((void **)&scal_h_, 64 * sizeof(double)) != cudaSuccess) {
     set_last_error("out of device memory while allocating the system");
@@ -318,12 +358,12 @@ int System::build_blocks() {
     w->graph = nullptr;
     w->graph_ncol = -1;
   }
-  if (blk_info_) cudaFree(blk_info_);
-  if (blk_minv_) cudaFree(blk_minv_);
+  release(blk_info_);
+  release(blk_minv_);
   blk_info_ = nullptr;
   blk_minv_ = nullptr;
   if (n > 0) {
-    if (dalloc(blk_info_, (size_t)n) || dalloc(blk_minv_, minv.size())) {
+    if (alloc(blk_info_, (size_t)n) || alloc(blk_minv_, minv.size())) {
       set_last_error("out of device memory for the block preconditioner");
       return kErrMemory;
     }
@@ -530,7 +570,7 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
     KEv e;
     if (ktime_on_) e = kt_begin(0, ncol);
     if (sym) {
-      gpu::launch_tmu_f64_sym(d_, ncol, x, y, dodiag, sym_scratch_, st_);
+      gpu::launch_tmu_f64_sym(d_, ncol, x, y, dodiag, sym_scratch_, st_, 4);
     } else {
       // the split partials hold two columns: larger blocks go two at a time
       const size_t nv = 3 * (size_t)d_.n;
@@ -548,7 +588,7 @@ int System::matvec64(int matv, int ncol, const double *x, double *y, bool dodiag
 // and FP32 share them: they run one after another on the system's stream)
 int System::ensure_sym_scratch() {
   if (sym_scratch_) return kOk;
-  if (dalloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 2))) {
+  if (alloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 4))) {
     sym_scratch_ = nullptr;
     cudaGetLastError();
     set_last_error("out of device memory for the symmetric-product accumulators");
@@ -563,7 +603,7 @@ int System::ensure_ds_scratch() {
   if (ds_scratch_) return kOk;
   nsplit_ds_ = gpu::tmu_ds_pick_split(d_, gpu::sm_count());
   nsplit_m2d_ds_ = gpu::m2d_ds_pick_split(d_, gpu::sm_count());
-  if (dalloc(ds_scratch_, (size_t)std::max(2 * nsplit_ds_, nsplit_m2d_ds_) * 3 * d_.n)) {
+  if (alloc(ds_scratch_, (size_t)std::max(2 * nsplit_ds_, nsplit_m2d_ds_) * 3 * d_.n)) {
     ds_scratch_ = nullptr;
     set_last_error("out of device memory for the double-single kernels");
     return kErrMemory;
@@ -577,10 +617,8 @@ int System::matvec_residual(int ncol, const double *x, double *y) {
   if (st) return st;
   // the symmetric double-single kernel shares the FP64 one's fixed-point
   // scratch (without it: the target-outer double-single kernel)
-  if (d_.n >= 2048 && !sym_scratch_ && dalloc(sym_scratch_, gpu::tmu_sym_scratch_doubles(d_, 2))) {
-    sym_scratch_ = nullptr;
+  if (d_.n >= 2048 && ensure_sym_scratch() != kOk)
     log_msg(kVerbHigh, nullptr, "symmetric T.mu scratch does not fit: using the target-outer kernel");
-  }
   KEv e;
   if (ktime_on_) e = kt_begin(2, ncol);
   gpu::launch_tmu_ds(d_, ncol, x, y, true, ds_scratch_, nsplit_ds_, sym_scratch_, st_);

@@ -36,6 +36,13 @@ struct Workspace {
   double *partial = nullptr;  // kRedBlocks x cap
   double *dots = nullptr;     // 3 x cap (+ fcap)
   double *hist = nullptr;     // cap x maxhist, or none
+  // block CG of the batch (block_cg.cu): next directions, Gram partials and
+  // results, coefficients, column maps, pinned host copy of the small matrices
+  float *t32 = nullptr;
+  double *gram = nullptr;
+  float *bcoef = nullptr;
+  int *bidx = nullptr;
+  double *bscal_h = nullptr;
   gpu::CgCol *cols = nullptr;
   gpu::CgCol *cols_h = nullptr;  // pinned
   double *scal_h = nullptr;      // pinned 3 x cap (+ fcap)
@@ -63,7 +70,11 @@ struct SolveStats {
   int ds_matvecs = 0;     // double-single residual products
 };
 
+class MultiSolver;
+
 class System {
+  friend class MultiSolver;
+
  public:
   ~System();
   static System *from_mmp(const std::string &path, std::string &err, int &status);
@@ -72,6 +83,12 @@ class System {
   static System *load_host(const std::string &path, std::string &err, int &status);
   int attach_device();
   size_t device_bytes_estimate() const;
+  // stream-ordered allocation (cudaMallocAsync / cudaFreeAsync on the
+  // system's own stream, from the device's default pool) of the system's
+  // resident buffers, for systems admitted and evicted by the request server
+  // while other systems' kernels run: cudaMalloc and cudaFree synchronise the
+  // device.  Set before attach_device.
+  void set_async_alloc(bool on) { async_alloc_ = on; }
 
   // --- reference API semantics -------------------------------------------------
   int set_external_field(const double *ext_host, int solver, int matv, bool add_mm);
@@ -89,6 +106,9 @@ class System {
   int solve_batch(int nf, const double *fields_dev, double *out_dev, double *energies);
   int solve_batch_host(int nf, const double *fields_host, double *out_host, double *energies);
   void set_use_graphs(bool on) { use_graphs_ = on; }
+  // block CG for the FP32 inner solve of batches of at least 4 columns
+  // (default on); off: independent scalar PCG per column
+  void set_block_cg(bool on) { block_cg_ = on; }
   int tmatvec(const double *x_host, double *y_host, int nrhs, bool dodiag, int matv);
   int tmatvec_f32(const double *x_host, double *y_host, int nrhs);
   int tmatvec_ds(const double *x_host, double *y_host, int nrhs);
@@ -163,6 +183,11 @@ class System {
 
  private:
   System() = default;
+  template <typename T>
+  int alloc(T *&p, size_t count);
+  void release(void *p);
+  bool async_alloc_ = false;
+  std::vector<void *> async_bufs_;
   int upload_static();
   int upload_geometry();
   int ensure_m2d();
@@ -178,6 +203,7 @@ class System {
   // solvers.cu: the same solvers on any workspace
   int cg64_ws(Workspace &w, int matv, int ncol, const double *rhs, double *x, int set0);
   int pcg32_ws(Workspace &w, int ncol, int max_it, double eta);
+  int bpcg32_ws(Workspace &w, int ncol, int max_it, double eta);
   int mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, int set0, bool have_guess);
   struct F32Shape {
     int g, nsplit, kver;  // group width, source splits, kernel version
@@ -285,6 +311,7 @@ class System {
   Workspace wsb_;  // batch buffers
   std::map<int, F32Shape> f32_tune_;  // columns -> tuned FP32 launch shape
   bool use_graphs_ = true;
+  bool block_cg_ = true;
   cudaEvent_t tev_[8] = {};
   void *flush_buf_ = nullptr;
   size_t flush_bytes_ = 0;

@@ -297,31 +297,62 @@ __global__ void k_tmu_finish(int n, int nrhs, int nsplit, const T *__restrict__ 
 // ---------------------------------------------------------------------------
 constexpr int SYM_TILE = 128;
 
+// dynamic shared memory of k_tmu_sym: the staged dipoles s_mu[C][128] and
+// the four warps' source-side sums s_accj[4][C][128] (C = 3 NRHS doubles)
+constexpr size_t sym_smem_bytes(int nrhs) { return (size_t)5 * 3 * nrhs * SYM_TILE * sizeof(double); }
+
+// A launch serves the products of several systems (same column count and
+// damping kind): job j covers the items [item0, item0 + base[j+1] - base[j])
+// of its system's product, whose item space is fixed per system, so that a
+// product may also be spread over several launches (its fixed-point sums add
+// up across them).  A one-job table is the single-system product.
+struct Sym64Job {
+  const Pos64 *pos;
+  const double *damp;
+  const float2 *wa;
+  const double *x;
+  unsigned long long *lo, *hi, *bad;
+  int n, ntile, K, chunk, nchunk, item0;
+  double thr;
+  float thr2m;
+};
+struct Sym64Table {
+  int njobs;
+  int base[kMaxSymSlices + 1];
+  Sym64Job job[kMaxSymSlices];
+};
+
 template <int NRHS, bool AMOEBA>
-__global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, int chunk, int nchunk, int nitems,
-                                                       unsigned *__restrict__ next,
-                                                       const Pos64 *__restrict__ pos,
-                                                       const double *__restrict__ damp,
-                                                       const float2 *__restrict__ wa,
-                                                       const double *__restrict__ x,
-                                                       unsigned long long *__restrict__ acc_lo,
-                                                       unsigned long long *__restrict__ acc_hi,
-                                                       unsigned long long *__restrict__ bad, double thr,
-                                                       float thr2m) {
+__global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(const __grid_constant__ Sym64Table tab,
+                                                       unsigned *__restrict__ next) {
   constexpr int C = 3 * NRHS;
   __shared__ double s_x[SYM_TILE], s_y[SYM_TILE], s_z[SYM_TILE], s_w[SYM_TILE], s_a[SYM_TILE];
   __shared__ float2 s_wa[SYM_TILE];
-  __shared__ double s_mu[C][SYM_TILE];
-  __shared__ double s_accj[4][C][SYM_TILE];
+  extern __shared__ double sym_dyn[];
+  double(*s_mu)[SYM_TILE] = reinterpret_cast<double(*)[SYM_TILE]>(sym_dyn);
+  double(*s_accj)[C][SYM_TILE] = reinterpret_cast<double(*)[C][SYM_TILE]>(sym_dyn + C * SYM_TILE);
   __shared__ int s_item;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int total = tab.base[tab.njobs];
   for (;;) {
     __syncthreads();  // every thread has read the previous item
     if (tid == 0) s_item = (int)atomicAdd(next, 1u);
     __syncthreads();
     const int item = s_item;
-    if (item >= nitems) break;
-    const int I = item / nchunk;
+    if (item >= total) break;
+    int jx = 0;
+    while (jx + 1 < tab.njobs && tab.base[jx + 1] <= item) ++jx;
+    const Sym64Job &jb = tab.job[jx];
+    const int n = jb.n, ntile = jb.ntile, K = jb.K, chunk = jb.chunk, nchunk = jb.nchunk;
+    const Pos64 *__restrict__ pos = jb.pos;
+    const double *__restrict__ damp = jb.damp;
+    const float2 *__restrict__ wa = jb.wa;
+    const double *__restrict__ x = jb.x;
+    unsigned long long *acc_lo = jb.lo, *acc_hi = jb.hi, *bad = jb.bad;
+    const double thr = jb.thr;
+    const float thr2m = jb.thr2m;
+    const int local = jb.item0 + (item - tab.base[jx]);
+    const int I = local / nchunk;
     const int ti = I * SYM_TILE + tid;
     const bool vi = ti < n;
     const Pos64 pi = vi ? pos[ti] : Pos64{0, 0, 0, 0};
@@ -336,7 +367,7 @@ __global__ void __launch_bounds__(SYM_TILE) k_tmu_sym(int n, int ntile, int K, i
       afi[c] = 0.0;
       aki[c] = 0.0;
     }
-    const int k0 = (item - I * nchunk) * chunk;
+    const int k0 = (local - I * nchunk) * chunk;
     const int k1 = min(K + 1, k0 + chunk);
     for (int k = k0; k < k1; ++k) {
       int J = I + k;
@@ -581,27 +612,48 @@ __global__ void k_lu_solve(int nn, const double *A, const int *piv, double *b) {
 // ---------------------------------------------------------------------------
 // BLAS-1 with deterministic two-stage reductions
 // ---------------------------------------------------------------------------
+// Columns run side by side (blockIdx.y = column), not one after another
+// inside a block, and each thread sums about 8 elements of its column with
+// four independent loads in flight: a block-serial column loop with ~2
+// elements per thread left the 64-column dots of a batch latency-bound (1.4
+// TB/s).  gridDim.x blocks of a column write partial[b][k]; the rows from
+// gridDim.x to kRedBlocks are zeroed so that the fixed-order reduction over
+// kRedBlocks rows is unchanged.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_dots(int ncol, size_t n, const T *__restrict__ a,
                                                       const T *__restrict__ b, size_t bstride,
                                                       double *__restrict__ partial) {
   __shared__ double sh[kRedThreads / 32];
-  for (int k = 0; k < ncol; ++k) {
-    const T *ak = a + (size_t)k * n;
-    const T *bk = b + (size_t)k * bstride;
-    double acc = 0.0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-      acc += (double)ak[i] * (double)bk[i];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (int w = 0; w < kRedThreads / 32; ++w) s += sh[w];
-      partial[(size_t)blockIdx.x * ncol + k] = s;
-    }
-    __syncthreads();
+  const int k = blockIdx.y;
+  const T *ak = a + (size_t)k * n;
+  const T *bk = b + (size_t)k * bstride;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] += (double)ak[i + u * stride] * (double)bk[i + u * stride];
   }
+  for (; i < n; i += stride) acc[0] += (double)ak[i] * (double)bk[i];
+  double s0 = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kRedThreads / 32; ++w) s += sh[w];
+    partial[(size_t)blockIdx.x * ncol + k] = s;
+  }
+  if (blockIdx.x == 0)
+    for (int r = gridDim.x + threadIdx.x; r < kRedBlocks; r += blockDim.x) partial[(size_t)r * ncol + k] = 0.0;
+}
+
+// blocks per column of k_dots: about 8 elements per thread
+inline int dots_blocks(size_t n) {
+  size_t b = (n + (size_t)kRedThreads * 8 - 1) / ((size_t)kRedThreads * 8);
+  if (b < 1) b = 1;
+  if (b > (size_t)kRedBlocks) b = kRedBlocks;
+  return (int)b;
 }
 
 __global__ void k_reduce_partials(int ncol, int nb, const double *__restrict__ partial,
@@ -632,6 +684,17 @@ __global__ void k_to_f32(size_t n, const double *x, const double *scale, float *
     y[i] = (float)(x[i] * (scale ? *scale : 1.0));
 }
 
+// start of the inner PCG with the first r.z on the device (no host read)
+__global__ void k_cg_init(int ncol, const double *dots, CgCol *cols, double tol) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ncol) return;
+  CgCol c{};
+  c.gold = dots[k];
+  c.tol = tol;
+  c.active = dots[k] > 0.0 ? 1 : 0;
+  cols[k] = c;
+}
+
 __global__ void k_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ncol) return;
@@ -648,39 +711,38 @@ __global__ void k_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps
   cols[k] = c;
 }
 
+// one column per blockIdx.y (see k_dots)
 template <typename T>
 __global__ void k_cg_update(int ncol, int n, T *x, T *r, const T *p, const T *h, T *z,
                             const T *alpha_pol, const CgCol *cols, double *partial) {
   __shared__ double sh[kRedThreads / 32];
   size_t nv = 3 * (size_t)n;
-  for (int k = 0; k < ncol; ++k) {
-    double acc = 0.0;
-    if (cols[k].active) {
-      double al = cols[k].alpha;
-      T a = (T)al;
-      size_t off = (size_t)k * nv;
-      for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x) {
-        if (sizeof(T) == 8) {
-          x[off + i] += a * p[off + i];
-          r[off + i] -= a * h[off + i];
-        } else {
-          x[off + i] = (T)((double)x[off + i] + al * (double)p[off + i]);
-          r[off + i] = (T)((double)r[off + i] - al * (double)h[off + i]);
-        }
-        T zi = alpha_pol[i / 3] * r[off + i];
-        z[off + i] = zi;
-        acc += (double)r[off + i] * (double)zi;
+  const int k = blockIdx.y;
+  double acc = 0.0;
+  if (cols[k].active) {
+    double al = cols[k].alpha;
+    T a = (T)al;
+    size_t off = (size_t)k * nv;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x) {
+      if (sizeof(T) == 8) {
+        x[off + i] += a * p[off + i];
+        r[off + i] -= a * h[off + i];
+      } else {
+        x[off + i] = (T)((double)x[off + i] + al * (double)p[off + i]);
+        r[off + i] = (T)((double)r[off + i] - al * (double)h[off + i]);
       }
+      T zi = alpha_pol[i / 3] * r[off + i];
+      z[off + i] = zi;
+      acc += (double)r[off + i] * (double)zi;
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (int w = 0; w < kRedThreads / 32; ++w) s += sh[w];
-      partial[(size_t)blockIdx.x * ncol + k] = s;
-    }
-    __syncthreads();
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kRedThreads / 32; ++w) s += sh[w];
+    partial[(size_t)blockIdx.x * ncol + k] = s;
   }
 }
 
@@ -707,13 +769,12 @@ __global__ void k_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, doub
 template <typename T>
 __global__ void k_cg_pupdate(int ncol, int n, T *p, const T *z, const CgCol *cols) {
   size_t nv = 3 * (size_t)n;
-  for (int k = 0; k < ncol; ++k) {
-    if (!cols[k].active) continue;
-    T b = (T)cols[k].beta;
-    size_t off = (size_t)k * nv;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x)
-      p[off + i] = b * p[off + i] + z[off + i];
-  }
+  const int k = blockIdx.y;
+  if (!cols[k].active) return;
+  T b = (T)cols[k].beta;
+  size_t off = (size_t)k * nv;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x)
+    p[off + i] = b * p[off + i] + z[off + i];
 }
 
 __global__ void k_ir_accumulate(int ncol, int n, double *mu, const float *d32, const double *scale) {
@@ -1040,6 +1101,11 @@ void launch_tmu_finish64(const DevSites &s, int nrhs, const double *partial, con
   tmu_finish<double>(s, nrhs, 1, partial, s.pol_pos, s.pol_a, x, dodiag, y, 2, st);
 }
 
+void launch_tmu_finish32(const DevSites &s, int nrhs, const float *partial, const float *x, float *y,
+                         cudaStream_t st) {
+  tmu_finish<float>(s, nrhs, 1, partial, s.pol_pos32, s.pol_a32, x, true, y, 2, st);
+}
+
 void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
                     int nsplit, cudaStream_t st) {
   if (s.n == 0) return;
@@ -1062,11 +1128,10 @@ void launch_tmu_ds(const DevSites &s, int nrhs, const double *x, double *y, bool
       double *e = sym_scratch + 2 * C * s.n;
       unsigned long long *bad = reinterpret_cast<unsigned long long *>(sym_scratch + 3 * C * s.n);
       unsigned *next = reinterpret_cast<unsigned *>(bad + 1);
-      add_launch_count(2);
       cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
-      cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), st);  // flag and counter
+      cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st);
       launch_tmu_ds_sym_pairs(s, g, x + c * nv, lo, hi, bad, next, st);
-      k_fixed_to_double<<<blocks_for(C * s.n, 256), 256, 0, st>>>(C * s.n, lo, hi, bad, e);
+      launch_fixed_to_double(C * s.n, lo, hi, bad, e, st);
       tmu_finish<double>(s, g, 1, e, s.pol_pos, s.pol_a, x + c * nv, dodiag, y + c * nv, 2, st);
     } else {
       add_launch_count(1);
@@ -1082,13 +1147,19 @@ struct SymPlan {
   int ntile, K, chunk, nchunk, nitems, ctas;
 };
 template <int NRHS, bool AMOEBA>
-int sym_resident() {
-  static int r = 0;
-  if (!r) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_tmu_sym<NRHS, AMOEBA>, SYM_TILE, 0);
-    if (r < 1) r = 1;
+struct SymLaunch {
+  int resident = 0;
+  SymLaunch() {
+    const int smem = (int)sym_smem_bytes(NRHS);
+    cudaFuncSetAttribute(k_tmu_sym<NRHS, AMOEBA>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_tmu_sym<NRHS, AMOEBA>, SYM_TILE, smem);
+    if (resident < 1) resident = 1;
   }
-  return r;
+};
+template <int NRHS, bool AMOEBA>
+int sym_resident() {
+  static const SymLaunch<NRHS, AMOEBA> cfg;  // thread-safe one-time set-up
+  return cfg.resident;
 }
 
 // work items: about 16 per resident CTA, each a tile and a chunk of its slots
@@ -1106,25 +1177,80 @@ SymPlan sym_plan(int n, int ctas) {
   p.ctas = ctas < p.nitems ? ctas : p.nitems;
   return p;
 }
+
+int sym64_resident(int g, bool amoeba) {
+  if (g == 4) return amoeba ? sym_resident<4, true>() : sym_resident<4, false>();
+  if (g == 2) return amoeba ? sym_resident<2, true>() : sym_resident<2, false>();
+  return amoeba ? sym_resident<1, true>() : sym_resident<1, false>();
+}
+
+template <int NRHS, bool AMOEBA>
+void launch_sym64_table(const Sym64Table &tab, unsigned *next, cudaStream_t st) {
+  const int total = tab.base[tab.njobs];
+  if (total <= 0) return;
+  const int ctas_max = sym_resident<NRHS, AMOEBA>() * sm_count();
+  const int ctas = ctas_max < total ? ctas_max : total;
+  cudaMemsetAsync(next, 0, sizeof(unsigned), st);
+  k_tmu_sym<NRHS, AMOEBA><<<ctas, SYM_TILE, sym_smem_bytes(NRHS), st>>>(tab, next);
+}
 }  // namespace
+
+int tmu_f64_sym_items(const DevSites &s, int g) {
+  if (s.n == 0) return 0;
+  return sym_plan(s.n, sym64_resident(g, s.amoeba) * sm_count()).nitems;
+}
+
+void launch_tmu_f64_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st) {
+  Sym64Table tab{};
+  int total = 0;
+  for (int k = 0; k < nsl && tab.njobs < kMaxSymSlices; ++k) {
+    const DevSites &s = *sl[k].s;
+    if (sl[k].count <= 0 || s.n == 0) continue;
+    const SymPlan p = sym_plan(s.n, sym64_resident(g, amoeba) * sm_count());
+    Sym64Job &j = tab.job[tab.njobs];
+    j.pos = s.pol_pos, j.damp = s.pol_a, j.wa = s.pol_wa32, j.x = static_cast<const double *>(sl[k].x);
+    j.lo = sl[k].lo, j.hi = sl[k].hi, j.bad = sl[k].bad;
+    j.n = s.n, j.ntile = p.ntile, j.K = p.K, j.chunk = p.chunk, j.nchunk = p.nchunk, j.item0 = sl[k].item0;
+    j.thr = s.damp_thr;
+    j.thr2m = damp_thr2_margin(s);
+    tab.base[tab.njobs] = total;
+    total += sl[k].count;
+    ++tab.njobs;
+  }
+  tab.base[tab.njobs] = total;
+  if (!total) return;
+  add_launch_count(1);
+  if (g == 4)
+    amoeba ? launch_sym64_table<4, true>(tab, next, st) : launch_sym64_table<4, false>(tab, next, st);
+  else if (g == 2)
+    amoeba ? launch_sym64_table<2, true>(tab, next, st) : launch_sym64_table<2, false>(tab, next, st);
+  else
+    amoeba ? launch_sym64_table<1, true>(tab, next, st) : launch_sym64_table<1, false>(tab, next, st);
+}
+
+void launch_fixed_to_double(size_t total, const unsigned long long *lo, const unsigned long long *hi,
+                            const unsigned long long *bad, double *out, cudaStream_t st) {
+  add_launch_count(1);
+  k_fixed_to_double<<<blocks_for(total, 256), 256, 0, st>>>(total, lo, hi, bad, out);
+}
 
 size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs) {
   if (s.n == 0) return 0;
   // two 64-bit accumulator words and one double per value of a column group
-  // (at most two columns)
-  // (at most two columns), the error flag and the work counter
-  size_t C = 3 * (size_t)(nrhs < 2 ? nrhs : 2);
+  // (at most four columns), the error flag and the work counter
+  size_t C = 3 * (size_t)(nrhs < 4 ? nrhs : 4);
   return 3 * C * (size_t)s.n + 2;
 }
 
 void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
-                        cudaStream_t st) {
+                        cudaStream_t st, int gmax) {
   if (s.n == 0) return;
-  float thr2m = damp_thr2_margin(s);
-  // columns in groups of 2 (and a last single one) share the pair geometry
+  // columns in groups of 4 or 2 (gmax, what the scratch holds) and a last
+  // single one share the pair geometry
   int done = 0;
   while (done < nrhs) {
-    int g = (nrhs - done) >= 2 ? 2 : 1;
+    const int left = nrhs - done;
+    int g = (left >= 4 && gmax >= 4) ? 4 : (left >= 2 && gmax >= 2 ? 2 : 1);
     size_t C = 3 * (size_t)g;
     unsigned long long *lo = reinterpret_cast<unsigned long long *>(scratch);
     unsigned long long *hi = lo + C * s.n;
@@ -1132,38 +1258,12 @@ void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y,
     unsigned long long *bad = reinterpret_cast<unsigned long long *>(scratch + 3 * C * s.n);
     unsigned *next = reinterpret_cast<unsigned *>(bad + 1);
     const double *xg = x + (size_t)done * s.n * 3;
-    const int res = g == 2 ? (s.amoeba ? sym_resident<2, true>() : sym_resident<2, false>())
-                           : (s.amoeba ? sym_resident<1, true>() : sym_resident<1, false>());
-    const SymPlan p = sym_plan(s.n, res * sm_count());
-    add_launch_count(3);
     cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
-    cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), st);  // flag and counter
-#define OMMP_SYM_ARGS                                                                                         \
-  s.n, p.ntile, p.K, p.chunk, p.nchunk, p.nitems, next, s.pol_pos, s.pol_a, s.pol_wa32, xg, lo, hi, bad, \
-      s.damp_thr, thr2m
-    if (g == 2) {
-      if (s.amoeba)
-        k_tmu_sym<2, true><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
-      else
-        k_tmu_sym<2, false><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
-    } else {
-      if (s.amoeba)
-        k_tmu_sym<1, true><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
-      else
-        k_tmu_sym<1, false><<<p.ctas, SYM_TILE, 0, st>>>(OMMP_SYM_ARGS);
-    }
-#undef OMMP_SYM_ARGS
-    k_fixed_to_double<<<blocks_for(C * s.n, 256), 256, 0, st>>>(C * s.n, lo, hi, bad, e);
-    const float2 *wa = s.pol_wa32;
-    dim3 fgrid((s.n + 127) / 128, g);
-    if (s.amoeba)
-      k_tmu_finish<double, true><<<fgrid, 128, 0, st>>>(s.n, g, 1, e, s.pol_pos, s.pol_a, wa, xg, s.pol_alpha,
-                                                        dodiag, s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src,
-                                                        s.d2d_s, s.damp_thr, thr2m, y + (size_t)done * s.n * 3);
-    else
-      k_tmu_finish<double, false><<<fgrid, 128, 0, st>>>(s.n, g, 1, e, s.pol_pos, s.pol_a, wa, xg, s.pol_alpha,
-                                                         dodiag, s.d2d_nnz ? s.d2d_ri : nullptr, s.d2d_src,
-                                                         s.d2d_s, s.damp_thr, thr2m, y + (size_t)done * s.n * 3);
+    cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st);
+    SymSlice one{&s, xg, lo, hi, bad, 0, tmu_f64_sym_items(s, g)};
+    launch_tmu_f64_sym_multi(g, s.amoeba, &one, 1, next, st);
+    launch_fixed_to_double(C * s.n, lo, hi, bad, e, st);
+    launch_tmu_finish64(s, g, e, xg, dodiag, y + (size_t)done * s.n * 3, st);
     done += g;
   }
 }
@@ -1183,7 +1283,6 @@ void launch_tmu_f32(const DevSites &s, int nrhs, const float *x, float *y, float
       float *e = reinterpret_cast<float *>(sym_scratch + 2 * C * s.n);
       unsigned long long *bad = reinterpret_cast<unsigned long long *>(sym_scratch + 3 * C * s.n);
       unsigned *next = reinterpret_cast<unsigned *>(bad + 1);
-      add_launch_count(2);
       launch_tmu32_sym_pairs(s, g, x + c * nv, lo, hi, bad, next, e, st);
       tmu_finish<float>(s, g, 1, e, s.pol_pos32, s.pol_a32, x + c * nv, true, y + c * nv, 2, st);
       c += g;
@@ -1305,17 +1404,20 @@ void launch_lu_solve(int nn, const double *A, const int *piv, double *b, cudaStr
 
 // ---- BLAS-1 ---------------------------------------------------------------------
 void launch_dots(int ncol, size_t n, const double *a, const double *b, double *partial, cudaStream_t st) {
+  if (ncol < 1) return;
   add_launch_count(1);
-  k_dots<double><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, a, b, n, partial);
+  k_dots<double><<<dim3(dots_blocks(n), ncol), kRedThreads, 0, st>>>(ncol, n, a, b, n, partial);
 }
 void launch_dots_bcast(int ncol, size_t n, const double *a, const double *b, double *partial,
                        cudaStream_t st) {
+  if (ncol < 1) return;
   add_launch_count(1);
-  k_dots<double><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, a, b, 0, partial);
+  k_dots<double><<<dim3(dots_blocks(n), ncol), kRedThreads, 0, st>>>(ncol, n, a, b, 0, partial);
 }
 void launch_dots_f32(int ncol, size_t n, const float *a, const float *b, double *partial, cudaStream_t st) {
+  if (ncol < 1) return;
   add_launch_count(1);
-  k_dots<float><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, a, b, n, partial);
+  k_dots<float><<<dim3(dots_blocks(n), ncol), kRedThreads, 0, st>>>(ncol, n, a, b, n, partial);
 }
 void launch_reduce_partials(int ncol, const double *partial, double *result, cudaStream_t st) {
   add_launch_count(1);
@@ -1337,19 +1439,27 @@ void launch_to_f32(size_t n, const double *x, const double *scale, float *y, cud
   add_launch_count(1);
   k_to_f32<<<blocks_for(n, 256), 256, 0, st>>>(n, x, scale, y);
 }
+void launch_cg_init(int ncol, const double *dots, CgCol *cols, double tol, cudaStream_t st) {
+  add_launch_count(1);
+  k_cg_init<<<(ncol + 127) / 128, 128, 0, st>>>(ncol, dots, cols, tol);
+}
 void launch_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps, cudaStream_t st) {
   add_launch_count(1);
   k_cg_alpha<<<(ncol + 127) / 128, 128, 0, st>>>(ncol, dots, cols, eps);
 }
 void launch_cg_update(int ncol, int n, double *x, double *r, const double *p, const double *h, double *z,
                       const double *alpha_pol, const CgCol *cols, double *partial, cudaStream_t st) {
+  if (ncol < 1) return;
   add_launch_count(1);
-  k_cg_update<double><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, x, r, p, h, z, alpha_pol, cols, partial);
+  k_cg_update<double><<<dim3(kRedBlocks, ncol), kRedThreads, 0, st>>>(ncol, n, x, r, p, h, z, alpha_pol, cols,
+                                                                      partial);
 }
 void launch_cg_update_f32(int ncol, int n, float *x, float *r, const float *p, const float *h, float *z,
                           const float *alpha_pol, const CgCol *cols, double *partial, cudaStream_t st) {
+  if (ncol < 1) return;
   add_launch_count(1);
-  k_cg_update<float><<<kRedBlocks, kRedThreads, 0, st>>>(ncol, n, x, r, p, h, z, alpha_pol, cols, partial);
+  k_cg_update<float><<<dim3(kRedBlocks, ncol), kRedThreads, 0, st>>>(ncol, n, x, r, p, h, z, alpha_pol, cols,
+                                                                     partial);
 }
 void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double *hist, int hist_stride,
                     cudaStream_t st) {
@@ -1357,12 +1467,14 @@ void launch_cg_gnew(int ncol, int n, const double *dots, CgCol *cols, double *hi
   k_cg_gnew<<<(ncol + 127) / 128, 128, 0, st>>>(ncol, n, dots, cols, hist, hist_stride);
 }
 void launch_cg_pupdate(int ncol, int n, double *p, const double *z, const CgCol *cols, cudaStream_t st) {
+  if (ncol < 1) return;
   add_launch_count(1);
-  k_cg_pupdate<double><<<blocks_for(3 * (size_t)n, 256), 256, 0, st>>>(ncol, n, p, z, cols);
+  k_cg_pupdate<double><<<dim3(blocks_for(3 * (size_t)n, 256), ncol), 256, 0, st>>>(ncol, n, p, z, cols);
 }
 void launch_cg_pupdate_f32(int ncol, int n, float *p, const float *z, const CgCol *cols, cudaStream_t st) {
+  if (ncol < 1) return;
   add_launch_count(1);
-  k_cg_pupdate<float><<<blocks_for(3 * (size_t)n, 256), 256, 0, st>>>(ncol, n, p, z, cols);
+  k_cg_pupdate<float><<<dim3(blocks_for(3 * (size_t)n, 256), ncol), 256, 0, st>>>(ncol, n, p, z, cols);
 }
 void launch_ir_accumulate(int ncol, int n, double *mu, const float *d32, const double *scale, cudaStream_t st) {
   add_launch_count(1);

@@ -79,11 +79,15 @@ void launch_tmu_f64(const DevSites &s, int nrhs, const double *x, double *y, boo
 // u-scaled pair corrections, the sign and the 1/alpha diagonal
 void launch_tmu_finish64(const DevSites &s, int nrhs, const double *partial, const double *x, bool dodiag,
                          double *y, cudaStream_t st);
+// FP32 finishing pass (partial [nrhs][n][3], one split; diagonal included)
+void launch_tmu_finish32(const DevSites &s, int nrhs, const float *partial, const float *x, float *y,
+                         cudaStream_t st);
 // Same product with each unordered pair evaluated once (deterministic
 // half-shell schedule); scratch of tmu_sym_scratch_doubles(s, nrhs_max).
 size_t tmu_sym_scratch_doubles(const DevSites &s, int nrhs);
+// gmax (1, 2 or 4): the widest column group the scratch was sized for
 void launch_tmu_f64_sym(const DevSites &s, int nrhs, const double *x, double *y, bool dodiag, double *scratch,
-                        cudaStream_t st);
+                        cudaStream_t st, int gmax = 2);
 // FP32 inner operator with compensated cross-tile sums; x,y float.  Columns
 // go through the pair kernel in groups of up to gmax (8, 4, 2 or 1) sharing
 // the pair geometry; scratch holds nsplit * nrhs * n * 3 floats.
@@ -100,6 +104,34 @@ void launch_tmu32_sym_pairs(const DevSites &s, int g, const float *x, unsigned l
                             unsigned long long *hi, unsigned long long *bad, unsigned *next, float *out,
                             cudaStream_t st);
 int tmu32_sym_resident(int g, bool amoeba);
+
+// ---- multi-system symmetric products --------------------------------------
+// One system's share of a launch that serves several systems (the products
+// of uneven systems in one persistent kernel): the items [item0, item0 +
+// count) of its product, whose item space (super-tile, chunk of slots) is
+// fixed per system and product kind (*_sym_items), so that a product may be
+// spread over several launches; its fixed-point accumulators [g][n][3] and
+// error flag are zeroed by the caller before the first share.
+struct SymSlice {
+  const DevSites *s;
+  const void *x;  // [g][n][3]: float for the FP32 product, double otherwise
+  unsigned long long *lo, *hi, *bad;
+  int item0, count;
+};
+constexpr int kMaxSymSlices = 32;  // systems per launch
+int tmu32_sym_items(const DevSites &s, int g);
+// next: a device counter of the launch (zeroed by the launcher)
+void launch_tmu32_sym_multi(int g, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st);
+void launch_fixed_to_float(size_t total, const unsigned long long *lo, const unsigned long long *hi,
+                           const unsigned long long *bad, float *out, cudaStream_t st);
+// FP64 symmetric product (g = 1, 2 or 4; one damping kind per launch)
+int tmu_f64_sym_items(const DevSites &s, int g);
+void launch_tmu_f64_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st);
+void launch_fixed_to_double(size_t total, const unsigned long long *lo, const unsigned long long *hi,
+                            const unsigned long long *bad, double *out, cudaStream_t st);
+// double-single symmetric product (g = 1 or 2; one damping kind per launch)
+int tmu_ds_sym_items(const DevSites &s, int g);
+void launch_tmu_ds_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st);
 void launch_tmu32_pairs(const DevSites &s, int g, const float *x, float *partial, int nsplit, cudaStream_t st);
 // source splits an FP32 scratch must hold (per column) for every shape the
 // autotuner may pick
@@ -144,6 +176,18 @@ void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double
                       cudaStream_t st);
 void launch_batch_scatter(int n, int nf, int nipd, int nsolved, const double *x, double *out, cudaStream_t st);
 
+// ---- block CG (block_cg.cu) -----------------------------------------------
+// out[a][b] = sum_i U[ua[a]][i] V[vb[b]][i] (FP32 tiles, FP64 across tiles,
+// fixed order); partial of block_cg_gram_doubles(smax)
+size_t block_cg_gram_doubles(int smax);
+int block_cg_max_columns();
+void launch_gram(size_t nv, int sa, const float *U, const int *ua, int sb, const float *V, const int *vb,
+                 double *partial, double *out, cudaStream_t st);
+// out[oc[k]] = base[bc[k]] + sum_j in[ic[j]] C[j][k], C [nin][nout] (device)
+void launch_combine(size_t nv, int nin, const float *in, const int *ic, int nout, float *out, const int *oc,
+                    const float *base, const int *bc, const float *C, cudaStream_t st);
+void launch_scale_alpha32(int ncol, int n, const float *alpha, const float *r, float *z, cudaStream_t st);
+
 // ---- dense T (incore matvec / inversion) ---------------------------------
 void launch_build_tmat(const DevSites &s, double *tmat, cudaStream_t st);  // [3n][3n] col-major
 void launch_gemv(int nn, const double *A, const double *x, double *y, bool dodiag,
@@ -183,6 +227,8 @@ struct CgCol {
   int converged;  // rms < tol
   int iters;
 };
+// cols[k] = {gold = dots[k], tol, active = dots[k] > 0} (inner PCG start)
+void launch_cg_init(int ncol, const double *dots, CgCol *cols, double tol, cudaStream_t st);
 // gama_k = (h.p)_k from reduced dots; alpha = gold/gama; quick-exit flags.
 void launch_cg_alpha(int ncol, const double *dots, CgCol *cols, double eps, cudaStream_t st);
 // x += alpha p; r -= alpha h; z = alpha_pol r; partial r.z per column

@@ -4,12 +4,19 @@
 // device upload, E_M2D, solve) or "follow-up" (a new field on a resident
 // instance, warm-started from its last dipoles, as in successive SCF
 // iterations of a QM/MM calculation; the reference's ipd_use_guess,
-// src/mod_polarization.F90:195-210).  Worker slots each run one request at a
-// time on the instance's own CUDA stream, so solves of different instances
-// overlap on the device.  A request is admitted as soon as a slot is free
-// and its device memory fits the budget; idle resident instances are evicted
-// least-recently-used first to make room.  Follow-ups on one instance run in
-// submission order.
+// src/mod_polarization.F90:195-210).  Worker slots each carry one request at
+// a time: host setup, admission, upload and E_M2D on the instance's own CUDA
+// stream.  In the mixed modes the solve itself then joins the multi-system
+// engine (multisolve.cu), whose rounds advance every admitted solve together
+// on one stream, the pair products of all of them sharing persistent
+// multi-system launches, so a request that arrives while others are on the
+// GPU starts iterating at the next round; in FP64 the worker solves on the
+// instance's stream.  A request is admitted as soon as a slot is free and its
+// device memory fits the budget; idle resident instances are evicted
+// least-recently-used first to make room.  Instances allocate and free their
+// device memory stream-ordered (cudaMallocAsync / cudaFreeAsync), so
+// admission and eviction do not synchronise the device.  Follow-ups on one
+// instance run in submission order.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -26,6 +33,7 @@
 #include "../../include/openmmpol_gb300.h"
 #include "engine.h"
 #include "log.h"
+#include "multisolve.h"
 
 namespace ommp {
 namespace {
@@ -66,7 +74,8 @@ struct Instance {
 class Server {
  public:
   Server(size_t budget, int slots, int precision, double tol)
-      : budget_(budget), precision_(precision), tol_(tol) {
+      : budget_(budget), precision_(precision), tol_(tol), use_engine_(precision != kPrecFP64) {
+    if (use_engine_) engine_thread_ = std::thread([this] { engine_loop(); });
     for (int k = 0; k < slots; ++k) workers_.emplace_back([this] { work(); });
   }
   ~Server() {
@@ -76,6 +85,20 @@ class Server {
     }
     cv_.notify_all();
     for (auto &t : workers_) t.join();
+    if (use_engine_) {
+      {
+        std::lock_guard<std::mutex> lk(emu_);
+        estop_ = true;
+      }
+      ecv_.notify_all();
+      engine_thread_.join();
+    }
+  }
+
+  void engine_stats(long long *out) {
+    MultiSolver::Stats s = engine_.stats();
+    out[0] = s.ticks, out[1] = s.launches, out[2] = s.shared_launches, out[3] = s.max_systems,
+    out[4] = s.spread_products;
   }
 
   long long submit(Request *r) {
@@ -271,6 +294,7 @@ class Server {
       start_locked();
       lk.unlock();
       dead.clear();  // free evicted systems' device memory outside the lock
+      sys->set_async_alloc(true);
       int st = sys->attach_device();
       if (st == kOk) {
         sys->set_precision(precision_);
@@ -295,12 +319,46 @@ class Server {
     }
   }
 
+  // the engine thread: one round at a time while any solve is admitted
+  void engine_loop() {
+    std::unique_lock<std::mutex> lk(emu_);
+    while (true) {
+      ecv_.wait(lk, [&] { return estop_ || !engine_.idle(); });
+      if (estop_ && engine_.idle()) return;
+      lk.unlock();
+      engine_.tick();
+      lk.lock();
+      ecv_.notify_all();
+    }
+  }
+
   int run(System *s, Request *r) {
     const int n = s->model().npol;
     if (r->pol_atoms != n) {
       set_last_error("server: the field has " + std::to_string(r->pol_atoms) + " sites, the system " +
                      std::to_string(n));
       return kErrBadArg;
+    }
+    if (use_engine_) {
+      int st = kOk;
+      const long long id = engine_.add(s, r->field.data(), st);
+      if (id < 0) return st;
+      int jst = kOk;
+      double e = 0.0;
+      std::string err;
+      {
+        std::unique_lock<std::mutex> lk(emu_);
+        ecv_.notify_all();
+        ecv_.wait(lk, [&] { return engine_.take(id, jst, e, err); });
+      }
+      if (jst) {
+        set_last_error(err);
+        return jst;
+      }
+      r->energy = e;
+      const int nipd = s->model().n_ipd;
+      r->ipd.assign(s->ipd_host(), s->ipd_host() + (size_t)nipd * n * 3);
+      return kOk;
     }
     int st = s->set_external_field(r->field.data(), kSolverNone, kMatvNone, true);
     if (st) return st;
@@ -327,6 +385,12 @@ class Server {
   size_t budget_, used_ = 0, peak_used_ = 0;
   int precision_;
   double tol_;
+  bool use_engine_;
+  MultiSolver engine_;
+  std::thread engine_thread_;
+  std::mutex emu_;
+  std::condition_variable ecv_;  // work for the engine / a round finished
+  bool estop_ = false;
   std::mutex mu_;
   std::condition_variable cv_;
   std::deque<Request *> queue_;
@@ -396,5 +460,11 @@ int32_t ommp_gpu_server_cancel(void *server, int64_t request_id) {
 }
 
 void ommp_gpu_server_stats(void *server, double *out7) { static_cast<Server *>(server)->stats(out7); }
+
+void ommp_gpu_server_engine_stats(void *server, int64_t *out5) {
+  long long v[5] = {0, 0, 0, 0, 0};
+  static_cast<Server *>(server)->engine_stats(v);
+  for (int k = 0; k < 5; ++k) out5[k] = v[k];
+}
 
 }  // extern "C"

@@ -38,11 +38,12 @@ void System::free_ws(Workspace &w) {
   w.graph_ncol = -1;
   if (!w.owned) return;
   void *b[] = {w.x, w.r, w.p, w.h, w.z, w.rhs, w.fields, w.out, w.x32, w.r32, w.p32, w.h32, w.z32,
-               w.scratch32, w.partial, w.dots, w.hist, w.cols};
+               w.scratch32, w.partial, w.dots, w.hist, w.cols, w.t32, w.gram, w.bcoef, w.bidx};
   for (void *p : b)
     if (p) cudaFree(p);
   if (w.cols_h) cudaFreeHost(w.cols_h);
   if (w.scal_h) cudaFreeHost(w.scal_h);
+  if (w.bscal_h) cudaFreeHost(w.bscal_h);
   w = Workspace();
 }
 
@@ -63,8 +64,13 @@ int System::ensure_batch_ws(int ncol, int nf) {
   bad |= walloc(w.scratch32, (size_t)s0 * ncol * nv);
   bad |= walloc(w.partial, (size_t)gpu::kRedBlocks * std::max(ncol, nf)) |
          walloc(w.dots, 3 * (size_t)ncol + nf) | walloc(w.cols, ncol);
+  // block CG buffers (sized for the widest block)
+  const int smax = gpu::block_cg_max_columns();
+  bad |= walloc(w.t32, ncol * nv) | walloc(w.gram, gpu::block_cg_gram_doubles(smax)) |
+         walloc(w.bcoef, 2 * (size_t)smax * smax) | walloc(w.bidx, 2 * (size_t)smax);
   if (bad || cudaMallocHost((void **)&w.cols_h, ncol * sizeof(gpu::CgCol)) != cudaSuccess ||
-      cudaMallocHost((void **)&w.scal_h, (3 * (size_t)ncol + nf) * sizeof(double)) != cudaSuccess) {
+      cudaMallocHost((void **)&w.scal_h, (3 * (size_t)ncol + nf) * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost((void **)&w.bscal_h, (2 * (size_t)smax * smax + smax) * sizeof(double)) != cudaSuccess) {
     w.owned = true;
     free_ws(w);
     set_last_error("out of device memory for the batch workspace");
@@ -401,7 +407,11 @@ int System::mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, in
     }
     cudaMemcpyAsync(w.dots + cap, w.scal_h + cap, 2 * cap * sizeof(double), cudaMemcpyHostToDevice, st_);
     for (int k = 0; k < ncol; ++k) gpu::launch_to_f32(nv, w.r + k * nv, w.dots + cap + k, w.r32 + k * nv, st_);
-    st = pcg32_ws(w, ncol, 200, eta);
+    // batches of at least 4 columns share one Krylov space (block CG)
+    if (block_cg_ && w.t32 && ncol >= 4 && ncol <= gpu::block_cg_max_columns())
+      st = bpcg32_ws(w, ncol, 200, eta);
+    else
+      st = pcg32_ws(w, ncol, 200, eta);
     if (st) return st;
     gpu::launch_ir_accumulate(ncol, n, x, w.x32, w.dots + 2 * cap, st_);
     st = matvec_residual(ncol, x, w.h);

@@ -314,8 +314,8 @@ __device__ __forceinline__ void box_of_supertile(const float4 *__restrict__ boxe
 // loops overflowed the instruction cache (ncu: issue stalled on instruction
 // fetch, 44 % issue activity).
 template <bool NEAR, bool AMOEBA, int G>
-__device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, int lane, const float4 (&pt)[2],
-                                         const float (&at)[2], const float (&mt)[2][3 * G],
+__device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, int lane,
+                                         const float4 (&pt)[2], const float (&at)[2], const float (&mt)[2][3 * G],
                                          const float (&mt3)[2][3 * G], const int (&pl)[2], float thr,
                                          float (&af)[2][3 * G], float (&ak)[2][3 * G]) {
   constexpr int C = 3 * G;
@@ -390,29 +390,53 @@ __device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, in
   }
 }
 
-template <int G, bool AMOEBA>
-__global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, int ntile, int nbox, int K, int chunk, int nchunk,
-                                                        int nitems, unsigned *__restrict__ next,
-                                                        const float4 *__restrict__ pos,
-                                                        const float *__restrict__ damp,
-                                                        const float4 *__restrict__ boxes,
-                                                        const float *__restrict__ x,
-                                                        unsigned long long *__restrict__ acc_lo,
-                                                        unsigned long long *__restrict__ acc_hi,
-                                                        unsigned long long *__restrict__ bad, float thr,
-                                                        float r2max) {
+// One launch serves the products of several systems (a multi-system work
+// queue): job j covers the items [item0, item0 + base[j+1] - base[j]) of
+// its system's product, and the persistent CTAs take global items in order
+// from one counter.  A product's item space is fixed per system (the super-
+// tile I and a chunk of its slots), so a product may also be spread over
+// several launches; its fixed-point sums add up across them.  A one-job
+// table is the single-system product.
+struct S32Job {
+  const float4 *pos;
+  const float *damp;
+  const float4 *boxes;
+  const float *x;
+  unsigned long long *lo, *hi, *bad;
+  int n, ntile, nbox, K, chunk, nchunk, item0, amoeba;
+  float thr, r2max;
+};
+struct S32Table {
+  int njobs;
+  int base[kMaxSymSlices + 1];  // first global item of each job; base[njobs] = total
+  S32Job job[kMaxSymSlices];
+};
+
+template <int G>
+__global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(const __grid_constant__ S32Table tab,
+                                                                       unsigned *__restrict__ next) {
   constexpr int C = 3 * G;
   extern __shared__ float4 s32_dyn[];
   S32Smem<G> &sm = *reinterpret_cast<S32Smem<G> *>(s32_dyn);
   __shared__ int s_item;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int total = tab.base[tab.njobs];
   for (;;) {
     __syncthreads();  // every thread has read the previous item and its sums
     if (tid == 0) s_item = (int)atomicAdd(next, 1u);
     __syncthreads();
     const int item = s_item;
-    if (item >= nitems) break;
-    const int I = item / nchunk;
+    if (item >= total) break;
+    int jx = 0;
+    while (jx + 1 < tab.njobs && tab.base[jx + 1] <= item) ++jx;
+    const S32Job &jb = tab.job[jx];
+    const int n = jb.n, ntile = jb.ntile, nchunk = jb.nchunk;
+    const float4 *__restrict__ pos = jb.pos;
+    const float *__restrict__ damp = jb.damp;
+    const float *__restrict__ x = jb.x;
+    const bool amoeba = jb.amoeba != 0;
+    const int local = jb.item0 + (item - tab.base[jx]);
+    const int I = local / nchunk;
     float4 pt[2];
     float at[2], mt[2][C], mt3[2][C];
     int pl[2];
@@ -423,7 +447,7 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, in
       const int ti = I * S32_TILE + pl[u];
       vt[u] = ti < n;
       pt[u] = vt[u] ? pos[ti] : make_float4(S32_FAR, S32_FAR, S32_FAR, 0.f);
-      at[u] = (AMOEBA && vt[u]) ? damp[ti] : 0.f;
+      at[u] = (amoeba && vt[u]) ? damp[ti] : 0.f;
 #pragma unroll
       for (int c = 0; c < C; ++c) {
         mt[u][c] = vt[u] ? x[((size_t)(c / 3) * n + ti) * 3 + (c % 3)] : 0.f;
@@ -431,14 +455,14 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, in
       }
     }
     float4 ilo, ihi;
-    box_of_supertile(boxes, nbox, I, ilo, ihi);
+    box_of_supertile(jb.boxes, jb.nbox, I, ilo, ihi);
     float sum[2][C], cmp[2][C];
 #pragma unroll
     for (int u = 0; u < 2; ++u)
 #pragma unroll
       for (int c = 0; c < C; ++c) sum[u][c] = cmp[u][c] = 0.f;
-    const int k0 = (item - I * nchunk) * chunk;
-    const int k1 = min(K + 1, k0 + chunk);
+    const int k0 = (local - I * nchunk) * jb.chunk;
+    const int k1 = min(jb.K + 1, k0 + jb.chunk);
     for (int k = k0; k < k1; ++k) {
       int J = I + k;
       if (J >= ntile) J -= ntile;
@@ -454,7 +478,7 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, in
         const int sb = q >> 5, e = q & 31;
         sm.pos[sb][e] = p;
         sm.pos[sb][e + S32_SUB] = p;
-        const float a = (AMOEBA && v) ? damp[sj] : 0.f;
+        const float a = (amoeba && v) ? damp[sj] : 0.f;
 #pragma unroll
         for (int col = 0; col < G; ++col) {
           float4 m = make_float4(0.f, 0.f, 0.f, a);
@@ -470,11 +494,11 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, in
       bool far = false;
       if (!diag) {
         float4 jlo, jhi;
-        box_of_supertile(boxes, nbox, J, jlo, jhi);
+        box_of_supertile(jb.boxes, jb.nbox, J, jlo, jhi);
         const float gx = fmaxf(0.f, fmaxf(jlo.x - ihi.x, ilo.x - jhi.x));
         const float gy = fmaxf(0.f, fmaxf(jlo.y - ihi.y, ilo.y - jhi.y));
         const float gz = fmaxf(0.f, fmaxf(jlo.z - ihi.z, ilo.z - jhi.z));
-        far = gx * gx + gy * gy + gz * gz > r2max;
+        far = gx * gx + gy * gy + gz * gz > jb.r2max;
       }
       float af[2][C], ak[2][C];
 #pragma unroll
@@ -482,9 +506,11 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, in
 #pragma unroll
         for (int c = 0; c < C; ++c) af[u][c] = ak[u][c] = 0.f;
       if (far)
-        s32_slot<false, AMOEBA, G>(false, sm, warp, lane, pt, at, mt, mt3, pl, thr, af, ak);
+        s32_slot<false, false, G>(false, sm, warp, lane, pt, at, mt, mt3, pl, jb.thr, af, ak);
+      else if (amoeba)
+        s32_slot<true, true, G>(diag, sm, warp, lane, pt, at, mt, mt3, pl, jb.thr, af, ak);
       else
-        s32_slot<true, AMOEBA, G>(diag, sm, warp, lane, pt, at, mt, mt3, pl, thr, af, ak);
+        s32_slot<true, false, G>(diag, sm, warp, lane, pt, at, mt, mt3, pl, jb.thr, af, ak);
       // the slot's target sums, compensated across slots
 #pragma unroll
       for (int u = 0; u < 2; ++u)
@@ -506,7 +532,7 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, in
             for (int c = 0; c < C; ++c) {
               const float v = ((sm.accj[0][c][q] + sm.accj[1][c][q]) + sm.accj[2][c][q]) + sm.accj[3][c][q];
               const size_t o = ((size_t)(c / 3) * n + sj) * 3 + (c % 3);
-              fixed_add_f32(acc_lo + o, acc_hi + o, 3.f * v, bad);
+              fixed_add_f32(jb.lo + o, jb.hi + o, 3.f * v, jb.bad);
             }
           }
         }
@@ -519,7 +545,7 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(int n, in
 #pragma unroll
       for (int c = 0; c < C; ++c) {
         const size_t o = ((size_t)(c / 3) * n + ti) * 3 + (c % 3);
-        fixed_add_f32(acc_lo + o, acc_hi + o, sum[u][c] - cmp[u][c], bad);
+        fixed_add_f32(jb.lo + o, jb.hi + o, sum[u][c] - cmp[u][c], jb.bad);
       }
     }
   }
@@ -534,63 +560,108 @@ __global__ void k_fixed_to_float(size_t total, const unsigned long long *__restr
     out[k] = nan ? __int_as_float(0x7fc00000) : (float)fixed_value(lo[k], hi[k]);
 }
 
-template <int G, bool AMOEBA>
+template <int G>
 struct S32Launch {
   int resident = 0;
   S32Launch() {
     const int smem = (int)sizeof(S32Smem<G>);
-    cudaFuncSetAttribute(k_tmu32_sym<G, AMOEBA>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_tmu32_sym<G, AMOEBA>, S32_TPB, smem);
+    cudaFuncSetAttribute(k_tmu32_sym<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_tmu32_sym<G>, S32_TPB, smem);
     if (resident < 1) resident = 1;
   }
 };
+template <int G>
+int s32_resident() {
+  static const S32Launch<G> cfg;  // thread-safe one-time set-up
+  return cfg.resident;
+}
 
-template <int G, bool AMOEBA>
-void launch_s32(const DevSites &s, const float *x, unsigned long long *lo, unsigned long long *hi,
-                unsigned long long *bad, unsigned *next, cudaStream_t st) {
-  static const S32Launch<G, AMOEBA> cfg;  // thread-safe one-time set-up
-  const int ntile = (s.n + S32_TILE - 1) / S32_TILE;
-  const int K = ntile / 2;
-  const int ctas_max = cfg.resident * sm_count();
-  // about 16 work items per resident CTA
-  long long chunk = (long long)ntile * (K + 1) / (16LL * ctas_max);
-  if (chunk < 1) chunk = 1;
-  if (chunk > K + 1) chunk = K + 1;
-  const int nchunk = (int)((K + 1 + chunk - 1) / chunk);
-  const int nitems = ntile * nchunk;
-  const int ctas = ctas_max < nitems ? ctas_max : nitems;
-  k_tmu32_sym<G, AMOEBA><<<ctas, S32_TPB, sizeof(S32Smem<G>), st>>>(
-      s.n, ntile, s.ntile, K, (int)chunk, nchunk, nitems, next, s.pol_pos32, s.pol_a32, s.tile_box32, x, lo, hi,
-      bad, (float)s.damp_thr, s.damp_r2max32);
+// the item space of one system's product: super-tiles x chunks of slots,
+// about 16 items per resident CTA of the whole GPU
+void s32_schedule(int n, int g, int &ntile, int &K, int &chunk, int &nchunk) {
+  ntile = (n + S32_TILE - 1) / S32_TILE;
+  K = ntile / 2;
+  const int ctas_max = (g == 2 ? s32_resident<2>() : s32_resident<1>()) * sm_count();
+  long long c = (long long)ntile * (K + 1) / (16LL * ctas_max);
+  if (c < 1) c = 1;
+  if (c > K + 1) c = K + 1;
+  chunk = (int)c;
+  nchunk = (K + 1 + chunk - 1) / chunk;
+}
+
+template <int G>
+void launch_s32_table(const S32Table &tab, unsigned *next, cudaStream_t st) {
+  const int total = tab.base[tab.njobs];
+  if (total <= 0) return;
+  const int ctas_max = s32_resident<G>() * sm_count();
+  const int ctas = ctas_max < total ? ctas_max : total;
+  cudaMemsetAsync(next, 0, sizeof(unsigned), st);
+  k_tmu32_sym<G><<<ctas, S32_TPB, sizeof(S32Smem<G>), st>>>(tab, next);
+}
+
+void fill_s32_job(S32Job &j, const DevSites &s, int g, const float *x, unsigned long long *lo,
+                  unsigned long long *hi, unsigned long long *bad, int item0) {
+  j.pos = s.pol_pos32;
+  j.damp = s.pol_a32;
+  j.boxes = s.tile_box32;
+  j.x = x;
+  j.lo = lo, j.hi = hi, j.bad = bad;
+  j.n = s.n;
+  j.nbox = s.ntile;
+  s32_schedule(s.n, g, j.ntile, j.K, j.chunk, j.nchunk);
+  j.item0 = item0;
+  j.amoeba = s.amoeba ? 1 : 0;
+  j.thr = (float)s.damp_thr;
+  j.r2max = s.damp_r2max32;
 }
 
 }  // namespace
 
-int tmu32_sym_resident(int g, bool amoeba) {
-  if (g == 2) return amoeba ? S32Launch<2, true>().resident : S32Launch<2, false>().resident;
-  return amoeba ? S32Launch<1, true>().resident : S32Launch<1, false>().resident;
+int tmu32_sym_resident(int g, bool) { return g == 2 ? s32_resident<2>() : s32_resident<1>(); }
+
+int tmu32_sym_items(const DevSites &s, int g) {
+  if (s.n == 0) return 0;
+  int ntile, K, chunk, nchunk;
+  s32_schedule(s.n, g, ntile, K, chunk, nchunk);
+  return ntile * nchunk;
+}
+
+void launch_tmu32_sym_multi(int g, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st) {
+  S32Table tab{};
+  int total = 0;
+  for (int k = 0; k < nsl && tab.njobs < kMaxSymSlices; ++k) {
+    if (sl[k].count <= 0 || sl[k].s->n == 0) continue;
+    fill_s32_job(tab.job[tab.njobs], *sl[k].s, g, static_cast<const float *>(sl[k].x), sl[k].lo, sl[k].hi,
+                 sl[k].bad, sl[k].item0);
+    tab.base[tab.njobs] = total;
+    total += sl[k].count;
+    ++tab.njobs;
+  }
+  tab.base[tab.njobs] = total;
+  if (!total) return;
+  add_launch_count(1);
+  if (g == 2)
+    launch_s32_table<2>(tab, next, st);
+  else
+    launch_s32_table<1>(tab, next, st);
+}
+
+void launch_fixed_to_float(size_t total, const unsigned long long *lo, const unsigned long long *hi,
+                           const unsigned long long *bad, float *out, cudaStream_t st) {
+  add_launch_count(1);
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 4 * 152 * 4) blocks = 4 * 152 * 4;
+  k_fixed_to_float<<<blocks < 1 ? 1 : blocks, 256, 0, st>>>(total, lo, hi, bad, out);
 }
 
 void launch_tmu32_sym_pairs(const DevSites &s, int g, const float *x, unsigned long long *lo, unsigned long long *hi,
                             unsigned long long *bad, unsigned *next, float *out, cudaStream_t st) {
   const size_t C = 3 * (size_t)g;
   cudaMemsetAsync(lo, 0, 2 * C * s.n * sizeof(unsigned long long), st);
-  cudaMemsetAsync(bad, 0, 2 * sizeof(unsigned long long), st);  // flag and counter
-  if (g == 2) {
-    if (s.amoeba)
-      launch_s32<2, true>(s, x, lo, hi, bad, next, st);
-    else
-      launch_s32<2, false>(s, x, lo, hi, bad, next, st);
-  } else {
-    if (s.amoeba)
-      launch_s32<1, true>(s, x, lo, hi, bad, next, st);
-    else
-      launch_s32<1, false>(s, x, lo, hi, bad, next, st);
-  }
-  const size_t total = C * s.n;
-  int blocks = (int)((total + 255) / 256);
-  if (blocks > 4 * 152 * 4) blocks = 4 * 152 * 4;
-  k_fixed_to_float<<<blocks, 256, 0, st>>>(total, lo, hi, bad, out);
+  cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st);
+  SymSlice one{&s, x, lo, hi, bad, 0, tmu32_sym_items(s, g)};
+  launch_tmu32_sym_multi(g, &one, 1, next, st);
+  launch_fixed_to_float(C * s.n, lo, hi, bad, out, st);
 }
 
 // one column group through the v2 pair kernel (g = 1, 2, 4 or 8)

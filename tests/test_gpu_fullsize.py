@@ -30,7 +30,13 @@ def w30k(tmp_path_factory):
     g = OMMPSystem(p)
     cmm = g.cmm
     ef, _, _ = synth.point_charge_field(g.cpol, w.box_center(), seed=103, all_sites_bohr=cmm)
+    g.center = w.box_center()
     return p, g, ef
+
+
+@pytest.fixture(scope="module")
+def w30k_oracle(w30k):
+    return OracleSystem(w30k[0])
 
 
 def _check_against_fixture(g, ref, tol):
@@ -41,11 +47,12 @@ def _check_against_fixture(g, ref, tol):
     assert np.linalg.norm(samp - ref["ipd_sample"]) <= tol * np.linalg.norm(ref["ipd_sample"])
 
 
-def _sampled_residual(p, g, ef, nrows=256):
+def _sampled_residual(p, g, ef, nrows=256, ipd_d=None, o=None):
     """max over sampled rows of |E - T mu| / max |E| for the D set, via the oracle."""
-    o = OracleSystem(p)
+    o = o or OracleSystem(p)
+    ipd_d = g.ipd[0] if ipd_d is None else ipd_d
     rows = np.sort(np.random.default_rng(11).choice(g.pol_atoms, nrows, replace=False)).astype(np.int32)
-    tmu = o.tmatvec_rows(g.ipd[0], rows)
+    tmu = o.tmatvec_rows(ipd_d, rows)
     rhs = g.e_m2d()[0][rows] + ef[rows]
     return np.abs(rhs - tmu).max() / np.abs(rhs).max()
 
@@ -89,3 +96,25 @@ def test_w30k_mixed_ds_matches_oracle_fixture(w30k):
     assert g.counter(0) == 0 and g.counter(4) >= 1
     assert _sampled_residual(p, g, ef) < 1e-7
     g.set_precision("fp64")
+
+
+def test_b64_full_batch_columns_pinned_by_oracle(w30k, w30k_oracle):
+    """The batching configuration at its full size: 64 fields of 30 point
+    charges (seeds 1000..1063) on the 90,000-site box in one batched strict
+    mixed solve.  Three columns are checked against the oracle's residual rows
+    (E - T mu on 256 sampled rows below 1e-7 of max |E|) and against single
+    plain-FP64 solves of the same fields (1e-7 relative)."""
+    p, g, _ = w30k
+    fields = np.stack([synth.point_charge_field(g.cpol, g.center, seed=1000 + r, all_sites_bohr=g.cmm)[0]
+                       for r in range(64)])
+    g.set_precision("mixed")
+    g.set_solver_tol(1e-10)
+    ipd, en = g.set_external_fields_batch(fields)
+    assert np.array_equal(ipd[:, 0], ipd[:, 1])  # water: D and P coincide
+    g.set_precision("fp64")
+    for r in (0, 31, 63):
+        assert _sampled_residual(p, g, fields[r], ipd_d=ipd[r, 0], o=w30k_oracle) < 1e-7
+        g.clear_guess()
+        g.set_external_field(fields[r])
+        assert np.linalg.norm(ipd[r] - g.ipd) <= 1e-7 * np.linalg.norm(g.ipd)
+        assert abs(en[r] - g.get_polelec_energy()) <= 1e-7 * abs(g.get_polelec_energy())

@@ -92,6 +92,19 @@ def test_results_same_alone_and_in_the_mix(systems, precision):
     assert st["peak_concurrent"] >= 2
 
 
+def test_engine_serves_uneven_systems_in_shared_launches(systems):
+    """In the mixed modes the server's solves run in the multi-system
+    engine: systems of 120 to 2,700 sites in flight together share product
+    launches, and each result still equals its solve alone."""
+    srv = Server(8 << 30, slots=len(systems), precision="mixed-ds", tol=1e-10)
+    first, second = served(srv, systems)
+    es = srv.engine_stats()
+    srv.close()
+    check(systems, first, second, "mixed-ds")
+    assert es["max_systems_per_launch"] >= 2 and es["shared_launches"] >= 1
+    assert es["rounds"] > 0 and es["launches"] >= es["shared_launches"]
+
+
 def test_eviction_under_small_budget(systems):
     # size every system on the device, then give room for the largest two only
     srv = Server(8 << 30, slots=1, precision="mixed", tol=1e-10)

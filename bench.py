@@ -110,6 +110,8 @@ def parse():
     ap.add_argument("--slots", type=int, default=8, help="s1024: concurrent requests on the GPU")
     ap.add_argument("--hbm-budget-gib", type=float, default=4.0, help="s1024: device memory for systems")
     ap.add_argument("--loads", default="0.5,0.7,0.9", help="s1024: offered loads, fractions of saturation")
+    ap.add_argument("--cached-geometries", action="store_true",
+                    help="s1024: map request sizes to 32 cached clusters instead of a fresh geometry per request")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "ommp_gb300_bench"))
     return ap.parse_args()
 
@@ -917,6 +919,45 @@ def serve_pool(cache, levels=32):
     return sizes, pool
 
 
+def _fresh_cluster(job):
+    """Worker of the fresh-geometry pool: one water cluster written as .mmp
+    plus its coordinates (seeded by the request)."""
+    nw, seed, path = job
+    sys.path.insert(0, ROOT)
+    from openmmpol_gb300 import synth
+    w = synth.water_cluster(nw, seed=seed)
+    synth.write_mmp(path + ".tmp", w)
+    np.save(path + ".xyz.npy", w.coords)
+    os.replace(path + ".tmp", path)
+    return path
+
+
+def serve_fresh_pool(plan, workers=None):
+    """One new geometry per new request of the plan (its drawn size, seed
+    100000 + request id), written in parallel into a scratch directory (the
+    RAM disk when there is one) before the stream starts; returns the pool
+    keyed by request id and the directory (removed by the caller)."""
+    import multiprocessing as mp
+    import shutil
+    from openmmpol_gb300 import synth
+    base = "/dev/shm" if os.path.isdir("/dev/shm") else tempfile.gettempdir()
+    d = tempfile.mkdtemp(prefix="ommp_fresh_", dir=base)
+    ks = [k for k, p in enumerate(plan) if p["parent"] is None]
+    jobs = [(plan[k]["drawn"], 100000 + k, os.path.join(d, f"req{k}.mmp")) for k in ks]
+    workers = workers or max(1, (os.cpu_count() or 2) - 2)
+    try:
+        with mp.get_context("spawn").Pool(workers) as pool:
+            pool.map(_fresh_cluster, jobs, chunksize=1)
+    except Exception:
+        shutil.rmtree(d, ignore_errors=True)
+        raise
+    out = {}
+    for (nw, seed, path), k in zip(jobs, ks):
+        c = np.load(path + ".xyz.npy")
+        out[k] = {"path": path, "cpol": c * synth.ANG2AU, "center": 0.5 * (c.min(axis=0) + c.max(axis=0))}
+    return out, d
+
+
 def serve_plan(nreq, sizes, seed=2024, followup_frac=0.3):
     """Request k: a new cluster (log-uniform size, field of 30 fresh charges
     with seed 10000 + k) or, with probability 0.3, a follow-up SCF iteration
@@ -932,13 +973,15 @@ def serve_plan(nreq, sizes, seed=2024, followup_frac=0.3):
             nw = float(np.exp(rng.uniform(np.log(300), np.log(60000))))
             plan.append({"parent": None, "size": int(sizes[int(np.argmin(np.abs(logs - np.log(nw))))]),
                          "drawn": int(round(nw))})
-    for k, p in enumerate(plan):  # resolve follow-up chains to their cluster
+    for k, p in enumerate(plan):  # resolve follow-up chains to their cluster and its first request
         if p["parent"] is not None:
             p["size"] = plan[p["parent"]]["size"]
+            p["drawn"] = plan[p["parent"]]["drawn"]
+            p["root"] = plan[p["parent"]].get("root", p["parent"])
     return plan
 
 
-def serve_stream(srv, plan, pool, rate, keep, seed=77):
+def serve_stream(srv, plan, pool, rate, keep, seed=77, fresh=False):
     """Run the plan through the server with Poisson arrivals at `rate`
     requests/s (None: all at t = 0).  A follow-up is submitted when both its
     arrival time has passed and its parent is done (the next SCF iteration
@@ -959,7 +1002,8 @@ def serve_stream(srv, plan, pool, rate, keep, seed=77):
     def one(k):
         p = plan[k]
         try:
-            g = pool[p["size"]]
+            # fresh geometries: keyed by the request that created the cluster
+            g = pool[p.get("root", k)] if fresh else pool[p["size"]]
             nipd = 2
             if p["parent"] is None:
                 field, _, _ = synth.point_charge_field(g["cpol"], g["center"], seed=10000 + k)
@@ -983,12 +1027,13 @@ def serve_stream(srv, plan, pool, rate, keep, seed=77):
                 r = srv.wait(srv.submit(g["path"], field, nipd))
             out[k] = {"instance": r["instance"], "field": field, "latency_ms": r["latency_ms"],
                       "energy": r["energy"], "ipd": r["ipd"] if k in keep else None,
-                      "sites": 3 * p["size"], "followup": p["parent"] is not None, "readmit": readmit,
-                      "t_done": time.perf_counter()}
+                      "sites": 3 * (p["drawn"] if fresh else p["size"]), "followup": p["parent"] is not None,
+                      "readmit": readmit, "t_done": time.perf_counter()}
         except Exception as ex:  # recorded and reported
             errors.append(f"request {k}: {ex!r}")
-            out[k] = {"instance": -1, "field": np.zeros((3 * p["size"], 3)), "latency_ms": float("nan"),
-                      "energy": float("nan"), "ipd": None, "sites": 3 * p["size"],
+            nsite = 3 * (p["drawn"] if fresh else p["size"])
+            out[k] = {"instance": -1, "field": np.zeros((nsite, 3)), "latency_ms": float("nan"),
+                      "energy": float("nan"), "ipd": None, "sites": nsite,
                       "followup": p["parent"] is not None, "readmit": False, "t_done": time.perf_counter()}
         finally:
             done[k].set()
@@ -1013,9 +1058,19 @@ def run_s1024(args):
     b.build()
     L = _lib.load()
     og.set_verbose(0)
-    sizes, pool = serve_pool(os.path.join(args.cache, "serve"))
     nreq, n64 = args.requests, min(args.fp64_requests, args.requests)
-    plan = serve_plan(nreq, sizes)
+    fresh = not args.cached_geometries
+    fresh_dir, prep_s = None, 0.0
+    if fresh:
+        # one new geometry per new request (its drawn size), made before the stream
+        sizes = sorted(set(int(round(x)) for x in np.exp(np.linspace(np.log(300), np.log(60000), 32))))
+        plan = serve_plan(nreq, sizes)
+        t0 = time.perf_counter()
+        pool, fresh_dir = serve_fresh_pool(plan)
+        prep_s = time.perf_counter() - t0
+    else:
+        sizes, pool = serve_pool(os.path.join(args.cache, "serve"))
+        plan = serve_plan(nreq, sizes)
     keep = set(range(n64))
     budget = int(args.hbm_budget_gib * (1 << 30))
     res = {}
@@ -1034,8 +1089,9 @@ def run_s1024(args):
         for phase in phases:
             rate = None if phase == "saturation" else float(phase[4:]) / 100 * r["saturation"]["requests_per_s"]
             srv = og.Server(budget, slots=args.slots, precision=prec, tol=1e-10)
-            out, wall, errors = serve_stream(srv, pl, pool, rate, keep)
+            out, wall, errors = serve_stream(srv, pl, pool, rate, keep, fresh=fresh)
             st = srv.stats()
+            est = srv.engine_stats()
             srv.close()
             lat = np.array([o["latency_ms"] for o in out if np.isfinite(o["latency_ms"])])
             lat_new = np.array([o["latency_ms"] for o in out if not o["followup"] and np.isfinite(o["latency_ms"])])
@@ -1049,7 +1105,8 @@ def run_s1024(args):
                         "followups": int(sum(o["followup"] for o in out)),
                         "readmitted_followups": int(sum(o["readmit"] for o in out)),
                         "evictions": int(st["evictions"]), "peak_concurrent": int(st["peak_concurrent"]),
-                        "peak_bytes": int(st["peak_bytes"]), "errors": errors[:5], "n_errors": len(errors)}
+                        "peak_bytes": int(st["peak_bytes"]), "engine": est, "errors": errors[:5],
+                        "n_errors": len(errors)}
             if phase == "saturation":
                 r["results"] = {k: (out[k]["ipd"], out[k]["energy"]) for k in keep if k < nr}
         res[label] = r
@@ -1082,8 +1139,11 @@ def run_s1024(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+f64",
             "data": "synthetic",
             "config": {"workload": f"{nreq} requests: AMOEBA water clusters of log-uniform 300..60,000 molecules "
-                                   f"({len(sizes)} cached geometries), 30-charge field per new request, 30 % "
+                                   + ("(a fresh geometry per new request, seed 100000 + id)" if fresh else
+                                      f"({len(sizes)} cached geometries)")
+                                   + ", 30-charge field per new request, 30 % "
                                    "follow-ups (field x (1 + 0.01 N(0,1)), warm start), D+P to RMS 1e-10",
+                       "geometry_prep_s": prep_s,
                        "hbm_budget_gib": args.hbm_budget_gib, "slots": args.slots, "precision": args.precision,
                        "fp64_requests": n64, "arrivals": "all at t=0 (saturation), then Poisson at the "
                                                          "listed fractions of the saturation rate"},
@@ -1098,6 +1158,9 @@ def run_s1024(args):
                                      "dipoles_rel_l2_max": max(err_ipd) if err_ipd else None,
                                      "energy_rel_max": max(err_e) if err_e else None},
             "gpu_launches": int(launches), "clocks": clocks}
+    if fresh_dir:
+        import shutil
+        shutil.rmtree(fresh_dir, ignore_errors=True)
     print(json.dumps(line), flush=True)
 
 

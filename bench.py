@@ -110,6 +110,7 @@ def parse():
     ap.add_argument("--slots", type=int, default=8, help="s1024: concurrent requests on the GPU")
     ap.add_argument("--hbm-budget-gib", type=float, default=4.0, help="s1024: device memory for systems")
     ap.add_argument("--loads", default="0.5,0.7,0.9", help="s1024: offered loads, fractions of saturation")
+    ap.add_argument("--round-ms", type=float, default=4.0, help="s1024: work per product kind in one engine round")
     ap.add_argument("--cached-geometries", action="store_true",
                     help="s1024: map request sizes to 32 cached clusters instead of a fresh geometry per request")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "ommp_gb300_bench"))
@@ -1089,6 +1090,8 @@ def run_s1024(args):
         for phase in phases:
             rate = None if phase == "saturation" else float(phase[4:]) / 100 * r["saturation"]["requests_per_s"]
             srv = og.Server(budget, slots=args.slots, precision=prec, tol=1e-10)
+            if prec != "fp64":
+                srv.set_round_ms(args.round_ms)
             out, wall, errors = serve_stream(srv, pl, pool, rate, keep, fresh=fresh)
             st = srv.stats()
             est = srv.engine_stats()
@@ -1109,6 +1112,7 @@ def run_s1024(args):
                         "n_errors": len(errors)}
             if phase == "saturation":
                 r["results"] = {k: (out[k]["ipd"], out[k]["energy"]) for k in keep if k < nr}
+                r["fields"] = {k: out[k]["field"] for k in keep if k < nr}
         res[label] = r
     clocks = clk.stop()
     launches = L.ommp_gpu_kernel_launch_count() - l0
@@ -1120,8 +1124,31 @@ def run_s1024(args):
             continue
         err_ipd.append(float(np.linalg.norm(a - f) / np.linalg.norm(f)))
         err_e.append(float(abs(ea - ef) / abs(ef)))
+    # the oracle's residual E - T mu of served mixed dipoles on 256 sampled
+    # rows, for up to four of the smaller new clusters among the compared ones
+    oracle_rows = []
+    try:
+        from oracle import oracle as orc
+        orc.build()
+        orc.set_num_threads(os.cpu_count() or 1)
+        cand = [k for k in sorted(keep) if plan[k]["parent"] is None and plan[k]["drawn"] <= 3000]
+        for k in cand[:4]:
+            a, _ = res["mixed"]["results"][k]
+            if a is None:
+                continue
+            g = pool[k] if fresh else pool[plan[k]["size"]]
+            o = orc.OracleSystem(g["path"])
+            rows = np.sort(np.random.default_rng(k).choice(o.pol_atoms, min(256, o.pol_atoms),
+                                                           replace=False)).astype(np.int32)
+            rhs = o.e_m2d()[0][rows] + res["mixed"]["fields"][k][rows]
+            tmu = o.tmatvec_rows(a[0], rows)
+            oracle_rows.append({"request": k, "sites": int(o.pol_atoms),
+                                "max_residual_rel": float(np.abs(rhs - tmu).max() / np.abs(rhs).max())})
+    except Exception as ex:  # reported, not hidden
+        oracle_rows.append({"error": repr(ex)})
     for prec in res:
         res[prec].pop("results")
+        res[prec].pop("fields", None)
     mx, f64 = res["mixed"], res["fp64"]
     # the knee: the highest offered load whose median latency stays within 3x
     # of the lightest load's (beyond it queueing dominates the median; the p99
@@ -1145,6 +1172,7 @@ def run_s1024(args):
                                    "follow-ups (field x (1 + 0.01 N(0,1)), warm start), D+P to RMS 1e-10",
                        "geometry_prep_s": prep_s,
                        "hbm_budget_gib": args.hbm_budget_gib, "slots": args.slots, "precision": args.precision,
+                       "round_ms": args.round_ms,
                        "fp64_requests": n64, "arrivals": "all at t=0 (saturation), then Poisson at the "
                                                          "listed fractions of the saturation rate"},
             "p50_ms": mx["load70"]["p50_ms"], "p99_ms": mx["load70"]["p99_ms"],
@@ -1154,6 +1182,7 @@ def run_s1024(args):
             "mixed": mx, "fp64": f64,
             "speedup_mixed_over_fp64_saturation": (mx["saturation"]["sites_per_s"] /
                                                    f64["saturation"]["sites_per_s"]),
+            "oracle_residual_rows": oracle_rows,
             "errors_mixed_vs_fp64": {"requests_compared": len(err_ipd),
                                      "dipoles_rel_l2_max": max(err_ipd) if err_ipd else None,
                                      "energy_rel_max": max(err_e) if err_e else None},

@@ -428,6 +428,10 @@ void ommp_gpu_server_stats(void *server, double *out7);
  * launches that served two or more systems, most systems in one launch,
  * products spread over several rounds (zeros in FP64) */
 void ommp_gpu_server_engine_stats(void *server, int64_t *out5);
+/* work per product kind in one round of the engine, in milliseconds of GPU
+ * time (default 4): shorter rounds let small systems iterate faster beside
+ * large ones, longer ones spend less on the per-round bookkeeping */
+int32_t ommp_gpu_server_set_round_ms(void *server, double ms);
 
 /* No counterpart in the reference.  y = T x (dodiag = 1) or y = -E_dd(x)
  * (dodiag = 0) for nrhs (1|2) columns [nrhs][pol_atoms][3], with x and y in

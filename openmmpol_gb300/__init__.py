@@ -551,6 +551,10 @@ class Server:
         """True when the request was still queued and is now cancelled."""
         return self._L.ommp_gpu_server_cancel(self._h, int(rid)) == 0
 
+    def set_round_ms(self, ms: float) -> None:
+        """Work per product kind in one round of the mixed modes' engine (ms)."""
+        _check(self._L.ommp_gpu_server_set_round_ms(self._h, float(ms)))
+
     def engine_stats(self) -> dict:
         """The multi-system engine of the mixed modes (zeros in FP64)."""
         o = np.zeros(5, dtype=np.int64)

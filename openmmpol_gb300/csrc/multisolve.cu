@@ -17,7 +17,8 @@
 //     (system, super-tile, chunk of slots), taken in order from one counter
 //     (the launch_*_sym_multi kernels);
 //   * a product gets a bounded share of each round (about 4 ms of work per
-//     kind: a fair share per system first, then the shortest products), so
+//     kind by default, set_round_ms: a fair share per system first, then the
+//     shortest products), so
 //     small systems finish their iterations while a large system's product
 //     is spread over several rounds; its fixed-point sums simply continue;
 //   * after the launches, every system whose product completed runs its CG
@@ -53,9 +54,10 @@ enum Stage {
 enum Kind { kNone, kF32, kF64, kDS };
 constexpr int kMaxOuter = 30;
 constexpr int kMaxInner = 200;
-// pair budget of one round per product kind (~4 ms of work on GB300 at the
-// measured pair rates of the symmetric kernels)
-constexpr double kBudgetPairs[4] = {0.0, 3.4e9, 7.0e7, 3.4e8};
+// pairs per millisecond of the symmetric kernels on GB300 per product kind
+// (measured: FP32 8.6e11, FP64 1.76e10, double-single 8.6e10 pairs/s); a
+// round's budget is round_ms_ of work per kind
+constexpr double kPairsPerMs[4] = {0.0, 8.6e8, 1.76e7, 8.6e7};
 }  // namespace
 
 struct MultiSolver::Job {
@@ -145,6 +147,11 @@ long long MultiSolver::add(System *s, const double *ext_host, int &status) {
   return j->id;
 }
 
+void MultiSolver::set_round_ms(double ms) {
+  std::lock_guard<std::mutex> lk(mu_);
+  if (ms > 0.0 && std::isfinite(ms)) round_ms_ = ms;
+}
+
 bool MultiSolver::idle() {
   std::lock_guard<std::mutex> lk(mu_);
   return pending_.empty() && jobs_.empty();
@@ -190,7 +197,7 @@ int MultiSolver::launch_products(std::vector<Job *> &active) {
       const double n = j->s->d_.n;
       return std::max(1.0, 0.5 * n * (n - 1.0) / std::max(1, j->items));
     };
-    const double budget = kBudgetPairs[kind];
+    const double budget = kPairsPerMs[kind] * round_ms_;
     double used = 0.0;
     const double share = budget / js.size();
     for (Job *j : js) {

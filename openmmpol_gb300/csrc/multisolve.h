@@ -42,6 +42,11 @@ class MultiSolver {
   // finished in this round.  Called by one thread.
   int tick();
   bool idle();
+  // work per product kind in one round, in milliseconds of GPU time at the
+  // symmetric kernels' measured pair rates (default 4): shorter rounds let
+  // small systems iterate faster beside large ones, longer rounds spend less
+  // of the GPU on the per-round bookkeeping
+  void set_round_ms(double ms);
   // a finished job's status, energy and error text; false while running
   bool take(long long id, int &status, double &energy, std::string &err);
   Stats stats();
@@ -58,6 +63,7 @@ class MultiSolver {
   std::vector<Job *> jobs_;       // in rounds (engine thread only)
   std::map<long long, Job *> done_;
   long long next_id_ = 0;
+  double round_ms_ = 4.0;
   Stats stats_;
 };
 

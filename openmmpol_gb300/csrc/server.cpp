@@ -95,6 +95,8 @@ class Server {
     }
   }
 
+  void set_round_ms(double ms) { engine_.set_round_ms(ms); }
+
   void engine_stats(long long *out) {
     MultiSolver::Stats s = engine_.stats();
     out[0] = s.ticks, out[1] = s.launches, out[2] = s.shared_launches, out[3] = s.max_systems,
@@ -460,6 +462,15 @@ int32_t ommp_gpu_server_cancel(void *server, int64_t request_id) {
 }
 
 void ommp_gpu_server_stats(void *server, double *out7) { static_cast<Server *>(server)->stats(out7); }
+
+int32_t ommp_gpu_server_set_round_ms(void *server, double ms) {
+  if (!(ms > 0.0) || !(ms < 1e6)) {
+    ommp::set_last_error("server: the round length must be a positive number of milliseconds");
+    return ommp::kErrBadArg;
+  }
+  static_cast<Server *>(server)->set_round_ms(ms);
+  return ommp::kOk;
+}
 
 void ommp_gpu_server_engine_stats(void *server, int64_t *out5) {
   long long v[5] = {0, 0, 0, 0, 0};

@@ -97,6 +97,9 @@ def test_engine_serves_uneven_systems_in_shared_launches(systems):
     engine: systems of 120 to 2,700 sites in flight together share product
     launches, and each result still equals its solve alone."""
     srv = Server(8 << 30, slots=len(systems), precision="mixed-ds", tol=1e-10)
+    with pytest.raises(OMMPError):
+        srv.set_round_ms(-1.0)
+    srv.set_round_ms(1.0)  # short rounds: more of them, same results
     first, second = served(srv, systems)
     es = srv.engine_stats()
     srv.close()

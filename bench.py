@@ -28,10 +28,10 @@ in the reference (src/mod_electrostatics.F90:1487-1596, M2D_done cache).
   the oracle's gradient on the host cores (3,000-molecule sample scaled).
 * ``cpu_baseline``: the C/OpenMP oracle (restatement of the reference's
   OpenMP path) timed on two whole T.mu products of the box on all host cores,
-  scaled to a solve by the oracle's own product count (19).
+  scaled to a solve by the oracle's own product count (20).
 
 ``--impl reference`` times that CPU implementation alone and prints its line:
-each step is one whole oracle T.mu product (1/19 of a solve, so
+each step is one whole oracle T.mu product (1/20 of a solve, so
 ``ms_per_step`` is the real step time and ``value`` the solves/s it implies),
 and one whole oracle solve of the box outside the timed steps gives the
 measured solve time and product count beside the per-step figure.
@@ -232,7 +232,7 @@ def cpu_full_products(o, count):
 # field of seed 100 (D: 16 iterations and its residual products; P, seeded
 # with D, converges at once), counted by its whole solve of that box; the
 # reference arm counts them again in its own whole solve
-ORACLE_MV_PER_SOLVE = 19
+ORACLE_MV_PER_SOLVE = 20
 
 
 def run_reference(args):
@@ -282,12 +282,11 @@ def run_reference(args):
             t0 = time.perf_counter()
             o.e_m2d()
             m2d_s = time.perf_counter() - t0
-            mv0 = o.matvec_count()
             o.clear_guess()
             t0 = time.perf_counter()
             o.set_external_field(f)
             full_s = time.perf_counter() - t0
-            mv_full = o.matvec_count() - mv0
+            mv_full = o.matvec_count()  # the oracle counts the products of its last solve
             mv_per_solve = mv_full
             full = {"measured_full_solve_s": full_s, "t_mu_products": mv_full,
                     "cg_iterations": [o.last_iterations(0), o.last_iterations(1)],
@@ -373,7 +372,12 @@ def roofline_of(kstats, total_ms, n=30000):
                             f"conventional {FLOP_PER_PAIR:.0f} flop per ordered pair)" if sym else
                             f"{FLOP_PER_PAIR:.0f} flop per ordered pair x N(N-1) pairs") +
                            f" x right-hand sides ({d['columns']} columns over {d['launches']} launches)",
-            "share_of_timed": d["total_ms"] / total_ms}
+            "share_of_timed": d["total_ms"] / total_ms,
+            # GB300 nominal pipe rates beside the measured ones: FP64 1.25 TFLOP/s (0.625 T FMA
+            # instructions/s); FP32 152 SMs x 128 lanes x 2.07 GHz = 40.3 T instructions/s
+            "peak_nominal": 0.625 if dom == "tmu_fp64" else 40.3,
+            "frac_nominal": ((d["achieved_tops"] if (ds or sym) else d["achieved_tflops"] / 2.0) /
+                             (0.625 if dom == "tmu_fp64" else 40.3))}
 
 
 def rel_err(a, b):

@@ -683,6 +683,11 @@ __global__ void k_to_f32(size_t n, const double *x, const double *scale, float *
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     y[i] = (float)(x[i] * (scale ? *scale : 1.0));
 }
+// ncol columns of nv values, column k scaled by scale[k], in one launch
+__global__ void k_to_f32_cols(size_t nv, size_t tot, const double *x, const double *scale, float *y) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)(x[i] * scale[i / nv]);
+}
 
 // start of the inner PCG with the first r.z on the device (no host read)
 __global__ void k_cg_init(int ncol, const double *dots, CgCol *cols, double tol) {
@@ -1434,6 +1439,12 @@ void launch_add(size_t n, const double *a, const double *b, double *out, cudaStr
 void launch_scale_by_alpha(int nrhs, int n, const double *alpha, const double *x, double *y, cudaStream_t st) {
   add_launch_count(1);
   k_scale_alpha<<<blocks_for((size_t)nrhs * n * 3, 256), 256, 0, st>>>(nrhs, n, alpha, x, y);
+}
+void launch_to_f32_cols(int ncol, size_t nv, const double *x, const double *scale, float *y, cudaStream_t st) {
+  if (ncol < 1 || nv == 0) return;
+  add_launch_count(1);
+  const size_t tot = nv * (size_t)ncol;
+  k_to_f32_cols<<<blocks_for(tot, 256), 256, 0, st>>>(nv, tot, x, scale, y);
 }
 void launch_to_f32(size_t n, const double *x, const double *scale, float *y, cudaStream_t st) {
   add_launch_count(1);

@@ -216,6 +216,8 @@ void launch_add(size_t n, const double *a, const double *b, double *out, cudaStr
 void launch_scale_by_alpha(int nrhs, int n, const double *alpha, const double *x, double *y,
                            cudaStream_t st);
 void launch_to_f32(size_t n, const double *x, const double *scale, float *y, cudaStream_t st);
+// y[k][i] = x[k][i] * scale[k] for ncol columns of nv values (one launch)
+void launch_to_f32_cols(int ncol, size_t nv, const double *x, const double *scale, float *y, cudaStream_t st);
 
 // Multi-column PCG state kept on the device (one entry per column).
 struct CgCol {

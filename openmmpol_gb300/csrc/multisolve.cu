@@ -311,8 +311,7 @@ int MultiSolver::tick() {
       case kInnerInit: {
         // pcg32_ws's start, with the first r.z kept on the device
         cudaMemcpyAsync(w.dots + cap, w.scal_h + cap, 2 * cap * sizeof(double), cudaMemcpyHostToDevice, st_);
-        for (int k = 0; k < ncol; ++k)
-          gpu::launch_to_f32(nv, w.r + k * nv, w.dots + cap + k, w.r32 + k * nv, st_);
+        gpu::launch_to_f32_cols(ncol, nv, w.r, w.dots + cap, w.r32, st_);
         cudaMemsetAsync(w.x32, 0, ncol * nv * sizeof(float), st_);
         cudaMemsetAsync(w.p32, 0, ncol * nv * sizeof(float), st_);
         cudaMemsetAsync(w.h32, 0, ncol * nv * sizeof(float), st_);

@@ -406,7 +406,7 @@ int System::mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, in
       if (rms[k] >= tol_) eta = std::max(eta, std::min(1e-2, 0.3 * tol_ / rms[k]));
     }
     cudaMemcpyAsync(w.dots + cap, w.scal_h + cap, 2 * cap * sizeof(double), cudaMemcpyHostToDevice, st_);
-    for (int k = 0; k < ncol; ++k) gpu::launch_to_f32(nv, w.r + k * nv, w.dots + cap + k, w.r32 + k * nv, st_);
+    gpu::launch_to_f32_cols(ncol, nv, w.r, w.dots + cap, w.r32, st_);
     // batches of at least 4 columns share one Krylov space (block CG)
     if (block_cg_ && w.t32 && ncol >= 4 && ncol <= gpu::block_cg_max_columns())
       st = bpcg32_ws(w, ncol, 200, eta);

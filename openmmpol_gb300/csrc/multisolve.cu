@@ -275,6 +275,87 @@ int MultiSolver::launch_products(std::vector<Job *> &active) {
   return nlaunch;
 }
 
+// The bookkeeping after a system's product (which 0: the rest of the FP32
+// inner PCG iteration; 1: the refinement residual and its rms), on the
+// engine stream.  It is the same dozen small launches every time for a given
+// system, column count and preconditioner, so it is captured once as a CUDA
+// graph and replayed (one launch instead of a dozen); when the capture
+// fails the launches are made directly.
+void MultiSolver::enqueue_tail(Job &j, int which) {
+  System &s = *j.s;
+  const gpu::DevSites &d = s.d_;
+  const int n = d.n, ncol = j.ncol;
+  const size_t nv = 3 * (size_t)n, C = 3 * (size_t)ncol;
+  Workspace &w = s.ws_;
+  unsigned long long *lo = reinterpret_cast<unsigned long long *>(s.sym_scratch_);
+  unsigned long long *hi = lo + C * n;
+  unsigned long long *bad = reinterpret_cast<unsigned long long *>(s.sym_scratch_ + 3 * C * n);
+  if (which == 0) {
+    float *e = reinterpret_cast<float *>(s.sym_scratch_ + 2 * C * n);
+    gpu::launch_fixed_to_float(C * n, lo, hi, bad, e, st_);
+    gpu::launch_tmu_finish32(d, ncol, e, w.p32, w.h32, st_);
+    // the rest of pcg32_ws's iteration
+    gpu::launch_dots_f32(ncol, nv, w.h32, w.p32, w.partial, st_);
+    gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
+    gpu::launch_cg_alpha(ncol, w.dots, w.cols, 1e-300, st_);
+    gpu::launch_cg_update_f32(ncol, n, w.x32, w.r32, w.p32, w.h32, w.z32, s.alpha32_, w.cols, w.partial, st_);
+    if (s.inner_precond_ == 1 && s.blk_info_) {
+      gpu::launch_block_apply(ncol, n, s.blk_info_, s.blk_minv_, w.r32, w.z32, st_);
+      gpu::launch_dots_f32(ncol, nv, w.r32, w.z32, w.partial, st_);
+    }
+    gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
+    gpu::launch_cg_gnew(ncol, n, w.dots, w.cols, nullptr, 0, st_);
+    gpu::launch_cg_pupdate_f32(ncol, n, w.p32, w.z32, w.cols, st_);
+    cudaMemcpyAsync(w.cols_h, w.cols, ncol * sizeof(gpu::CgCol), cudaMemcpyDeviceToHost, st_);
+  } else {
+    double *e = s.sym_scratch_ + 2 * C * n;
+    gpu::launch_fixed_to_double(C * n, lo, hi, bad, e, st_);
+    gpu::launch_tmu_finish64(d, ncol, e, s.x_, true, w.h, st_);
+    gpu::launch_residual(ncol * nv, s.rhs_, w.h, w.r, st_);
+    gpu::launch_scale_by_alpha(ncol, n, d.pol_alpha, w.r, w.z, st_);
+    gpu::launch_dots(ncol, nv, w.r, w.z, w.partial, st_);
+    gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
+    cudaMemcpyAsync(w.scal_h, w.dots, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  }
+}
+
+void MultiSolver::tail(Job &j, int which) {
+  Workspace &w = j.s->ws_;
+  const int ci = j.ncol - 1;
+  const int prec = (j.s->inner_precond_ == 1 && j.s->blk_info_) ? 1 : 0;
+  cudaGraphExec_t &g = w.ms_tail[which][ci];
+  if (g && w.ms_tail_prec[which][ci] != prec) {
+    cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  if (!g) {
+    cudaGraph_t graph = nullptr;
+    const long long before = gpu::thread_launch_count();
+    if (cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      enqueue_tail(j, which);
+      cudaError_t e = cudaStreamEndCapture(st_, &graph);
+      const long long k = gpu::thread_launch_count() - before;
+      gpu::add_launch_count(-k);  // captured, not launched
+      if (e == cudaSuccess && graph && cudaGraphInstantiate(&g, graph, 0) == cudaSuccess) {
+        w.ms_tail_prec[which][ci] = prec;
+        w.ms_tail_kernels[which][ci] = k;
+      } else {
+        g = nullptr;
+        cudaGetLastError();
+      }
+      if (graph) cudaGraphDestroy(graph);
+    } else {
+      cudaGetLastError();
+    }
+  }
+  if (g) {
+    cudaGraphLaunch(g, st_);
+    gpu::add_launch_count(w.ms_tail_kernels[which][ci]);
+  } else {
+    enqueue_tail(j, which);
+  }
+}
+
 int MultiSolver::tick() {
   {
     std::lock_guard<std::mutex> lk(mu_);
@@ -375,49 +456,20 @@ int MultiSolver::tick() {
     Job &j = *jp;
     if (j.stage != kProduct || j.done < j.items) continue;
     System &s = *j.s;
-    const gpu::DevSites &d = s.d_;
-    const int n = d.n, ncol = j.ncol;
-    const size_t nv = 3 * (size_t)n, C = 3 * (size_t)ncol;
-    Workspace &w = s.ws_;
-    unsigned long long *lo = reinterpret_cast<unsigned long long *>(s.sym_scratch_);
-    unsigned long long *hi = lo + C * n;
-    unsigned long long *bad = reinterpret_cast<unsigned long long *>(s.sym_scratch_ + 3 * C * n);
     if (j.launches > 1) {
       std::lock_guard<std::mutex> lk(mu_);
       stats_.spread_products += 1;
     }
     if (j.kind == kF32) {
-      float *e = reinterpret_cast<float *>(s.sym_scratch_ + 2 * C * n);
-      gpu::launch_fixed_to_float(C * n, lo, hi, bad, e, st_);
-      gpu::launch_tmu_finish32(d, ncol, e, w.p32, w.h32, st_);
       s.stats_.f32_matvecs += 1;
-      // the rest of pcg32_ws's iteration
-      gpu::launch_dots_f32(ncol, nv, w.h32, w.p32, w.partial, st_);
-      gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
-      gpu::launch_cg_alpha(ncol, w.dots, w.cols, 1e-300, st_);
-      gpu::launch_cg_update_f32(ncol, n, w.x32, w.r32, w.p32, w.h32, w.z32, s.alpha32_, w.cols, w.partial, st_);
-      if (s.inner_precond_ == 1 && s.blk_info_) {
-        gpu::launch_block_apply(ncol, n, s.blk_info_, s.blk_minv_, w.r32, w.z32, st_);
-        gpu::launch_dots_f32(ncol, nv, w.r32, w.z32, w.partial, st_);
-      }
-      gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
-      gpu::launch_cg_gnew(ncol, n, w.dots, w.cols, nullptr, 0, st_);
-      gpu::launch_cg_pupdate_f32(ncol, n, w.p32, w.z32, w.cols, st_);
-      cudaMemcpyAsync(w.cols_h, w.cols, ncol * sizeof(gpu::CgCol), cudaMemcpyDeviceToHost, st_);
+      tail(j, 0);
       j.stage = kAwaitInner;
     } else {
-      double *e = s.sym_scratch_ + 2 * C * n;
-      gpu::launch_fixed_to_double(C * n, lo, hi, bad, e, st_);
-      gpu::launch_tmu_finish64(d, ncol, e, s.x_, true, w.h, st_);
       if (j.kind == kDS)
         s.stats_.ds_matvecs += 1;
       else
         s.stats_.f64_matvecs += 1;
-      gpu::launch_residual(ncol * nv, s.rhs_, w.h, w.r, st_);
-      gpu::launch_scale_by_alpha(ncol, n, d.pol_alpha, w.r, w.z, st_);
-      gpu::launch_dots(ncol, nv, w.r, w.z, w.partial, st_);
-      gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
-      cudaMemcpyAsync(w.scal_h, w.dots, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
+      tail(j, 1);
       j.stage = kAwaitCheck;
     }
     j.kind = kNone;

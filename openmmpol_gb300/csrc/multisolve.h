@@ -54,6 +54,8 @@ class MultiSolver {
  private:
   struct Job;
   int launch_products(std::vector<Job *> &active);
+  void enqueue_tail(Job &j, int which);
+  void tail(Job &j, int which);
   void fail(Job &j, int status, const std::string &err);
 
   cudaStream_t st_ = nullptr;

@@ -110,7 +110,7 @@ def parse():
     ap.add_argument("--slots", type=int, default=8, help="s1024: concurrent requests on the GPU")
     ap.add_argument("--hbm-budget-gib", type=float, default=4.0, help="s1024: device memory for systems")
     ap.add_argument("--loads", default="0.5,0.7,0.9", help="s1024: offered loads, fractions of saturation")
-    ap.add_argument("--round-ms", type=float, default=4.0, help="s1024: work per product kind in one engine round")
+    ap.add_argument("--round-ms", type=float, default=1.5, help="s1024: work per product kind in one engine round")
     ap.add_argument("--cached-geometries", action="store_true",
                     help="s1024: map request sizes to 32 cached clusters instead of a fresh geometry per request")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "ommp_gb300_bench"))

@@ -429,7 +429,7 @@ void ommp_gpu_server_stats(void *server, double *out7);
  * products spread over several rounds (zeros in FP64) */
 void ommp_gpu_server_engine_stats(void *server, int64_t *out5);
 /* work per product kind in one round of the engine, in milliseconds of GPU
- * time (default 4): shorter rounds let small systems iterate faster beside
+ * time (default 1.5): shorter rounds let small systems iterate faster beside
  * large ones, longer ones spend less on the per-round bookkeeping */
 int32_t ommp_gpu_server_set_round_ms(void *server, double ms);
 

@@ -20,6 +20,7 @@
 // product is fused into a later addition behind the error-free
 // transformations' back (every intended FMA is an explicit fmaf), and with
 // -ftz=true (the reciprocal-square-root seed is the plain MUFU estimate).
+#include <algorithm>
 #include <cmath>
 
 #include "ds_math.cuh"
@@ -744,11 +745,13 @@ int ds_sym_res(int g, bool amoeba) {
 }
 
 // the item space of one system's product: about 16 items per resident CTA
-void ds_sym_schedule(int n, int g, bool amoeba, int &ntile, int &K, int &chunk, int &nchunk) {
+// (round_pairs > 0: at most a quarter of a CTA's share of round_pairs)
+void ds_sym_schedule(int n, int g, bool amoeba, double round_pairs, int &ntile, int &K, int &chunk, int &nchunk) {
   ntile = (n + DS_TILE - 1) / DS_TILE;
   K = ntile / 2;
   const int ctas_max = ds_sym_res(g, amoeba) * sm_count();
   long long c = (long long)ntile * (K + 1) / (16LL * ctas_max);
+  if (round_pairs > 0.0) c = std::min(c, (long long)(round_pairs / (4.0 * ctas_max * DS_TILE * DS_TILE)));
   if (c < 1) c = 1;
   if (c > K + 1) c = K + 1;
   chunk = (int)c;
@@ -766,10 +769,10 @@ void launch_ds_sym_table(const DsSymTable &tab, unsigned *next, cudaStream_t st)
 }
 }  // namespace
 
-int tmu_ds_sym_items(const DevSites &s, int g) {
+int tmu_ds_sym_items(const DevSites &s, int g, double round_pairs) {
   if (s.n == 0) return 0;
   int ntile, K, chunk, nchunk;
-  ds_sym_schedule(s.n, g, s.amoeba, ntile, K, chunk, nchunk);
+  ds_sym_schedule(s.n, g, s.amoeba, round_pairs, ntile, K, chunk, nchunk);
   return ntile * nchunk;
 }
 
@@ -784,7 +787,7 @@ void launch_tmu_ds_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, un
     j.boxes = s.tile_box32, j.x = static_cast<const double *>(sl[k].x);
     j.lo = sl[k].lo, j.hi = sl[k].hi, j.bad = sl[k].bad;
     j.n = s.n;
-    ds_sym_schedule(s.n, g, amoeba, j.ntile, j.K, j.chunk, j.nchunk);
+    ds_sym_schedule(s.n, g, amoeba, sl[k].round_pairs, j.ntile, j.K, j.chunk, j.nchunk);
     j.item0 = sl[k].item0;
     j.thr = s.damp_thr;
     j.thr2m = (float)(s.damp_thr * s.damp_thr * (1.0 + 1e-5));

@@ -19,6 +19,7 @@
 //                    (src/mod_polarization.F90:459-504).
 // Source tiles are staged in shared memory by the whole CTA with coalesced
 // loads and broadcast to all threads; each thread owns one target site.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -1168,12 +1169,17 @@ int sym_resident() {
 }
 
 // work items: about 16 per resident CTA, each a tile and a chunk of its slots
-SymPlan sym_plan(int n, int ctas) {
+// (round_pairs > 0: at most a quarter of a CTA's share of round_pairs)
+SymPlan sym_plan(int n, int ctas, double round_pairs) {
   SymPlan p;
   p.ntile = (n + SYM_TILE - 1) / SYM_TILE;
   p.K = p.ntile / 2;
   const long long units = (long long)p.ntile * (p.K + 1);
   long long chunk = units / (16LL * ctas);
+  if (round_pairs > 0.0) {
+    const long long cap = (long long)(round_pairs / (4.0 * ctas * SYM_TILE * SYM_TILE));
+    chunk = std::min(chunk, cap);
+  }
   if (chunk < 1) chunk = 1;
   if (chunk > p.K + 1) chunk = p.K + 1;
   p.chunk = (int)chunk;
@@ -1200,9 +1206,9 @@ void launch_sym64_table(const Sym64Table &tab, unsigned *next, cudaStream_t st) 
 }
 }  // namespace
 
-int tmu_f64_sym_items(const DevSites &s, int g) {
+int tmu_f64_sym_items(const DevSites &s, int g, double round_pairs) {
   if (s.n == 0) return 0;
-  return sym_plan(s.n, sym64_resident(g, s.amoeba) * sm_count()).nitems;
+  return sym_plan(s.n, sym64_resident(g, s.amoeba) * sm_count(), round_pairs).nitems;
 }
 
 void launch_tmu_f64_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st) {
@@ -1211,7 +1217,7 @@ void launch_tmu_f64_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, u
   for (int k = 0; k < nsl && tab.njobs < kMaxSymSlices; ++k) {
     const DevSites &s = *sl[k].s;
     if (sl[k].count <= 0 || s.n == 0) continue;
-    const SymPlan p = sym_plan(s.n, sym64_resident(g, amoeba) * sm_count());
+    const SymPlan p = sym_plan(s.n, sym64_resident(g, amoeba) * sm_count(), sl[k].round_pairs);
     Sym64Job &j = tab.job[tab.njobs];
     j.pos = s.pol_pos, j.damp = s.pol_a, j.wa = s.pol_wa32, j.x = static_cast<const double *>(sl[k].x);
     j.lo = sl[k].lo, j.hi = sl[k].hi, j.bad = sl[k].bad;

@@ -112,25 +112,31 @@ int tmu32_sym_resident(int g, bool amoeba);
 // fixed per system and product kind (*_sym_items), so that a product may be
 // spread over several launches; its fixed-point accumulators [g][n][3] and
 // error flag are zeroed by the caller before the first share.
+// round_pairs: the pairs one round of a caller that spreads products over
+// launches spends on this product kind; items are then cut to about a
+// quarter of a resident CTA's share of such a round, so that a round keeps
+// every CTA busy (0: items sized for one launch of the whole product).  The
+// value is part of the item space and stays fixed for a product.
 struct SymSlice {
   const DevSites *s;
   const void *x;  // [g][n][3]: float for the FP32 product, double otherwise
   unsigned long long *lo, *hi, *bad;
   int item0, count;
+  double round_pairs = 0.0;
 };
 constexpr int kMaxSymSlices = 32;  // systems per launch
-int tmu32_sym_items(const DevSites &s, int g);
+int tmu32_sym_items(const DevSites &s, int g, double round_pairs = 0.0);
 // next: a device counter of the launch (zeroed by the launcher)
 void launch_tmu32_sym_multi(int g, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st);
 void launch_fixed_to_float(size_t total, const unsigned long long *lo, const unsigned long long *hi,
                            const unsigned long long *bad, float *out, cudaStream_t st);
 // FP64 symmetric product (g = 1, 2 or 4; one damping kind per launch)
-int tmu_f64_sym_items(const DevSites &s, int g);
+int tmu_f64_sym_items(const DevSites &s, int g, double round_pairs = 0.0);
 void launch_tmu_f64_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st);
 void launch_fixed_to_double(size_t total, const unsigned long long *lo, const unsigned long long *hi,
                             const unsigned long long *bad, double *out, cudaStream_t st);
 // double-single symmetric product (g = 1 or 2; one damping kind per launch)
-int tmu_ds_sym_items(const DevSites &s, int g);
+int tmu_ds_sym_items(const DevSites &s, int g, double round_pairs = 0.0);
 void launch_tmu_ds_sym_multi(int g, bool amoeba, const SymSlice *sl, int nsl, unsigned *next, cudaStream_t st);
 void launch_tmu32_pairs(const DevSites &s, int g, const float *x, float *partial, int nsplit, cudaStream_t st);
 // source splits an FP32 scratch must hold (per column) for every shape the

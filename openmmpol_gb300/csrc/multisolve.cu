@@ -16,11 +16,14 @@
 //     product) and column width: a persistent kernel whose work items are
 //     (system, super-tile, chunk of slots), taken in order from one counter
 //     (the launch_*_sym_multi kernels);
-//   * a product gets a bounded share of each round (about 4 ms of work per
+//   * a product gets a bounded share of each round (about 1.5 ms of work per
 //     kind by default, set_round_ms: a fair share per system first, then the
 //     shortest products), so
 //     small systems finish their iterations while a large system's product
 //     is spread over several rounds; its fixed-point sums simply continue;
+//     work items are cut to a quarter of a resident CTA's share of a round
+//     (SymSlice::round_pairs), so that every CTA stays busy for the whole
+//     round whatever the systems' sizes;
 //   * after the launches, every system whose product completed runs its CG
 //     bookkeeping (finishing pass, dots, updates, convergence flags) on the
 //     same stream, and one synchronisation per round brings the flags to
@@ -67,6 +70,7 @@ struct MultiSolver::Job {
   bool copy_p = false, guess = false;
   int stage = kStart;
   int kind = kNone, items = 0, done = 0, launches = 0;
+  double round_pairs = 0.0;  // item size of the product in flight (SymSlice::round_pairs)
   int outer = 0, inner = 0;
   double eta = 1e-5;
   int status = kOk;
@@ -152,6 +156,11 @@ void MultiSolver::set_round_ms(double ms) {
   if (ms > 0.0 && std::isfinite(ms)) round_ms_ = ms;
 }
 
+double MultiSolver::round_pairs(int kind) {
+  std::lock_guard<std::mutex> lk(mu_);
+  return kPairsPerMs[kind] * round_ms_;
+}
+
 bool MultiSolver::idle() {
   std::lock_guard<std::mutex> lk(mu_);
   return pending_.empty() && jobs_.empty();
@@ -197,7 +206,7 @@ int MultiSolver::launch_products(std::vector<Job *> &active) {
       const double n = j->s->d_.n;
       return std::max(1.0, 0.5 * n * (n - 1.0) / std::max(1, j->items));
     };
-    const double budget = kPairsPerMs[kind] * round_ms_;
+    const double budget = round_pairs(kind);
     double used = 0.0;
     const double share = budget / js.size();
     for (Job *j : js) {
@@ -252,7 +261,7 @@ int MultiSolver::launch_products(std::vector<Job *> &active) {
         unsigned long long *lo = reinterpret_cast<unsigned long long *>(s->sym_scratch_);
         const void *x = j->kind == kF32 ? static_cast<const void *>(s->ws_.p32) : static_cast<const void *>(s->x_);
         sl.push_back({&s->d_, x, lo, lo + C * n, reinterpret_cast<unsigned long long *>(s->sym_scratch_ + 3 * C * n),
-                      j->done, take[j]});
+                      j->done, take[j], j->round_pairs});
       }
       const int g = kv.first.g;
       if (kv.first.kind == kF32)
@@ -377,7 +386,9 @@ int MultiSolver::tick() {
         if (j.guess) {
           j.stage = kProduct;
           j.kind = s.precision_ == kPrecMixedDS ? kDS : kF64;
-          j.items = j.kind == kDS ? gpu::tmu_ds_sym_items(d, ncol) : gpu::tmu_f64_sym_items(d, ncol);
+          j.round_pairs = round_pairs(j.kind);
+          j.items = j.kind == kDS ? gpu::tmu_ds_sym_items(d, ncol, j.round_pairs)
+                                  : gpu::tmu_f64_sym_items(d, ncol, j.round_pairs);
           j.done = j.launches = 0;
         } else {
           cudaMemcpyAsync(w.r, s.rhs_, ncol * nv * sizeof(double), cudaMemcpyDeviceToDevice, st_);
@@ -413,7 +424,8 @@ int MultiSolver::tick() {
         gpu::launch_cg_init(ncol, w.dots, w.cols, j.eta, st_);
         j.stage = kProduct;
         j.kind = kF32;
-        j.items = gpu::tmu32_sym_items(d, ncol);
+        j.round_pairs = round_pairs(kF32);
+        j.items = gpu::tmu32_sym_items(d, ncol, j.round_pairs);
         j.done = j.launches = 0;
         j.inner = 1;
         work = true;
@@ -423,7 +435,9 @@ int MultiSolver::tick() {
         gpu::launch_ir_accumulate(ncol, n, s.x_, w.x32, w.dots + 2 * cap, st_);
         j.stage = kProduct;
         j.kind = s.precision_ == kPrecMixedDS ? kDS : kF64;
-        j.items = j.kind == kDS ? gpu::tmu_ds_sym_items(d, ncol) : gpu::tmu_f64_sym_items(d, ncol);
+        j.round_pairs = round_pairs(j.kind);
+        j.items = j.kind == kDS ? gpu::tmu_ds_sym_items(d, ncol, j.round_pairs)
+                                : gpu::tmu_f64_sym_items(d, ncol, j.round_pairs);
         j.done = j.launches = 0;
         ++j.outer;
         work = true;
@@ -523,7 +537,8 @@ int MultiSolver::tick() {
       if (any && j.inner < kMaxInner) {
         j.stage = kProduct;
         j.kind = kF32;
-        j.items = gpu::tmu32_sym_items(s.d_, ncol);
+        j.round_pairs = round_pairs(kF32);
+        j.items = gpu::tmu32_sym_items(s.d_, ncol, j.round_pairs);
         j.done = j.launches = 0;
         ++j.inner;
       } else {

@@ -55,6 +55,7 @@ class MultiSolver {
   struct Job;
   int launch_products(std::vector<Job *> &active);
   void enqueue_tail(Job &j, int which);
+  double round_pairs(int kind);  // pairs of one round's budget for a product kind
   void tail(Job &j, int which);
   void fail(Job &j, int status, const std::string &err);
 
@@ -65,7 +66,7 @@ class MultiSolver {
   std::vector<Job *> jobs_;       // in rounds (engine thread only)
   std::map<long long, Job *> done_;
   long long next_id_ = 0;
-  double round_ms_ = 4.0;
+  double round_ms_ = 1.5;
   Stats stats_;
 };
 

@@ -24,6 +24,7 @@
 //
 // The symmetric form (k_tmu32_sym, further down) evaluates each unordered
 // pair once and accumulates both directions, as the FP64 product does.
+#include <algorithm>
 #include <cmath>
 
 #include "kernels.h"
@@ -578,11 +579,13 @@ int s32_resident() {
 
 // the item space of one system's product: super-tiles x chunks of slots,
 // about 16 items per resident CTA of the whole GPU
-void s32_schedule(int n, int g, int &ntile, int &K, int &chunk, int &nchunk) {
+void s32_schedule(int n, int g, double round_pairs, int &ntile, int &K, int &chunk, int &nchunk) {
   ntile = (n + S32_TILE - 1) / S32_TILE;
   K = ntile / 2;
   const int ctas_max = (g == 2 ? s32_resident<2>() : s32_resident<1>()) * sm_count();
   long long c = (long long)ntile * (K + 1) / (16LL * ctas_max);
+  // round_pairs > 0: at most a quarter of a CTA's share of round_pairs
+  if (round_pairs > 0.0) c = std::min(c, (long long)(round_pairs / (4.0 * ctas_max * S32_TILE * S32_TILE)));
   if (c < 1) c = 1;
   if (c > K + 1) c = K + 1;
   chunk = (int)c;
@@ -600,7 +603,7 @@ void launch_s32_table(const S32Table &tab, unsigned *next, cudaStream_t st) {
 }
 
 void fill_s32_job(S32Job &j, const DevSites &s, int g, const float *x, unsigned long long *lo,
-                  unsigned long long *hi, unsigned long long *bad, int item0) {
+                  unsigned long long *hi, unsigned long long *bad, int item0, double round_pairs) {
   j.pos = s.pol_pos32;
   j.damp = s.pol_a32;
   j.boxes = s.tile_box32;
@@ -608,7 +611,7 @@ void fill_s32_job(S32Job &j, const DevSites &s, int g, const float *x, unsigned 
   j.lo = lo, j.hi = hi, j.bad = bad;
   j.n = s.n;
   j.nbox = s.ntile;
-  s32_schedule(s.n, g, j.ntile, j.K, j.chunk, j.nchunk);
+  s32_schedule(s.n, g, round_pairs, j.ntile, j.K, j.chunk, j.nchunk);
   j.item0 = item0;
   j.amoeba = s.amoeba ? 1 : 0;
   j.thr = (float)s.damp_thr;
@@ -619,10 +622,10 @@ void fill_s32_job(S32Job &j, const DevSites &s, int g, const float *x, unsigned 
 
 int tmu32_sym_resident(int g, bool) { return g == 2 ? s32_resident<2>() : s32_resident<1>(); }
 
-int tmu32_sym_items(const DevSites &s, int g) {
+int tmu32_sym_items(const DevSites &s, int g, double round_pairs) {
   if (s.n == 0) return 0;
   int ntile, K, chunk, nchunk;
-  s32_schedule(s.n, g, ntile, K, chunk, nchunk);
+  s32_schedule(s.n, g, round_pairs, ntile, K, chunk, nchunk);
   return ntile * nchunk;
 }
 
@@ -632,7 +635,7 @@ void launch_tmu32_sym_multi(int g, const SymSlice *sl, int nsl, unsigned *next, 
   for (int k = 0; k < nsl && tab.njobs < kMaxSymSlices; ++k) {
     if (sl[k].count <= 0 || sl[k].s->n == 0) continue;
     fill_s32_job(tab.job[tab.njobs], *sl[k].s, g, static_cast<const float *>(sl[k].x), sl[k].lo, sl[k].hi,
-                 sl[k].bad, sl[k].item0);
+                 sl[k].bad, sl[k].item0, sl[k].round_pairs);
     tab.base[tab.njobs] = total;
     total += sl[k].count;
     ++tab.njobs;

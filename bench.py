@@ -63,6 +63,13 @@ FLOP_PER_PAIR = 45.0  # per ordered T.mu pair and right-hand side (conventional 
 # conversions and the damping pre-test run on other pipes
 FP64_SYM_OPS_PER_PAIR = 32.0
 SYM_MIN_SITES = 2048  # the engine's automatic choice of the symmetric product
+# FP32 lane operations (an FMA counts once, a paired instruction twice) per
+# unordered pair and right-hand side of the symmetric FP32 product
+# (k_tmu32_sym, openmmpol_gb300/csrc/tmu32.cu): 3 coordinate differences, r^2
+# (3), r^-2 / r^-3 / r^-5 (3), -r^-3/3 for the source side (1) and per
+# direction mu.d (3), the field factor (1) and six accumulations (6); the
+# reciprocal square root runs on the MUFU
+FP32_SYM_OPS_PER_PAIR = 30.0
 # FP32 operations (an FMA counts once) per undamped ordered pair of the
 # double-single kernel, counted in openmmpol_gb300/csrc/ds_kernels.cu: 3 coordinate differences
 # (33), r^2 (31), reciprocal square root (17 + 1 MUFU), r^-2 / r^-3 / 3 r^-5
@@ -312,8 +319,9 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def kernel_table(kst, n, peak64, peak32):
-    """Per pair kernel: launches, columns, time and the rate against its pipe."""
+def kernel_table(kst, n, peak64, peak32, fp32_shape=None):
+    """Per pair kernel: launches, columns, time and the rate against its pipe.
+    fp32_shape: the autotuned FP32 launch shape of one column, if known."""
     pairs = float(n) * (n - 1)
     out = {}
     for name, (cnt, ms, cols), pk in (("tmu_fp64", kst[0], peak64), ("tmu_fp32", kst[1], peak32),
@@ -330,6 +338,15 @@ def kernel_table(kst, n, peak64, peak32):
             ops = FP64_SYM_OPS_PER_PAIR * pairs / 2 * cols / (ms * 1e-3) / 1e12
             out[name].update({"fp64_flop_equivalent_tflops": ach, "achieved_tops": ops, "peak_tops": pk / 2,
                               "frac": ops / (pk / 2) if pk else None})
+        if name == "tmu_fp32" and fp32_shape is not None:
+            out[name]["kernel"] = fp32_shape[0]
+            if fp32_shape[0] == "symmetric":
+                # FP32 lanes: operations of the symmetric product per second
+                # against the FMA-pipe lane rate (peak flop / 2)
+                ops = FP32_SYM_OPS_PER_PAIR * pairs / 2 * cols / (ms * 1e-3) / 1e12
+                out[name].update({"conventional_tflops": ach, "achieved_tops": ops, "peak_tops": pk / 2,
+                                  "frac": ops / (pk / 2) if pk else None, "peak_nominal_tops": 40.3,
+                                  "frac_nominal": ops / 40.3})
         if name == "tmu_ds":
             # FP32 pipe: double-single operations issued per second against
             # the FMA-pipe instruction rate (peak flop / 2)
@@ -589,7 +606,7 @@ def run_gb300(args):
             t = torch.tensor([total_ms], dtype=torch.float64)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             total_ms = float(t.item())
-        kstats = kernel_table(kst, n, peak64.value, peak32.value)
+        kstats = kernel_table(kst, n, peak64.value, peak32.value, sys_.fp32_shape(1))
         res = {"value": ws * K / (total_ms * 1e-3), "ms_per_step": total_ms / K, "steps_ms": step_ms,
                "solver_counters_per_step": counters, "gpu_launches": int(launches), "wall_s_timed": wall,
                "clocks": clocks, "kernels": kstats, "roofline": roofline_of(kstats, total_ms, n),

@@ -298,6 +298,10 @@ int32_t ommp_gpu_field_ext(OMMP_SYSTEM_PRT s, int32_t which, int32_t n, const do
  * unordered pair once for both directions, tile-classified, deterministic
  * fixed-point sums) */
 int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
+/* the FP32 launch shape the autotuner chose for ncol columns: shape[0] the
+ * kernel (1, 2 or 3 as above), shape[1] the columns per launch, shape[2] the
+ * source splits; zeros before the first mixed solve with ncol columns */
+int32_t ommp_gpu_get_fp32_shape(OMMP_SYSTEM_PRT s, int32_t ncol, int32_t *shape);
 /* preconditioner of the FP32 inner solver of the mixed modes: 0 the
  * reference's diagonal (alpha), 1 block Jacobi over runs of bonded sites
  * (default).  The FP64 solver and the outer convergence test always use the

@@ -359,6 +359,16 @@ class OMMPSystem:
         m = {"auto": 0, "pairwise": 1, "tiled": 2, "symmetric": 3}.get(mode, mode)
         _check(self._L.ommp_gpu_set_fp32_kernel(self._h, int(m)))
 
+    def fp32_shape(self, ncol: int = 1):
+        """The autotuned FP32 launch shape for ncol columns: (kernel, columns
+        per launch, source splits) with kernel 'pairwise' | 'tiled' |
+        'symmetric', or None before the first mixed solve with ncol columns."""
+        out = (C.c_int32 * 3)()
+        _check(self._L.ommp_gpu_get_fp32_shape(self._h, int(ncol), out))
+        if out[0] == 0:
+            return None
+        return ({1: "pairwise", 2: "tiled", 3: "symmetric"}[out[0]], int(out[1]), int(out[2]))
+
     def clear_guess(self) -> None:
         self._L.ommp_gpu_clear_guess(self._h)
 

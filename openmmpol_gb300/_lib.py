@@ -63,6 +63,7 @@ SIGNATURES = {
     "ommp_gpu_set_precision": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_fp64_kernel": (C.c_int32, [_vp, C.c_int32]),
     "ommp_gpu_set_fp32_kernel": (C.c_int32, [_vp, C.c_int32]),
+    "ommp_gpu_get_fp32_shape": (C.c_int32, [_vp, C.c_int32, C.POINTER(C.c_int32)]),
     "ommp_gpu_set_inner_preconditioner": (C.c_int32, [_vp, C.c_int32]),
     "ommp_gpu_set_inner_blocks": (C.c_int32, [_vp, C.c_int32, C.c_double]),
     "ommp_gpu_potential_ext": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp, _dp]),

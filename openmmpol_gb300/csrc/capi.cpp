@@ -247,6 +247,9 @@ void ommp_gpu_set_solver_maxiter(OMMP_SYSTEM_PRT s, int32_t n) { S(s)->set_maxit
 void ommp_gpu_set_precision(OMMP_SYSTEM_PRT s, int32_t mode) { S(s)->set_precision(mode); }
 int32_t ommp_gpu_set_fp64_kernel(OMMP_SYSTEM_PRT s, int32_t mode) { return S(s)->set_fp64_kernel(mode); }
 int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode) { return S(s)->set_fp32_kernel(mode); }
+int32_t ommp_gpu_get_fp32_shape(OMMP_SYSTEM_PRT s, int32_t ncol, int32_t *shape) {
+  return S(s)->fp32_shape(ncol, shape);
+}
 int32_t ommp_gpu_set_inner_preconditioner(OMMP_SYSTEM_PRT s, int32_t mode) {
   return S(s)->set_inner_preconditioner(mode);
 }

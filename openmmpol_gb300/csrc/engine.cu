@@ -998,6 +998,18 @@ int System::set_fp32_kernel(int mode) {
   return kOk;
 }
 
+int System::fp32_shape(int ncol, int32_t *shape) const {
+  if (!shape) {
+    set_last_error("fp32_shape: null output");
+    return kErrBadArg;
+  }
+  const auto it = f32_tune_.find(ncol);
+  shape[0] = it == f32_tune_.end() ? 0 : it->second.kver;
+  shape[1] = it == f32_tune_.end() ? 0 : it->second.g;
+  shape[2] = it == f32_tune_.end() ? 0 : it->second.nsplit;
+  return kOk;
+}
+
 int System::set_default_solver(int s) {
   if (s != kSolverCG && s != kSolverInversion && s != kSolverDIIS) {
     set_last_error("Unrecognized setting for default solver method");

@@ -153,6 +153,7 @@ class System {
   // pairs (target-outer), 2 symmetric (unordered pairs)
   int set_fp64_kernel(int mode);
   int set_fp32_kernel(int mode);
+  int fp32_shape(int ncol, int32_t *shape) const;
   int set_inner_preconditioner(int mode);
   // runs of the block-Jacobi inner preconditioner: at most max_sites
   // consecutive polarizable sites, each within link_bohr of an earlier one

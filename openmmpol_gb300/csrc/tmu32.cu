@@ -223,24 +223,37 @@ void launch_g(const DevSites &s, const float *x, float *partial, int nsplit, cud
 // Symmetric FP32 operator.  The ordered kernel above spends ~20 FP32
 // instructions per ordered pair, half of them on the geometry (differences,
 // r^2, powers), which T_ij = T_ji lets two directions share.  Here every
-// unordered pair is evaluated once: 9 geometry instructions and 10 per
+// unordered pair is evaluated once: 9 geometry operations and 10 per
 // direction (mu.d, the field factor, six accumulations), 29 in all instead of
 // 40, on the half-shell schedule of the symmetric FP64 product (super-tile I
 // meets the slots k = 0..ntile/2 of J = I + k, handed out by an atomic
 // counter to a persistent grid).
 //
+// The arithmetic runs on pairs of sources with the paired FP32 instructions
+// of sm_100 and later (__fadd2_rn, __fmul2_rn, __ffma2_rn: two FP32 lanes
+// per instruction), so that 29 paired operations serve two pairs and the
+// kernel, which with scalar instructions was bound by instruction issue
+// (77 % issue activity, FMA pipe 65 %), issues about half as many
+// instructions per pair.  Only the reciprocal square root (and the damping
+// of near pairs) stays per lane.
+//
 // Per CTA 128 threads own a super-tile of 256 targets, two per thread (lanes
-// l and l + 32 of a 64-target warp slice), so that each source read from
-// shared memory feeds two pairs.  A warp pairs its targets with each 32-site
-// sub-tile of J in 32 rotation steps: at step t lane l meets source
-// (l + t) mod 32 and the source-side sums travel one lane per step by
-// shuffle (three per column and step, 1.5 per pair).  Every sub-tile is
-// staged twice in a row, so the lane's read address is its base plus t with
-// no wrap-around, an immediate offset.  The target side keeps the field's two
-// sums (f d and k3 mu, f = k5 mu.d) and applies the factor 3 once per slot;
-// the source side uses its own dipoles divided by 3 (held in registers), so
-// g d - k3 mu/3 needs no extra instruction and the factor 3 is applied when
-// the four warps' sums are combined in shared memory.
+// l and l + 32 of a 64-target warp slice).  J is staged as four sub-tiles of
+// 64 sources, each as 32 source pairs (sources p and p + 32 of the sub-tile)
+// in float4 records of two fields each ({f_a, f_b, g_a, g_b}: x, y, z, then
+// mx, my, mz per column), every record twice in a row.  A warp meets a
+// sub-tile in 32 rotation steps: at step t lane l takes pair (l + t) mod 32
+// from its base address plus t (an immediate offset, no wrap-around) and
+// evaluates it against both its targets (four pairs per step); the pair's
+// source-side sums travel one lane per step by shuffle (two per component,
+// 1.5 per pair).  The target side keeps the field's two sums (f d and k3 mu,
+// f = k5 mu.d, each as a pair of partial sums over the two halves) and
+// applies the factor 3 once per slot; the source side accumulates
+// g d - (k3/3) mu (one extra product for -k3/3 per target and pair, where
+// a second set of target dipoles would cost 12 registers per column) and
+// the factor 3 is applied when the four warps' sums are combined.  The
+// targets' compensated cross-slot sums live in shared memory.  The
+// differences are taken as source minus target: every term is even in d.
 //
 // Slots whose tile boxes are farther apart than the damping range run an
 // undamped loop; near slots and the diagonal slot (target side only, all
@@ -252,15 +265,23 @@ void launch_g(const DevSites &s, const float *x, float *partial, int nsplit, cud
 // ---------------------------------------------------------------------------
 constexpr int S32_TPB = 128;
 constexpr int S32_TILE = 256;
-constexpr int S32_SUB = 32;
+constexpr int S32_SUB = 64;  // sources per sub-tile (32 pairs)
 constexpr int S32_NSUB = S32_TILE / S32_SUB;
 constexpr float S32_FAR = 1.0e15f;
 
+// float4 records per source pair: fields x, y, z, then mx, my, mz of each
+// column, two fields per record
+template <int G>
+__host__ __device__ constexpr int s32_records() {
+  return (3 + 3 * G + 1) / 2;
+}
+
 template <int G>
 struct S32Smem {
-  float4 pos[S32_NSUB][2 * S32_SUB];    // each sub-tile twice in a row
-  float4 mu[G][S32_NSUB][2 * S32_SUB];  // x, y, z; w = damping a of the source
-  float accj[4][3 * G][S32_TILE];       // source-side sums of the four warps
+  float4 rec[s32_records<G>()][S32_NSUB][2 * 32];  // each pair twice in a row
+  float4 thole[S32_NSUB][2 * 32];                  // {w_a, w_b, a_a, a_b}: Thole factor, damping a
+  float accj[4][3 * G][S32_TILE];                  // source-side sums of the four warps
+  float sum[2][3 * G][S32_TPB], cmp[2][3 * G][S32_TPB];  // targets' compensated sums over slots
 };
 
 // fixed_add (pair_math.cuh) for an FP32 value, with integer operations only:
@@ -310,83 +331,105 @@ __device__ __forceinline__ void box_of_supertile(const float4 *__restrict__ boxe
   }
 }
 
+// a target's values as lane pairs, the same value in both halves
+struct S32Target {
+  float2 nx, ny, nz;  // minus the position
+  float w, a;         // Thole factor and damping a (near slots)
+  int idx;            // index in the super-tile
+};
+
 // one slot: the warp's 64 targets against the 256 staged sources.  The far
 // loop is unrolled by 8 and the near one not at all: fully unrolled, the two
 // loops overflowed the instruction cache (ncu: issue stalled on instruction
 // fetch, 44 % issue activity).
 template <bool NEAR, bool AMOEBA, int G>
-__device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, int lane,
-                                         const float4 (&pt)[2], const float (&at)[2], const float (&mt)[2][3 * G],
-                                         const float (&mt3)[2][3 * G], const int (&pl)[2], float thr,
-                                         float (&af)[2][3 * G], float (&ak)[2][3 * G]) {
-  constexpr int C = 3 * G;
+__device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, int lane, const S32Target (&tg)[2],
+                                         const float2 (&mt)[2][3 * G], float thr,
+                                         float2 (&af)[2][3 * G], float2 (&ak)[2][3 * G]) {
+  constexpr int C = 3 * G, R = s32_records<G>();
   const int src = (lane + 1) & 31;
   const bool source_side = !NEAR || !diag;
 #pragma unroll 1
   for (int js = 0; js < S32_NSUB; ++js) {
-    float aj[C];
+    float2 aj[C];
 #pragma unroll
-    for (int c = 0; c < C; ++c) aj[c] = 0.f;
-    const float4 *pb = &sm.pos[js][lane];
-    const float4 *mb[G];
-#pragma unroll
-    for (int col = 0; col < G; ++col) mb[col] = &sm.mu[col][js][lane];
+    for (int c = 0; c < C; ++c) aj[c] = make_float2(0.f, 0.f);
     auto step = [&](int t) {
-      const float4 ps = pb[t];
-      float4 m[G];
+      float2 f[2 * R];  // x, y, z, mx, my, mz, ... of the pair
 #pragma unroll
-      for (int col = 0; col < G; ++col) m[col] = mb[col][t];
+      for (int r = 0; r < R; ++r) {
+        const float4 v = sm.rec[r][js][lane + t];
+        f[2 * r] = make_float2(v.x, v.y);
+        f[2 * r + 1] = make_float2(v.z, v.w);
+      }
+      float4 th;
+      if (NEAR) th = sm.thole[js][lane + t];
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
-        const float dx = pt[u].x - ps.x, dy = pt[u].y - ps.y, dz = pt[u].z - ps.z;
-        float k3, k5;
+        const float2 dx = __fadd2_rn(f[0], tg[u].nx), dy = __fadd2_rn(f[1], tg[u].ny),
+                     dz = __fadd2_rn(f[2], tg[u].nz);
+        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+        float2 k3, k5;
         if (NEAR) {
           // the self pair of the diagonal slot contributes nothing
-          const bool self = diag && (js * S32_SUB + ((lane + t) & 31)) == pl[u];
-          const float r2 = self ? 1.f : fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          damped_factors<AMOEBA>(r2, pt[u].w, ps.w, at[u], m[0].w, thr, k3, k5);
-          if (self) k3 = k5 = 0.f;
+          const int p = (lane + t) & 31;
+          const bool self_a = diag && js * S32_SUB + p == tg[u].idx;
+          const bool self_b = diag && js * S32_SUB + 32 + p == tg[u].idx;
+          damped_factors<AMOEBA>(self_a ? 1.f : r2.x, tg[u].w, th.x, tg[u].a, th.z, thr, k3.x, k5.x);
+          damped_factors<AMOEBA>(self_b ? 1.f : r2.y, tg[u].w, th.y, tg[u].a, th.w, thr, k3.y, k5.y);
+          if (self_a) k3.x = k5.x = 0.f;
+          if (self_b) k3.y = k5.y = 0.f;
         } else {
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const float rinv = rsqrtf(r2);
-          const float ir2 = rinv * rinv;
-          k3 = rinv * ir2;
-          k5 = k3 * ir2;
+          const float2 rinv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+          const float2 ir2 = __fmul2_rn(rinv, rinv);
+          k3 = __fmul2_rn(rinv, ir2);
+          k5 = __fmul2_rn(k3, ir2);
         }
+        float2 k3n;
+        if (source_side) k3n = __fmul2_rn(k3, make_float2(-1.f / 3.f, -1.f / 3.f));
 #pragma unroll
         for (int col = 0; col < G; ++col) {
-          const float f = k5 * fmaf(m[col].x, dx, fmaf(m[col].y, dy, m[col].z * dz));
-          af[u][3 * col + 0] = fmaf(f, dx, af[u][3 * col + 0]);
-          af[u][3 * col + 1] = fmaf(f, dy, af[u][3 * col + 1]);
-          af[u][3 * col + 2] = fmaf(f, dz, af[u][3 * col + 2]);
-          ak[u][3 * col + 0] = fmaf(k3, m[col].x, ak[u][3 * col + 0]);
-          ak[u][3 * col + 1] = fmaf(k3, m[col].y, ak[u][3 * col + 1]);
-          ak[u][3 * col + 2] = fmaf(k3, m[col].z, ak[u][3 * col + 2]);
+          const float2 mx = f[3 + 3 * col], my = f[4 + 3 * col], mz = f[5 + 3 * col];
+          const float2 fs = __fmul2_rn(k5, __ffma2_rn(mx, dx, __ffma2_rn(my, dy, __fmul2_rn(mz, dz))));
+          af[u][3 * col + 0] = __ffma2_rn(fs, dx, af[u][3 * col + 0]);
+          af[u][3 * col + 1] = __ffma2_rn(fs, dy, af[u][3 * col + 1]);
+          af[u][3 * col + 2] = __ffma2_rn(fs, dz, af[u][3 * col + 2]);
+          ak[u][3 * col + 0] = __ffma2_rn(k3, mx, ak[u][3 * col + 0]);
+          ak[u][3 * col + 1] = __ffma2_rn(k3, my, ak[u][3 * col + 1]);
+          ak[u][3 * col + 2] = __ffma2_rn(k3, mz, ak[u][3 * col + 2]);
           if (source_side) {
-            const float g = k5 * fmaf(mt[u][3 * col], dx, fmaf(mt[u][3 * col + 1], dy, mt[u][3 * col + 2] * dz));
-            aj[3 * col + 0] = fmaf(g, dx, fmaf(-k3, mt3[u][3 * col + 0], aj[3 * col + 0]));
-            aj[3 * col + 1] = fmaf(g, dy, fmaf(-k3, mt3[u][3 * col + 1], aj[3 * col + 1]));
-            aj[3 * col + 2] = fmaf(g, dz, fmaf(-k3, mt3[u][3 * col + 2], aj[3 * col + 2]));
+            const float2 g = __fmul2_rn(
+                k5, __ffma2_rn(mt[u][3 * col], dx,
+                               __ffma2_rn(mt[u][3 * col + 1], dy, __fmul2_rn(mt[u][3 * col + 2], dz))));
+            aj[3 * col + 0] = __ffma2_rn(g, dx, __ffma2_rn(k3n, mt[u][3 * col + 0], aj[3 * col + 0]));
+            aj[3 * col + 1] = __ffma2_rn(g, dy, __ffma2_rn(k3n, mt[u][3 * col + 1], aj[3 * col + 1]));
+            aj[3 * col + 2] = __ffma2_rn(g, dz, __ffma2_rn(k3n, mt[u][3 * col + 2], aj[3 * col + 2]));
           }
         }
       }
       if (source_side) {
-        // the sums of source s move to the lane that meets s next
+        // the sums of pair p move to the lane that meets p next
 #pragma unroll
-        for (int c = 0; c < C; ++c) aj[c] = __shfl_sync(0xffffffffu, aj[c], src);
+        for (int c = 0; c < C; ++c) {
+          aj[c].x = __shfl_sync(0xffffffffu, aj[c].x, src);
+          aj[c].y = __shfl_sync(0xffffffffu, aj[c].y, src);
+        }
       }
     };
     if (NEAR) {
 #pragma unroll 1
-      for (int t = 0; t < S32_SUB; ++t) step(t);
+      for (int t = 0; t < 32; ++t) step(t);
     } else {
 #pragma unroll 8  // far steps
-      for (int t = 0; t < S32_SUB; ++t) step(t);
+      for (int t = 0; t < 32; ++t) step(t);
     }
     if (source_side) {
-      // after 32 steps lane l holds the sums of source js*32 + l
+      // after 32 steps lane l holds the sums of pair l: sources l and l + 32
 #pragma unroll
-      for (int c = 0; c < C; ++c) sm.accj[warp][c][js * S32_SUB + lane] = aj[c];
+      for (int c = 0; c < C; ++c) {
+        sm.accj[warp][c][js * S32_SUB + lane] = aj[c].x;
+        sm.accj[warp][c][js * S32_SUB + 32 + lane] = aj[c].y;
+      }
     }
   }
 }
@@ -414,9 +457,9 @@ struct S32Table {
 };
 
 template <int G>
-__global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(const __grid_constant__ S32Table tab,
+__global__ void __launch_bounds__(S32_TPB, G == 1 ? 5 : 3) k_tmu32_sym(const __grid_constant__ S32Table tab,
                                                                        unsigned *__restrict__ next) {
-  constexpr int C = 3 * G;
+  constexpr int C = 3 * G, R = s32_records<G>();
   extern __shared__ float4 s32_dyn[];
   S32Smem<G> &sm = *reinterpret_cast<S32Smem<G> *>(s32_dyn);
   __shared__ int s_item;
@@ -438,30 +481,26 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(const __g
     const bool amoeba = jb.amoeba != 0;
     const int local = jb.item0 + (item - tab.base[jx]);
     const int I = local / nchunk;
-    float4 pt[2];
-    float at[2], mt[2][C], mt3[2][C];
-    int pl[2];
-    bool vt[2];
+    S32Target tg[2];
+    float2 mt[2][C];
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-      pl[u] = warp * 64 + u * 32 + lane;
-      const int ti = I * S32_TILE + pl[u];
-      vt[u] = ti < n;
-      pt[u] = vt[u] ? pos[ti] : make_float4(S32_FAR, S32_FAR, S32_FAR, 0.f);
-      at[u] = (amoeba && vt[u]) ? damp[ti] : 0.f;
+      tg[u].idx = warp * 64 + u * 32 + lane;
+      const int ti = I * S32_TILE + tg[u].idx;
+      const bool v = ti < n;
+      const float4 p = v ? pos[ti] : make_float4(S32_FAR, S32_FAR, S32_FAR, 0.f);
+      tg[u].nx = make_float2(-p.x, -p.x), tg[u].ny = make_float2(-p.y, -p.y), tg[u].nz = make_float2(-p.z, -p.z);
+      tg[u].w = p.w;
+      tg[u].a = (amoeba && v) ? damp[ti] : 0.f;
 #pragma unroll
       for (int c = 0; c < C; ++c) {
-        mt[u][c] = vt[u] ? x[((size_t)(c / 3) * n + ti) * 3 + (c % 3)] : 0.f;
-        mt3[u][c] = mt[u][c] * (1.f / 3.f);
+        const float m = v ? x[((size_t)(c / 3) * n + ti) * 3 + (c % 3)] : 0.f;
+        mt[u][c] = make_float2(m, m);
+        sm.sum[u][c][tid] = sm.cmp[u][c][tid] = 0.f;
       }
     }
     float4 ilo, ihi;
     box_of_supertile(jb.boxes, jb.nbox, I, ilo, ihi);
-    float sum[2][C], cmp[2][C];
-#pragma unroll
-    for (int u = 0; u < 2; ++u)
-#pragma unroll
-      for (int c = 0; c < C; ++c) sum[u][c] = cmp[u][c] = 0.f;
     const int k0 = (local - I * nchunk) * jb.chunk;
     const int k1 = min(jb.K + 1, k0 + jb.chunk);
     for (int k = k0; k < k1; ++k) {
@@ -470,26 +509,31 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(const __g
       if (k > 0 && 2 * k == ntile && I >= ntile / 2) continue;  // the other tile of the pair owns it
       const bool diag = (k == 0);
       __syncthreads();  // the previous slot's staging and sums are read
+      {
+        // thread tid stages pair (tid mod 32) of sub-tile tid / 32
+        const int sb = tid >> 5, p = tid & 31;
+        const int sa = J * S32_TILE + sb * S32_SUB + p, sbb = sa + 32;
+        const bool va = sa < n, vb = sbb < n;
+        const float4 pa = va ? pos[sa] : make_float4(-S32_FAR, -S32_FAR, -S32_FAR, 0.f);
+        const float4 pb = vb ? pos[sbb] : make_float4(-S32_FAR, -S32_FAR, -S32_FAR, 0.f);
+        float fa[2 * R], fb[2 * R];
+        fa[0] = pa.x, fa[1] = pa.y, fa[2] = pa.z;
+        fb[0] = pb.x, fb[1] = pb.y, fb[2] = pb.z;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int q = h * S32_TPB + tid;
-        const int sj = J * S32_TILE + q;
-        const bool v = sj < n;
-        const float4 p = v ? pos[sj] : make_float4(-S32_FAR, -S32_FAR, -S32_FAR, 0.f);
-        const int sb = q >> 5, e = q & 31;
-        sm.pos[sb][e] = p;
-        sm.pos[sb][e + S32_SUB] = p;
-        const float a = (amoeba && v) ? damp[sj] : 0.f;
-#pragma unroll
-        for (int col = 0; col < G; ++col) {
-          float4 m = make_float4(0.f, 0.f, 0.f, a);
-          if (v) {
-            const float *xs = x + ((size_t)col * n + sj) * 3;
-            m.x = xs[0], m.y = xs[1], m.z = xs[2];
-          }
-          sm.mu[col][sb][e] = m;
-          sm.mu[col][sb][e + S32_SUB] = m;
+        for (int c = 0; c < C; ++c) {
+          fa[3 + c] = va ? x[((size_t)(c / 3) * n + sa) * 3 + (c % 3)] : 0.f;
+          fb[3 + c] = vb ? x[((size_t)(c / 3) * n + sbb) * 3 + (c % 3)] : 0.f;
         }
+        if (2 * R > 3 + C) fa[2 * R - 1] = fb[2 * R - 1] = 0.f;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const float4 v = make_float4(fa[2 * r], fb[2 * r], fa[2 * r + 1], fb[2 * r + 1]);
+          sm.rec[r][sb][p] = v;
+          sm.rec[r][sb][p + 32] = v;
+        }
+        const float4 th = make_float4(pa.w, pb.w, (amoeba && va) ? damp[sa] : 0.f, (amoeba && vb) ? damp[sbb] : 0.f);
+        sm.thole[sb][p] = th;
+        sm.thole[sb][p + 32] = th;
       }
       __syncthreads();
       bool far = false;
@@ -501,26 +545,27 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(const __g
         const float gz = fmaxf(0.f, fmaxf(jlo.z - ihi.z, ilo.z - jhi.z));
         far = gx * gx + gy * gy + gz * gz > jb.r2max;
       }
-      float af[2][C], ak[2][C];
+      float2 af[2][C], ak[2][C];
 #pragma unroll
       for (int u = 0; u < 2; ++u)
 #pragma unroll
-        for (int c = 0; c < C; ++c) af[u][c] = ak[u][c] = 0.f;
+        for (int c = 0; c < C; ++c) af[u][c] = ak[u][c] = make_float2(0.f, 0.f);
       if (far)
-        s32_slot<false, false, G>(false, sm, warp, lane, pt, at, mt, mt3, pl, jb.thr, af, ak);
+        s32_slot<false, false, G>(false, sm, warp, lane, tg, mt, jb.thr, af, ak);
       else if (amoeba)
-        s32_slot<true, true, G>(diag, sm, warp, lane, pt, at, mt, mt3, pl, jb.thr, af, ak);
+        s32_slot<true, true, G>(diag, sm, warp, lane, tg, mt, jb.thr, af, ak);
       else
-        s32_slot<true, false, G>(diag, sm, warp, lane, pt, at, mt, mt3, pl, jb.thr, af, ak);
+        s32_slot<true, false, G>(diag, sm, warp, lane, tg, mt, jb.thr, af, ak);
       // the slot's target sums, compensated across slots
 #pragma unroll
       for (int u = 0; u < 2; ++u)
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-          const float y = fmaf(3.f, af[u][c], -ak[u][c]) - cmp[u][c];
-          const float s = sum[u][c] + y;
-          cmp[u][c] = (s - sum[u][c]) - y;
-          sum[u][c] = s;
+          const float s0 = sm.sum[u][c][tid];
+          const float y = fmaf(3.f, af[u][c].x + af[u][c].y, -(ak[u][c].x + ak[u][c].y)) - sm.cmp[u][c][tid];
+          const float s = s0 + y;
+          sm.cmp[u][c][tid] = (s - s0) - y;
+          sm.sum[u][c][tid] = s;
         }
       if (!diag) {
         __syncthreads();
@@ -541,12 +586,12 @@ __global__ void __launch_bounds__(S32_TPB, G == 1 ? 6 : 4) k_tmu32_sym(const __g
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-      if (!vt[u]) continue;
-      const int ti = I * S32_TILE + pl[u];
+      const int ti = I * S32_TILE + tg[u].idx;
+      if (ti >= n) continue;
 #pragma unroll
       for (int c = 0; c < C; ++c) {
         const size_t o = ((size_t)(c / 3) * n + ti) * 3 + (c % 3);
-        fixed_add_f32(jb.lo + o, jb.hi + o, sum[u][c] - cmp[u][c], jb.bad);
+        fixed_add_f32(jb.lo + o, jb.hi + o, sm.sum[u][c][tid] - sm.cmp[u][c][tid], jb.bad);
       }
     }
   }

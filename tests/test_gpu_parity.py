@@ -388,7 +388,7 @@ def test_symmetric_fp32_operator_two_columns_and_determinism(case, w1k, chains, 
         assert rel(g.tmatvec_fp32(x[c]), y64[c]) < 1e-5
 
 
-@pytest.mark.parametrize("kernel", ["pairwise", "tiled", "symmetric"])
+@pytest.mark.parametrize("kernel", ["pairwise", "tiled", "symmetric", "auto"])
 def test_mixed_solve_with_each_fp32_kernel(kernel, chains):
     p, ef = chains
     ref = converged_reference(p, ef).ipd
@@ -396,8 +396,12 @@ def test_mixed_solve_with_each_fp32_kernel(kernel, chains):
     g.set_fp32_kernel(kernel)
     g.set_solver_tol(1e-10)
     g.set_precision("mixed")
+    assert g.fp32_shape(1) is None  # nothing tuned before the first solve
     g.set_external_field(ef)
     assert rel(g.ipd, ref) < 1e-7
+    shape = g.fp32_shape(1)
+    assert shape is not None and shape[1] == 1 and shape[2] >= 1
+    assert shape[0] == kernel if kernel != "auto" else shape[0] in ("pairwise", "tiled", "symmetric")
 
 
 def test_chain_system_wang_exclusions(chains):

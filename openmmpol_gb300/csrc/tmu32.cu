@@ -457,7 +457,7 @@ struct S32Table {
 };
 
 template <int G>
-__global__ void __launch_bounds__(S32_TPB, G == 1 ? 5 : 3) k_tmu32_sym(const __grid_constant__ S32Table tab,
+__global__ void __launch_bounds__(S32_TPB, G == 1 ? 4 : 3) k_tmu32_sym(const __grid_constant__ S32Table tab,
                                                                        unsigned *__restrict__ next) {
   constexpr int C = 3 * G, R = s32_records<G>();
   extern __shared__ float4 s32_dyn[];

@@ -593,7 +593,7 @@ def run_gb300(args):
         wall0 = time.perf_counter()
         for k in range(W, W + K):
             step_ms.append(one_step(sys_, k))
-            counters.append([sys_.counter(c) for c in range(5)])
+            counters.append([sys_.counter(c) for c in range(6)])
         sys_.synchronize()
         wall = time.perf_counter() - wall0
         clocks = clk.stop()
@@ -608,7 +608,10 @@ def run_gb300(args):
             total_ms = float(t.item())
         kstats = kernel_table(kst, n, peak64.value, peak32.value, sys_.fp32_shape(1))
         res = {"value": ws * K / (total_ms * 1e-3), "ms_per_step": total_ms / K, "steps_ms": step_ms,
-               "solver_counters_per_step": counters, "gpu_launches": int(launches), "wall_s_timed": wall,
+               "solver_counters_per_step": counters,
+               "solver_counters": "FP64 products, FP32 products, refinement steps, inner FP32 iterations, "
+                                  "double-single products, residuals updated by an FP32 product",
+               "gpu_launches": int(launches), "wall_s_timed": wall,
                "clocks": clocks, "kernels": kstats, "roofline": roofline_of(kstats, total_ms, n),
                "ipd": sys_.ipd.copy(), "energy": sys_.get_polelec_energy()}
         # e2e through the reference-facing call with host buffers
@@ -627,6 +630,18 @@ def run_gb300(args):
         return res
 
     main = timed_pass(sys_)
+    # the strict mode with its later refinement residuals updated by the FP32
+    # product of the correction (opt-in): the same iterates, one FP64 product
+    # fewer per solve
+    upd = None
+    if args.precision == "mixed":
+        sys_.set_residual_update("update")
+        u = timed_pass(sys_)
+        sys_.set_residual_update("auto")
+        upd = {"value": u["value"], "ms_per_step": u["ms_per_step"], "e2e": u["e2e"]["value"],
+               "solver_counters_per_step": u["solver_counters_per_step"][0],
+               "rel_diff_ipd_vs_recompute": rel_err(u["ipd"], main["ipd"]),
+               "rel_diff_energy_vs_recompute": float(abs(u["energy"] - main["energy"]) / abs(main["energy"]))}
     setup = setup_pass(path, og) if not args.no_grad else None
     grad = None
     if not args.no_grad:
@@ -646,6 +661,15 @@ def run_gb300(args):
         ds = timed_pass(g2)
         ds["m2d_first_solve_s"] = m2d_ds_s
         ds["e_m2d"] = e_ds
+        # the same steps with every refinement residual recomputed in
+        # double-single (no update by the FP32 product of the correction)
+        g2.set_residual_update("recompute")
+        rc = timed_pass(g2)
+        ds["recompute_every_residual"] = {
+            "value": rc["value"], "ms_per_step": rc["ms_per_step"],
+            "solver_counters_per_step": rc["solver_counters_per_step"][0],
+            "rel_diff_ipd_vs_update": rel_err(rc["ipd"], ds["ipd"]),
+            "rel_diff_energy_vs_update": float(abs(rc["energy"] - ds["energy"]) / abs(ds["energy"]))}
         g2.close()
     # plain FP64 solve of the last timed field, and the errors against it
     fp64 = None
@@ -719,6 +743,8 @@ def run_gb300(args):
             "roofline": main["roofline"], "clocks": main["clocks"], "energy": main["energy"], "fp64": fp64}
     if ds:
         line["mixed_ds"] = ds
+    if upd:
+        line["mixed_residual_update"] = upd
     if grad:
         line["geomgrad"] = grad
     if setup:
@@ -865,7 +891,7 @@ def run_b64(args):
     clocks = clk.stop()
     launches = L.ommp_gpu_kernel_launch_count() - l0
     s.enable_kernel_timing(False)
-    counters = [s.counter(k) for k in range(5)]
+    counters = [s.counter(k) for k in range(6)]
     k64, k32, kds = s.kernel_stats(0), s.kernel_stats(1), s.kernel_stats(2)
     value = nf * args.steps / (sum(times) * 1e-3)
     ipd_b = np.zeros((nf, s.n_ipd, n, 3))

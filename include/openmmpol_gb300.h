@@ -319,6 +319,14 @@ void ommp_gpu_set_use_graphs(OMMP_SYSTEM_PRT s, int32_t on);
  * block CG, the columns sharing one Krylov space; 0 the scalar PCG per
  * column */
 void ommp_gpu_set_block_cg(OMMP_SYSTEM_PRT s, int32_t on);
+/* refinement residuals of the mixed modes once one has been recomputed:
+ * 0 recompute r = E - T mu with the mode's residual product (FP64 or
+ * double-single) at every step; 1 update r -= T d with the FP32 product of
+ * the step's correction d when the bound on its error (1e-5 of the residual,
+ * the FP32 operator's tested accuracy) is below a tenth of the tolerance,
+ * recomputing otherwise; -1 (default) by mode: 1 in mixed-ds, 0 in the
+ * strict mixed mode, whose every residual stays an FP64 product */
+int32_t ommp_gpu_set_residual_update(OMMP_SYSTEM_PRT s, int32_t mode);
 
 /* Batched right-hand sides: nfields external fields (e.g. from several QM
  * densities) solved together, each as ommp_set_external_field would solve it
@@ -340,7 +348,8 @@ int32_t ommp_gpu_set_external_fields_batch_device(OMMP_SYSTEM_PRT s, int32_t nfi
 int32_t ommp_gpu_get_iterations(OMMP_SYSTEM_PRT s, int32_t set);
 int32_t ommp_gpu_get_residual_history(OMMP_SYSTEM_PRT s, int32_t set, double *out, int32_t maxn);
 /* counters of the last solve: 0 FP64 T.mu products, 1 FP32 products,
- * 2 refinement steps, 3 inner FP32 iterations */
+ * 2 refinement steps, 3 inner FP32 iterations, 4 double-single products,
+ * 5 refinement residuals updated by an FP32 product */
 int64_t ommp_gpu_get_counter(OMMP_SYSTEM_PRT s, int32_t which);
 /* device time of the last polarization solve (ms, CUDA events) */
 double ommp_gpu_last_solve_ms(OMMP_SYSTEM_PRT s);

@@ -186,6 +186,15 @@ class OMMPSystem:
         FP32 inner solve (default) or the scalar PCG per column."""
         self._L.ommp_gpu_set_block_cg(self._h, int(on))
 
+    def set_residual_update(self, mode) -> None:
+        """Refinement residuals of the mixed modes after the first recomputed
+        one: 'recompute' (the mode's residual product every step), 'update'
+        (r -= T d by the FP32 product of the correction when its error bound
+        is below a tenth of the tolerance) or 'auto' (update in mixed-ds,
+        recompute in the strict mixed mode; the default)."""
+        m = {"auto": -1, "recompute": 0, "update": 1}.get(mode, mode)
+        _check(self._L.ommp_gpu_set_residual_update(self._h, int(m)))
+
     def get_polelec_energy(self) -> float:
         e = C.c_double(0.0)
         _check(self._L.ommp_gpu_get_polelec_energy(self._h, C.byref(e)))

@@ -114,6 +114,7 @@ SIGNATURES = {
     "ommp_qm_helper_get_qm_atoms": (C.c_int32, [_vp]),
     "ommp_gpu_set_use_graphs": (None, [_vp, C.c_int32]),
     "ommp_gpu_set_block_cg": (None, [_vp, C.c_int32]),
+    "ommp_gpu_set_residual_update": (C.c_int32, [_vp, C.c_int32]),
     "ommp_gpu_set_external_fields_batch": (C.c_int32, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ommp_gpu_set_external_fields_batch_device": (C.c_int32, [_vp, C.c_int32, _vp, _vp, _dp]),
     "ommp_gpu_clear_guess": (None, [_vp]),

@@ -258,6 +258,7 @@ int32_t ommp_gpu_set_inner_blocks(OMMP_SYSTEM_PRT s, int32_t max_sites, double l
 }
 void ommp_gpu_set_use_graphs(OMMP_SYSTEM_PRT s, int32_t on) { S(s)->set_use_graphs(on != 0); }
 void ommp_gpu_set_block_cg(OMMP_SYSTEM_PRT s, int32_t on) { S(s)->set_block_cg(on != 0); }
+int32_t ommp_gpu_set_residual_update(OMMP_SYSTEM_PRT s, int32_t mode) { return S(s)->set_residual_update(mode); }
 int32_t ommp_gpu_set_external_fields_batch(OMMP_SYSTEM_PRT s, int32_t nfields, const double *fields, double *ipd_out,
                                            double *energies) {
   return S(s)->solve_batch_host(nfields, fields, ipd_out, energies);
@@ -283,6 +284,7 @@ int64_t ommp_gpu_get_counter(OMMP_SYSTEM_PRT s, int32_t which) {
     case 2: return st.outer;
     case 3: return st.inner_iters;
     case 4: return st.ds_matvecs;
+    case 5: return st.updates;
     default: return -1;
   }
 }

@@ -998,6 +998,15 @@ int System::set_fp32_kernel(int mode) {
   return kOk;
 }
 
+int System::set_residual_update(int mode) {
+  if (mode < -1 || mode > 1) {
+    set_last_error("residual update mode must be -1 (by precision mode), 0 or 1");
+    return kErrBadArg;
+  }
+  residual_update_ = mode;
+  return kOk;
+}
+
 int System::fp32_shape(int ncol, int32_t *shape) const {
   if (!shape) {
     set_last_error("fp32_shape: null output");

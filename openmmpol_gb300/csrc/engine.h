@@ -48,11 +48,11 @@ struct Workspace {
   double *scal_h = nullptr;      // pinned 3 x cap (+ fcap)
   bool owned = false;
   // the multi-system engine's captured bookkeeping after a product
-  // ([0] FP32 inner iteration, [1] refinement residual; by column count 1|2)
-  // and the preconditioner it was captured with
-  cudaGraphExec_t ms_tail[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  int ms_tail_prec[2][2] = {{-1, -1}, {-1, -1}};
-  long long ms_tail_kernels[2][2] = {{0, 0}, {0, 0}};
+  // ([0] FP32 inner iteration, [1] refinement residual, [2] residual update;
+  // by column count 1|2) and the preconditioner it was captured with
+  cudaGraphExec_t ms_tail[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  int ms_tail_prec[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+  long long ms_tail_kernels[3][2] = {{0, 0}, {0, 0}, {0, 0}};
   // captured inner FP32 iteration (CUDA graph) and what it was built for
   cudaGraphExec_t graph = nullptr;
   int graph_ncol = -1, graph_gmax = 0, graph_nsplit = 0, graph_kver = 0, graph_prec = -1;
@@ -74,7 +74,12 @@ struct SolveStats {
   int f64_matvecs = 0;
   int f32_matvecs = 0;
   int ds_matvecs = 0;     // double-single residual products
+  int updates = 0;        // refinement residuals updated by an FP32 product
 };
+
+// relative accuracy of the FP32 operator against T assumed by the residual
+// update (the bound its accuracy tests hold it to)
+constexpr double kResidualUpdateRel = 1e-5;
 
 class MultiSolver;
 
@@ -115,6 +120,14 @@ class System {
   // block CG for the FP32 inner solve of batches of at least 4 columns
   // (default on); off: independent scalar PCG per column
   void set_block_cg(bool on) { block_cg_ = on; }
+  // refinement residuals of the mixed modes after a recomputed one: -1 by
+  // mode (update in mixed-ds, recompute in the strict mixed mode), 0 always
+  // recompute E - T mu with the residual product, 1 update r -= T32 d by the
+  // FP32 product of the correction d when its error bound allows
+  int set_residual_update(int mode);
+  bool residual_update() const {
+    return residual_update_ < 0 ? precision_ == kPrecMixedDS : residual_update_ == 1;
+  }
   int tmatvec(const double *x_host, double *y_host, int nrhs, bool dodiag, int matv);
   int tmatvec_f32(const double *x_host, double *y_host, int nrhs);
   int tmatvec_ds(const double *x_host, double *y_host, int nrhs);
@@ -216,6 +229,7 @@ class System {
     int g, nsplit, kver;  // group width, source splits, kernel version
   };
   int tune_f32(Workspace &w, int ncol, F32Shape &shape);
+  bool update_allowed(const std::vector<double> &rms) const;
   void f32_product(Workspace &w, int ncol, const F32Shape &shape);
   int ensure_batch_ws(int ncol, int nf);
   void free_ws(Workspace &w);
@@ -319,6 +333,7 @@ class System {
   std::map<int, F32Shape> f32_tune_;  // columns -> tuned FP32 launch shape
   bool use_graphs_ = true;
   bool block_cg_ = true;
+  int residual_update_ = -1;
   cudaEvent_t tev_[8] = {};
   void *flush_buf_ = nullptr;
   size_t flush_bytes_ = 0;

@@ -790,6 +790,13 @@ __global__ void k_ir_accumulate(int ncol, int n, double *mu, const float *d32, c
     mu[i] += scale[i / nv] * (double)d32[i];
 }
 
+__global__ void k_residual_update(int ncol, int n, double *r, const float *t32, const double *scale) {
+  size_t nv = 3 * (size_t)n;
+  size_t tot = nv * ncol;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x)
+    r[i] -= scale[i / nv] * (double)t32[i];
+}
+
 __global__ void k_residual(size_t tot, const double *rhs, const double *tmu, double *r) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x)
     r[i] = rhs[i] - tmu[i];
@@ -1496,6 +1503,10 @@ void launch_cg_pupdate_f32(int ncol, int n, float *p, const float *z, const CgCo
 void launch_ir_accumulate(int ncol, int n, double *mu, const float *d32, const double *scale, cudaStream_t st) {
   add_launch_count(1);
   k_ir_accumulate<<<blocks_for((size_t)ncol * n * 3, 256), 256, 0, st>>>(ncol, n, mu, d32, scale);
+}
+void launch_residual_update(int ncol, int n, double *r, const float *t32, const double *scale, cudaStream_t st) {
+  add_launch_count(1);
+  k_residual_update<<<blocks_for((size_t)ncol * n * 3, 256), 256, 0, st>>>(ncol, n, r, t32, scale);
 }
 void launch_residual(size_t total, const double *rhs, const double *tmu, double *r, cudaStream_t st) {
   add_launch_count(1);

@@ -260,6 +260,10 @@ void launch_ir_accumulate(int ncol, int n, double *mu, const float *d32, const d
 // r = rhs - Tmu (all columns), into r; and r32 = r / scale
 void launch_residual(size_t total, const double *rhs, const double *tmu, double *r,
                      cudaStream_t st);
+// r[k] -= scale[k] * t32[k]  (refinement residual updated by the FP32
+// product of the correction instead of a recomputed product)
+void launch_residual_update(int ncol, int n, double *r, const float *t32, const double *scale,
+                            cudaStream_t st);
 // DIIS: x_new = sum_i c_i X[:, i]
 void launch_lincomb(int nvec, size_t n, const double *X, size_t ldx, const double *c, double *out,
                     cudaStream_t st);

@@ -71,6 +71,8 @@ struct MultiSolver::Job {
   int stage = kStart;
   int kind = kNone, items = 0, done = 0, launches = 0;
   double round_pairs = 0.0;  // item size of the product in flight (SymSlice::round_pairs)
+  bool update = false;       // the FP32 product in flight updates the residual
+  std::vector<double> rms;   // residual rms of the last check, per column
   int outer = 0, inner = 0;
   double eta = 1e-5;
   int status = kOk;
@@ -299,7 +301,17 @@ void MultiSolver::enqueue_tail(Job &j, int which) {
   unsigned long long *lo = reinterpret_cast<unsigned long long *>(s.sym_scratch_);
   unsigned long long *hi = lo + C * n;
   unsigned long long *bad = reinterpret_cast<unsigned long long *>(s.sym_scratch_ + 3 * C * n);
-  if (which == 0) {
+  if (which == 2) {
+    // r -= rms T32 d: the FP32 product of the correction (System::update_allowed)
+    float *e = reinterpret_cast<float *>(s.sym_scratch_ + 2 * C * n);
+    gpu::launch_fixed_to_float(C * n, lo, hi, bad, e, st_);
+    gpu::launch_tmu_finish32(d, ncol, e, w.p32, w.h32, st_);
+    gpu::launch_residual_update(ncol, n, w.r, w.h32, w.dots + 2 * w.cap, st_);
+    gpu::launch_scale_by_alpha(ncol, n, d.pol_alpha, w.r, w.z, st_);
+    gpu::launch_dots(ncol, nv, w.r, w.z, w.partial, st_);
+    gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
+    cudaMemcpyAsync(w.scal_h, w.dots, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
+  } else if (which == 0) {
     float *e = reinterpret_cast<float *>(s.sym_scratch_ + 2 * C * n);
     gpu::launch_fixed_to_float(C * n, lo, hi, bad, e, st_);
     gpu::launch_tmu_finish32(d, ncol, e, w.p32, w.h32, st_);
@@ -434,10 +446,19 @@ int MultiSolver::tick() {
       case kAccumulate:
         gpu::launch_ir_accumulate(ncol, n, s.x_, w.x32, w.dots + 2 * cap, st_);
         j.stage = kProduct;
-        j.kind = s.precision_ == kPrecMixedDS ? kDS : kF64;
-        j.round_pairs = round_pairs(j.kind);
-        j.items = j.kind == kDS ? gpu::tmu_ds_sym_items(d, ncol, j.round_pairs)
-                                : gpu::tmu_f64_sym_items(d, ncol, j.round_pairs);
+        j.update = s.update_allowed(j.rms);
+        if (j.update) {
+          // the residual is updated by the FP32 product of the correction
+          cudaMemcpyAsync(w.p32, w.x32, ncol * nv * sizeof(float), cudaMemcpyDeviceToDevice, st_);
+          j.kind = kF32;
+          j.round_pairs = round_pairs(kF32);
+          j.items = gpu::tmu32_sym_items(d, ncol, j.round_pairs);
+        } else {
+          j.kind = s.precision_ == kPrecMixedDS ? kDS : kF64;
+          j.round_pairs = round_pairs(j.kind);
+          j.items = j.kind == kDS ? gpu::tmu_ds_sym_items(d, ncol, j.round_pairs)
+                                  : gpu::tmu_f64_sym_items(d, ncol, j.round_pairs);
+        }
         j.done = j.launches = 0;
         ++j.outer;
         work = true;
@@ -474,7 +495,13 @@ int MultiSolver::tick() {
       std::lock_guard<std::mutex> lk(mu_);
       stats_.spread_products += 1;
     }
-    if (j.kind == kF32) {
+    if (j.kind == kF32 && j.update) {
+      s.stats_.f32_matvecs += 1;
+      s.stats_.updates += 1;
+      tail(j, 2);
+      j.update = false;
+      j.stage = kAwaitCheck;
+    } else if (j.kind == kF32) {
       s.stats_.f32_matvecs += 1;
       tail(j, 0);
       j.stage = kAwaitInner;
@@ -513,6 +540,7 @@ int MultiSolver::tick() {
         if (k < 2) s.stats_.hist[k].push_back(rms[k]);
         if (!(rms[k] < s.tol_)) done = false;
       }
+      j.rms = rms;
       bool finite = true;
       for (double r : rms) finite = finite && std::isfinite(r);
       if (!finite) {

@@ -363,6 +363,20 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
 // ---------------------------------------------------------------------------
 // Iterative refinement: FP64 residual, FP32 inner PCG, FP64 accumulation
 // ---------------------------------------------------------------------------
+// The refinement residual after a step may be updated, r -= T d, with the
+// FP32 product of the step's correction d (rms times the inner solution)
+// instead of recomputing E - T mu: the FP32 operator is within 1e-5 of T
+// (relative, the tested bound), so the updated residual is within 1e-5 rms
+// of the recomputed one, which must stay below a tenth of the tolerance for
+// every unconverged column (a converged column's correction is zero).  The
+// first step (r = E) never qualifies: its correction is the whole solution.
+bool System::update_allowed(const std::vector<double> &rms) const {
+  if (!residual_update()) return false;
+  for (double r : rms)
+    if (r >= tol_ && !(kResidualUpdateRel * r <= 0.1 * tol_)) return false;
+  return true;
+}
+
 int System::mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, int set0, bool have_guess) {
   const int n = d_.n;
   const size_t nv = 3 * (size_t)n;
@@ -419,9 +433,21 @@ int System::mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, in
       st = pcg32_ws(w, ncol, 200, eta);
     if (st) return st;
     gpu::launch_ir_accumulate(ncol, n, x, w.x32, w.dots + 2 * cap, st_);
-    st = matvec_residual(ncol, x, w.h);
-    if (st) return st;
-    gpu::launch_residual(ncol * nv, rhs, w.h, w.r, st_);
+    if (update_allowed(rms)) {
+      // r -= rms T32 x32: the FP32 product of this step's correction
+      F32Shape shape{1, 1, 2};
+      st = tune_f32(w, ncol, shape);
+      if (st) return st;
+      cudaMemcpyAsync(w.p32, w.x32, ncol * nv * sizeof(float), cudaMemcpyDeviceToDevice, st_);
+      f32_product(w, ncol, shape);
+      stats_.f32_matvecs += 1;
+      stats_.updates += 1;
+      gpu::launch_residual_update(ncol, n, w.r, w.h32, w.dots + 2 * cap, st_);
+    } else {
+      st = matvec_residual(ncol, x, w.h);
+      if (st) return st;
+      gpu::launch_residual(ncol * nv, rhs, w.h, w.r, st_);
+    }
     ++outer;
   }
   stats_.outer += outer;

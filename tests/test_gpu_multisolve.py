@@ -65,6 +65,8 @@ def test_solve_multi_matches_single_solves(mix, precision):
     en, st = og.solve_multi(systems, fields)
     assert st["max_systems_per_launch"] >= 2 and st["shared_launches"] >= 1
     assert st["spread_products"] >= 1  # the 30,000-site products took several rounds
+    # mixed-ds updates its later refinement residuals by FP32 products
+    assert any(g.counter(5) >= 1 for g in systems) == (precision == "mixed-ds")
     singles = _systems(mix, precision)
     for g, s1, f, e in zip(systems, singles, fields, en):
         s1.set_external_field(f)

@@ -339,6 +339,34 @@ def test_mixed_ds_solve(case, w1k, chains):
     assert g.residual_history(0)[-1] < 1e-10
 
 
+@pytest.mark.parametrize("case", ["w1k", "chains"])
+def test_refinement_residual_update_and_recompute(case, w1k, chains):
+    """mixed-ds updates the refinement residual after the first recomputed
+    one by the FP32 product of the step's correction (fewer double-single
+    products); the strict mode recomputes every residual in FP64 unless told
+    to update.  Every variant reaches the converged reference within 1e-7 and
+    its certified residual below the tolerance."""
+    p, ef = {"w1k": w1k, "chains": chains}[case]
+    ref = converged_reference(p, ef)
+    res = {}
+    for prec, mode in (("mixed-ds", "auto"), ("mixed-ds", "recompute"), ("mixed", "auto"), ("mixed", "update")):
+        g = OMMPSystem(p)
+        g.set_solver_tol(1e-10)
+        g.set_precision(prec)
+        g.set_residual_update(mode)
+        g.set_external_field(ef)
+        assert rel(g.ipd, ref.ipd) < 1e-7, (prec, mode)
+        assert abs(g.get_polelec_energy() - ref.get_polelec_energy()) <= 1e-7 * abs(ref.get_polelec_energy())
+        assert g.residual_history(0)[-1] < 1e-10
+        expect_update = mode == "update" or (mode == "auto" and prec == "mixed-ds")
+        assert (g.counter(5) >= 1) == expect_update, (prec, mode, g.counter(5))
+        res[(prec, mode)] = g
+    assert res[("mixed-ds", "auto")].counter(4) < res[("mixed-ds", "recompute")].counter(4)
+    assert res[("mixed", "update")].counter(0) < res[("mixed", "auto")].counter(0)
+    with pytest.raises(Exception):
+        res[("mixed", "auto")].set_residual_update(2)
+
+
 @pytest.mark.parametrize("precond", ["diagonal", "block"])
 @pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba"])
 def test_mixed_solve_with_each_inner_preconditioner(case, precond, w1k, chains, golden, golden_mmp):

@@ -107,6 +107,8 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="target rows of the CPU sample (0 = auto)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-ds", action="store_true", help="leave out the double-single pass")
+    ap.add_argument("--no-update", action="store_true",
+                    help="leave out the strict-mode pass with the refinement residual update")
     ap.add_argument("--no-grad", action="store_true", help="leave out the polarization-gradient pass")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-ds"],
                     help="mixed: FP64 refinement residual products; mixed-ds: double-single ones")
@@ -634,7 +636,7 @@ def run_gb300(args):
     # product of the correction (opt-in): the same iterates, one FP64 product
     # fewer per solve
     upd = None
-    if args.precision == "mixed":
+    if args.precision == "mixed" and not args.no_update:
         sys_.set_residual_update("update")
         u = timed_pass(sys_)
         sys_.set_residual_update("auto")

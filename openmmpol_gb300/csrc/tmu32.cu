@@ -331,6 +331,35 @@ __device__ __forceinline__ void box_of_supertile(const float4 *__restrict__ boxe
   }
 }
 
+// damped_factors for a pair of sources against one target: the powers of
+// 1/r on paired instructions, the damping test per half (a half beyond the
+// damping range keeps its factors exactly: e = 0, or the factor 1)
+template <bool AMOEBA>
+__device__ __forceinline__ void damped_factors2(float2 r2, float wt, float2 ws, float at, float2 as, float thr,
+                                                float2 &k3, float2 &k5) {
+  const float2 rinv = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+  const float2 ir2 = __fmul2_rn(rinv, rinv);
+  k3 = __fmul2_rn(rinv, ir2);
+  k5 = __fmul2_rn(k3, ir2);
+  const float2 u = __fmul2_rn(__fmul2_rn(r2, rinv), __fmul2_rn(make_float2(wt, wt), ws));
+  const float2 one = make_float2(1.f, 1.f);
+  if (AMOEBA) {
+    const float2 am = make_float2(fminf(at, as.x), fminf(at, as.y));
+    const float2 au3 = __fmul2_rn(__fmul2_rn(__fmul2_rn(am, u), u), u);
+    if (au3.x < thr || au3.y < thr) {
+      const float2 e = make_float2(au3.x < thr ? __expf(-au3.x) : 0.f, au3.y < thr ? __expf(-au3.y) : 0.f);
+      k3 = __fmul2_rn(k3, __ffma2_rn(make_float2(-1.f, -1.f), e, one));
+      k5 = __fmul2_rn(k5, __ffma2_rn(make_float2(-1.f - au3.x, -1.f - au3.y), e, one));
+    }
+  } else if (u.x < 1.f || u.y < 1.f) {
+    const float2 u3 = __fmul2_rn(__fmul2_rn(u, u), u);
+    const float2 u4 = __fmul2_rn(u3, u);
+    const float2 f3 = __ffma2_rn(make_float2(4.f, 4.f), u3, __fmul2_rn(make_float2(-3.f, -3.f), u4));
+    k3 = __fmul2_rn(k3, make_float2(u.x < 1.f ? f3.x : 1.f, u.y < 1.f ? f3.y : 1.f));
+    k5 = __fmul2_rn(k5, make_float2(u.x < 1.f ? u4.x : 1.f, u.y < 1.f ? u4.y : 1.f));
+  }
+}
+
 // a target's values as lane pairs, the same value in both halves
 struct S32Target {
   float2 nx, ny, nz;  // minus the position
@@ -375,8 +404,8 @@ __device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, in
           const int p = (lane + t) & 31;
           const bool self_a = diag && js * S32_SUB + p == tg[u].idx;
           const bool self_b = diag && js * S32_SUB + 32 + p == tg[u].idx;
-          damped_factors<AMOEBA>(self_a ? 1.f : r2.x, tg[u].w, th.x, tg[u].a, th.z, thr, k3.x, k5.x);
-          damped_factors<AMOEBA>(self_b ? 1.f : r2.y, tg[u].w, th.y, tg[u].a, th.w, thr, k3.y, k5.y);
+          damped_factors2<AMOEBA>(make_float2(self_a ? 1.f : r2.x, self_b ? 1.f : r2.y), tg[u].w,
+                                  make_float2(th.x, th.y), tg[u].a, make_float2(th.z, th.w), thr, k3, k5);
           if (self_a) k3.x = k5.x = 0.f;
           if (self_b) k3.y = k5.y = 0.f;
         } else {
@@ -417,7 +446,7 @@ __device__ __forceinline__ void s32_slot(bool diag, S32Smem<G> &sm, int warp, in
       }
     };
     if (NEAR) {
-#pragma unroll 1
+#pragma unroll 1  // near steps
       for (int t = 0; t < 32; ++t) step(t);
     } else {
 #pragma unroll 8  // far steps

@@ -1147,6 +1147,7 @@ def run_s1024(args):
             out, wall, errors = serve_stream(srv, pl, pool, rate, keep, fresh=fresh)
             st = srv.stats()
             est = srv.engine_stats()
+            phs = srv.phase_stats()
             srv.close()
             lat = np.array([o["latency_ms"] for o in out if np.isfinite(o["latency_ms"])])
             lat_new = np.array([o["latency_ms"] for o in out if not o["followup"] and np.isfinite(o["latency_ms"])])
@@ -1160,7 +1161,8 @@ def run_s1024(args):
                         "followups": int(sum(o["followup"] for o in out)),
                         "readmitted_followups": int(sum(o["readmit"] for o in out)),
                         "evictions": int(st["evictions"]), "peak_concurrent": int(st["peak_concurrent"]),
-                        "peak_bytes": int(st["peak_bytes"]), "engine": est, "errors": errors[:5],
+                        "peak_bytes": int(st["peak_bytes"]), "engine": est, "new_system_phases_mean": phs,
+                        "errors": errors[:5],
                         "n_errors": len(errors)}
             if phase == "saturation":
                 r["results"] = {k: (out[k]["ipd"], out[k]["energy"]) for k in keep if k < nr}

@@ -441,6 +441,17 @@ void ommp_gpu_server_stats(void *server, double *out7);
  * launches that served two or more systems, most systems in one launch,
  * products spread over several rounds (zeros in FP64) */
 void ommp_gpu_server_engine_stats(void *server, int64_t *out5);
+/* where the engine's rounds spent their time, in milliseconds summed over
+ * rounds: [0] GPU time of the product launches, [1] GPU time of the
+ * per-system bookkeeping after them, [2] host wall time of the rounds */
+void ommp_gpu_server_engine_times(void *server, double *out3);
+/* where the new systems' latency went, summed over those that completed
+ * without error: [0] their count, then milliseconds [1] waiting for a
+ * worker slot, [2] in host setup (file, topology, lists, rotation), [3]
+ * waiting for device memory, [4] uploading, [5] forming the permanent field
+ * and right-hand side (mixed modes; 0 in FP64, where it is part of [6]),
+ * [6] solving */
+void ommp_gpu_server_phase_stats(void *server, double *out7);
 /* work per product kind in one round of the engine, in milliseconds of GPU
  * time (default 1.5): shorter rounds let small systems iterate faster beside
  * large ones, longer ones spend less on the per-round bookkeeping */

@@ -579,7 +579,23 @@ class Server:
         o = np.zeros(5, dtype=np.int64)
         self._L.ommp_gpu_server_engine_stats(self._h, o.ctypes.data_as(C.POINTER(C.c_int64)))
         keys = ("rounds", "launches", "shared_launches", "max_systems_per_launch", "spread_products")
-        return dict(zip(keys, (int(v) for v in o)))
+        out = dict(zip(keys, (int(v) for v in o)))
+        t = np.zeros(3)
+        self._L.ommp_gpu_server_engine_times(self._h, t.ctypes.data_as(_lib._dp))
+        out.update({"product_gpu_ms": float(t[0]), "bookkeeping_gpu_ms": float(t[1]), "round_wall_ms": float(t[2])})
+        return out
+
+    def phase_stats(self) -> dict:
+        """Mean milliseconds per phase of the new systems that completed:
+        waiting for a worker, host setup, waiting for device memory, upload,
+        permanent field (mixed modes), solve; and their count."""
+        o = np.zeros(7)
+        self._L.ommp_gpu_server_phase_stats(self._h, o.ctypes.data_as(_lib._dp))
+        n = int(o[0])
+        keys = ("queue_ms", "host_setup_ms", "admission_ms", "upload_ms", "field_ms", "solve_ms")
+        out = {k: (float(v) / n if n else 0.0) for k, v in zip(keys, o[1:])}
+        out["new_systems"] = n
+        return out
 
     def stats(self) -> dict:
         o = np.zeros(7)

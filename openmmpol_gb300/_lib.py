@@ -152,6 +152,8 @@ SIGNATURES = {
     "ommp_gpu_server_cancel": (C.c_int32, [_vp, C.c_int64]),
     "ommp_gpu_server_stats": (None, [_vp, _dp]),
     "ommp_gpu_server_engine_stats": (None, [_vp, _i64p]),
+    "ommp_gpu_server_phase_stats": (None, [_vp, _dp]),
+    "ommp_gpu_server_engine_times": (None, [_vp, _dp]),
     "ommp_gpu_server_set_round_ms": (C.c_int32, [_vp, C.c_double]),
 }
 

@@ -38,6 +38,43 @@ int dalloc(T *&p, size_t count) {
 void set_last_error(const std::string &s) { g_last_error = s; }
 const char *last_error() { return g_last_error.c_str(); }
 
+namespace {
+std::mutex g_pin_mu;
+std::map<size_t, std::vector<void *>> g_pin_free;  // size class -> returned buffers
+std::map<void *, size_t> g_pin_class;               // every pool buffer -> its size class
+size_t pin_class(size_t bytes) {
+  size_t c = 256;
+  while (c < bytes) c <<= 1;
+  return c;
+}
+}  // namespace
+
+cudaError_t pinned_alloc(void **p, size_t bytes) {
+  const size_t c = pin_class(bytes);
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    std::vector<void *> &fl = g_pin_free[c];
+    if (!fl.empty()) {
+      *p = fl.back();
+      fl.pop_back();
+      return cudaSuccess;
+    }
+  }
+  cudaError_t e = cudaMallocHost(p, c);
+  if (e == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    g_pin_class[*p] = c;
+  }
+  return e;
+}
+
+void pinned_free(void *p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  auto it = g_pin_class.find(p);
+  if (it != g_pin_class.end()) g_pin_free[it->second].push_back(p);
+}
+
 int System::check(cudaError_t e, const char *what) {
   if (e == cudaSuccess) return kOk;
   set_last_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
@@ -107,11 +144,11 @@ System::~System() {
   }
   for (auto ev : tev_)
     if (ev) cudaEventDestroy(ev);
-  if (cols_h_) cudaFreeHost(cols_h_);
-  if (scal_h_) cudaFreeHost(scal_h_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
-  if (st_) cudaStreamSynchronize(st_);  // stream-ordered frees
+  if (st_) cudaStreamSynchronize(st_);  // stream-ordered frees and read-backs
+  pinned_free(cols_h_);
+  pinned_free(scal_h_);
   if (st_) cudaStreamDestroy(st_);
 }
 
@@ -210,8 +247,8 @@ int System::upload_static() {
   bad |= alloc(d_.mm_pos32, mm) | alloc(d_.mm_pos32lo, mm) | alloc(d_.mm_tile_box32, 2 * (size_t)((mm + 127) / 128));
   bad |= alloc(partial_, (size_t)gpu::kRedBlocks * 32) | alloc(dots_, 64) | alloc(hist_, 2 * (size_t)maxhist_);
   bad |= alloc(cols_, 2) | alloc(flag_, 1) | alloc(info_, 1);
-  if (bad || cudaMallocHost((void **)&cols_h_, 2 * sizeof(gpu::CgCol)) != cudaSuccess ||
-      cudaMallocHost((void **)&scal_h_, 64 * sizeof(double)) != cudaSuccess) {
+  if (bad || pinned_alloc((void **)&cols_h_, 2 * sizeof(gpu::CgCol)) != cudaSuccess ||
+      pinned_alloc((void **)&scal_h_, 64 * sizeof(double)) != cudaSuccess) {
     set_last_error("out of device memory while allocating the system");
     return kErrMemory;
   }

@@ -354,4 +354,13 @@ int noalloc_prepare_device();
 void set_last_error(const std::string &s);
 const char *last_error();
 
+// Page-locked host buffers for the solvers' small asynchronous read-backs,
+// from a process-wide pool: a buffer returned by pinned_free is kept for the
+// next pinned_alloc of its size class instead of being released, because
+// cudaFreeHost waits for the whole device (a request server freeing an
+// evicted system would stall every solve in flight).  The caller must have
+// completed all copies into or out of a buffer before returning it.
+cudaError_t pinned_alloc(void **p, size_t bytes);
+void pinned_free(void *p);
+
 }  // namespace ommp

@@ -33,6 +33,7 @@
 // are the same symmetric kernels (the FP64 one also below 2048 sites, where
 // the single-system path uses the target-outer kernel).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -82,6 +83,7 @@ struct MultiSolver::Job {
 
 MultiSolver::MultiSolver() {
   cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
+  for (cudaEvent_t &e : ev_) cudaEventCreate(&e);
   cudaMalloc((void **)&counters_, 64 * sizeof(unsigned));
 }
 
@@ -91,6 +93,8 @@ MultiSolver::~MultiSolver() {
   for (Job *j : jobs_) delete j;
   for (auto &kv : done_) delete kv.second;
   if (counters_) cudaFree(counters_);
+  for (cudaEvent_t e : ev_)
+    if (e) cudaEventDestroy(e);
   if (st_) cudaStreamDestroy(st_);
 }
 
@@ -384,6 +388,7 @@ int MultiSolver::tick() {
     pending_.clear();
   }
   if (jobs_.empty()) return 0;
+  const auto wall0 = std::chrono::steady_clock::now();
   bool work = false;
   // ---- steps decided in the previous round ----------------------------------
   for (Job *jp : jobs_) {
@@ -485,7 +490,10 @@ int MultiSolver::tick() {
     }
   }
   // ---- this round's share of every product -----------------------------------
-  if (launch_products(jobs_) > 0) work = true;
+  cudaEventRecord(ev_[0], st_);
+  const bool launched = launch_products(jobs_) > 0;
+  if (launched) work = true;
+  cudaEventRecord(ev_[1], st_);
   // ---- bookkeeping of the products that completed ----------------------------
   for (Job *jp : jobs_) {
     Job &j = *jp;
@@ -516,9 +524,18 @@ int MultiSolver::tick() {
     j.kind = kNone;
     work = true;
   }
+  cudaEventRecord(ev_[2], st_);
   if (work) {
     cudaError_t e = cudaStreamSynchronize(st_);
     if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) {
+      float pm = 0.f, tm = 0.f;
+      cudaEventElapsedTime(&pm, ev_[0], ev_[1]);
+      cudaEventElapsedTime(&tm, ev_[1], ev_[2]);
+      std::lock_guard<std::mutex> lk(mu_);
+      stats_.product_ms += pm;
+      stats_.tail_ms += tm;
+    }
     if (e != cudaSuccess) {
       const std::string msg = std::string("multi-system solver: ") + cudaGetErrorString(e);
       for (Job *j : jobs_) fail(*j, kErrCuda, msg);
@@ -589,6 +606,7 @@ int MultiSolver::tick() {
   std::vector<Job *> keep;
   std::lock_guard<std::mutex> lk(mu_);
   stats_.ticks += 1;
+  stats_.wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   for (Job *j : jobs_) {
     if (j->stage == kFinished) {
       done_[j->id] = j;

@@ -21,6 +21,11 @@ class MultiSolver {
     long long max_systems = 0;     // most systems served by one launch
     long long spread_products = 0; // products spread over more than one launch
     long long finished = 0;
+    // where the rounds' time went: GPU time of the product launches and of
+    // the per-system bookkeeping after them (CUDA events on the engine
+    // stream), and host wall time of the rounds (from the start of a round's
+    // preparation steps to its decisions)
+    double product_ms = 0.0, tail_ms = 0.0, wall_ms = 0.0;
   };
 
   MultiSolver();
@@ -43,7 +48,7 @@ class MultiSolver {
   int tick();
   bool idle();
   // work per product kind in one round, in milliseconds of GPU time at the
-  // symmetric kernels' measured pair rates (default 4): shorter rounds let
+  // symmetric kernels' measured pair rates (default 1.5): shorter rounds let
   // small systems iterate faster beside large ones, longer rounds spend less
   // of the GPU on the per-round bookkeeping
   void set_round_ms(double ms);
@@ -60,6 +65,7 @@ class MultiSolver {
   void fail(Job &j, int status, const std::string &err);
 
   cudaStream_t st_ = nullptr;
+  cudaEvent_t ev_[3] = {nullptr, nullptr, nullptr};  // products start / end, bookkeeping end
   unsigned *counters_ = nullptr;  // one work counter per launch of a round
   std::mutex mu_;
   std::vector<Job *> pending_;    // added, not yet in a round

@@ -59,6 +59,9 @@ struct Request {
   int status = kOk;
   std::string err;
   double t_submit = 0, t_done = 0;
+  // phases of a new system: worker picked it up, host setup done, admitted
+  // to device memory, uploaded, permanent field and right-hand side formed
+  double t_setup0 = 0, t_setup1 = 0, t_admit = 0, t_upload = 0, t_field = 0;
   bool done = false;
 };
 
@@ -101,6 +104,11 @@ class Server {
     MultiSolver::Stats s = engine_.stats();
     out[0] = s.ticks, out[1] = s.launches, out[2] = s.shared_launches, out[3] = s.max_systems,
     out[4] = s.spread_products;
+  }
+
+  void engine_times(double *out) {
+    MultiSolver::Stats s = engine_.stats();
+    out[0] = s.product_ms, out[1] = s.tail_ms, out[2] = s.wall_ms;
   }
 
   long long submit(Request *r) {
@@ -153,6 +161,14 @@ class Server {
     auto it = inst_.find(inst);
     if (it != inst_.end()) it->second.released = true;
     cv_.notify_all();
+  }
+
+  // sums over the new systems that completed without error: count, then the
+  // milliseconds waiting for a worker, in host setup, waiting for admission,
+  // uploading, forming the permanent field and right-hand side, solving
+  void phase_stats(double *out) {
+    std::lock_guard<std::mutex> lk(mu_);
+    for (int k = 0; k < 7; ++k) out[k] = phase_sum_[k];
   }
 
   void stats(double *out) {
@@ -265,9 +281,11 @@ class Server {
         // host setup (file parse, topology, pair lists) outside the lock,
         // then back to the head of the queue to wait for device memory
         lk.unlock();
+        r->t_setup0 = now_ms();
         std::string err;
         int st = kOk;
         std::unique_ptr<System> sys(System::load_host(r->path, err, st));
+        r->t_setup1 = now_ms();
         size_t need = sys ? sys->device_bytes_estimate() : 0;
         lk.lock();
         if (!sys) {
@@ -295,9 +313,11 @@ class Server {
       std::unique_ptr<System> sys = std::move(r->staged);
       start_locked();
       lk.unlock();
+      r->t_admit = now_ms();
       dead.clear();  // free evicted systems' device memory outside the lock
       sys->set_async_alloc(true);
       int st = sys->attach_device();
+      r->t_upload = now_ms();
       if (st == kOk) {
         sys->set_precision(precision_);
         sys->set_tol(tol_);
@@ -307,6 +327,13 @@ class Server {
       if (!(st == kOk || st == kErrNotConverged || st == kErrNumeric)) sys.reset();
       lk.lock();
       --running_;
+      if (st == kOk) {
+        const double t_field = r->t_field > 0 ? r->t_field : r->t_upload;
+        const double ph[6] = {r->t_setup0 - r->t_submit, r->t_setup1 - r->t_setup0, r->t_admit - r->t_setup1,
+                              r->t_upload - r->t_admit, t_field - r->t_upload, now_ms() - t_field};
+        phase_sum_[0] += 1.0;
+        for (int k = 0; k < 6; ++k) phase_sum_[k + 1] += ph[k];
+      }
       if (sys) {
         Instance &inst = inst_[id];
         inst.id = id;
@@ -345,6 +372,7 @@ class Server {
       int st = kOk;
       const long long id = engine_.add(s, r->field.data(), st);
       if (id < 0) return st;
+      if (!r->followup) r->t_field = now_ms();
       int jst = kOk;
       double e = 0.0;
       std::string err;
@@ -402,6 +430,7 @@ class Server {
   std::vector<std::unique_ptr<System>> retired_;
   std::vector<std::thread> workers_;
   long long next_id_ = 0, next_inst_ = 0, evictions_ = 0, completed_ = 0;
+  double phase_sum_[7] = {0, 0, 0, 0, 0, 0, 0};
   int running_ = 0, peak_running_ = 0;
   bool stop_ = false;
 };
@@ -470,6 +499,14 @@ int32_t ommp_gpu_server_set_round_ms(void *server, double ms) {
   }
   static_cast<Server *>(server)->set_round_ms(ms);
   return ommp::kOk;
+}
+
+void ommp_gpu_server_engine_times(void *server, double *out3) {
+  static_cast<Server *>(server)->engine_times(out3);
+}
+
+void ommp_gpu_server_phase_stats(void *server, double *out7) {
+  static_cast<Server *>(server)->phase_stats(out7);
 }
 
 void ommp_gpu_server_engine_stats(void *server, int64_t *out5) {

@@ -46,9 +46,10 @@ void System::free_ws(Workspace &w) {
                w.scratch32, w.partial, w.dots, w.hist, w.cols, w.t32, w.gram, w.bcoef, w.bidx};
   for (void *p : b)
     if (p) cudaFree(p);
-  if (w.cols_h) cudaFreeHost(w.cols_h);
-  if (w.scal_h) cudaFreeHost(w.scal_h);
-  if (w.bscal_h) cudaFreeHost(w.bscal_h);
+  if (st_) cudaStreamSynchronize(st_);  // read-backs into the pinned buffers
+  pinned_free(w.cols_h);
+  pinned_free(w.scal_h);
+  pinned_free(w.bscal_h);
   w = Workspace();
 }
 
@@ -73,9 +74,9 @@ int System::ensure_batch_ws(int ncol, int nf) {
   const int smax = gpu::block_cg_max_columns();
   bad |= walloc(w.t32, ncol * nv) | walloc(w.gram, gpu::block_cg_gram_doubles(smax)) |
          walloc(w.bcoef, 2 * (size_t)smax * smax) | walloc(w.bidx, 2 * (size_t)smax);
-  if (bad || cudaMallocHost((void **)&w.cols_h, ncol * sizeof(gpu::CgCol)) != cudaSuccess ||
-      cudaMallocHost((void **)&w.scal_h, (3 * (size_t)ncol + nf) * sizeof(double)) != cudaSuccess ||
-      cudaMallocHost((void **)&w.bscal_h, (2 * (size_t)smax * smax + smax) * sizeof(double)) != cudaSuccess) {
+  if (bad || pinned_alloc((void **)&w.cols_h, ncol * sizeof(gpu::CgCol)) != cudaSuccess ||
+      pinned_alloc((void **)&w.scal_h, (3 * (size_t)ncol + nf) * sizeof(double)) != cudaSuccess ||
+      pinned_alloc((void **)&w.bscal_h, (2 * (size_t)smax * smax + smax) * sizeof(double)) != cudaSuccess) {
     w.owned = true;
     free_ws(w);
     set_last_error("out of device memory for the batch workspace");

@@ -80,8 +80,17 @@ def test_results_same_alone_and_in_the_mix(systems, precision):
     first, second = served(srv, systems)
     launched = kernel_launch_count() - l0
     st = srv.stats()
+    ph = srv.phase_stats()
     srv.close()
     check(systems, first, second, precision)
+    # where the new systems' latency went: every phase accounted, the sum
+    # within the mean latency of the new requests
+    assert ph["new_systems"] == len(systems)
+    phases = [ph[k] for k in ("queue_ms", "host_setup_ms", "admission_ms", "upload_ms", "field_ms", "solve_ms")]
+    assert min(phases) >= 0.0 and ph["host_setup_ms"] > 0.0 and ph["solve_ms"] > 0.0
+    assert (ph["field_ms"] > 0.0) == (precision != "fp64")
+    mean_new = np.mean([a["latency_ms"] for a in first])
+    assert sum(phases) <= mean_new * 1.01 + 1.0
     # the launch count stays exact while solves on several threads capture
     # and replay CUDA graphs (10 solves of at most a few hundred kernels)
     assert 0 < launched < 20000
@@ -106,6 +115,9 @@ def test_engine_serves_uneven_systems_in_shared_launches(systems):
     check(systems, first, second, "mixed-ds")
     assert es["max_systems_per_launch"] >= 2 and es["shared_launches"] >= 1
     assert es["rounds"] > 0 and es["launches"] >= es["shared_launches"]
+    # the rounds' time: GPU time of products and bookkeeping within the rounds' wall time
+    assert es["product_gpu_ms"] > 0.0 and es["bookkeeping_gpu_ms"] > 0.0
+    assert es["round_wall_ms"] >= es["product_gpu_ms"]
 
 
 def test_eviction_under_small_budget(systems):

@@ -394,11 +394,6 @@ int System::build_blocks() {
     if (w->graph) cudaGraphExecDestroy(w->graph);
     w->graph = nullptr;
     w->graph_ncol = -1;
-    for (auto &row : w->ms_tail)
-      for (auto &g : row) {
-        if (g) cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
   }
   release(blk_info_);
   release(blk_minv_);

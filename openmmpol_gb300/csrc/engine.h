@@ -47,12 +47,6 @@ struct Workspace {
   gpu::CgCol *cols_h = nullptr;  // pinned
   double *scal_h = nullptr;      // pinned 3 x cap (+ fcap)
   bool owned = false;
-  // the multi-system engine's captured bookkeeping after a product
-  // ([0] FP32 inner iteration, [1] refinement residual, [2] residual update;
-  // by column count 1|2) and the preconditioner it was captured with
-  cudaGraphExec_t ms_tail[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
-  int ms_tail_prec[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
-  long long ms_tail_kernels[3][2] = {{0, 0}, {0, 0}, {0, 0}};
   // captured inner FP32 iteration (CUDA graph) and what it was built for
   cudaGraphExec_t graph = nullptr;
   int graph_ncol = -1, graph_gmax = 0, graph_nsplit = 0, graph_kver = 0, graph_prec = -1;

@@ -291,11 +291,11 @@ int MultiSolver::launch_products(std::vector<Job *> &active) {
 }
 
 // The bookkeeping after a system's product (which 0: the rest of the FP32
-// inner PCG iteration; 1: the refinement residual and its rms), on the
-// engine stream.  It is the same dozen small launches every time for a given
-// system, column count and preconditioner, so it is captured once as a CUDA
-// graph and replayed (one launch instead of a dozen); when the capture
-// fails the launches are made directly.
+// inner PCG iteration; 1: the refinement residual and its rms; 2: the
+// residual updated by the FP32 product of the correction), on the engine
+// stream, launched directly.  Capturing it as a CUDA graph per system and
+// column count was measured slower in a request stream: every new system
+// paid the graph's instantiation, more than its replays saved.
 void MultiSolver::enqueue_tail(Job &j, int which) {
   System &s = *j.s;
   const gpu::DevSites &d = s.d_;
@@ -341,43 +341,6 @@ void MultiSolver::enqueue_tail(Job &j, int which) {
     gpu::launch_dots(ncol, nv, w.r, w.z, w.partial, st_);
     gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
     cudaMemcpyAsync(w.scal_h, w.dots, ncol * sizeof(double), cudaMemcpyDeviceToHost, st_);
-  }
-}
-
-void MultiSolver::tail(Job &j, int which) {
-  Workspace &w = j.s->ws_;
-  const int ci = j.ncol - 1;
-  const int prec = (j.s->inner_precond_ == 1 && j.s->blk_info_) ? 1 : 0;
-  cudaGraphExec_t &g = w.ms_tail[which][ci];
-  if (g && w.ms_tail_prec[which][ci] != prec) {
-    cudaGraphExecDestroy(g);
-    g = nullptr;
-  }
-  if (!g) {
-    cudaGraph_t graph = nullptr;
-    const long long before = gpu::thread_launch_count();
-    if (cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      enqueue_tail(j, which);
-      cudaError_t e = cudaStreamEndCapture(st_, &graph);
-      const long long k = gpu::thread_launch_count() - before;
-      gpu::add_launch_count(-k);  // captured, not launched
-      if (e == cudaSuccess && graph && cudaGraphInstantiate(&g, graph, 0) == cudaSuccess) {
-        w.ms_tail_prec[which][ci] = prec;
-        w.ms_tail_kernels[which][ci] = k;
-      } else {
-        g = nullptr;
-        cudaGetLastError();
-      }
-      if (graph) cudaGraphDestroy(graph);
-    } else {
-      cudaGetLastError();
-    }
-  }
-  if (g) {
-    cudaGraphLaunch(g, st_);
-    gpu::add_launch_count(w.ms_tail_kernels[which][ci]);
-  } else {
-    enqueue_tail(j, which);
   }
 }
 
@@ -506,19 +469,19 @@ int MultiSolver::tick() {
     if (j.kind == kF32 && j.update) {
       s.stats_.f32_matvecs += 1;
       s.stats_.updates += 1;
-      tail(j, 2);
+      enqueue_tail(j, 2);
       j.update = false;
       j.stage = kAwaitCheck;
     } else if (j.kind == kF32) {
       s.stats_.f32_matvecs += 1;
-      tail(j, 0);
+      enqueue_tail(j, 0);
       j.stage = kAwaitInner;
     } else {
       if (j.kind == kDS)
         s.stats_.ds_matvecs += 1;
       else
         s.stats_.f64_matvecs += 1;
-      tail(j, 1);
+      enqueue_tail(j, 1);
       j.stage = kAwaitCheck;
     }
     j.kind = kNone;

@@ -61,7 +61,6 @@ class MultiSolver {
   int launch_products(std::vector<Job *> &active);
   void enqueue_tail(Job &j, int which);
   double round_pairs(int kind);  // pairs of one round's budget for a product kind
-  void tail(Job &j, int which);
   void fail(Job &j, int status, const std::string &err);
 
   cudaStream_t st_ = nullptr;

@@ -36,11 +36,6 @@ void System::free_ws(Workspace &w) {
   if (w.graph) cudaGraphExecDestroy(w.graph);
   w.graph = nullptr;
   w.graph_ncol = -1;
-  for (auto &row : w.ms_tail)
-    for (auto &g : row) {
-      if (g) cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
   if (!w.owned) return;
   void *b[] = {w.x, w.r, w.p, w.h, w.z, w.rhs, w.fields, w.out, w.x32, w.r32, w.p32, w.h32, w.z32,
                w.scratch32, w.partial, w.dots, w.hist, w.cols, w.t32, w.gram, w.bcoef, w.bidx};

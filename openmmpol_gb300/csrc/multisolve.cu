@@ -82,7 +82,15 @@ struct MultiSolver::Job {
 };
 
 MultiSolver::MultiSolver() {
-  cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
+  // the rounds run at the highest stream priority: their products and
+  // bookkeeping go ahead of work queued on other streams (a request server's
+  // uploads and permanent fields of new systems), which fills the gaps
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (cudaStreamCreateWithPriority(&st_, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+    cudaGetLastError();
+    cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
+  }
   for (cudaEvent_t &e : ev_) cudaEventCreate(&e);
   cudaMalloc((void **)&counters_, 64 * sizeof(unsigned));
 }

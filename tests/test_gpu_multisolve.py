@@ -106,3 +106,26 @@ def test_solve_multi_follow_up_warm_start(mix):
         ref.set_external_field(f)
         assert rel(g.ipd, ref.ipd) < 1e-7
         assert g.counter(2) <= o0
+
+
+def test_solve_multi_residual_update_matches_recompute(mix):
+    """In the engine too, updating the later refinement residuals by the
+    FP32 product of the correction changes only the convergence certificate:
+    the dipoles equal those of recomputed residuals, with fewer
+    double-single products."""
+    out = {}
+    for mode in ("update", "recompute"):
+        systems = _systems(mix, "mixed-ds")
+        for g in systems:
+            g.set_residual_update(mode)
+        fields = _fields(systems, 90)
+        og.solve_multi(systems, fields)
+        out[mode] = systems
+    for gu, gr in zip(out["update"], out["recompute"]):
+        assert gr.counter(5) == 0
+        assert gu.counter(4) <= gr.counter(4)
+        if gu.counter(2) == gr.counter(2):
+            assert rel(gu.ipd, gr.ipd) < 1e-12
+        assert gu.residual_history(0)[-1] < 1e-10
+    assert sum(g.counter(5) for g in out["update"]) >= 1
+

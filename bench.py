@@ -133,6 +133,23 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_time_ms(local_ms, dist=None):
+    """The timed region of an N-replica run: the maximum over the ranks of
+    each rank's own time (every rank solves its own copy of the workload)."""
+    if dist is None:
+        return float(local_ms)
+    import torch
+    t = torch.tensor([float(local_ms)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ws, steps, total_ms):
+    """Whole-job solves/s of N replicas: all ranks' solves over the slowest
+    rank's time (weak scaling: the work per GPU is fixed)."""
+    return ws * steps / (total_ms * 1e-3)
+
+
 def workload(cfg, cache):
     from openmmpol_gb300 import synth
     nw = {"w30k": 30000, "w10k": 10000, "w1k": 1000, "b64": 30000}[cfg]
@@ -602,14 +619,9 @@ def run_gb300(args):
         launches = L.ommp_gpu_kernel_launch_count() - launches0
         sys_.enable_kernel_timing(False)
         kst = [sys_.kernel_stats(c) for c in range(3)]
-        total_ms = sum(step_ms)
-        if dist:
-            import torch
-            t = torch.tensor([total_ms], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total_ms = float(t.item())
+        total_ms = replica_time_ms(sum(step_ms), dist)
         kstats = kernel_table(kst, n, peak64.value, peak32.value, sys_.fp32_shape(1))
-        res = {"value": ws * K / (total_ms * 1e-3), "ms_per_step": total_ms / K, "steps_ms": step_ms,
+        res = {"value": replica_value(ws, K, total_ms), "ms_per_step": total_ms / K, "steps_ms": step_ms,
                "solver_counters_per_step": counters,
                "solver_counters": "FP64 products, FP32 products, refinement steps, inner FP32 iterations, "
                                   "double-single products, residuals updated by an FP32 product",

@@ -339,14 +339,18 @@ def test_mixed_ds_solve(case, w1k, chains):
     assert g.residual_history(0)[-1] < 1e-10
 
 
-@pytest.mark.parametrize("case", ["w1k", "chains"])
-def test_refinement_residual_update_and_recompute(case, w1k, chains):
+@pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba"])
+def test_refinement_residual_update_and_recompute(case, w1k, chains, golden, golden_mmp):
     """mixed-ds updates the refinement residual after the first recomputed
     one by the FP32 product of the step's correction (fewer double-single
     products); the strict mode recomputes every residual in FP64 unless told
     to update.  Every variant reaches the converged reference within 1e-7 and
-    its certified residual below the tolerance."""
-    p, ef = {"w1k": w1k, "chains": chains}[case]
+    its certified residual below the tolerance.  The protein's D and P
+    right-hand sides differ, so its products and updates take two columns."""
+    if case in ("w1k", "chains"):
+        p, ef = {"w1k": w1k, "chains": chains}[case]
+    else:
+        p, ef = golden_mmp[case], golden[case + "_ef1"]
     ref = converged_reference(p, ef)
     res = {}
     for prec, mode in (("mixed-ds", "auto"), ("mixed-ds", "recompute"), ("mixed", "auto"), ("mixed", "update")):

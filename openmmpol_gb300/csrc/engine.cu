@@ -208,6 +208,30 @@ size_t System::device_bytes_estimate() const {
   return bytes + (size_t(4) << 20);  // events, flags, rounding
 }
 
+// A copy from pageable memory is staged by the driver on the calling thread
+// and, in a request server, held up the engine thread's launches (uploads of
+// new systems took 20-40 ms under load against 2-6 ms alone); from a
+// page-locked buffer the copy is asynchronous.  The buffer comes from the
+// process-wide pool and goes back at h2d_release(), after a synchronisation
+// of the system's stream.
+void System::h2d(void *dst, const void *src, size_t bytes) {
+  if (!bytes) return;
+  void *buf = nullptr;
+  if (pinned_alloc(&buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
+    return;
+  }
+  std::memcpy(buf, src, bytes);
+  cudaMemcpyAsync(dst, buf, bytes, cudaMemcpyHostToDevice, st_);
+  staged_.push_back(buf);
+}
+
+void System::h2d_release() {
+  for (void *b : staged_) pinned_free(b);
+  staged_.clear();
+}
+
 int System::upload_static() {
   const HostModel &m = m_;
   int n = m.npol, mm = m.mm;
@@ -262,9 +286,7 @@ int System::upload_static() {
   ws_.owned = false;
   d_.m2d_nnz = (int)m2d_pairs_.src.size();
   d_.d2d_nnz = (int)d2d_pairs_.src.size();
-  auto up = [&](void *dst, const void *src, size_t bytes) {
-    if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
-  };
+  auto up = [&](void *dst, const void *src, size_t bytes) { h2d(dst, src, bytes); };
   up(d_.m2d_ri, m2d_pairs_.ri.data(), (n + 1) * sizeof(int));
   up(d_.m2d_src, m2d_pairs_.src.data(), m2d_pairs_.src.size() * sizeof(int));
   up(d_.m2d_sP, m2d_pairs_.sP.data(), m2d_pairs_.sP.size() * sizeof(double));
@@ -308,7 +330,6 @@ int System::upload_static() {
     d_.m2d_r2max32 = gpu::m2d_r2max32(m.amoeba, d_.damp_thr, w.data(), m.damping.data(), n, mw.data(), ma.data(), mm);
   }
   up(d_.mm_wa32, mwa.data(), mm * sizeof(float2));
-  cudaStreamSynchronize(st_);  // pwa / mwa are host temporaries
   cudaMemsetAsync(ipd_, 0, nv * nipd * sizeof(double), st_);
   cudaMemsetAsync(e_m2d_, 0, nv * nipd * sizeof(double), st_);
   ipd_h_.assign(nv * nipd, 0.0);
@@ -318,7 +339,9 @@ int System::upload_static() {
   // place the no-allocation entry point's static scratch on this device now,
   // while the system allocates anyway (a failure here is retried by that call)
   noalloc_prepare_device();
-  return check(cudaStreamSynchronize(st_), "upload");
+  st = check(cudaStreamSynchronize(st_), "upload");
+  h2d_release();
+  return st;
 }
 
 int System::upload_geometry() {
@@ -349,12 +372,12 @@ int System::upload_geometry() {
     mp[i] = gpu::Pos64{x[0], x[1], x[2], t > 0.0 ? 1.0 / t : inf};
     if (m.mm_polar[i] >= 0) ma[i] = m.damping[m.mm_polar[i]];
   }
-  cudaMemcpyAsync(d_.pol_pos, pp.data(), n * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
-  cudaMemcpyAsync(d_.pol_pos32, pp32.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st_);
-  cudaMemcpyAsync(d_.pol_pos32lo, pp32lo.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st_);
+  h2d(d_.pol_pos, pp.data(), n * sizeof(gpu::Pos64));
+  h2d(d_.pol_pos32, pp32.data(), n * sizeof(float4));
+  h2d(d_.pol_pos32lo, pp32lo.data(), n * sizeof(float4));
   std::vector<float4> boxes(2 * (size_t)d_.ntile);
   gpu::tile_boxes32(pp32.data(), n, boxes.data());
-  if (n) cudaMemcpyAsync(d_.tile_box32, boxes.data(), boxes.size() * sizeof(float4), cudaMemcpyHostToDevice, st_);
+  if (n) h2d(d_.tile_box32, boxes.data(), boxes.size() * sizeof(float4));
   // static sites in double-single for the double-single E_M2D
   std::vector<float4> mp32(mm), mp32lo(mm);
   for (int i = 0; i < mm; ++i) {
@@ -367,19 +390,21 @@ int System::upload_geometry() {
   std::vector<float4> mboxes(2 * (size_t)((mm + 127) / 128));
   gpu::tile_boxes32(mp32.data(), mm, mboxes.data());
   if (mm) {
-    cudaMemcpyAsync(d_.mm_pos32, mp32.data(), mm * sizeof(float4), cudaMemcpyHostToDevice, st_);
-    cudaMemcpyAsync(d_.mm_pos32lo, mp32lo.data(), mm * sizeof(float4), cudaMemcpyHostToDevice, st_);
-    cudaMemcpyAsync(d_.mm_tile_box32, mboxes.data(), mboxes.size() * sizeof(float4), cudaMemcpyHostToDevice, st_);
+    h2d(d_.mm_pos32, mp32.data(), mm * sizeof(float4));
+    h2d(d_.mm_pos32lo, mp32lo.data(), mm * sizeof(float4));
+    h2d(d_.mm_tile_box32, mboxes.data(), mboxes.size() * sizeof(float4));
   }
-  cudaMemcpyAsync(d_.mm_pos, mp.data(), mm * sizeof(gpu::Pos64), cudaMemcpyHostToDevice, st_);
-  cudaMemcpyAsync(d_.mm_a, ma.data(), mm * sizeof(double), cudaMemcpyHostToDevice, st_);
-  cudaMemcpyAsync(d_.mm_q, m.q.data(), m.q.size() * sizeof(double), cudaMemcpyHostToDevice, st_);
+  h2d(d_.mm_pos, mp.data(), mm * sizeof(gpu::Pos64));
+  h2d(d_.mm_a, ma.data(), mm * sizeof(double));
+  h2d(d_.mm_q, m.q.data(), m.q.size() * sizeof(double));
   // the host vectors above die at return: wait for the copies
   fmm_invalidate();  // the tree follows the geometry
   // block-Jacobi preconditioner of the FP32 inner solver (geometry-dependent)
   int bst = build_blocks();
   if (bst) return bst;
-  return check(cudaStreamSynchronize(st_), "geometry upload");
+  const int st = check(cudaStreamSynchronize(st_), "geometry upload");
+  h2d_release();
+  return st;
 }
 
 int System::build_blocks() {
@@ -404,11 +429,13 @@ int System::build_blocks() {
       set_last_error("out of device memory for the block preconditioner");
       return kErrMemory;
     }
-    cudaMemcpyAsync(blk_info_, info.data(), info.size() * sizeof(int), cudaMemcpyHostToDevice, st_);
-    cudaMemcpyAsync(blk_minv_, minv.data(), minv.size() * sizeof(float), cudaMemcpyHostToDevice, st_);
+    h2d(blk_info_, info.data(), info.size() * sizeof(int));
+    h2d(blk_minv_, minv.data(), minv.size() * sizeof(float));
   }
   // the host vectors die at return
-  return check(cudaStreamSynchronize(st_), "block preconditioner upload");
+  const int st = check(cudaStreamSynchronize(st_), "block preconditioner upload");
+  h2d_release();
+  return st;
 }
 
 int System::set_inner_blocks(int max_sites, double link_bohr) {

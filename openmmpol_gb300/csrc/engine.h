@@ -200,6 +200,11 @@ class System {
   template <typename T>
   int alloc(T *&p, size_t count);
   void release(void *p);
+  // host-to-device copy of set-up data through a page-locked pool buffer
+  // (h2d), returned to the pool by h2d_release once the stream has caught up
+  void h2d(void *dst, const void *src, size_t bytes);
+  void h2d_release();
+  std::vector<void *> staged_;
   bool async_alloc_ = false;
   std::vector<void *> async_bufs_;
   int upload_static();

@@ -231,11 +231,12 @@ void launch_g(const DevSites &s, const float *x, float *partial, int nsplit, cud
 //
 // The arithmetic runs on pairs of sources with the paired FP32 instructions
 // of sm_100 and later (__fadd2_rn, __fmul2_rn, __ffma2_rn: two FP32 lanes
-// per instruction), so that 29 paired operations serve two pairs and the
-// kernel, which with scalar instructions was bound by instruction issue
-// (77 % issue activity, FMA pipe 65 %), issues about half as many
-// instructions per pair.  Only the reciprocal square root (and the damping
-// of near pairs) stays per lane.
+// per instruction), so that 30 paired operations (with -k3/3 below) serve
+// two pairs.  With scalar instructions the kernel was bound by instruction
+// issue (77 % issue activity, FMA pipe 65 %); paired, it issues ~40 % fewer
+// instructions per pair and the FMA pipe bounds it (a paired instruction
+// holds the pipe for two cycles: the lane rate is the same).  Only the
+// reciprocal square root and the damping test of near pairs stay per lane.
 //
 // Per CTA 128 threads own a super-tile of 256 targets, two per thread (lanes
 // l and l + 32 of a 64-target warp slice).  J is staged as four sub-tiles of

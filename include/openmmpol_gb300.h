@@ -303,9 +303,12 @@ int32_t ommp_gpu_set_fp32_kernel(OMMP_SYSTEM_PRT s, int32_t mode);
  * source splits; zeros before the first mixed solve with ncol columns */
 int32_t ommp_gpu_get_fp32_shape(OMMP_SYSTEM_PRT s, int32_t ncol, int32_t *shape);
 /* preconditioner of the FP32 inner solver of the mixed modes: 0 the
- * reference's diagonal (alpha), 1 block Jacobi over runs of bonded sites
- * (default).  The FP64 solver and the outer convergence test always use the
- * reference's diagonal. */
+ * reference's diagonal (alpha), 1 block Jacobi over runs of bonded sites,
+ * 2 (default) block Jacobi with a first-order Neumann step over the
+ * near-field couplings between the runs (z = B^-1 r - B^-1 N B^-1 r, N the
+ * blocks of T between sites of different runs within 6.5 bohr).  The FP64
+ * solver and the outer convergence test always use the reference's
+ * diagonal. */
 int32_t ommp_gpu_set_inner_preconditioner(OMMP_SYSTEM_PRT s, int32_t mode);
 /* runs of the block-Jacobi inner preconditioner: at most max_sites (1..32)
  * consecutive polarizable sites, each within link_bohr of an earlier site of

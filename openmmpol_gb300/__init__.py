@@ -352,9 +352,11 @@ class OMMPSystem:
         _check(self._L.ommp_gpu_set_fp64_kernel(self._h, int(m)))
 
     def set_inner_preconditioner(self, mode) -> None:
-        """'diagonal' (the reference's alpha) | 'block' (block Jacobi, default)
-        for the FP32 inner solver of the mixed modes."""
-        m = {"diagonal": 0, "block": 1}.get(mode, mode)
+        """'diagonal' (the reference's alpha) | 'block' (block Jacobi) |
+        'near' (block Jacobi with a Neumann step over the near-field
+        couplings between the blocks; the default) for the FP32 inner solver
+        of the mixed modes."""
+        m = {"diagonal": 0, "block": 1, "near": 2}.get(mode, mode)
         _check(self._L.ommp_gpu_set_inner_preconditioner(self._h, int(m)))
 
     def set_inner_blocks(self, max_sites: int, link_bohr: float) -> None:

@@ -241,12 +241,17 @@ int System::bpcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
   F32Shape shape{1, 1, 2};
   int st = tune_f32(w, std::min(ncol, 8), shape);
   if (st) return st;
-  const bool blocks = inner_precond_ == 1 && blk_info_;
+  const bool blocks = inner_precond_ >= 1 && blk_info_;
+  const bool near = blocks && near_precond();
   auto precondition = [&](int nc) {
-    if (blocks)
+    if (blocks) {
       gpu::launch_block_apply(nc, n, blk_info_, blk_minv_, w.r32, w.z32, st_);
-    else
+      // the next direction block (w.t32) is written only after this: scratch
+      if (near)
+        gpu::launch_near_correct(nc, n, blk_info_, blk_minv_, near_ri_, near_ci_, near_blk_, w.z32, w.t32, st_);
+    } else {
       gpu::launch_scale_alpha32(nc, n, alpha32_, w.r32, w.z32, st_);
+    }
   };
   // index maps in w.bidx: [0, smax) identity, then the active columns
   std::vector<int> idx(2 * (size_t)smax);

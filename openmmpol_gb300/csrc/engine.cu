@@ -130,7 +130,8 @@ System::~System() {
                   d_.mm_a, d_.mm_q, d_.m2d_ri, d_.m2d_src, d_.m2d_sP, d_.m2d_sD, d_.d2d_ri, d_.d2d_src,
                   d_.d2d_s, e_m2d_, ipd_, rhs_, ext_, x_, r_, p_, h_, z_, x32_, r32_, p32_, h32_, z32_,
                   alpha32_, scratch_, scratch32_, partial_, dots_, hist_, cols_, flag_, tmat_, piv_,
-                  info_, diis_x_, diis_e_, d_.tile_box32, ext_buf_, blk_info_, blk_minv_};
+                  info_, diis_x_, diis_e_, d_.tile_box32, ext_buf_, blk_info_, blk_minv_, near_ri_, near_ci_,
+                  near_blk_};
   for (void *b : bufs) release(b);
   if (flush_buf_) cudaFree(flush_buf_);
   release(sym_scratch_);
@@ -205,6 +206,8 @@ size_t System::device_bytes_estimate() const {
   // double-single kernels' split partials (allocated in that mode only)
   const size_t ds_split = std::max(2 * gpu::tmu_ds_pick_split(d, sms), gpu::m2d_ds_pick_split(d, sms));
   bytes += 16 * (n + 2 * m + 2 * ((m + 127) / 128)) + 8 * ds_split * nv;
+  // near-field couplings of the Neumann step (about a dozen per site in water)
+  if (inner_precond_ == 2) bytes += 4 * (n + 1) + 40 * 24 * n;
   return bytes + (size_t(4) << 20);  // events, flags, rounding
 }
 
@@ -432,8 +435,42 @@ int System::build_blocks() {
     h2d(blk_info_, info.data(), info.size() * sizeof(int));
     h2d(blk_minv_, minv.data(), minv.size() * sizeof(float));
   }
+  // the near-field couplings follow the geometry: built again at the next
+  // mixed solve (ensure_near)
+  release(near_ri_);
+  release(near_ci_);
+  release(near_blk_);
+  near_ri_ = near_ci_ = nullptr;
+  near_blk_ = nullptr;
+  blk_runs_.assign(info.begin(), info.end());
   // the host vectors die at return
   const int st = check(cudaStreamSynchronize(st_), "block preconditioner upload");
+  h2d_release();
+  return st;
+}
+
+// The near-field couplings of the Neumann step, built before the first mixed
+// solve that uses them (on the calling thread: a request server's worker,
+// not the engine), so that systems solved in FP64 never pay for them.
+int System::ensure_near() {
+  if (inner_precond_ != 2 || near_ri_ || !blk_info_ || d_.n == 0) return kOk;
+  std::vector<int> ri, ci;
+  std::vector<float> blk;
+  build_near_field(m_, d2d_pairs_, d_.damp_thr, blk_runs_, kNearBohr, ri, ci, blk);
+  if (alloc(near_ri_, ri.size()) || alloc(near_ci_, ci.size()) || alloc(near_blk_, blk.size())) {
+    set_last_error("out of device memory for the near-field preconditioner");
+    return kErrMemory;
+  }
+  // a captured inner iteration was built without the Neumann step
+  for (Workspace *w : {&ws_, &wsb_}) {
+    if (w->graph) cudaGraphExecDestroy(w->graph);
+    w->graph = nullptr;
+    w->graph_ncol = -1;
+  }
+  h2d(near_ri_, ri.data(), ri.size() * sizeof(int));
+  h2d(near_ci_, ci.data(), ci.size() * sizeof(int));
+  h2d(near_blk_, blk.data(), blk.size() * sizeof(float));
+  const int st = check(cudaStreamSynchronize(st_), "near-field preconditioner upload");
   h2d_release();
   return st;
 }
@@ -1039,8 +1076,9 @@ int System::set_fp64_kernel(int mode) {
 }
 
 int System::set_inner_preconditioner(int mode) {
-  if (mode < 0 || mode > 1) {
-    set_last_error("inner preconditioner must be 0 (diagonal) or 1 (block Jacobi)");
+  if (mode < 0 || mode > 2) {
+    set_last_error("inner preconditioner must be 0 (diagonal), 1 (block Jacobi) or 2 (block Jacobi with the "
+                   "near-field Neumann step)");
     return kErrBadArg;
   }
   inner_precond_ = mode;

@@ -261,7 +261,14 @@ class System {
   int fp64_kernel_ = 0;
   int4 *blk_info_ = nullptr;   // block-Jacobi preconditioner (build_block_jacobi)
   float *blk_minv_ = nullptr;
-  int inner_precond_ = 1;       // FP32 inner solver: 0 diagonal, 1 block Jacobi
+  int *near_ri_ = nullptr, *near_ci_ = nullptr;  // near-field couplings (build_near_field)
+  float *near_blk_ = nullptr;
+  std::vector<int> blk_runs_;  // the runs of the block preconditioner (host copy of its info)
+  int ensure_near();
+  // FP32 inner solver: 0 diagonal, 1 block Jacobi, 2 block Jacobi with the
+  // near-field Neumann step (default)
+  int inner_precond_ = 2;
+  bool near_precond() const { return inner_precond_ == 2 && blk_info_ && near_ri_; }
   int blk_max_ = kMaxBlock;
   double blk_link_ = kBlockLinkBohr;
   int build_blocks();

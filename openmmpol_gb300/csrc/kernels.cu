@@ -1336,6 +1336,61 @@ __global__ void k_block_apply(int n, const int4 *__restrict__ info, const float 
   zz[2] = z2;
 }
 
+// z -= B^-1 w, the second half of the Neumann step (w read over the run,
+// z[j] read and written by its own thread, so z may hold z0 in place)
+__global__ void k_block_apply_sub(int n, const int4 *__restrict__ info, const float *__restrict__ minv,
+                                  const float *__restrict__ w, float *__restrict__ z) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const size_t co = (size_t)blockIdx.y * 3 * n;
+  const int4 b = info[j];
+  const int wd = 3 * b.y;
+  const float *ww = w + co + 3 * (size_t)b.x;
+  const float *m0 = minv + b.z + (size_t)(3 * b.w) * wd;
+  const float *m1 = m0 + wd, *m2 = m1 + wd;
+  float t0 = 0.f, t1 = 0.f, t2 = 0.f;
+  for (int l = 0; l < wd; ++l) {
+    const float v = ww[l];
+    t0 = fmaf(m0[l], v, t0);
+    t1 = fmaf(m1[l], v, t1);
+    t2 = fmaf(m2[l], v, t2);
+  }
+  float *zz = z + co + 3 * (size_t)j;
+  zz[0] -= t0;
+  zz[1] -= t1;
+  zz[2] -= t2;
+}
+
+// y[j] = sum over the near-field row j of N_ji x[i] (3x3 FP32 blocks)
+__global__ void k_near_apply(int n, const int *__restrict__ ri, const int *__restrict__ ci,
+                             const float *__restrict__ blk, const float *__restrict__ x, float *__restrict__ y) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const size_t co = (size_t)blockIdx.y * 3 * n;
+  float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+  for (int e = ri[j]; e < ri[j + 1]; ++e) {
+    const float *b = blk + 9 * (size_t)e;
+    const float *xi = x + co + 3 * (size_t)ci[e];
+    const float a = xi[0], c = xi[1], d = xi[2];
+    y0 = fmaf(b[0], a, fmaf(b[1], c, fmaf(b[2], d, y0)));
+    y1 = fmaf(b[3], a, fmaf(b[4], c, fmaf(b[5], d, y1)));
+    y2 = fmaf(b[6], a, fmaf(b[7], c, fmaf(b[8], d, y2)));
+  }
+  float *yy = y + co + 3 * (size_t)j;
+  yy[0] = y0;
+  yy[1] = y1;
+  yy[2] = y2;
+}
+
+void launch_near_correct(int ncol, int n, const int4 *info, const float *minv, const int *ri, const int *ci,
+                         const float *blk, float *z, float *w, cudaStream_t st) {
+  if (n == 0) return;
+  add_launch_count(2);
+  dim3 grid((n + 127) / 128, ncol);
+  k_near_apply<<<grid, 128, 0, st>>>(n, ri, ci, blk, z, w);
+  k_block_apply_sub<<<grid, 128, 0, st>>>(n, info, minv, w, z);
+}
+
 void launch_block_apply(int ncol, int n, const int4 *info, const float *minv, const float *r, float *z,
                         cudaStream_t st) {
   if (n == 0) return;

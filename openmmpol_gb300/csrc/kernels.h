@@ -177,6 +177,11 @@ void launch_grad_ds_dip(const DevSites &s, const double *ipd, double *partial, i
 // build_block_jacobi), columns [ncol][n][3], FP32
 void launch_block_apply(int ncol, int n, const int4 *info, const float *minv, const float *r, float *z,
                         cudaStream_t st);
+// the Neumann step of the near-field preconditioner on z = B^-1 r:
+// w = N z (near-field rows ri/ci/blk of build_near_field), z -= B^-1 w;
+// w is a scratch of the same shape as z
+void launch_near_correct(int ncol, int n, const int4 *info, const float *minv, const int *ri, const int *ci,
+                         const float *blk, float *z, float *w, cudaStream_t st);
 // batched fields: rhs[s*nf+f] = E_M2D[s] + field[f]; solution scatter to [f][s]
 void launch_batch_rhs(int n, int nf, int nset, const double *e_m2d, const double *fields, double *rhs,
                       cudaStream_t st);

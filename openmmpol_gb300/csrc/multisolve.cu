@@ -129,6 +129,7 @@ long long MultiSolver::add(System *s, const double *ext_host, int &status) {
     cudaMemcpyAsync(s->ext_, ext_host, nv * sizeof(double), cudaMemcpyHostToDevice, sst);
     st = s->ensure_m2d();
     if (!st) st = s->ensure_sym_scratch();
+    if (!st) st = s->ensure_near();
   }
   auto *j = new Job();
   j->s = s;
@@ -332,8 +333,11 @@ void MultiSolver::enqueue_tail(Job &j, int which) {
     gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
     gpu::launch_cg_alpha(ncol, w.dots, w.cols, 1e-300, st_);
     gpu::launch_cg_update_f32(ncol, n, w.x32, w.r32, w.p32, w.h32, w.z32, s.alpha32_, w.cols, w.partial, st_);
-    if (s.inner_precond_ == 1 && s.blk_info_) {
+    if (s.inner_precond_ >= 1 && s.blk_info_) {
       gpu::launch_block_apply(ncol, n, s.blk_info_, s.blk_minv_, w.r32, w.z32, st_);
+      if (s.near_precond())
+        gpu::launch_near_correct(ncol, n, s.blk_info_, s.blk_minv_, s.near_ri_, s.near_ci_, s.near_blk_, w.z32, w.h32,
+                                 st_);
       gpu::launch_dots_f32(ncol, nv, w.r32, w.z32, w.partial, st_);
     }
     gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);
@@ -403,8 +407,11 @@ int MultiSolver::tick() {
         }
         cudaMemcpyAsync(w.cols, w.cols_h, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
         gpu::launch_cg_update_f32(ncol, n, w.x32, w.r32, w.p32, w.h32, w.z32, s.alpha32_, w.cols, w.partial, st_);
-        if (s.inner_precond_ == 1 && s.blk_info_) {
+        if (s.inner_precond_ >= 1 && s.blk_info_) {
           gpu::launch_block_apply(ncol, n, s.blk_info_, s.blk_minv_, w.r32, w.z32, st_);
+          if (s.near_precond())
+            gpu::launch_near_correct(ncol, n, s.blk_info_, s.blk_minv_, s.near_ri_, s.near_ci_, s.near_blk_, w.z32,
+                                     w.h32, st_);
           gpu::launch_dots_f32(ncol, nv, w.r32, w.z32, w.partial, st_);
         }
         gpu::launch_reduce_partials(ncol, w.partial, w.dots, st_);

@@ -85,5 +85,13 @@ constexpr double kBlockLinkBohr = 3.0;
 constexpr int kMaxBlockLimit = 32;
 void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_thr, int max_sites,
                         double link_bohr, std::vector<int> &info, std::vector<float> &minv);
+// Near-field couplings of the inner preconditioner's Neumann step: for each
+// polarizable site j (row), the sites i of other runs (info from
+// build_block_jacobi) within rc, with the 3x3 block of T between them,
+// -s (3 k5 d d^T - k3 I) with the damping and the D2D scale of the product
+// (row-major, FP32): CSR ri [n + 1], ci [nnz], blk [nnz][9]
+constexpr double kNearBohr = 6.5;
+void build_near_field(const HostModel &m, const ScaledPairs &d2d, double damp_thr, const std::vector<int> &info,
+                      double rc, std::vector<int> &ri, std::vector<int> &ci, std::vector<float> &blk);
 
 }  // namespace ommp

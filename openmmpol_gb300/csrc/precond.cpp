@@ -169,4 +169,111 @@ void build_block_jacobi(const HostModel &m, const ScaledPairs &d2d, double damp_
   for (auto &x : th) x.join();
 }
 
+
+// Near-field couplings (build_near_field): the sites are binned in cubic
+// cells of side rc and packed in cell order (position, Thole factor, damping
+// a, run, index), so that the candidates of a row are contiguous records;
+// each row scans the 27 cells around its own in a fixed order, so the lists
+// are the same on any number of threads.  Rows are counted in a first pass
+// and filled in a second.
+void build_near_field(const HostModel &m, const ScaledPairs &d2d, double damp_thr, const std::vector<int> &info,
+                      double rc, std::vector<int> &ri, std::vector<int> &ci, std::vector<float> &blk) {
+  const int n = m.npol;
+  ri.assign((size_t)n + 1, 0);
+  ci.clear();
+  blk.clear();
+  if (n == 0) return;
+  struct Site {
+    double x, y, z, w, a;
+    int run, idx;
+  };
+  auto pos = [&](int j) { return &m.cmm[3 * (size_t)m.polar_mm[j]]; };
+  double lo[3] = {pos(0)[0], pos(0)[1], pos(0)[2]}, hi[3] = {lo[0], lo[1], lo[2]};
+  for (int j = 1; j < n; ++j)
+    for (int c = 0; c < 3; ++c) lo[c] = std::min(lo[c], pos(j)[c]), hi[c] = std::max(hi[c], pos(j)[c]);
+  long dim[3];
+  for (int c = 0; c < 3; ++c) dim[c] = std::max(1L, std::min(1024L, (long)((hi[c] - lo[c]) / rc) + 1));
+  auto cell_of = [&](const double *p, long *q) {
+    for (int c = 0; c < 3; ++c) q[c] = std::min(dim[c] - 1, std::max(0L, (long)((p[c] - lo[c]) / rc)));
+    return (size_t)((q[2] * dim[1] + q[1]) * dim[0] + q[0]);
+  };
+  const size_t ncell = (size_t)dim[0] * dim[1] * dim[2];
+  std::vector<int> cstart(ncell + 1, 0), cell(n);
+  for (int j = 0; j < n; ++j) {
+    long q[3];
+    cell[j] = (int)cell_of(pos(j), q);
+    ++cstart[cell[j] + 1];
+  }
+  for (size_t c = 0; c < ncell; ++c) cstart[c + 1] += cstart[c];
+  std::vector<Site> site(n);
+  {
+    std::vector<int> fill(cstart.begin(), cstart.end() - 1);
+    for (int j = 0; j < n; ++j) {
+      const double *p = pos(j);
+      site[fill[cell[j]]++] = Site{p[0], p[1], p[2], 1.0 / m.thole[m.polar_mm[j]], m.amoeba ? m.damping[j] : 0.0,
+                                   info[4 * (size_t)j], j};
+    }
+  }
+  const double rc2 = rc * rc;
+  // visit the candidates of site s (a packed record) in a fixed order
+  auto scan = [&](const Site &sj, auto &&f) {
+    long q[3];
+    const double pj[3] = {sj.x, sj.y, sj.z};
+    cell_of(pj, q);
+    for (long z = std::max(0L, q[2] - 1); z <= std::min(dim[2] - 1, q[2] + 1); ++z)
+      for (long y = std::max(0L, q[1] - 1); y <= std::min(dim[1] - 1, q[1] + 1); ++y) {
+        const size_t row = (z * dim[1] + y) * dim[0];
+        const int k0 = cstart[row + std::max(0L, q[0] - 1)], k1 = cstart[row + std::min(dim[0] - 1, q[0] + 1) + 1];
+        for (int k = k0; k < k1; ++k) {
+          const Site &si = site[k];
+          if (si.run == sj.run) continue;  // same run: in the block
+          const double d[3] = {sj.x - si.x, sj.y - si.y, sj.z - si.z};
+          const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          if (r2 < rc2) f(si, d, r2);
+        }
+      }
+  };
+  auto scale = [&](int j, int i) {
+    for (int k = d2d.ri[j]; k < d2d.ri[j + 1]; ++k)
+      if (d2d.src[k] == i) return d2d.sP[k];
+    return 1.0;
+  };
+  const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), n / 4096));
+  auto parallel = [&](auto &&body) {
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(body, (int)((long)n * t / nt), (int)((long)n * (t + 1) / nt));
+    body(0, (int)((long)n / nt));
+    for (auto &x : th) x.join();
+  };
+  // rows in cell order (packed index s), written at their site's place
+  parallel([&](int s0, int s1) {
+    for (int s = s0; s < s1; ++s) {
+      const Site &sj = site[s];
+      int cnt = 0;
+      scan(sj, [&](const Site &si, const double *, double) { cnt += scale(sj.idx, si.idx) != 0.0; });
+      ri[sj.idx + 1] = cnt;
+    }
+  });
+  for (int j = 0; j < n; ++j) ri[j + 1] += ri[j];
+  ci.resize(ri[n]);
+  blk.resize(9 * (size_t)ri[n]);
+  parallel([&](int s0, int s1) {
+    for (int s = s0; s < s1; ++s) {
+      const Site &sj = site[s];
+      int e = ri[sj.idx];
+      scan(sj, [&](const Site &si, const double *d, double r2) {
+        const double sc = scale(sj.idx, si.idx);
+        if (sc == 0.0) return;
+        double k3, k5;
+        damped_k35(m.amoeba, r2, sj.w, si.w, sj.a, si.a, damp_thr, k3, k5);
+        ci[e] = si.idx;
+        for (int p = 0; p < 3; ++p)
+          for (int q = 0; q < 3; ++q)
+            blk[9 * (size_t)e + 3 * p + q] = (float)(-sc * (3.0 * k5 * d[p] * d[q] - (p == q ? k3 : 0.0)));
+        ++e;
+      });
+    }
+  });
+}
+
 }  // namespace ommp

@@ -269,10 +269,13 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
   }
   cudaMemcpyAsync(w.cols, w.cols_h, ncol * sizeof(gpu::CgCol), cudaMemcpyHostToDevice, st_);
   // z = M^-1 r: the diagonal (fused in the update) or the block-Jacobi blocks
-  const bool blocks = inner_precond_ == 1 && blk_info_;
+  const bool blocks = inner_precond_ >= 1 && blk_info_;
+  const bool near = blocks && near_precond();
   auto precondition = [&]() {
     if (!blocks) return;
     gpu::launch_block_apply(ncol, n, blk_info_, blk_minv_, w.r32, w.z32, st_);
+    // h32 (T p) is spent by the update above: scratch of the Neumann step
+    if (near) gpu::launch_near_correct(ncol, n, blk_info_, blk_minv_, near_ri_, near_ci_, near_blk_, w.z32, w.h32, st_);
     gpu::launch_dots_f32(ncol, nv, w.r32, w.z32, w.partial, st_);
   };
   gpu::launch_cg_update_f32(ncol, n, w.x32, w.r32, w.p32, w.h32, w.z32, alpha32_, w.cols, w.partial, st_);
@@ -305,7 +308,7 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
   // capture one iteration as a graph (kernel arguments and buffers are fixed
   // per workspace, width and launch shape; the tolerance lives in w.cols)
   if (use_graphs_ && (w.graph_ncol != ncol || w.graph_gmax != shape.g || w.graph_nsplit != shape.nsplit ||
-                     w.graph_kver != shape.kver || w.graph_prec != (blocks ? 1 : 0))) {
+                     w.graph_kver != shape.kver || w.graph_prec != (near ? 2 : blocks ? 1 : 0))) {
     if (w.graph) cudaGraphExecDestroy(w.graph);
     w.graph = nullptr;
     w.graph_ncol = -1;
@@ -321,7 +324,7 @@ int System::pcg32_ws(Workspace &w, int ncol, int max_it, double eta) {
         w.graph_gmax = shape.g;
         w.graph_nsplit = shape.nsplit;
         w.graph_kver = shape.kver;
-        w.graph_prec = blocks ? 1 : 0;
+        w.graph_prec = near ? 2 : blocks ? 1 : 0;
         w.graph_kernels = kernels;
       } else {
         w.graph = nullptr;
@@ -379,6 +382,10 @@ int System::mixed_ir_ws(Workspace &w, int ncol, const double *rhs, double *x, in
   const int max_outer = 30;
   const int cap = w.cap;
   log_msg(kVerbLow, nullptr, "Solving linear system with mixed-precision CG (FP32 inner, FP64 refinement)");
+  {
+    const int pst = ensure_near();
+    if (pst) return pst;
+  }
   if (have_guess) {
     int st0 = matvec_residual(ncol, x, w.h);
     if (st0) return st0;

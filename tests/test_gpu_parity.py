@@ -371,7 +371,7 @@ def test_refinement_residual_update_and_recompute(case, w1k, chains, golden, gol
         res[("mixed", "auto")].set_residual_update(2)
 
 
-@pytest.mark.parametrize("precond", ["diagonal", "block"])
+@pytest.mark.parametrize("precond", ["diagonal", "block", "near"])
 @pytest.mark.parametrize("case", ["w1k", "chains", "1crn_amoeba", "1crn_wang", "nma_amoeba"])
 def test_mixed_solve_with_each_inner_preconditioner(case, precond, w1k, chains, golden, golden_mmp):
     """The inner preconditioner changes only the FP32 inner iterations: both
@@ -393,7 +393,7 @@ def test_mixed_solve_with_each_inner_preconditioner(case, precond, w1k, chains, 
 def test_block_preconditioner_saves_inner_iterations(w1k):
     p, ef = w1k
     counts = {}
-    for precond in ("diagonal", "block"):
+    for precond in ("diagonal", "block", "near"):
         g = OMMPSystem(p)
         g.set_solver_tol(1e-10)
         g.set_precision("mixed")
@@ -401,6 +401,7 @@ def test_block_preconditioner_saves_inner_iterations(w1k):
         g.set_external_field(ef)
         counts[precond] = g.counter(1)
     assert counts["block"] < counts["diagonal"]
+    assert counts["near"] <= counts["block"]  # the Neumann step over the near field
 
 
 @pytest.mark.parametrize("case", ["w1k", "1crn_amoeba", "chains"])
